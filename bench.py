@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark: 1M-particle 3-D PBF dam break, steps/s on one GB300.
+
+Workload: 128 x 128 x 64 = 1,048,576 fluid particles, lattice spacing h/2
+(h = 0.1), jitter U(-0.01h, 0.01h), in the corner of a 4:1 box; poly6 /
+spiky kernels, 4 Jacobi iterations with the neighbour grid rebuilt every
+iteration, s_corr k = 0.1 n = 4 dq = 0.2h, XSPH c = 0.01, dt = 1/120, FP32.
+Synthetic seeded data (the reference publishes no dataset or numbers).
+
+One "step" is one full pbd update (prediction, 4 x (grid build, lambda,
+fused delta + walls), velocity, XSPH), replayed from a captured CUDA graph.
+Steps are timed one by one with CUDA events on the launching stream; L2 is
+flushed (256 MiB write) before each timed step, outside the timed span.
+
+--impl reference times the reference path on the host cores: the oracle
+(the FP64 C restatement of the reference step, all host threads) on the
+same workload -- the reference's own GPU code does not build on CUDA 13 and
+its CPU solver is 2-D and O(N^2).
+
+Under torchrun (N > 1) every rank runs its own replica of the scene (the
+single-scene step has no independent partition), and value is the total
+steps/s over all replicas ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "1M-particle PBF steps/s: plain vs batched/adjoint, same GPU, <=1e-5 proj err"
+UNIT = "steps/s"
+
+# Algorithmic bytes (compulsory FP32 traffic, each array touched once per pass)
+B_LAMBDA = 20      # read x* 16 + write lambda 4, per particle
+B_DELTA = 36       # read x* 16 + read lambda_i 4 + write x 16, per particle
+B_STEP_FIXED = 189  # predict 48 + grid 77 + finalize 64
+B_ITER = 56        # lambda + delta
+
+
+def dist_env():
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def read_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic():
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.file:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[1]), smax=float(parts[2]), power=float(parts[3]),
+                                 hw=parts[5], hwt=parts[6], swt=parts[7], pcap=parts[8]))
+            except ValueError:
+                continue
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        reasons = set()
+        for r in rows:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("pcap", "sw_power_cap")):
+                if r[key].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
+                "power_w_max": max(r["power"] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def cpu_baseline_sample(scene, threads: int):
+    """One oracle update of the full workload on the host cores."""
+    from oracle import Oracle
+    from particlesolver_gb300 import default_params
+    from particlesolver_gb300 import workloads as W
+
+    o = Oracle(default_params(**scene.params), scene.n, threads=threads)
+    W.apply_to(scene, o)
+    t0 = time.perf_counter()
+    o.update(scene.dt)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from particlesolver_gb300 import workloads as W
+
+    sc = W.dam_break(args.nx, args.ny, args.nz)
+    threads = os.cpu_count() or 1
+    from oracle import Oracle
+    from particlesolver_gb300 import PbdParams
+
+    p = PbdParams().update(**{**_param_defaults(), **sc.params})
+    o = Oracle(p, sc.n, threads=threads)
+    W.apply_to(sc, o)
+    budget = args.ref_budget_s
+    t_start = time.perf_counter()
+    for _ in range(min(args.warmup, 1)):
+        o.update(sc.dt)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.update(sc.dt)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget:
+            break
+    v = len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": len(times), "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded dam break)",
+            "config": {"workload": f"pbf_dam_break_{sc.n}", "particles": sc.n, "iterations": 4,
+                       "lattice": [args.nx, args.ny, args.nz], "h": 0.1, "dt": sc.dt},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{len(times)} full oracle updates of the {sc.n}-particle dam break "
+                                       f"(the reference GPU path does not build on CUDA 13; its CPU path is "
+                                       f"2-D O(N^2)); steps capped by a {budget:.0f} s budget"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _param_defaults():
+    return dict(particle_radius=0.25, kernel_radius=2.0, cell_size=0.5, grid_size=[64, 64, 64],
+                world_origin=[0, 0, 0], gravity=[0, -9.8, 0], box_min=[-50, 0, -50], box_max=[50, 200, 50],
+                iterations=5, max_dt=0.05, relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0,
+                contact_static_friction=0.005, contact_kinetic_friction=0.0002, wall_static_friction=0.005,
+                wall_kinetic_friction=0.0002, max_neighbors=500, twod_z=0.0, flags=0)
+
+
+def run_ours(args, world, rank, local_rank):
+    import numpy as np
+    import torch
+
+    from particlesolver_gb300 import ParticleSystem, default_params
+    from particlesolver_gb300 import workloads as W
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    sc = W.dam_break(args.nx, args.ny, args.nz)
+    n = sc.n
+    sysm = ParticleSystem(default_params(**sc.params), n)
+    W.apply_to(sc, sysm)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # warm-up (captures the step graph on the first call)
+    warm = max(3, args.warmup)
+    for _ in range(warm):
+        sysm.update_graph(sc.dt, 1, sh)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, L2 flushed before each, device events
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sysm.reset_profile()
+    barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(local_rank) as clocks:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                sysm.update_graph(sc.dt, 1, sh)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t_wall0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1e3
+    launches = sysm.profile()["kernel_launches"]
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * args.steps / total_s
+
+    # ---- per-stage device times (eager, events between stage groups)
+    sysm.set_profiling(True)
+    sysm.reset_profile()
+    prof_steps = 3
+    for _ in range(prof_steps):
+        flush.zero_()
+        sysm.update(sc.dt, sh)
+    prof = sysm.profile()
+    sysm.set_profiling(False)
+
+    # ---- end to end through the public API with host buffers
+    pos_h = torch.from_numpy(sc.pos_w.copy()).pin_memory()
+    vel_h = torch.zeros((n, 4), dtype=torch.float32).pin_memory()
+    out_h = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    lib = sysm.lib
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sysm._check(lib.pbd_set_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
+        sysm._check(lib.pbd_set_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
+        sysm.update_graph(sc.dt, 1, sh)
+        sysm._check(lib.pbd_get_positions(sysm.h, 0, n, out_h.data_ptr(), 0, sh))
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * e2e_steps / e2e_s
+    sysm.check_finite(sh)
+
+    if rank != 0:
+        return
+
+    # roofline of the dominant single-kernel stage
+    per_launch = {}
+    for st, b in (("lambda", B_LAMBDA), ("solve", B_DELTA)):
+        nl = prof["stage_launches"][st]
+        if nl:
+            per_launch[st] = (prof["stage_ms"][st] / nl, b * n)
+    dom = max(per_launch, key=lambda k: per_launch[k][0] * prof["stage_launches"][k])
+    dom_ms, dom_bytes = per_launch[dom]
+    peak, peak_kind = read_peaks()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic_tab = read_traffic()
+    traffic = None
+    if traffic_tab and dom in traffic_tab.get("per_launch_bytes", {}):
+        traffic = traffic_tab["per_launch_bytes"][dom]
+    step_bytes = (B_STEP_FIXED + 4 * B_ITER) * n
+    ms_per_step = 1e3 * total_s / args.steps
+
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dt_cpu = cpu_baseline_sample(sc, threads)
+        cpu = {"value": 1.0 / dt_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"1 full oracle update (FP64 restatement of the reference step) of the {n}-particle "
+                         f"dam break on {threads} host threads"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, splitmix64)",
+        "config": {"workload": f"pbf_dam_break_{n}", "particles": n, "lattice": [args.nx, args.ny, args.nz],
+                   "h": 0.1, "iterations": 4, "grid_rebuild": "every iteration", "xsph_c": 0.01,
+                   "dt": sc.dt, "l2": "flushed before each timed step (256 MiB write)",
+                   "timing": "per-step CUDA events on the launching stream, CUDA graph replay",
+                   "particle_iterations_per_s": value * n * 4,
+                   "step_bytes_algorithmic": step_bytes,
+                   "step_achieved_gbs": step_bytes / (ms_per_step * 1e-3) / 1e9,
+                   "wall_s_timed_region": wall},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "stage_ms_per_step": {k: v / prof_steps for k, v in prof["stage_ms"].items()},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * n, "d2h_bytes_per_step": 16 * n,
+                "steps": e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nx", type=int, default=128)
+    ap.add_argument("--ny", type=int, default=128)
+    ap.add_argument("--nz", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-budget-s", type=float, default=120.0)
+    args = ap.parse_args()
+    world, rank, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", init_method="env://")
+    try:
+        run_ours(args, world, rank, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

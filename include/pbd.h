@@ -1,0 +1,295 @@
+/*
+ * pbd.h -- C ABI of the GB300 (sm_103a) unified position-based-dynamics step.
+ *
+ * One opaque handle (pbd_system) replaces the reference's ParticleSystem
+ * object together with the global thrust vectors its .cu files own
+ * (gpu/src/cuda/integration.cu:23-34, shared_variables.cu:8-10,
+ * solver.cu:32-41).  Any number of handles may coexist; each handle is used
+ * by one host thread at a time.  Every call returns a pbd_status (0 = OK) and
+ * never exits the process (the reference's checkCudaErrors exits); the text
+ * of the last error is available from pbd_last_error().
+ *
+ * Array arguments are plain host pointers unless a parameter says otherwise.
+ * Positions travel as float4 (x, y, z, inverse mass w), the layout of the
+ * reference's position VBO plus its W array (particlesystem.cpp:315-319,
+ * shared_variables.cu:71-89).  Stream arguments are cudaStream_t passed as
+ * void* (NULL = legacy default stream).
+ *
+ * Reference interfaces replaced (file:line in ebirenbaum/ParticleSolver):
+ *   ParticleSystem class ............ gpu/src/particlesystem.h:22-53
+ *   extern "C" device wrappers ...... gpu/src/cuda/wrappers.cuh:10-99
+ *   SimParams ........................ gpu/src/cuda/kernel.cuh:9-22
+ *   phase constants .................. gpu/src/cuda/shared_variables.cuh:4-9
+ */
+#ifndef PBD_H
+#define PBD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBD_ABI_VERSION 1
+
+typedef enum pbd_status {
+    PBD_OK = 0,
+    PBD_ERR_INVALID_ARGUMENT = 1, /* bad handle, index, size or parameter   */
+    PBD_ERR_CAPACITY = 2,         /* would exceed max_particles (the
+                                     reference silently ignored the add,
+                                     particlesystem.cpp:311-312,335-336)     */
+    PBD_ERR_CUDA = 3,             /* a CUDA runtime call failed              */
+    PBD_ERR_STATE = 4,            /* call not valid in the current state    */
+    PBD_ERR_NONFINITE = 5         /* NaN/Inf found by pbd_check_finite       */
+} pbd_status;
+
+/* Particle phases (gpu/src/cuda/shared_variables.cuh:4-9).  Rigid objects,
+ * ropes and cloths use PBD_PHASE_RIGID + object id; particles of one such
+ * object never collide with each other (integration_kernel.cuh:336). */
+#define PBD_PHASE_FLUID 0
+#define PBD_PHASE_GAS 1
+#define PBD_PHASE_CLOTH 2
+#define PBD_PHASE_SOLID 3
+#define PBD_PHASE_RIGID 4
+
+/* Behaviour flags.  With flags == 0 the step reproduces the reference GPU
+ * formulas; each flag selects the documented alternative. */
+#define PBD_FLAG_TWOD (1u << 0)
+/* 2-D mode: the TWOD build of integration_kernel.cuh:111-129 (z walls off,
+ * z pinned to twod_z). */
+#define PBD_FLAG_DENSITY_NEIGHBOR_MASS (1u << 1)
+/* PBF density sums m_j W (cpu totalfluidconstraint.cpp:66) instead of the
+ * GPU's own-mass W / w_i (integration_kernel.cuh:577,589). */
+#define PBD_FLAG_DELTA_OVER_RHO0 (1u << 2)
+/* PBF position delta divided by rho0 (Macklin & Mueller 2013, eq. 12)
+ * instead of (rho0 + neighbour count) (integration_kernel.cuh:640). */
+#define PBD_FLAG_DISTANCE_MASS_WEIGHTED (1u << 3)
+/* Distance correction weighted w_i/(w_i+w_j) (cpu distanceconstraint.cpp:
+ * 33-37) instead of 1/2 each (solver_kernel.cuh:53-64). */
+#define PBD_FLAG_KERNEL_UNITS (1u << 4)
+/* relaxation and s_corr are dimensionless, in kernel-radius units: lambda =
+ * -C / (sum |grad C|^2 + relaxation / h^2) and the artificial pressure
+ * enters lambda_i + lambda_j + h^2 s_corr.  lambda carries units of
+ * length^2 while the published s_corr is a pure number, so without this
+ * flag the balance of the two terms depends on the scene's length unit
+ * (the reference tuned its literal constants for h = 2,
+ * integration_kernel.cuh:25-35,592,634). */
+#define PBD_FLAGS_ALL 0x1fu
+
+/* Simulation parameters (replaces SimParams, kernel.cuh:9-22, plus the
+ * compile-time constants of integration_kernel.cuh:20-42 and
+ * particlesystem.cpp:52-66, which become runtime values). */
+typedef struct pbd_params {
+    float particle_radius;   /* r: contact distance 2.001 r, wall offset r  */
+    float kernel_radius;     /* h: PBF smoothing radius (reference H = 2)    */
+    float cell_size;         /* grid cell edge (reference 2 r)              */
+    uint32_t grid_size[3];   /* cells per axis, each a power of two; cell
+                                coordinates wrap (integration_kernel.cuh:
+                                197-203)                                    */
+    float world_origin[3];   /* grid origin                                 */
+    float gravity[3];        /* reference (0, -9.8, 0)                      */
+    float box_min[3];        /* world box (reference int3 minBounds)        */
+    float box_max[3];        /* world box (reference int3 maxBounds)        */
+    uint32_t iterations;     /* solver iterations per update                */
+    float max_dt;            /* update() clamps dt (reference 0.05)         */
+    float relaxation;        /* lambda denominator epsilon (0.01)           */
+    float scorr_k;           /* artificial pressure k (0.1)                 */
+    float scorr_n;           /* artificial pressure exponent n (4)          */
+    float scorr_dq;          /* artificial pressure dq as a fraction of h   */
+    float xsph_c;            /* XSPH viscosity c (0 = off; reference has none) */
+    float contact_static_friction;  /* S_FRICTION in collideD (0.005)       */
+    float contact_kinetic_friction; /* K_FRICTION in collideD (0.0002)      */
+    float wall_static_friction;     /* S_FRICTION under sqrt at walls       */
+    float wall_kinetic_friction;    /* K_FRICTION under sqrt at walls       */
+    uint32_t max_neighbors;  /* per-particle neighbour cap (500)            */
+    float twod_z;            /* z of every particle in PBD_FLAG_TWOD mode   */
+    uint32_t flags;          /* PBD_FLAG_*                                  */
+} pbd_params;
+
+typedef struct pbd_system pbd_system;
+
+/* Raw device pointers of one system, for callers that render or post-process
+ * in place (the reference mapped its GL VBO, particlesystem.cpp:160). */
+typedef struct pbd_device_buffers {
+    void *positions;   /* float4[capacity], original particle order */
+    void *velocities;  /* float4[capacity]                          */
+    void *phases;      /* int32[capacity]                           */
+    uint32_t num_particles;
+    uint32_t capacity;
+} pbd_device_buffers;
+
+/* ---------------------------------------------------------------- setup */
+
+int pbd_abi_version(void);
+/* Fills the reference defaults: r 0.25, h 2, cell 2r, grid 64^3, box
+ * (-50,0,-50)..(50,200,50), 5 iterations (particleapp.cpp:23-38,
+ * particlesystem.cpp:52-66, integration_kernel.cuh:20-42). */
+void pbd_default_params(pbd_params *out);
+/* Replaces ParticleSystem::ParticleSystem (particlesystem.cpp:36-69). */
+int pbd_create(const pbd_params *params, uint32_t max_particles, pbd_system **out);
+/* Replaces ParticleSystem::~ParticleSystem / _finalize (particlesystem.cpp:72-134). */
+int pbd_destroy(pbd_system *sys);
+/* Last error text of sys; sys == NULL gives the calling thread's last
+ * pbd_create failure. */
+const char *pbd_last_error(const pbd_system *sys);
+/* Replaces setParameters (integration.cu:96-100). */
+int pbd_set_params(pbd_system *sys, const pbd_params *params);
+int pbd_get_params(const pbd_system *sys, pbd_params *out);
+/* Replaces getNumParticles (particlesystem.h:48). */
+uint32_t pbd_num_particles(const pbd_system *sys);
+uint32_t pbd_capacity(const pbd_system *sys);
+
+/* --------------------------------------------------------- scene content */
+
+/* Appends n particles (replaces addParticleMultiple, particlesystem.cpp:
+ * 333-348, with appendIntegrationParticle integration.cu:50-72 and
+ * appendPhaseAndMass shared_variables.cu:71-89).  pos_w: 4n floats (xyz,
+ * inverse mass); vel: 4n floats or NULL (zero); phase: n ints;
+ * rest_density: n floats or NULL (1.0).  *first_index receives the index of
+ * the first new particle.  Returns PBD_ERR_CAPACITY past max_particles. */
+int pbd_add_particles(pbd_system *sys, uint32_t n, const float *pos_w, const float *vel,
+                      const int32_t *phase, const float *rest_density, uint32_t *first_index);
+/* Distance constraints (replaces addDistanceConstraint, solver.cu:125-156).
+ * pairs: 2m particle indices; rest: m lengths; stiffness: m values in
+ * [0,1] or NULL (1.0; the reference has no stiffness). */
+int pbd_add_distance_constraints(pbd_system *sys, uint32_t m, const uint32_t *pairs,
+                                 const float *rest, const float *stiffness);
+/* Pins (replaces addPointConstraint, solver.cu:108-123).  points: 3p floats. */
+int pbd_add_point_constraints(pbd_system *sys, uint32_t p, const uint32_t *index,
+                              const float *points);
+/* Shape-matched rigid body over particles [first, first+count) (no GPU
+ * counterpart in the reference, whose rigid_body_functor is empty,
+ * solver_kernel.cuh:289-312; rest offsets as in the CPU createRigidBody,
+ * cpu/src/simulation.cpp:371-406).  Every particle needs w > 0. */
+int pbd_add_rigid_body(pbd_system *sys, uint32_t first, uint32_t count, float stiffness,
+                       uint32_t *body_index);
+/* The six uniforms the reference drew from cuRAND for the wall jitter every
+ * iteration (integration.cu:326); here an explicit input, default zeros. */
+int pbd_set_wall_jitter(pbd_system *sys, const float rands[6]);
+/* Overwrite state of particles [first, first+count) (replaces setArray,
+ * particlesystem.cpp:701-713).  src_on_device != 0: src is a device pointer. */
+int pbd_set_positions(pbd_system *sys, uint32_t first, uint32_t count, const float *src,
+                      int src_on_device, void *stream);
+int pbd_set_velocities(pbd_system *sys, uint32_t first, uint32_t count, const float *src,
+                       int src_on_device, void *stream);
+int pbd_get_positions(pbd_system *sys, uint32_t first, uint32_t count, float *dst,
+                      int dst_on_device, void *stream);
+int pbd_get_velocities(pbd_system *sys, uint32_t first, uint32_t count, float *dst,
+                       int dst_on_device, void *stream);
+int pbd_get_phases(pbd_system *sys, int32_t *dst);
+int pbd_get_device_buffers(pbd_system *sys, pbd_device_buffers *out);
+
+/* Scene builders of the reference class, with its lattice spacings and
+ * phases; jitter comes from a seeded splitmix64 stream instead of rand(). */
+/* addFluid (particlesystem.cpp:357-405): spacing 2.5 r, phase FLUID. */
+int pbd_add_fluid(pbd_system *sys, const int32_t ll[3], const int32_t ur[3], float mass,
+                  float density, uint64_t seed);
+/* addParticleGrid (particlesystem.cpp:408-458): spacing 2.002 r, SOLID. */
+int pbd_add_particle_grid(pbd_system *sys, const int32_t ll[3], const int32_t ur[3],
+                          float mass, int jitter, uint64_t seed);
+/* addHorizCloth (particlesystem.cpp:461-568). */
+int pbd_add_horiz_cloth(pbd_system *sys, const int32_t ll[2], const int32_t ur[2],
+                        const float spacing[3], const float dist[2], float mass,
+                        int hold_edges);
+/* addRope (particlesystem.cpp:570-616). */
+int pbd_add_rope(pbd_system *sys, const float start[3], const float spacing[3], float dist,
+                 int32_t links, float mass, int pin_start);
+/* addStaticSphere (particlesystem.cpp:618-687). */
+int pbd_add_static_sphere(pbd_system *sys, const int32_t ll[3], const int32_t ur[3],
+                          float spacing);
+
+/* ------------------------------------------------------------------ step */
+
+/* One simulation step (replaces ParticleSystem::update, particlesystem.cpp:
+ * 144-246): predict, then per iteration the grid build, contacts, PBF,
+ * walls, distance constraints, pins and shape matching, then the velocity
+ * update and XSPH.  Asynchronous on stream. */
+int pbd_update(pbd_system *sys, float dt, void *stream);
+/* nsteps updates captured once into a CUDA graph and replayed (same
+ * results as nsteps pbd_update calls). */
+int pbd_update_graph(pbd_system *sys, float dt, uint32_t nsteps, void *stream);
+
+/* Stage entry points, one per reference wrapper (wrappers.cuh:10-99). */
+/* integrateSystem (integration.cu:122-135): x_old = x; x += (v + g dt) dt. */
+int pbd_integrate(pbd_system *sys, float dt, void *stream);
+/* calcHash + sortParticles + reorderDataAndFindCellStart
+ * (integration.cu:161-275). */
+int pbd_build_grid(pbd_system *sys, void *stream);
+/* collide (integration.cu:338-386): contacts with friction, non-fluids. */
+int pbd_collide(pbd_system *sys, void *stream);
+/* solveFluids (integration.cu:453-508): PBF lambda then delta. */
+int pbd_solve_fluids(pbd_system *sys, void *stream);
+/* collideWorld (integration.cu:319-336): box walls with friction. */
+int pbd_collide_world(pbd_system *sys, void *stream);
+/* solveDistanceConstraints (solver.cu:196-231). */
+int pbd_solve_distance_constraints(pbd_system *sys, void *stream);
+/* solvePointConstraints (solver.cu:180-194). */
+int pbd_solve_point_constraints(pbd_system *sys, void *stream);
+/* Shape matching of every rigid body (no GPU counterpart in the reference). */
+int pbd_solve_shapes(pbd_system *sys, void *stream);
+/* calcVelocity (integration.cu:416-426): v = (x - x_old) / dt. */
+int pbd_calc_velocity(pbd_system *sys, float dt, void *stream);
+/* XSPH viscosity on fluid velocities (not in the reference). */
+int pbd_apply_xsph(pbd_system *sys, void *stream);
+
+/* ------------------------------------------------------------ inspection */
+
+/* Grid of the last build in the reference layout (after sortParticles and
+ * reorderDataAndFindCellStartD, integration_kernel.cuh:229-299): sorted
+ * hashes and particle indices (num_particles each), cell start / end
+ * (num cells each; start 0xffffffff and end 0 for empty cells).  Host
+ * buffers; any may be NULL. */
+int pbd_get_grid(pbd_system *sys, uint32_t *sorted_hash, uint32_t *sorted_index,
+                 uint32_t *cell_start, uint32_t *cell_end);
+/* PBF lambda of every particle from the last solve, in particle order. */
+int pbd_get_lambdas(pbd_system *sys, float *dst);
+uint32_t pbd_num_cells(const pbd_system *sys);
+/* Returns PBD_ERR_NONFINITE if a position or velocity is NaN/Inf. */
+int pbd_check_finite(pbd_system *sys, void *stream);
+/* Blocks until the system's work on stream is done. */
+int pbd_synchronize(pbd_system *sys, void *stream);
+
+/* --------------------------------------------------------------- timing */
+
+/* Kernel groups of one step, for the per-stage device timing (no
+ * counterpart in the reference, whose only readout was an FPS counter,
+ * cpu/src/view.cpp:66,189). */
+enum {
+    PBD_STAGE_PREDICT = 0,  /* prediction + first cell hash                 */
+    PBD_STAGE_GRID = 1,     /* hash, cell offsets, sort into cells, reorder */
+    PBD_STAGE_LAMBDA = 2,   /* PBF density / lambda (one kernel)            */
+    PBD_STAGE_SOLVE = 3,    /* contacts + PBF delta + walls (one kernel)    */
+    PBD_STAGE_DISTANCE = 4, /* distance constraints and pins                */
+    PBD_STAGE_SHAPES = 5,   /* shape matching                               */
+    PBD_STAGE_VELOCITY = 6, /* velocity update                              */
+    PBD_STAGE_XSPH = 7,     /* XSPH viscosity                               */
+    PBD_STAGE_COUNT = 8
+};
+
+typedef struct pbd_profile {
+    double stage_ms[PBD_STAGE_COUNT];        /* device time per stage group  */
+    uint64_t stage_launches[PBD_STAGE_COUNT]; /* kernels timed per stage     */
+    uint64_t kernel_launches;  /* every kernel this system enqueued (graph
+                                  replays count each captured kernel)        */
+    uint64_t steps;            /* updates enqueued                           */
+} pbd_profile;
+
+/* enable != 0: pbd_update brackets each stage group with CUDA events on its
+ * stream (eager updates only; captured graphs are not timed). */
+int pbd_set_profiling(pbd_system *sys, int enable);
+/* Synchronises, then returns the accumulated timings and counters. */
+int pbd_get_profile(pbd_system *sys, pbd_profile *out);
+int pbd_reset_profile(pbd_system *sys);
+
+/* Checkpoint of the whole dynamic state (positions, velocities, rigid body
+ * rotations) as one binary blob. */
+uint64_t pbd_state_size(const pbd_system *sys);
+int pbd_save_state(pbd_system *sys, void *dst, uint64_t size);
+int pbd_load_state(pbd_system *sys, const void *src, uint64_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBD_H */

@@ -1,0 +1,144 @@
+// Device-side parameter block and shared inline math of the PBD step.
+//
+// The reference kept SimParams in __constant__ memory, refreshed with
+// cudaMemcpyToSymbol every step (integration_kernel.cuh:55,
+// integration.cu:96-100), which ties the whole program to one system.  Here
+// the block travels by value as a kernel argument: several systems can run
+// side by side and a captured CUDA graph carries its own copy.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pbd {
+
+enum : int { kFluid = 0, kGas = 1, kCloth = 2, kSolid = 3, kRigid = 4 };
+
+enum : uint32_t {
+    kFlagTwoD = 1u << 0,
+    kFlagDensityNeighborMass = 1u << 1,
+    kFlagDeltaOverRho0 = 1u << 2,
+    kFlagDistanceMassWeighted = 1u << 3,
+    kFlagKernelUnits = 1u << 4,
+};
+
+// Stage mask of the fused per-particle solve kernel.
+enum : uint32_t { kDoContact = 1u, kDoFluid = 2u, kDoWorld = 4u };
+
+// Numeric constants the reference hard-codes (integration_kernel.cuh:20,
+// 319, 580, 626; solver_kernel.cuh:57).
+constexpr float kEps = 0.001f;           // EPS
+constexpr float kCollideScale = 2.001f;  // collideDist = r * 2.001
+constexpr float kMinSpikyLen = 0.0001f;  // spiky gradient cut-off
+constexpr float kMinDistLen = 0.0001f;   // distance constraint cut-off
+
+struct DevParams {
+    float3 gravity;
+    float r;             // particle radius
+    float h, h2;         // PBF kernel radius and its square
+    float cell;          // grid cell edge
+    float3 origin;       // grid origin
+    uint32_t gx, gy, gz; // cells per axis (powers of two)
+    uint32_t num_cells;
+    float3 bmin, bmax;   // world box
+    float poly6;         // 315 / (64 pi h^9)
+    float spiky;         // 45 / (pi h^6)
+    float poly6_self;    // poly6 * h^6
+    float scorr_k, scorr_n;
+    float scorr_inv_ref; // 1 / (poly6 * (h^2 - (dq h)^2)^3)
+    int scorr_n_int;     // n when integral (repeated product), else 0
+    float relax;
+    float xsph_c;
+    float cs, ck;        // contact static / kinetic friction
+    float ws, wk;        // sqrt of wall static / kinetic friction
+    float collide_dist, collide2;
+    int fluid_rad;       // ceil(h / cell)
+    uint32_t max_nb;
+    float twod_z;
+    uint32_t flags;
+    float rands[6];      // wall jitter uniforms
+};
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float3 operator-(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ void operator+=(float3 &a, float3 b) { a.x += b.x; a.y += b.y; a.z += b.z; }
+__device__ __forceinline__ void operator-=(float3 &a, float3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+
+// Squared distance with a fixed rounding sequence (no contraction choice left
+// to the compiler), so that the oracle can reproduce every neighbour test
+// bit for bit: d2 = fma(dz, dz, fma(dy, dy, dx * dx)).
+__device__ __forceinline__ float dist2_exact(float3 a, float3 b) {
+    float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// calcGridPos (integration_kernel.cuh:187-194) with IEEE division and
+// floor; the float-to-int conversion saturates (NaN -> 0).
+__device__ __forceinline__ int3 grid_pos(const DevParams &P, float3 p) {
+    int3 g;
+    g.x = __float2int_rd(__fdiv_rn(__fsub_rn(p.x, P.origin.x), P.cell));
+    g.y = __float2int_rd(__fdiv_rn(__fsub_rn(p.y, P.origin.y), P.cell));
+    g.z = __float2int_rd(__fdiv_rn(__fsub_rn(p.z, P.origin.z), P.cell));
+    return g;
+}
+
+// calcGridHash (integration_kernel.cuh:197-203): wrap each coordinate into
+// the power-of-two grid, then linearise x fastest.
+__device__ __forceinline__ uint32_t grid_hash(const DevParams &P, int3 g) {
+    uint32_t x = (uint32_t)g.x & (P.gx - 1u);
+    uint32_t y = (uint32_t)g.y & (P.gy - 1u);
+    uint32_t z = (uint32_t)g.z & (P.gz - 1u);
+    return (z * P.gy + y) * P.gx + x;
+}
+
+// Visits the candidate particles of the (2 rad + 1)^3 cell stencil around
+// cell g, in the reference's order (z outer, y, x inner, then ascending
+// sorted index; integration_kernel.cuh:388-398, 549-559).  cell_first holds
+// num_cells + 1 dense offsets into the sorted arrays, so a stencil row whose
+// cells do not wrap is one contiguous index range; a wrapping row falls back
+// to per-cell ranges, which also reproduces the double visit of aliased
+// cells when the stencil is wider than the grid.  f(j) returns false to
+// stop the walk.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const DevParams &P, int3 g, int rad,
+                                                   const uint32_t *__restrict__ cell_first, F &&f) {
+    for (int dz = -rad; dz <= rad; ++dz) {
+        const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
+        for (int dy = -rad; dy <= rad; ++dy) {
+            const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
+            const uint32_t row = (z * P.gy + y) * P.gx;
+            const int x0 = g.x - rad, x1 = g.x + rad;
+            if (x0 >= 0 && x1 < (int)P.gx) {
+                const uint32_t b = __ldg(cell_first + row + (uint32_t)x0);
+                const uint32_t e = __ldg(cell_first + row + (uint32_t)x1 + 1u);
+                for (uint32_t j = b; j < e; ++j)
+                    if (!f(j)) return;
+            } else {
+                for (int dx = -rad; dx <= rad; ++dx) {
+                    const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
+                    const uint32_t b = __ldg(cell_first + c), e = __ldg(cell_first + c + 1u);
+                    for (uint32_t j = b; j < e; ++j)
+                        if (!f(j)) return;
+                }
+            }
+        }
+    }
+}
+
+#endif  // __CUDACC__
+
+// Per-particle attributes gathered into sorted order with the positions.
+struct __align__(8) SortedAttr {
+    int phase;
+    float rho0;
+};
+
+}  // namespace pbd

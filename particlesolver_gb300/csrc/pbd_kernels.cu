@@ -1,0 +1,856 @@
+// sm_103a kernels of the unified PBD step: prediction, the neighbour grid
+// (cell hash, stable counting sort into cells, reorder into sorted SoA,
+// dense cell offsets), the PBF density/lambda solve, contacts with friction,
+// world walls, distance constraints and pins as a per-particle gather,
+// shape matching with a 3x3 rotation extraction, the velocity update and
+// XSPH.  Reference kernels are cited beside each replacement.
+#include "pbd_kernels.h"
+
+#include <cfloat>
+
+namespace pbd {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned blocks_for(uint32_t n, int per_block = kBlock) {
+    return (unsigned)((n + (uint32_t)per_block - 1u) / (uint32_t)per_block);
+}
+
+// ---------------------------------------------------------------- predict
+
+// integrate_functor + copyToXstar (integration_kernel.cuh:159-184,
+// shared_variables.cu:91-96): x_old = x; v' = v + g dt; x += v' dt.  The
+// reference does not store v'; neither do we (the velocity is recomputed
+// from positions at the end of the step).  When counts is given, the cell
+// hash of the predicted position is computed and counted here too, which is
+// the first grid build's calcHashD (integration_kernel.cuh:206-225).
+__global__ void __launch_bounds__(kBlock) k_predict(DevParams P, uint32_t n, float dt,
+                                                    float4 *__restrict__ x,
+                                                    const float4 *__restrict__ v,
+                                                    float4 *__restrict__ x_old,
+                                                    uint32_t *__restrict__ hash,
+                                                    uint32_t *__restrict__ slot,
+                                                    uint32_t *__restrict__ counts) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = x[i];
+    const float4 vel = v[i];
+    x_old[i] = p;
+    float3 vv = make_float3(vel.x, vel.y, vel.z) + P.gravity * dt;
+    p.x += vv.x * dt;
+    p.y += vv.y * dt;
+    p.z += vv.z * dt;
+    x[i] = p;
+    if (counts) {
+        const uint32_t h = grid_hash(P, grid_pos(P, f3(p)));
+        hash[i] = h;
+        slot[i] = atomicAdd(counts + h, 1u);
+    }
+}
+
+// calcHashD (integration_kernel.cuh:206-225) plus the per-cell count of the
+// counting sort.  The arrival slot is only used to bucket indices; the final
+// order inside a cell is fixed by original index in k_rank_reorder.
+__global__ void __launch_bounds__(kBlock) k_hash_count(DevParams P, uint32_t n,
+                                                       const float4 *__restrict__ x,
+                                                       uint32_t *__restrict__ hash,
+                                                       uint32_t *__restrict__ slot,
+                                                       uint32_t *__restrict__ counts) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t h = grid_hash(P, grid_pos(P, f3(x[i])));
+    hash[i] = h;
+    slot[i] = atomicAdd(counts + h, 1u);
+}
+
+// ------------------------------------------------------------------- scan
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    return x;
+}
+
+// Exclusive scan of one value per thread over a 1024-thread block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *smem,
+                                                         uint32_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_inclusive_scan(v);
+    if (lane == 31) smem[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t s = warp_inclusive_scan(smem[lane]);
+        smem[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t prefix = warp ? smem[warp - 1] : 0u;
+    total = smem[31];
+    __syncthreads();
+    return prefix + inc - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__restrict__ data,
+                                                              uint32_t elements,
+                                                              uint32_t *__restrict__ partials) {
+    __shared__ uint32_t smem[32];
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < elements) s += data[base + k];
+    uint32_t total;
+    block_exclusive_scan(s, smem, total);
+    if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t *__restrict__ partials,
+                                                                uint32_t count) {
+    __shared__ uint32_t smem[32];
+    uint32_t carry = 0;
+    for (uint32_t chunk = 0; chunk < count; chunk += kScanTile) {
+        const uint32_t base = chunk + threadIdx.x * kScanItems;
+        uint32_t v[kScanItems], s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = (base + k < count) ? partials[base + k] : 0u;
+            s += v[k];
+        }
+        uint32_t total;
+        uint32_t run = carry + block_exclusive_scan(s, smem, total);
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (base + k < count) partials[base + k] = run;
+            run += v[k];
+        }
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint32_t *__restrict__ data,
+                                                             uint32_t elements,
+                                                             const uint32_t *__restrict__ partials) {
+    __shared__ uint32_t smem[32];
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < elements) ? data[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = partials[blockIdx.x] + block_exclusive_scan(s, smem, total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < elements) data[base + k] = run;
+        run += v[k];
+    }
+}
+
+// ------------------------------------------------------------- sort finish
+
+__global__ void __launch_bounds__(kBlock) k_bucket(uint32_t n, const uint32_t *__restrict__ hash,
+                                                   const uint32_t *__restrict__ slot,
+                                                   const uint32_t *__restrict__ cell_first,
+                                                   uint32_t *__restrict__ tmp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    tmp[cell_first[hash[i]] + slot[i]] = i;
+}
+
+// Stable placement and reorder: the rank of particle i inside its cell is
+// the number of bucket-mates with a smaller original index, so the sorted
+// order is (hash, original index) -- the order of the reference's stable
+// key-value sort seeded with index = i (integration_kernel.cuh:224,
+// integration.cu:270-275).  The same thread gathers the particle's data into
+// the sorted SoA arrays (reorderDataAndFindCellStartD,
+// integration_kernel.cuh:287-295); the cell start/end of the reference are
+// the dense offsets cell_first[c], cell_first[c + 1].
+__global__ void __launch_bounds__(kBlock) k_rank_reorder(uint32_t n, const uint32_t *__restrict__ hash,
+                                                         const uint32_t *__restrict__ cell_first,
+                                                         const uint32_t *__restrict__ tmp,
+                                                         const float4 *__restrict__ x,
+                                                         const int *__restrict__ phase,
+                                                         const float *__restrict__ rho0,
+                                                         uint32_t *__restrict__ sorted_idx,
+                                                         float4 *__restrict__ sorted_x,
+                                                         SortedAttr *__restrict__ sorted_attr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t h = hash[i];
+    const uint32_t b = cell_first[h], e = cell_first[h + 1];
+    uint32_t rank = 0;
+    for (uint32_t k = b; k < e; ++k) rank += (tmp[k] < i) ? 1u : 0u;
+    const uint32_t p = b + rank;
+    sorted_idx[p] = i;
+    sorted_x[p] = x[i];
+    SortedAttr a;
+    a.phase = phase[i];
+    a.rho0 = rho0[i];
+    sorted_attr[p] = a;
+}
+
+__global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uint32_t *__restrict__ sorted_idx,
+                                                           const float4 *__restrict__ x,
+                                                           float4 *__restrict__ sorted_x) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sorted_x[i] = x[sorted_idx[i]];
+}
+
+// ----------------------------------------------------------------- lambda
+
+// findLambdasD + collideCellRadius (integration_kernel.cuh:481-593): for a
+// fluid particle, neighbours are all particles with |r|^2 < h^2 in the
+// (2 ceil(h/cell) + 1)^3 stencil (no phase filter), capped at max_nb in
+// visiting order.  rho = sum poly6(r) / w_i + poly6(0) / w_i (own inverse
+// mass; PBD_FLAG_DENSITY_NEIGHBOR_MASS uses m_j), grad_j = spiky(r) / rho0,
+// lambda = -(rho / rho0 - 1) / (sum |grad_j|^2 + |sum grad_j|^2 + eps).
+// Non-fluid particles get lambda = 0 (the reference left their slots
+// unwritten and read whatever was there, integration_kernel.cuh:636).
+__global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
+                                                   const float4 *__restrict__ sx,
+                                                   const SortedAttr *__restrict__ sattr,
+                                                   const uint32_t *__restrict__ cell_first,
+                                                   float *__restrict__ lambda) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SortedAttr a = sattr[i];
+    if (a.phase != kFluid) {
+        lambda[i] = 0.f;
+        return;
+    }
+    const float4 pi4 = sx[i];
+    const float3 pi = f3(pi4);
+    const float w = pi4.w;
+    const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
+    uint32_t nb = 0;
+    float ro = 0.f, denom = 0.f;
+    float3 grad = make_float3(0.f, 0.f, 0.f);
+    const float inv_rho0 = 1.f / a.rho0;
+    for_each_candidate(P, grid_pos(P, pi), P.fluid_rad, cell_first, [&](uint32_t j) {
+        if (j == i) return true;
+        const float4 pj4 = sx[j];
+        const float d2 = dist2_exact(pi, f3(pj4));
+        if (d2 < P.h2) {
+            if (nb >= P.max_nb) return false;
+            ++nb;
+            const float3 r = pi - f3(pj4);
+            const float rlen = sqrtf(d2);
+            const float hm2 = P.h2 - d2;
+            const float hm = P.h - rlen;
+            const float wpoly = P.poly6 * hm2 * hm2 * hm2;
+            if (nb_mass) ro += (pj4.w > 0.f) ? wpoly / pj4.w : 0.f;
+            else ro += wpoly / w;
+            float3 sg = make_float3(0.f, 0.f, 0.f);
+            if (rlen >= kMinSpikyLen) sg = (r / rlen) * (-P.spiky * hm * hm);
+            sg = sg * inv_rho0;
+            grad -= sg;
+            denom += dot3(sg, sg);
+        }
+        return true;
+    });
+    ro += P.poly6_self / w;
+    denom += dot3(grad, grad);
+    lambda[i] = -(ro * inv_rho0 - 1.f) / (denom + P.relax);
+}
+
+// --------------------------------------------------------- fused particle
+
+__device__ __forceinline__ float scorr_pow(const DevParams &P, float ratio) {
+    if (P.scorr_n_int > 0) {
+        float r = ratio;
+        for (int k = 1; k < P.scorr_n_int; ++k) r *= ratio;
+        return r;
+    }
+    return powf(ratio, P.scorr_n);
+}
+
+// solveFluidsD (integration_kernel.cuh:596-642): same neighbour set as the
+// lambda pass; delta = sum (lambda_i + lambda_j + s_corr) spiky(r) with
+// s_corr = -k (W(r) / W(dq h))^n and the (0, EPS, 0) direction for r ~ 0;
+// divided by (rho0 + n) (or rho0 with PBD_FLAG_DELTA_OVER_RHO0).
+__device__ __forceinline__ float3 fluid_delta(const DevParams &P, uint32_t i, float3 pi,
+                                              float rho0, const float4 *__restrict__ sx,
+                                              const float *__restrict__ lambda,
+                                              const uint32_t *__restrict__ cell_first) {
+    const float lam_i = lambda[i];
+    uint32_t nb = 0;
+    float3 delta = make_float3(0.f, 0.f, 0.f);
+    for_each_candidate(P, grid_pos(P, pi), P.fluid_rad, cell_first, [&](uint32_t j) {
+        if (j == i) return true;
+        const float3 pj = f3(sx[j]);
+        const float d2 = dist2_exact(pi, pj);
+        if (d2 < P.h2) {
+            if (nb >= P.max_nb) return false;
+            ++nb;
+            const float3 r = pi - pj;
+            const float rlen = sqrtf(d2);
+            const float hm2 = P.h2 - d2;
+            const float hm = P.h - rlen;
+            const float s = -P.spiky * hm * hm;
+            const float3 sg = (rlen < kMinSpikyLen) ? make_float3(0.f, kEps * s, 0.f) : (r / rlen) * s;
+            const float ratio = P.poly6 * hm2 * hm2 * hm2 * P.scorr_inv_ref;
+            const float corr = -P.scorr_k * scorr_pow(P, ratio);
+            delta += (lam_i + lambda[j] + corr) * sg;
+        }
+        return true;
+    });
+    const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
+    return delta / div;
+}
+
+__device__ __forceinline__ bool contact_candidate(const DevParams &P, int ph, int phj, float3 pi,
+                                                  float3 pj) {
+    if (ph > kSolid && ph == phj) return false;
+    return dist2_exact(pi, pj) < P.collide2;
+}
+
+__device__ __forceinline__ float scaled_inv_mass(float w, float y) {
+    return (w != 0.f) ? (1.f / ((1.f / w) * expf(-y))) : w;
+}
+
+// collideD + collideCell (integration_kernel.cuh:303-462): contacts of a
+// non-fluid particle with every particle closer than 2.001 r in the 27-cell
+// stencil (same-object pairs skipped, capped at max_nb), each averaged over
+// the contact count; solid-solid pairs use the height-scaled inverse mass
+// w e^y (both evaluated at this particle's y, as in the reference) and get
+// static/kinetic friction against the start-of-step positions.  Pairs with
+// zero total inverse mass or zero separation are skipped (the reference
+// produced NaN there).
+__device__ __forceinline__ float3 contact_delta(const DevParams &P, uint32_t i, float4 pi4, int ph,
+                                                uint32_t orig, const float4 *__restrict__ sx,
+                                                const SortedAttr *__restrict__ sattr,
+                                                const uint32_t *__restrict__ sidx,
+                                                const uint32_t *__restrict__ cell_first,
+                                                const float4 *__restrict__ x_old) {
+    const float3 pi = f3(pi4);
+    const int3 g = grid_pos(P, pi);
+    uint32_t nb = 0;
+    for_each_candidate(P, g, 1, cell_first, [&](uint32_t j) {
+        if (j == i) return true;
+        if (contact_candidate(P, ph, sattr[j].phase, pi, f3(sx[j]))) {
+            if (nb >= P.max_nb) return false;
+            ++nb;
+        }
+        return true;
+    });
+    float3 delta = make_float3(0.f, 0.f, 0.f);
+    if (nb == 0) return delta;
+    const float w = pi4.w;
+    const float sw = scaled_inv_mass(w, pi.y);
+    const float3 prev = f3(x_old[orig]);
+    const float fnb = (float)nb;
+    uint32_t seen = 0;
+    for_each_candidate(P, g, 1, cell_first, [&](uint32_t j) {
+        if (j == i) return true;
+        const float4 pj4 = sx[j];
+        const int phj = sattr[j].phase;
+        const float3 pj = f3(pj4);
+        if (!contact_candidate(P, ph, phj, pi, pj)) return true;
+        if (seen >= nb) return false;
+        ++seen;
+        const float3 diff = pi - pj;
+        const float dist = len3(diff);
+        const float mag = dist - P.collide_dist;
+        float colw = w, colw2 = pj4.w;
+        if (ph >= kSolid && phj >= kSolid) {
+            colw = sw;
+            colw2 = scaled_inv_mass(pj4.w, pi.y);
+        }
+        const float wsum = colw + colw2;
+        if (wsum == 0.f || dist == 0.f) return true;
+        const float scale = mag / wsum;
+        const float3 dp = diff * (scale / dist);
+        const float3 dp1 = (-colw * dp) / fnb;
+        const float3 dp2 = (colw2 * dp) / fnb;
+        delta += dp1;
+        if (ph < kSolid || phj < kSolid) return true;
+        const float3 prev2 = f3(x_old[sidx[j]]);
+        const float3 nf = diff * rsqrtf(dot3(diff, diff));
+        const float3 dprel = (pi + dp1 - prev) - (prev + dp2 - prev2);
+        const float3 dpt = dprel - nf * dot3(dprel, nf);
+        const float ldpt = len3(dpt);
+        if (ldpt < kEps) return true;
+        if (ldpt < P.cs * dist) delta -= dpt * colw / wsum;
+        else delta -= dpt * fminf(P.ck * dist / ldpt, 1.f);
+        return true;
+    });
+    return delta;
+}
+
+// collide_world_functor (integration_kernel.cuh:57-157): clamp into the box
+// shrunk by r with the jitter uniforms, then boundary friction against the
+// start-of-step position for phases >= CLOTH.
+__device__ __forceinline__ float3 world_collide(const DevParams &P, float3 e, int phase,
+                                                const float4 *__restrict__ x_old, uint32_t orig) {
+    const float d = P.r;
+    float eps = (phase < kSolid) ? d * 0.01f : d * 0.f;
+    float3 nrm = make_float3(0.f, 0.f, 0.f);
+    const bool twod = (P.flags & kFlagTwoD) != 0u;
+    if (e.y < P.bmin.y + P.r) {
+        e.y = P.bmin.y + P.r + P.rands[5] * eps;
+        nrm.y += 1.f;
+    }
+    eps = d * 0.01f;
+    if (e.x > P.bmax.x - P.r) {
+        e.x = P.bmax.x - (P.r + P.rands[0] * eps);
+        nrm.x += -1.f;
+    }
+    if (e.x < P.bmin.x + P.r) {
+        e.x = P.bmin.x + (P.r + P.rands[1] * eps);
+        nrm.x += 1.f;
+    }
+    if (e.y > P.bmax.y - P.r) {
+        e.y = P.bmax.y - (P.r + P.rands[2] * eps);
+        nrm.y += -1.f;
+    }
+    if (!twod) {
+        if (e.z > P.bmax.z - P.r) {
+            e.z = P.bmax.z - (P.r + P.rands[3] * eps);
+            nrm.z += -1.f;
+        }
+        if (e.z < P.bmin.z + P.r) {
+            e.z = P.bmin.z + (P.r + P.rands[4] * eps);
+            nrm.z += 1.f;
+        }
+    } else {
+        e.z = P.twod_z;
+    }
+    if (len3(nrm) < kEps || phase < kCloth) return e;
+    float3 pos = f3(x_old[orig]);
+    if (twod) pos.z = P.twod_z;
+    const float3 dp = e - pos;
+    const float3 dpt = dp - nrm * dot3(dp, nrm);
+    const float ldpt = len3(dpt);
+    if (ldpt < kEps) return e;
+    if (ldpt < P.ws * d) e -= dpt;
+    else e -= dpt * fminf(P.wk * d / ldpt, 1.f);
+    return e;
+}
+
+// One thread per sorted particle: the reference's collide, the delta half of
+// solveFluids and collideWorld, which touch disjoint particle sets and read
+// only the sorted start-of-iteration positions, fused into one pass with one
+// write per particle.  mask selects the stages (the stage entry points run
+// them one at a time).
+__global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint32_t mask,
+                                                  const float4 *__restrict__ sx,
+                                                  const SortedAttr *__restrict__ sattr,
+                                                  const uint32_t *__restrict__ sidx,
+                                                  const uint32_t *__restrict__ cell_first,
+                                                  const float *__restrict__ lambda,
+                                                  const float4 *__restrict__ x_old,
+                                                  float4 *__restrict__ x) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SortedAttr a = sattr[i];
+    const uint32_t orig = sidx[i];
+    const float4 pi4 = sx[i];
+    float3 np = f3(pi4);
+    bool touched = false;
+    if ((mask & kDoFluid) && a.phase == kFluid) {
+        np = np + fluid_delta(P, i, np, a.rho0, sx, lambda, cell_first);
+        touched = true;
+    } else if ((mask & kDoContact) && a.phase >= kCloth) {
+        np = np + contact_delta(P, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
+        touched = true;
+    }
+    if (mask & kDoWorld) {
+        if (!touched) np = f3(x[orig]);
+        np = world_collide(P, np, a.phase, x_old, orig);
+        touched = true;
+    }
+    if (touched) x[orig] = make_float4(np.x, np.y, np.z, pi4.w);
+}
+
+// -------------------------------------------------------------- distance
+
+// delta_computing_functor + sort_by_key + reduce_by_key +
+// distance_constraint_functor (solver_kernel.cuh:27-72,155-163,
+// solver.cu:196-231) as a gather: each constrained particle sums the
+// corrections of its incident constraints, d = (x_k - x_o) / |x_k - x_o| *
+// (rest - |x_k - x_o|) / 2 (times stiffness), in the order the reference's
+// stable sort produced (constraints where k is the first endpoint, then the
+// second), and divides by its constraint count.  The reference applied the
+// k-th reduced segment to particle k (solver.cu:227-230); here each sum goes
+// to its own particle.
+__global__ void __launch_bounds__(kBlock) k_distance_gather(DevParams P, uint32_t count,
+                                                            const uint32_t *__restrict__ particle,
+                                                            const uint32_t *__restrict__ row,
+                                                            const uint32_t *__restrict__ other,
+                                                            const float *__restrict__ rest,
+                                                            const float *__restrict__ stiff,
+                                                            const float *__restrict__ occ,
+                                                            const float4 *__restrict__ x,
+                                                            float4 *__restrict__ out) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= count) return;
+    const uint32_t k = particle[s];
+    const float4 xk4 = x[k];
+    const float3 xk = f3(xk4);
+    const bool mass_weighted = (P.flags & kFlagDistanceMassWeighted) != 0u;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const uint32_t e1 = row[s + 1];
+    for (uint32_t e = row[s]; e < e1; ++e) {
+        const float4 xo4 = x[other[e]];
+        const float3 rel = xk - f3(xo4);
+        const float dist = len3(rel);
+        if (dist > kMinDistLen) {
+            float mag;
+            if (mass_weighted) {
+                const float ws = xk4.w + xo4.w;
+                mag = (ws > 0.f) ? (rest[e] - dist) * (xk4.w / ws) : 0.f;
+            } else {
+                mag = (rest[e] - dist) * .5f;
+            }
+            acc += (rel / dist) * (mag * stiff[e]);
+        }
+    }
+    const float o = occ[s];
+    out[s] = make_float4(xk.x + acc.x / o, xk.y + acc.y / o, xk.z + acc.z / o, xk4.w);
+}
+
+// Writes the gathered positions back and applies pins last
+// (point_constraint_functor, solver_kernel.cuh:10-25).
+__global__ void __launch_bounds__(kBlock) k_distance_apply(uint32_t count,
+                                                           const uint32_t *__restrict__ particle,
+                                                           const float4 *__restrict__ tmp,
+                                                           const float4 *__restrict__ pin,
+                                                           int apply_distance, int apply_pins,
+                                                           float4 *__restrict__ x) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= count) return;
+    const uint32_t k = particle[s];
+    const bool pinned = apply_pins && pin[s].w != 0.f;
+    if (!apply_distance && !pinned) return;
+    float4 p = apply_distance ? tmp[s] : x[k];
+    if (pinned) {
+        const float4 q = pin[s];
+        p.x = q.x;
+        p.y = q.y;
+        p.z = q.z;
+    }
+    x[k] = p;
+}
+
+// ---------------------------------------------------------- shape matching
+
+struct Quat {
+    float x, y, z, w;
+};
+
+__device__ __forceinline__ void quat_to_mat(const Quat &q, float R[3][3]) {
+    const float xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z;
+    const float xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
+    const float wx = q.w * q.x, wy = q.w * q.y, wz = q.w * q.z;
+    R[0][0] = 1.f - 2.f * (yy + zz); R[0][1] = 2.f * (xy - wz);       R[0][2] = 2.f * (xz + wy);
+    R[1][0] = 2.f * (xy + wz);       R[1][1] = 1.f - 2.f * (xx + zz); R[1][2] = 2.f * (yz - wx);
+    R[2][0] = 2.f * (xz - wy);       R[2][1] = 2.f * (yz + wx);       R[2][2] = 1.f - 2.f * (xx + yy);
+}
+
+// Rotation part of A (row-major A[row][col]) by the iterative method of
+// Mueller, Bender, Chentanez and Macklin, "A Robust Method to Extract the
+// Rotational Part of Deformations" (MIG 2016): starting from q, rotate by
+// the axis-angle omega = sum_c (R e_c x A e_c) / (|sum_c R e_c . A e_c| +
+// 1e-9) until |omega| vanishes.  Warm-started with the previous rotation, it
+// stays well defined for flat or degenerate point sets.
+__device__ Quat extract_rotation(const float A[3][3], Quat q, int max_iter) {
+    for (int it = 0; it < max_iter; ++it) {
+        float R[3][3];
+        quat_to_mat(q, R);
+        float ox = 0.f, oy = 0.f, oz = 0.f, dsum = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float rx = R[0][c], ry = R[1][c], rz = R[2][c];
+            const float ax = A[0][c], ay = A[1][c], az = A[2][c];
+            ox += ry * az - rz * ay;
+            oy += rz * ax - rx * az;
+            oz += rx * ay - ry * ax;
+            dsum += rx * ax + ry * ay + rz * az;
+        }
+        const float inv = 1.f / (fabsf(dsum) + 1.0e-9f);
+        ox *= inv;
+        oy *= inv;
+        oz *= inv;
+        const float wlen = sqrtf(ox * ox + oy * oy + oz * oz);
+        if (wlen < 1.0e-9f) break;
+        const float half = 0.5f * wlen;
+        const float sh = sinf(half) / wlen, ch = cosf(half);
+        const Quat d = {ox * sh, oy * sh, oz * sh, ch};
+        Quat r;  // d * q
+        r.w = d.w * q.w - d.x * q.x - d.y * q.y - d.z * q.z;
+        r.x = d.w * q.x + d.x * q.w + d.y * q.z - d.z * q.y;
+        r.y = d.w * q.y - d.x * q.z + d.y * q.w + d.z * q.x;
+        r.z = d.w * q.z + d.x * q.y - d.y * q.x + d.z * q.w;
+        const float qn = rsqrtf(r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w);
+        q = {r.x * qn, r.y * qn, r.z * qn, r.w * qn};
+    }
+    return q;
+}
+
+constexpr int kShapeIters = 24;
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Shape matching (Mueller, Heidelberger, Teschner, Gross 2005): one warp per
+// body computes the mass-weighted centre c and A = sum m (x - c) q^T with
+// warp-shuffle reductions, extracts R, and moves every particle by
+// stiffness * (c + R q - x).  The reference's 2-D counterpart is
+// TotalShapeConstraint::project with Body::updateCOM
+// (cpu/src/constraint/totalshapeconstraint.cpp:14-24,
+// cpu/src/solver/particle.cpp:15-57).
+__global__ void __launch_bounds__(kBlock) k_shapes(uint32_t bodies, const uint4 *__restrict__ range,
+                                                   const float *__restrict__ stiff,
+                                                   const float4 *__restrict__ rest,
+                                                   float4 *__restrict__ quat,
+                                                   float4 *__restrict__ x) {
+    const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= bodies) return;
+    const uint4 rg = range[b];
+    const uint32_t first = rg.x, count = rg.y, roff = rg.z;
+    float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
+    for (uint32_t k = lane; k < count; k += 32) {
+        const float4 p = x[first + k];
+        const float m = rest[roff + k].w;
+        sx += m * p.x;
+        sy += m * p.y;
+        sz += m * p.z;
+        sm += m;
+    }
+    sx = warp_sum(sx);
+    sy = warp_sum(sy);
+    sz = warp_sum(sz);
+    sm = warp_sum(sm);
+    const float3 c = make_float3(sx / sm, sy / sm, sz / sm);
+    float A[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    for (uint32_t k = lane; k < count; k += 32) {
+        const float4 p = x[first + k];
+        const float4 q = rest[roff + k];
+        const float dx = q.w * (p.x - c.x), dy = q.w * (p.y - c.y), dz = q.w * (p.z - c.z);
+        A[0][0] += dx * q.x; A[0][1] += dx * q.y; A[0][2] += dx * q.z;
+        A[1][0] += dy * q.x; A[1][1] += dy * q.y; A[1][2] += dy * q.z;
+        A[2][0] += dz * q.x; A[2][1] += dz * q.y; A[2][2] += dz * q.z;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) A[r][cc] = warp_sum(A[r][cc]);
+    float4 q4 = quat[b];
+    Quat q = {q4.x, q4.y, q4.z, q4.w};
+    q = extract_rotation(A, q, kShapeIters);  // every lane computes the same
+    if (lane == 0) quat[b] = make_float4(q.x, q.y, q.z, q.w);
+    float R[3][3];
+    quat_to_mat(q, R);
+    const float st = stiff[b];
+    for (uint32_t k = lane; k < count; k += 32) {
+        float4 p = x[first + k];
+        const float4 r = rest[roff + k];
+        const float gx = c.x + R[0][0] * r.x + R[0][1] * r.y + R[0][2] * r.z;
+        const float gy = c.y + R[1][0] * r.x + R[1][1] * r.y + R[1][2] * r.z;
+        const float gz = c.z + R[2][0] * r.x + R[2][1] * r.y + R[2][2] * r.z;
+        p.x += (gx - p.x) * st;
+        p.y += (gy - p.y) * st;
+        p.z += (gz - p.z) * st;
+        x[first + k] = p;
+    }
+}
+
+// --------------------------------------------------------------- velocity
+
+// subtract_functor (integration_kernel.cuh:465-475): v = (x_old - x) / -dt.
+__global__ void __launch_bounds__(kBlock) k_velocity(uint32_t n, float dt, const float4 *__restrict__ x,
+                                                     const float4 *__restrict__ x_old,
+                                                     float4 *__restrict__ v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = x[i], o = x_old[i];
+    const float nd = -dt;
+    v[i] = make_float4((o.x - p.x) / nd, (o.y - p.y) / nd, (o.z - p.z) / nd, 0.f);
+}
+
+// ------------------------------------------------------------------- XSPH
+
+__global__ void __launch_bounds__(kBlock) k_xsph_gather(uint32_t n, const uint32_t *__restrict__ sidx,
+                                                        const float4 *__restrict__ x,
+                                                        const float4 *__restrict__ v,
+                                                        float4 *__restrict__ xs, float4 *__restrict__ vs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = sidx[i];
+    xs[i] = x[o];
+    vs[i] = v[o];
+}
+
+// XSPH viscosity (Macklin & Mueller 2013, eq. 17) on fluid particles, made
+// dimensionless with the rest density: v_i += c sum_j m_j (v_j - v_i)
+// poly6(x_i - x_j) / rho0_i over fluid neighbours within h at the final
+// positions, candidates taken from the last grid.
+__global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const float4 *__restrict__ sx,
+                                                 const SortedAttr *__restrict__ sattr,
+                                                 const uint32_t *__restrict__ sidx,
+                                                 const uint32_t *__restrict__ cell_first,
+                                                 const float4 *__restrict__ xs,
+                                                 const float4 *__restrict__ vs,
+                                                 float4 *__restrict__ v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SortedAttr a = sattr[i];
+    if (a.phase != kFluid) return;
+    const float3 xi = f3(xs[i]);
+    const float4 vi4 = vs[i];
+    const float3 vi = f3(vi4);
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    uint32_t nb = 0;
+    for_each_candidate(P, grid_pos(P, f3(sx[i])), P.fluid_rad, cell_first, [&](uint32_t j) {
+        if (j == i || sattr[j].phase != kFluid) return true;
+        const float4 xj4 = xs[j];
+        const float d2 = dist2_exact(xi, f3(xj4));
+        if (d2 < P.h2) {
+            if (nb >= P.max_nb) return false;
+            ++nb;
+            const float hm2 = P.h2 - d2;
+            const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
+            acc += (f3(vs[j]) - vi) * wgt;
+        }
+        return true;
+    });
+    const float3 nv = vi + acc * (P.xsph_c / a.rho0);
+    v[sidx[i]] = make_float4(nv.x, nv.y, nv.z, vi4.w);
+}
+
+__global__ void __launch_bounds__(kBlock) k_finite(uint32_t n, const float4 *__restrict__ x,
+                                                   const float4 *__restrict__ v,
+                                                   uint32_t *__restrict__ flag) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = x[i], q = v[i];
+    const bool ok = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(q.x) &&
+                    isfinite(q.y) && isfinite(q.z);
+    if (!ok) atomicOr(flag, 1u);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- launchers
+
+size_t scan_partial_count(uint32_t elements) {
+    return (elements + kScanTile - 1) / kScanTile;
+}
+
+cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, const float4 *v,
+                           float4 *x_old, uint32_t *hash, uint32_t *slot, uint32_t *counts,
+                           cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_predict<<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash,
+                              uint32_t *slot, uint32_t *counts, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_hash_count<<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exclusive_scan(uint32_t *data, uint32_t elements, uint32_t *partials,
+                                  cudaStream_t s) {
+    const uint32_t tiles = (uint32_t)scan_partial_count(elements);
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(data, elements, partials);
+    k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, tiles);
+    k_scan_apply<<<tiles, kScanThreads, 0, s>>>(data, elements, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers &g,
+                               const float4 *x, const int *phase, const float *rho0,
+                               cudaStream_t s) {
+    cudaError_t e = launch_exclusive_scan(g.cell_first, P.num_cells + 1u, g.scan_part, s);
+    if (e != cudaSuccess || n == 0) return e;
+    k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.slot, g.cell_first, g.tmp);
+    k_rank_reorder<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.cell_first, g.tmp, x, phase, rho0,
+                                                    g.sorted_idx, g.sorted_x, g.sorted_attr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4 *x,
+                                  cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_refresh_sorted<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, x, g.sorted_x);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float *lambda,
+                          cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_lambda<<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, lambda);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
+                         const float *lambda, const float4 *x_old, float4 *x, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_solve<<<blocks_for(n), kBlock, 0, s>>>(P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx,
+                                             g.cell_first, lambda, x_old, x);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_distance(const DevParams &P, const ConstraintBuffers &c, float4 *x,
+                            bool apply_distance, bool apply_pins, cudaStream_t s) {
+    if (c.count == 0) return cudaSuccess;
+    apply_distance = apply_distance && c.any_distance;
+    apply_pins = apply_pins && c.any_pin;
+    if (!apply_distance && !apply_pins) return cudaSuccess;
+    if (apply_distance)
+        k_distance_gather<<<blocks_for(c.count), kBlock, 0, s>>>(P, c.count, c.particle, c.row, c.other,
+                                                                 c.rest, c.stiff, c.occ, x, c.tmp);
+    k_distance_apply<<<blocks_for(c.count), kBlock, 0, s>>>(c.count, c.particle, c.tmp, c.pin,
+                                                            apply_distance ? 1 : 0, apply_pins ? 1 : 0, x);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shapes(const BodyBuffers &b, float4 *x, cudaStream_t s) {
+    if (b.count == 0) return cudaSuccess;
+    const uint32_t threads = b.count * 32u;
+    k_shapes<<<blocks_for(threads), kBlock, 0, s>>>(b.count, b.range, b.stiff, b.rest, b.quat, x);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 *x_old, float4 *v,
+                            cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_velocity<<<blocks_for(n), kBlock, 0, s>>>(n, dt, x, x_old, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
+                        float4 *v, float4 *xs_final, float4 *vs, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, x, v, xs_final, vs);
+    k_xsph<<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first,
+                                            xs_final, vs, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finite_check(uint32_t n, const float4 *x, const float4 *v, uint32_t *flag,
+                                cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_finite<<<blocks_for(n), kBlock, 0, s>>>(n, x, v, flag);
+    return cudaGetLastError();
+}
+
+}  // namespace pbd

@@ -1,0 +1,75 @@
+// Host-side launchers of the PBD kernels (implemented in pbd_kernels.cu).
+// All launchers are asynchronous on the given stream and return the launch
+// error (cudaSuccess when the launch was accepted).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pbd_device.cuh"
+
+namespace pbd {
+
+// Device arrays of one system's particle state and neighbour grid.
+struct GridBuffers {
+    uint32_t *hash;        // [cap] cell hash of each particle (original order)
+    uint32_t *slot;        // [cap] arrival slot inside its cell
+    uint32_t *cell_first;  // [num_cells + 1] counts, then dense offsets
+    uint32_t *scan_part;   // [scan partial sums]
+    uint32_t *tmp;         // [cap] unstable cell-bucketed indices
+    uint32_t *sorted_idx;  // [cap] original index of each sorted slot
+    float4 *sorted_x;      // [cap] positions (xyz, w) in sorted order
+    SortedAttr *sorted_attr;  // [cap] phase and rest density, sorted
+};
+
+struct ConstraintBuffers {
+    uint32_t count;        // constrained particles
+    uint32_t *particle;    // [count] particle index
+    uint32_t *row;         // [count + 1] CSR rows into the incidence list
+    uint32_t *other;       // [incidences] other endpoint
+    float *rest;           // [incidences] rest length
+    float *stiff;          // [incidences] stiffness
+    float *occ;            // [count] constraints touching the particle
+    float4 *pin;           // [count] pin point, w = 1 when pinned
+    float4 *tmp;           // [count] new positions
+    bool any_distance, any_pin;
+};
+
+struct BodyBuffers {
+    uint32_t count;        // bodies
+    uint4 *range;          // [count] first particle, particle count, rest offset
+    float *stiff;          // [count]
+    float4 *rest;          // [rigid particles] rest offset xyz, mass
+    float4 *quat;          // [count] rotation of the last solve (x, y, z, w)
+};
+
+size_t scan_partial_count(uint32_t elements);
+
+cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, const float4 *v,
+                           float4 *x_old, uint32_t *hash, uint32_t *slot, uint32_t *counts,
+                           cudaStream_t s);
+cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash,
+                              uint32_t *slot, uint32_t *counts, cudaStream_t s);
+// counts[0..cells] -> exclusive offsets; counts[cells] must be zero on entry.
+cudaError_t launch_exclusive_scan(uint32_t *data, uint32_t elements, uint32_t *partials,
+                                  cudaStream_t s);
+cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers &g,
+                               const float4 *x, const int *phase, const float *rho0,
+                               cudaStream_t s);
+cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4 *x,
+                                  cudaStream_t s);
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float *lambda,
+                          cudaStream_t s);
+cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
+                         const float *lambda, const float4 *x_old, float4 *x, cudaStream_t s);
+cudaError_t launch_distance(const DevParams &P, const ConstraintBuffers &c, float4 *x,
+                            bool apply_distance, bool apply_pins, cudaStream_t s);
+cudaError_t launch_shapes(const BodyBuffers &b, float4 *x, cudaStream_t s);
+cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 *x_old, float4 *v,
+                            cudaStream_t s);
+cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
+                        float4 *v, float4 *xs_final, float4 *vs, cudaStream_t s);
+cudaError_t launch_finite_check(uint32_t n, const float4 *x, const float4 *v, uint32_t *flag,
+                                cudaStream_t s);
+
+}  // namespace pbd

@@ -1,0 +1,1013 @@
+// C ABI of the PBD step: handle lifetime, scene content, the step driver
+// (the reference's ParticleSystem::update, gpu/src/particlesystem.cpp:
+// 144-246) and the per-stage entry points of gpu/src/cuda/wrappers.cuh.
+#include "pbd_system.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(pbd_system *s, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (s) s->err = buf;
+    else g_create_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(sys, call)                                                                    \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail((sys), PBD_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+inline bool is_pow2(uint32_t v) { return v && !(v & (v - 1u)); }
+
+int validate_params(const pbd_params *p, std::string &why) {
+    if (!p) { why = "params is NULL"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->particle_radius > 0.f)) { why = "particle_radius must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->kernel_radius > 0.f)) { why = "kernel_radius must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->cell_size > 0.f)) { why = "cell_size must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
+    uint64_t cells = 1;
+    for (int k = 0; k < 3; ++k) {
+        if (!is_pow2(p->grid_size[k])) { why = "grid_size entries must be powers of two"; return PBD_ERR_INVALID_ARGUMENT; }
+        cells *= p->grid_size[k];
+    }
+    if (cells >= (1ull << 31)) { why = "grid has too many cells (limit 2^31 - 1)"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (p->kernel_radius / p->cell_size > 8.f) { why = "kernel_radius / cell_size must be <= 8"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->max_dt > 0.f)) { why = "max_dt must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (p->max_neighbors == 0) { why = "max_neighbors must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->scorr_dq >= 0.f && p->scorr_dq < 1.f)) { why = "scorr_dq must be in [0, 1)"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (p->flags & ~PBD_FLAGS_ALL) { why = "unknown bits in flags"; return PBD_ERR_INVALID_ARGUMENT; }
+    return PBD_OK;
+}
+
+// Derived device constants (the reference's literal coefficients,
+// integration_kernel.cuh:25-35, recomputed for any h).
+pbd::DevParams make_dev(const pbd_params &p, const float rands[6]) {
+    pbd::DevParams d{};
+    const double h = p.kernel_radius, pi = 3.14159265358979323846;
+    d.gravity = make_float3(p.gravity[0], p.gravity[1], p.gravity[2]);
+    d.r = p.particle_radius;
+    d.h = p.kernel_radius;
+    d.h2 = p.kernel_radius * p.kernel_radius;
+    d.cell = p.cell_size;
+    d.origin = make_float3(p.world_origin[0], p.world_origin[1], p.world_origin[2]);
+    d.gx = p.grid_size[0];
+    d.gy = p.grid_size[1];
+    d.gz = p.grid_size[2];
+    d.num_cells = d.gx * d.gy * d.gz;
+    d.bmin = make_float3(p.box_min[0], p.box_min[1], p.box_min[2]);
+    d.bmax = make_float3(p.box_max[0], p.box_max[1], p.box_max[2]);
+    const double poly6 = 315.0 / (64.0 * pi * std::pow(h, 9.0));
+    const double spiky = 45.0 / (pi * std::pow(h, 6.0));
+    d.poly6 = (float)poly6;
+    d.spiky = (float)spiky;
+    d.poly6_self = (float)(poly6 * std::pow(h, 6.0));
+    const double dq = p.scorr_dq * h;
+    const double t2 = h * h - dq * dq;
+    d.scorr_inv_ref = (float)(1.0 / (poly6 * t2 * t2 * t2));
+    // kernel-radius units: s_corr enters lambda times h^2, relaxation / h^2
+    const bool ku = (p.flags & PBD_FLAG_KERNEL_UNITS) != 0u;
+    d.scorr_k = ku ? (float)((double)p.scorr_k * h * h) : p.scorr_k;
+    d.scorr_n = p.scorr_n;
+    const float rn = std::nearbyint(p.scorr_n);
+    d.scorr_n_int = (rn == p.scorr_n && rn >= 1.f && rn <= 16.f) ? (int)rn : 0;
+    d.relax = ku ? (float)((double)p.relaxation / (h * h)) : p.relaxation;
+    d.xsph_c = p.xsph_c;
+    d.cs = p.contact_static_friction;
+    d.ck = p.contact_kinetic_friction;
+    d.ws = sqrtf(p.wall_static_friction);
+    d.wk = sqrtf(p.wall_kinetic_friction);
+    d.collide_dist = p.particle_radius * pbd::kCollideScale;
+    d.collide2 = d.collide_dist * d.collide_dist;
+    d.fluid_rad = (int)std::ceil(p.kernel_radius / p.cell_size);
+    d.max_nb = p.max_neighbors;
+    d.twod_z = p.twod_z;
+    d.flags = p.flags;
+    for (int k = 0; k < 6; ++k) d.rands[k] = rands[k];
+    return d;
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+template <class T>
+void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void free_constraints(pbd_system *s) {
+    dfree(s->cons.particle);
+    dfree(s->cons.row);
+    dfree(s->cons.other);
+    dfree(s->cons.rest);
+    dfree(s->cons.stiff);
+    dfree(s->cons.occ);
+    dfree(s->cons.pin);
+    dfree(s->cons.tmp);
+    s->cons.count = 0;
+    s->cons.any_distance = s->cons.any_pin = false;
+}
+
+void free_bodies(pbd_system *s) {
+    dfree(s->bodies.range);
+    dfree(s->bodies.stiff);
+    dfree(s->bodies.rest);
+    dfree(s->bodies.quat);
+    s->bodies.count = 0;
+}
+
+void free_grid(pbd_system *s) {
+    dfree(s->grid.cell_first);
+    dfree(s->grid.scan_part);
+    s->grid_cells = 0;
+}
+
+void drop_graph(pbd_system *s) {
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    s->graph_exec = nullptr;
+}
+
+int alloc_grid(pbd_system *s) {
+    const uint32_t cells = s->dev.num_cells;
+    if (cells == s->grid_cells && s->grid.cell_first) return PBD_OK;
+    free_grid(s);
+    CUDA_TRY(s, dalloc(&s->grid.cell_first, (size_t)cells + 1u));
+    CUDA_TRY(s, dalloc(&s->grid.scan_part, pbd::scan_partial_count(cells + 1u)));
+    s->grid_cells = cells;
+    s->grid_valid = false;
+    return PBD_OK;
+}
+
+// Rebuilds the device CSR of distance constraints and pins from the host
+// lists.  Per constrained particle the incidences are ordered as the
+// reference's stable sort leaves them (first-endpoint occurrences in add
+// order, then second-endpoint ones), and occ counts both distance and point
+// constraints, as updateOccurences does for each (solver.cu:72-106,122,149).
+int upload_constraints(pbd_system *s) {
+    free_constraints(s);
+    const uint32_t n = s->n;
+    std::vector<uint32_t> occ(n, 0), first_cnt(n, 0), second_cnt(n, 0);
+    const size_t m = s->dist_a.size();
+    for (size_t c = 0; c < m; ++c) {
+        ++first_cnt[s->dist_a[c]];
+        ++second_cnt[s->dist_b[c]];
+        ++occ[s->dist_a[c]];
+        ++occ[s->dist_b[c]];
+    }
+    std::vector<int> pin_of(n, -1);
+    for (size_t k = 0; k < s->pin_idx.size(); ++k) {
+        ++occ[s->pin_idx[k]];
+        pin_of[s->pin_idx[k]] = (int)k;  // the last pin on a particle wins
+    }
+    std::vector<uint32_t> slot_of(n, UINT32_MAX), particle;
+    for (uint32_t k = 0; k < n; ++k)
+        if (occ[k]) {
+            slot_of[k] = (uint32_t)particle.size();
+            particle.push_back(k);
+        }
+    const uint32_t C = (uint32_t)particle.size();
+    if (C == 0) return PBD_OK;
+    std::vector<uint32_t> row(C + 1, 0);
+    for (uint32_t sidx = 0; sidx < C; ++sidx) {
+        const uint32_t k = particle[sidx];
+        row[sidx + 1] = row[sidx] + first_cnt[k] + second_cnt[k];
+    }
+    const uint32_t E = row[C];
+    std::vector<uint32_t> other(E), fill_first(C, 0), fill_second(C, 0);
+    std::vector<float> rest(E), stiff(E);
+    for (size_t c = 0; c < m; ++c) {
+        const uint32_t a = s->dist_a[c], b = s->dist_b[c];
+        const uint32_t sa = slot_of[a];
+        const uint32_t ea = row[sa] + fill_first[sa]++;
+        other[ea] = b;
+        rest[ea] = s->dist_rest[c];
+        stiff[ea] = s->dist_stiff[c];
+    }
+    for (size_t c = 0; c < m; ++c) {
+        const uint32_t a = s->dist_a[c], b = s->dist_b[c];
+        const uint32_t sb = slot_of[b];
+        const uint32_t eb = row[sb] + first_cnt[b] + fill_second[sb]++;
+        other[eb] = a;
+        rest[eb] = s->dist_rest[c];
+        stiff[eb] = s->dist_stiff[c];
+    }
+    std::vector<float> occf(C);
+    std::vector<float4> pin(C, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (uint32_t sidx = 0; sidx < C; ++sidx) {
+        const uint32_t k = particle[sidx];
+        occf[sidx] = (float)occ[k];
+        if (pin_of[k] >= 0) {
+            const float *pt = &s->pin_pts[3 * (size_t)pin_of[k]];
+            pin[sidx] = make_float4(pt[0], pt[1], pt[2], 1.f);
+        }
+    }
+    pbd::ConstraintBuffers &cb = s->cons;
+    CUDA_TRY(s, dalloc(&cb.particle, C));
+    CUDA_TRY(s, dalloc(&cb.row, C + 1));
+    CUDA_TRY(s, dalloc(&cb.other, std::max<uint32_t>(E, 1)));
+    CUDA_TRY(s, dalloc(&cb.rest, std::max<uint32_t>(E, 1)));
+    CUDA_TRY(s, dalloc(&cb.stiff, std::max<uint32_t>(E, 1)));
+    CUDA_TRY(s, dalloc(&cb.occ, C));
+    CUDA_TRY(s, dalloc(&cb.pin, C));
+    CUDA_TRY(s, dalloc(&cb.tmp, C));
+    CUDA_TRY(s, cudaMemcpy(cb.particle, particle.data(), C * 4ull, cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(cb.row, row.data(), (C + 1) * 4ull, cudaMemcpyHostToDevice));
+    if (E) {
+        CUDA_TRY(s, cudaMemcpy(cb.other, other.data(), E * 4ull, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(cb.rest, rest.data(), E * 4ull, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(cb.stiff, stiff.data(), E * 4ull, cudaMemcpyHostToDevice));
+    }
+    CUDA_TRY(s, cudaMemcpy(cb.occ, occf.data(), C * 4ull, cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(cb.pin, pin.data(), C * sizeof(float4), cudaMemcpyHostToDevice));
+    cb.count = C;
+    cb.any_distance = m > 0;
+    cb.any_pin = !s->pin_idx.empty();
+    return PBD_OK;
+}
+
+int upload_bodies(pbd_system *s, const std::vector<float4> &quats) {
+    free_bodies(s);
+    const uint32_t B = (uint32_t)s->body_range.size();
+    if (!B) return PBD_OK;
+    pbd::BodyBuffers &bb = s->bodies;
+    CUDA_TRY(s, dalloc(&bb.range, B));
+    CUDA_TRY(s, dalloc(&bb.stiff, B));
+    CUDA_TRY(s, dalloc(&bb.rest, s->body_rest.size()));
+    CUDA_TRY(s, dalloc(&bb.quat, B));
+    CUDA_TRY(s, cudaMemcpy(bb.range, s->body_range.data(), B * sizeof(uint4), cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(bb.stiff, s->body_stiff.data(), B * 4ull, cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(bb.rest, s->body_rest.data(), s->body_rest.size() * sizeof(float4),
+                           cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(bb.quat, quats.data(), B * sizeof(float4), cudaMemcpyHostToDevice));
+    bb.count = B;
+    return PBD_OK;
+}
+
+int check_sys(const pbd_system *s) {
+    if (!s) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "system handle is NULL");
+    return PBD_OK;
+}
+
+int use_device(pbd_system *s) {
+    CUDA_TRY(s, cudaSetDevice(s->device));
+    return PBD_OK;
+}
+
+#define SYS_GUARD(s)                          \
+    do {                                      \
+        if (int rc_ = check_sys(s)) return rc_; \
+        if (int rc_ = use_device(s)) return rc_; \
+    } while (0)
+
+int need_grid(pbd_system *s) {
+    if (!s->grid_valid) return fail(s, PBD_ERR_STATE, "no grid: call pbd_build_grid after the last change of the scene");
+    return PBD_OK;
+}
+
+// ------------------------------------------------------- stage timing
+
+cudaEvent_t take_event(pbd_system *s) {
+    if (!s->event_pool.empty()) {
+        cudaEvent_t e = s->event_pool.back();
+        s->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+// Brackets one stage group with events when profiling (never inside a
+// graph capture) and counts the kernels it launches.
+struct Stage {
+    pbd_system *s;
+    cudaStream_t st;
+    int stage;
+    uint32_t kernels;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Stage(pbd_system *s_, cudaStream_t st_, int stage_, uint32_t kernels_)
+        : s(s_), st(st_), stage(stage_), kernels(kernels_) {
+        if (s->profiling && !s->capturing && kernels) {
+            a = take_event(s);
+            b = take_event(s);
+            if (a && b) cudaEventRecord(a, st);
+        }
+    }
+    ~Stage() {
+        s->launches += kernels;
+        if (a && b) {
+            cudaEventRecord(b, st);
+            s->pending.push_back({stage, a, b});
+            s->stage_launches[stage] += kernels;
+        }
+    }
+};
+
+int collect_profile(pbd_system *s) {
+    for (auto &t : s->pending) {
+        CUDA_TRY(s, cudaEventSynchronize(t.stop));
+        float ms = 0.f;
+        CUDA_TRY(s, cudaEventElapsedTime(&ms, t.start, t.stop));
+        s->stage_ms[t.stage] += ms;
+        s->event_pool.push_back(t.start);
+        s->event_pool.push_back(t.stop);
+    }
+    s->pending.clear();
+    return PBD_OK;
+}
+
+// ------------------------------------------------------------- the step
+
+int build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict) {
+    const pbd::DevParams &P = s->dev;
+    Stage t(s, st, PBD_STAGE_GRID, (hashed_in_predict ? 0u : 1u) + 3u + (s->n ? 2u : 0u));
+    if (!hashed_in_predict) {
+        CUDA_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
+        CUDA_TRY(s, pbd::launch_hash_count(P, s->n, s->x, s->grid.hash, s->grid.slot, s->grid.cell_first, st));
+    }
+    CUDA_TRY(s, pbd::launch_grid_finish(P, s->n, s->grid, s->x, s->phase, s->rho0, st));
+    s->grid_valid = true;
+    return PBD_OK;
+}
+
+uint32_t solve_mask(const pbd_system *s) {
+    uint32_t m = pbd::kDoWorld;
+    if (s->n_fluid) m |= pbd::kDoFluid;
+    if (s->n_contact) m |= pbd::kDoContact;
+    return m;
+}
+
+// The step in the reference's order (particlesystem.cpp:144-246): predict,
+// then every iteration rebuilds the grid from the current positions and
+// runs contacts + PBF + walls (one fused pass), distance constraints with
+// pins, and shape matching; finally the velocity update and XSPH.
+int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
+    const pbd::DevParams &P = s->dev;
+    const uint32_t n = s->n;
+    {
+        // predict, with the first grid build's hash and cell counts fused in
+        Stage t(s, st, PBD_STAGE_PREDICT, 1);
+        CUDA_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
+        CUDA_TRY(s, pbd::launch_predict(P, n, dt, s->x, s->v, s->x_old, s->grid.hash, s->grid.slot,
+                                        s->grid.cell_first, st));
+    }
+    const uint32_t mask = solve_mask(s);
+    const uint32_t dist_kernels =
+        s->cons.count ? (s->cons.any_distance ? 2u : (s->cons.any_pin ? 1u : 0u)) : 0u;
+    for (uint32_t it = 0; it < s->params.iterations; ++it) {
+        if (int rc = build_grid(s, st, it == 0)) return rc;
+        if (s->n_fluid) {
+            Stage t(s, st, PBD_STAGE_LAMBDA, 1);
+            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->lambda, st));
+        }
+        {
+            Stage t(s, st, PBD_STAGE_SOLVE, 1);
+            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->lambda, s->x_old, s->x, st));
+        }
+        if (dist_kernels) {
+            Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
+            CUDA_TRY(s, pbd::launch_distance(P, s->cons, s->x, true, true, st));
+        }
+        if (s->bodies.count) {
+            Stage t(s, st, PBD_STAGE_SHAPES, 1);
+            CUDA_TRY(s, pbd::launch_shapes(s->bodies, s->x, st));
+        }
+    }
+    {
+        Stage t(s, st, PBD_STAGE_VELOCITY, 1);
+        CUDA_TRY(s, pbd::launch_velocity(n, dt, s->x, s->x_old, s->v, st));
+    }
+    if (s->params.xsph_c != 0.f && s->n_fluid && s->params.iterations > 0) {
+        Stage t(s, st, PBD_STAGE_XSPH, 2);
+        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->x, s->v, s->xs_final, s->vs, st));
+    }
+    ++s->steps;
+    return PBD_OK;
+}
+
+float clamp_dt(const pbd_system *s, float dt) { return std::min(dt, s->params.max_dt); }
+
+}  // namespace
+
+// =================================================================== ABI
+
+extern "C" {
+
+int pbd_abi_version(void) { return PBD_ABI_VERSION; }
+
+void pbd_default_params(pbd_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->particle_radius = 0.25f;
+    p->kernel_radius = 2.f;
+    p->cell_size = 0.5f;
+    p->grid_size[0] = p->grid_size[1] = p->grid_size[2] = 64;
+    p->gravity[1] = -9.8f;
+    p->box_min[0] = -50.f; p->box_min[1] = 0.f;   p->box_min[2] = -50.f;
+    p->box_max[0] = 50.f;  p->box_max[1] = 200.f; p->box_max[2] = 50.f;
+    p->iterations = 5;
+    p->max_dt = 0.05f;
+    p->relaxation = 0.01f;
+    p->scorr_k = 0.1f;
+    p->scorr_n = 4.f;
+    p->scorr_dq = 0.2f;
+    p->xsph_c = 0.f;
+    p->contact_static_friction = 0.005f;
+    p->contact_kinetic_friction = 0.0002f;
+    p->wall_static_friction = 0.005f;
+    p->wall_kinetic_friction = 0.0002f;
+    p->max_neighbors = 500;
+    p->twod_z = 0.f;
+    p->flags = 0;
+}
+
+const char *pbd_last_error(const pbd_system *s) {
+    return s ? s->err.c_str() : g_create_error.c_str();
+}
+
+int pbd_create(const pbd_params *params, uint32_t max_particles, pbd_system **out) {
+    if (!out) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    if (validate_params(params, why)) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "%s", why.c_str());
+    if (max_particles == 0 || max_particles >= (1u << 31))
+        return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "max_particles must be in [1, 2^31)");
+    pbd_system *s = new pbd_system();
+    s->params = *params;
+    s->cap = max_particles;
+    s->dev = make_dev(s->params, s->rands);
+    int rc = PBD_OK;
+    auto bail = [&](int code) {
+        g_create_error = s->err;
+        pbd_destroy(s);
+        return code;
+    };
+    if (cudaGetDevice(&s->device) != cudaSuccess) {
+        s->err = "no CUDA device";
+        return bail(PBD_ERR_CUDA);
+    }
+    const size_t c = max_particles;
+#define ALLOC(ptr, cnt)                                                                       \
+    do {                                                                                      \
+        cudaError_t e_ = dalloc(&(ptr), (cnt));                                               \
+        if (e_ != cudaSuccess) {                                                              \
+            s->err = std::string("cudaMalloc failed: ") + cudaGetErrorString(e_);             \
+            return bail(PBD_ERR_CUDA);                                                        \
+        }                                                                                     \
+    } while (0)
+    ALLOC(s->x, c);
+    ALLOC(s->v, c);
+    ALLOC(s->x_old, c);
+    ALLOC(s->phase, c);
+    ALLOC(s->rho0, c);
+    ALLOC(s->lambda, c);
+    ALLOC(s->flag, 1);
+    ALLOC(s->grid.hash, c);
+    ALLOC(s->grid.slot, c);
+    ALLOC(s->grid.tmp, c);
+    ALLOC(s->grid.sorted_idx, c);
+    ALLOC(s->grid.sorted_x, c);
+    ALLOC(s->grid.sorted_attr, c);
+#undef ALLOC
+    if ((rc = alloc_grid(s))) return bail(rc);
+    *out = s;
+    return PBD_OK;
+}
+
+int pbd_destroy(pbd_system *s) {
+    if (!s) return PBD_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->device);
+    drop_graph(s);
+    if (s->graph_stream) cudaStreamDestroy(s->graph_stream);
+    for (auto &t : s->pending) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+    dfree(s->x);
+    dfree(s->v);
+    dfree(s->x_old);
+    dfree(s->phase);
+    dfree(s->rho0);
+    dfree(s->lambda);
+    dfree(s->xs_final);
+    dfree(s->vs);
+    dfree(s->flag);
+    dfree(s->grid.hash);
+    dfree(s->grid.slot);
+    dfree(s->grid.tmp);
+    dfree(s->grid.sorted_idx);
+    dfree(s->grid.sorted_x);
+    dfree(s->grid.sorted_attr);
+    free_grid(s);
+    free_constraints(s);
+    free_bodies(s);
+    delete s;
+    return PBD_OK;
+}
+
+int pbd_set_params(pbd_system *s, const pbd_params *params) {
+    SYS_GUARD(s);
+    std::string why;
+    if (validate_params(params, why)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "%s", why.c_str());
+    s->params = *params;
+    s->dev = make_dev(s->params, s->rands);
+    if (int rc = alloc_grid(s)) return rc;
+    s->grid_valid = false;
+    ++s->version;
+    return PBD_OK;
+}
+
+int pbd_get_params(const pbd_system *s, pbd_params *out) {
+    if (!s || !out) return PBD_ERR_INVALID_ARGUMENT;
+    *out = s->params;
+    return PBD_OK;
+}
+
+uint32_t pbd_num_particles(const pbd_system *s) { return s ? s->n : 0u; }
+uint32_t pbd_capacity(const pbd_system *s) { return s ? s->cap : 0u; }
+uint32_t pbd_num_cells(const pbd_system *s) { return s ? s->dev.num_cells : 0u; }
+
+int pbd_set_wall_jitter(pbd_system *s, const float rands[6]) {
+    if (int rc = check_sys(s)) return rc;
+    if (!rands) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rands is NULL");
+    for (int k = 0; k < 6; ++k) {
+        if (!std::isfinite(rands[k])) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rands must be finite");
+        s->rands[k] = rands[k];
+        s->dev.rands[k] = rands[k];
+    }
+    ++s->version;
+    return PBD_OK;
+}
+
+int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float *vel,
+                      const int32_t *phase, const float *rest_density, uint32_t *first_index) {
+    SYS_GUARD(s);
+    if (n == 0) {
+        if (first_index) *first_index = s->n;
+        return PBD_OK;
+    }
+    if (!pos_w || !phase) return fail(s, PBD_ERR_INVALID_ARGUMENT, "pos_w and phase are required");
+    if ((uint64_t)s->n + n > s->cap)
+        return fail(s, PBD_ERR_CAPACITY, "adding %u particles to %u exceeds capacity %u", n, s->n, s->cap);
+    uint32_t nf = 0, nc = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float *p = pos_w + 4ull * i;
+        for (int k = 0; k < 4; ++k)
+            if (!std::isfinite(p[k])) return fail(s, PBD_ERR_INVALID_ARGUMENT, "particle %u has a non-finite position/mass", i);
+        if (p[3] < 0.f) return fail(s, PBD_ERR_INVALID_ARGUMENT, "particle %u has negative inverse mass", i);
+        if (phase[i] < 0) return fail(s, PBD_ERR_INVALID_ARGUMENT, "particle %u has negative phase", i);
+        if (phase[i] == PBD_PHASE_FLUID) {
+            if (!(p[3] > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "fluid particle %u needs inverse mass > 0", i);
+            if (rest_density && !(rest_density[i] > 0.f))
+                return fail(s, PBD_ERR_INVALID_ARGUMENT, "fluid particle %u needs rest density > 0", i);
+            ++nf;
+        }
+        if (phase[i] >= PBD_PHASE_CLOTH) ++nc;
+        if (vel)
+            for (int k = 0; k < 4; ++k)
+                if (!std::isfinite(vel[4ull * i + k])) return fail(s, PBD_ERR_INVALID_ARGUMENT, "particle %u has a non-finite velocity", i);
+    }
+    const uint32_t off = s->n;
+    CUDA_TRY(s, cudaMemcpy(s->x + off, pos_w, n * sizeof(float4), cudaMemcpyHostToDevice));
+    if (vel) {
+        CUDA_TRY(s, cudaMemcpy(s->v + off, vel, n * sizeof(float4), cudaMemcpyHostToDevice));
+    } else {
+        CUDA_TRY(s, cudaMemset(s->v + off, 0, n * sizeof(float4)));
+    }
+    CUDA_TRY(s, cudaMemcpy(s->phase + off, phase, n * 4ull, cudaMemcpyHostToDevice));
+    std::vector<float> ro(n, 1.f);
+    if (rest_density) std::copy(rest_density, rest_density + n, ro.begin());
+    CUDA_TRY(s, cudaMemcpy(s->rho0 + off, ro.data(), n * 4ull, cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(s->x_old + off, pos_w, n * sizeof(float4), cudaMemcpyHostToDevice));
+    s->n += n;
+    s->n_fluid += nf;
+    s->n_contact += nc;
+    if (s->n_fluid && !s->xs_final) {
+        CUDA_TRY(s, dalloc(&s->xs_final, s->cap));
+        CUDA_TRY(s, dalloc(&s->vs, s->cap));
+    }
+    s->grid_valid = false;
+    ++s->version;
+    if (first_index) *first_index = off;
+    if (!s->dist_a.empty() || !s->pin_idx.empty()) return upload_constraints(s);
+    return PBD_OK;
+}
+
+int pbd_add_distance_constraints(pbd_system *s, uint32_t m, const uint32_t *pairs,
+                                 const float *rest, const float *stiffness) {
+    SYS_GUARD(s);
+    if (m == 0) return PBD_OK;
+    if (!pairs || !rest) return fail(s, PBD_ERR_INVALID_ARGUMENT, "pairs and rest are required");
+    for (uint32_t c = 0; c < m; ++c) {
+        if (pairs[2 * c] >= s->n || pairs[2 * c + 1] >= s->n)
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u references a particle >= %u", c, s->n);
+        if (pairs[2 * c] == pairs[2 * c + 1])
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u joins a particle to itself", c);
+        if (!std::isfinite(rest[c]) || rest[c] < 0.f)
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u has an invalid rest length", c);
+        if (stiffness && !(stiffness[c] >= 0.f && stiffness[c] <= 1.f))
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u stiffness must be in [0, 1]", c);
+    }
+    for (uint32_t c = 0; c < m; ++c) {
+        s->dist_a.push_back(pairs[2 * c]);
+        s->dist_b.push_back(pairs[2 * c + 1]);
+        s->dist_rest.push_back(rest[c]);
+        s->dist_stiff.push_back(stiffness ? stiffness[c] : 1.f);
+    }
+    ++s->version;
+    return upload_constraints(s);
+}
+
+int pbd_add_point_constraints(pbd_system *s, uint32_t p, const uint32_t *index, const float *points) {
+    SYS_GUARD(s);
+    if (p == 0) return PBD_OK;
+    if (!index || !points) return fail(s, PBD_ERR_INVALID_ARGUMENT, "index and points are required");
+    for (uint32_t k = 0; k < p; ++k) {
+        if (index[k] >= s->n) return fail(s, PBD_ERR_INVALID_ARGUMENT, "pin %u references a particle >= %u", k, s->n);
+        for (int d = 0; d < 3; ++d)
+            if (!std::isfinite(points[3 * k + d])) return fail(s, PBD_ERR_INVALID_ARGUMENT, "pin %u point is not finite", k);
+    }
+    for (uint32_t k = 0; k < p; ++k) {
+        s->pin_idx.push_back(index[k]);
+        for (int d = 0; d < 3; ++d) s->pin_pts.push_back(points[3 * k + d]);
+    }
+    ++s->version;
+    return upload_constraints(s);
+}
+
+int pbd_add_rigid_body(pbd_system *s, uint32_t first, uint32_t count, float stiffness,
+                       uint32_t *body_index) {
+    SYS_GUARD(s);
+    if (count < 2) return fail(s, PBD_ERR_INVALID_ARGUMENT, "a rigid body needs at least 2 particles");
+    if ((uint64_t)first + count > s->n) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rigid body range exceeds the particle count");
+    if (!(stiffness >= 0.f && stiffness <= 1.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "stiffness must be in [0, 1]");
+    for (const uint4 &r : s->body_range)
+        if (first < r.x + r.y && r.x < first + count)
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "rigid body overlaps body starting at %u", r.x);
+    std::vector<float4> pos(count);
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    CUDA_TRY(s, cudaMemcpy(pos.data(), s->x + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
+    double cx = 0, cy = 0, cz = 0, msum = 0;
+    for (uint32_t k = 0; k < count; ++k) {
+        if (!(pos[k].w > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rigid particle %u needs inverse mass > 0", first + k);
+        const double m = 1.0 / pos[k].w;
+        cx += m * pos[k].x;
+        cy += m * pos[k].y;
+        cz += m * pos[k].z;
+        msum += m;
+    }
+    cx /= msum;
+    cy /= msum;
+    cz /= msum;
+    const uint32_t roff = (uint32_t)s->body_rest.size();
+    for (uint32_t k = 0; k < count; ++k)
+        s->body_rest.push_back(make_float4((float)(pos[k].x - cx), (float)(pos[k].y - cy),
+                                           (float)(pos[k].z - cz), (float)(1.0 / pos[k].w)));
+    // keep the rotations of existing bodies
+    std::vector<float4> quats(s->body_range.size() + 1, make_float4(0.f, 0.f, 0.f, 1.f));
+    if (s->bodies.count)
+        CUDA_TRY(s, cudaMemcpy(quats.data(), s->bodies.quat, s->bodies.count * sizeof(float4), cudaMemcpyDeviceToHost));
+    s->body_range.push_back(make_uint4(first, count, roff, 0));
+    s->body_stiff.push_back(stiffness);
+    if (body_index) *body_index = (uint32_t)s->body_range.size() - 1u;
+    ++s->version;
+    return upload_bodies(s, quats);
+}
+
+static int copy_state(pbd_system *s, float4 *buf, uint32_t first, uint32_t count, float *host_or_dev,
+                      int on_device, void *stream, bool to_sys) {
+    SYS_GUARD(s);
+    if ((uint64_t)first + count > s->n) return fail(s, PBD_ERR_INVALID_ARGUMENT, "range exceeds particle count %u", s->n);
+    if (count == 0) return PBD_OK;
+    if (!host_or_dev) return fail(s, PBD_ERR_INVALID_ARGUMENT, "buffer is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t bytes = (size_t)count * sizeof(float4);
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : (to_sys ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+    if (to_sys) CUDA_TRY(s, cudaMemcpyAsync(buf + first, host_or_dev, bytes, kind, st));
+    else CUDA_TRY(s, cudaMemcpyAsync(host_or_dev, buf + first, bytes, kind, st));
+    if (!on_device) CUDA_TRY(s, cudaStreamSynchronize(st));
+    if (to_sys) s->grid_valid = false;
+    return PBD_OK;
+}
+
+int pbd_set_positions(pbd_system *s, uint32_t first, uint32_t count, const float *src, int on_dev, void *st) {
+    return copy_state(s, s ? s->x : nullptr, first, count, const_cast<float *>(src), on_dev, st, true);
+}
+int pbd_set_velocities(pbd_system *s, uint32_t first, uint32_t count, const float *src, int on_dev, void *st) {
+    return copy_state(s, s ? s->v : nullptr, first, count, const_cast<float *>(src), on_dev, st, true);
+}
+int pbd_get_positions(pbd_system *s, uint32_t first, uint32_t count, float *dst, int on_dev, void *st) {
+    return copy_state(s, s ? s->x : nullptr, first, count, dst, on_dev, st, false);
+}
+int pbd_get_velocities(pbd_system *s, uint32_t first, uint32_t count, float *dst, int on_dev, void *st) {
+    return copy_state(s, s ? s->v : nullptr, first, count, dst, on_dev, st, false);
+}
+
+int pbd_get_phases(pbd_system *s, int32_t *dst) {
+    SYS_GUARD(s);
+    if (!dst) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dst is NULL");
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    if (s->n) CUDA_TRY(s, cudaMemcpy(dst, s->phase, s->n * 4ull, cudaMemcpyDeviceToHost));
+    return PBD_OK;
+}
+
+int pbd_get_device_buffers(pbd_system *s, pbd_device_buffers *out) {
+    if (int rc = check_sys(s)) return rc;
+    if (!out) return fail(s, PBD_ERR_INVALID_ARGUMENT, "out is NULL");
+    out->positions = s->x;
+    out->velocities = s->v;
+    out->phases = s->phase;
+    out->num_particles = s->n;
+    out->capacity = s->cap;
+    return PBD_OK;
+}
+
+// --------------------------------------------------------------- stepping
+
+int pbd_update(pbd_system *s, float dt, void *stream) {
+    SYS_GUARD(s);
+    if (!(dt > 0.f) || !std::isfinite(dt)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (s->n == 0) return PBD_OK;
+    return enqueue_update(s, clamp_dt(s, dt), (cudaStream_t)stream);
+}
+
+int pbd_update_graph(pbd_system *s, float dt, uint32_t nsteps, void *stream) {
+    SYS_GUARD(s);
+    if (!(dt > 0.f) || !std::isfinite(dt)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (s->n == 0 || nsteps == 0) return PBD_OK;
+    dt = clamp_dt(s, dt);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!s->graph_exec || s->graph_dt != dt || s->graph_version != s->version) {
+        drop_graph(s);
+        if (!s->graph_stream) CUDA_TRY(s, cudaStreamCreateWithFlags(&s->graph_stream, cudaStreamNonBlocking));
+        // capture on a private stream, ordered after the caller's work
+        CUDA_TRY(s, cudaStreamSynchronize(st));
+        CUDA_TRY(s, cudaStreamBeginCapture(s->graph_stream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t launches0 = s->launches, steps0 = s->steps;
+        s->capturing = true;
+        int rc = enqueue_update(s, dt, s->graph_stream);
+        s->capturing = false;
+        s->graph_kernels = s->launches - launches0;
+        s->launches = launches0;  // counted when replayed
+        s->steps = steps0;
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(s->graph_stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ce != cudaSuccess) return fail(s, PBD_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&s->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            s->graph_exec = nullptr;
+            return fail(s, PBD_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ce));
+        }
+        s->graph_dt = dt;
+        s->graph_version = s->version;
+    }
+    for (uint32_t k = 0; k < nsteps; ++k) CUDA_TRY(s, cudaGraphLaunch(s->graph_exec, st));
+    s->launches += s->graph_kernels * nsteps;
+    s->steps += nsteps;
+    s->grid_valid = true;
+    return PBD_OK;
+}
+
+int pbd_set_profiling(pbd_system *s, int enable) {
+    if (int rc = check_sys(s)) return rc;
+    s->profiling = enable != 0;
+    return PBD_OK;
+}
+
+int pbd_get_profile(pbd_system *s, pbd_profile *out) {
+    SYS_GUARD(s);
+    if (!out) return fail(s, PBD_ERR_INVALID_ARGUMENT, "out is NULL");
+    if (int rc = collect_profile(s)) return rc;
+    for (int k = 0; k < PBD_STAGE_COUNT; ++k) {
+        out->stage_ms[k] = s->stage_ms[k];
+        out->stage_launches[k] = s->stage_launches[k];
+    }
+    out->kernel_launches = s->launches;
+    out->steps = s->steps;
+    return PBD_OK;
+}
+
+int pbd_reset_profile(pbd_system *s) {
+    SYS_GUARD(s);
+    if (int rc = collect_profile(s)) return rc;
+    for (int k = 0; k < PBD_STAGE_COUNT; ++k) {
+        s->stage_ms[k] = 0.0;
+        s->stage_launches[k] = 0;
+    }
+    s->launches = 0;
+    s->steps = 0;
+    return PBD_OK;
+}
+
+int pbd_integrate(pbd_system *s, float dt, void *stream) {
+    SYS_GUARD(s);
+    if (!(dt > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    CUDA_TRY(s, pbd::launch_predict(s->dev, s->n, clamp_dt(s, dt), s->x, s->v, s->x_old, nullptr,
+                                    nullptr, nullptr, (cudaStream_t)stream));
+    s->launches += 1;
+    s->grid_valid = false;
+    return PBD_OK;
+}
+
+int pbd_build_grid(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    return build_grid(s, (cudaStream_t)stream, false);
+}
+
+int pbd_collide(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    if (int rc = need_grid(s)) return rc;
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->lambda, s->x_old, s->x,
+                                  (cudaStream_t)stream));
+    s->launches += 1;
+    return PBD_OK;
+}
+
+int pbd_solve_fluids(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    if (int rc = need_grid(s)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->lambda, st));
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->lambda, s->x_old, s->x, st));
+    s->launches += 2;
+    return PBD_OK;
+}
+
+int pbd_collide_world(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    if (int rc = need_grid(s)) return rc;
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->lambda, s->x_old, s->x,
+                                  (cudaStream_t)stream));
+    s->launches += 1;
+    return PBD_OK;
+}
+
+int pbd_solve_distance_constraints(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    CUDA_TRY(s, pbd::launch_distance(s->dev, s->cons, s->x, true, false, (cudaStream_t)stream));
+    return PBD_OK;
+}
+
+int pbd_solve_point_constraints(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    CUDA_TRY(s, pbd::launch_distance(s->dev, s->cons, s->x, false, true, (cudaStream_t)stream));
+    return PBD_OK;
+}
+
+int pbd_solve_shapes(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    CUDA_TRY(s, pbd::launch_shapes(s->bodies, s->x, (cudaStream_t)stream));
+    return PBD_OK;
+}
+
+int pbd_calc_velocity(pbd_system *s, float dt, void *stream) {
+    SYS_GUARD(s);
+    if (!(dt > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    CUDA_TRY(s, pbd::launch_velocity(s->n, clamp_dt(s, dt), s->x, s->x_old, s->v, (cudaStream_t)stream));
+    return PBD_OK;
+}
+
+int pbd_apply_xsph(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    if (int rc = need_grid(s)) return rc;
+    if (!s->xs_final) return PBD_OK;  // no fluid
+    CUDA_TRY(s, pbd::launch_xsph(s->dev, s->n, s->grid, s->x, s->v, s->xs_final, s->vs,
+                                 (cudaStream_t)stream));
+    return PBD_OK;
+}
+
+// ------------------------------------------------------------- inspection
+
+int pbd_get_grid(pbd_system *s, uint32_t *sorted_hash, uint32_t *sorted_index, uint32_t *cell_start,
+                 uint32_t *cell_end) {
+    SYS_GUARD(s);
+    if (int rc = need_grid(s)) return rc;
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    const uint32_t n = s->n, cells = s->dev.num_cells;
+    std::vector<uint32_t> hash(n), idx(n), first((size_t)cells + 1);
+    if (n) {
+        CUDA_TRY(s, cudaMemcpy(hash.data(), s->grid.hash, n * 4ull, cudaMemcpyDeviceToHost));
+        CUDA_TRY(s, cudaMemcpy(idx.data(), s->grid.sorted_idx, n * 4ull, cudaMemcpyDeviceToHost));
+    }
+    CUDA_TRY(s, cudaMemcpy(first.data(), s->grid.cell_first, ((size_t)cells + 1) * 4u, cudaMemcpyDeviceToHost));
+    for (uint32_t p = 0; p < n; ++p) {
+        if (sorted_index) sorted_index[p] = idx[p];
+        if (sorted_hash) sorted_hash[p] = hash[idx[p]];
+    }
+    for (uint32_t c = 0; c < cells; ++c) {
+        const bool full = first[c + 1] > first[c];
+        if (cell_start) cell_start[c] = full ? first[c] : 0xffffffffu;
+        if (cell_end) cell_end[c] = full ? first[c + 1] : 0u;
+    }
+    return PBD_OK;
+}
+
+int pbd_get_lambdas(pbd_system *s, float *dst) {
+    SYS_GUARD(s);
+    if (int rc = need_grid(s)) return rc;
+    if (!dst) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dst is NULL");
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    const uint32_t n = s->n;
+    if (!n) return PBD_OK;
+    std::vector<uint32_t> idx(n);
+    std::vector<float> lam(n);
+    CUDA_TRY(s, cudaMemcpy(idx.data(), s->grid.sorted_idx, n * 4ull, cudaMemcpyDeviceToHost));
+    CUDA_TRY(s, cudaMemcpy(lam.data(), s->lambda, n * 4ull, cudaMemcpyDeviceToHost));
+    for (uint32_t p = 0; p < n; ++p) dst[idx[p]] = lam[p];
+    return PBD_OK;
+}
+
+int pbd_check_finite(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(s, cudaMemsetAsync(s->flag, 0, 4, st));
+    CUDA_TRY(s, pbd::launch_finite_check(s->n, s->x, s->v, s->flag, st));
+    uint32_t f = 0;
+    CUDA_TRY(s, cudaMemcpyAsync(&f, s->flag, 4, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(s, cudaStreamSynchronize(st));
+    if (f) return fail(s, PBD_ERR_NONFINITE, "non-finite position or velocity");
+    return PBD_OK;
+}
+
+int pbd_synchronize(pbd_system *s, void *stream) {
+    SYS_GUARD(s);
+    CUDA_TRY(s, cudaStreamSynchronize((cudaStream_t)stream));
+    return PBD_OK;
+}
+
+// State blob: header {magic, version, n, bodies}, positions, velocities,
+// body rotations.
+static const uint32_t kStateMagic = 0x50424431u;  // "PBD1"
+
+uint64_t pbd_state_size(const pbd_system *s) {
+    if (!s) return 0;
+    return 16ull + 2ull * s->n * sizeof(float4) + (uint64_t)s->bodies.count * sizeof(float4);
+}
+
+int pbd_save_state(pbd_system *s, void *dst, uint64_t size) {
+    SYS_GUARD(s);
+    if (!dst || size < pbd_state_size(s)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "state buffer too small");
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    uint32_t hdr[4] = {kStateMagic, 1u, s->n, s->bodies.count};
+    char *p = (char *)dst;
+    std::memcpy(p, hdr, 16);
+    p += 16;
+    const size_t pb = (size_t)s->n * sizeof(float4);
+    if (pb) {
+        CUDA_TRY(s, cudaMemcpy(p, s->x, pb, cudaMemcpyDeviceToHost));
+        CUDA_TRY(s, cudaMemcpy(p + pb, s->v, pb, cudaMemcpyDeviceToHost));
+    }
+    p += 2 * pb;
+    if (s->bodies.count)
+        CUDA_TRY(s, cudaMemcpy(p, s->bodies.quat, s->bodies.count * sizeof(float4), cudaMemcpyDeviceToHost));
+    return PBD_OK;
+}
+
+int pbd_load_state(pbd_system *s, const void *src, uint64_t size) {
+    SYS_GUARD(s);
+    if (!src || size < 16) return fail(s, PBD_ERR_INVALID_ARGUMENT, "state buffer too small");
+    uint32_t hdr[4];
+    std::memcpy(hdr, src, 16);
+    if (hdr[0] != kStateMagic || hdr[1] != 1u) return fail(s, PBD_ERR_INVALID_ARGUMENT, "not a state blob");
+    if (hdr[2] != s->n || hdr[3] != s->bodies.count)
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "state blob holds %u particles / %u bodies, system has %u / %u",
+                    hdr[2], hdr[3], s->n, s->bodies.count);
+    if (size < pbd_state_size(s)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "state buffer too small");
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    const char *p = (const char *)src + 16;
+    const size_t pb = (size_t)s->n * sizeof(float4);
+    if (pb) {
+        CUDA_TRY(s, cudaMemcpy(s->x, p, pb, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(s->v, p + pb, pb, cudaMemcpyHostToDevice));
+    }
+    p += 2 * pb;
+    if (s->bodies.count)
+        CUDA_TRY(s, cudaMemcpy(s->bodies.quat, p, s->bodies.count * sizeof(float4), cudaMemcpyHostToDevice));
+    s->grid_valid = false;
+    return PBD_OK;
+}
+
+}  // extern "C"

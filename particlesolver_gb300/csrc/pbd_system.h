@@ -1,0 +1,72 @@
+// Host-side state of one pbd_system handle.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pbd.h"
+#include "pbd_kernels.h"
+
+struct pbd_system {
+    pbd_params params{};
+    pbd::DevParams dev{};
+    uint32_t cap = 0;  // max particles
+    uint32_t n = 0;    // live particles
+    int device = 0;
+
+    // particle state, original order
+    float4 *x = nullptr, *v = nullptr, *x_old = nullptr;
+    int *phase = nullptr;
+    float *rho0 = nullptr;
+    float *lambda = nullptr;  // sorted order
+    float4 *xs_final = nullptr, *vs = nullptr;  // XSPH scratch, sorted order
+    uint32_t *flag = nullptr;  // finite check
+
+    pbd::GridBuffers grid{};
+    uint32_t grid_cells = 0;  // cells the grid arrays were sized for
+    bool grid_valid = false;
+
+    // constraints (host lists in add order + device CSR)
+    std::vector<uint32_t> dist_a, dist_b;
+    std::vector<float> dist_rest, dist_stiff;
+    std::vector<uint32_t> pin_idx;
+    std::vector<float> pin_pts;
+    pbd::ConstraintBuffers cons{};
+
+    // rigid bodies
+    std::vector<uint4> body_range;
+    std::vector<float> body_stiff;
+    std::vector<float4> body_rest;
+    pbd::BodyBuffers bodies{};
+
+    // phase census for stage selection
+    uint32_t n_fluid = 0, n_contact = 0;
+
+    int rigid_index = 0;  // next object id for the scene builders
+    float rands[6] = {0, 0, 0, 0, 0, 0};
+
+    // stage timing and launch counters
+    bool profiling = false;
+    bool capturing = false;
+    struct TimedStage {
+        int stage;
+        cudaEvent_t start, stop;
+    };
+    std::vector<TimedStage> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double stage_ms[PBD_STAGE_COUNT] = {};
+    uint64_t stage_launches[PBD_STAGE_COUNT] = {};
+    uint64_t launches = 0;
+    uint64_t steps = 0;
+    uint64_t graph_kernels = 0;  // kernels in the captured step
+
+    // captured step graph
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    float graph_dt = 0.f;
+    uint64_t graph_version = 0;
+    uint64_t version = 1;  // bumped whenever a captured graph would go stale
+
+    std::string err;
+};

@@ -1,0 +1,253 @@
+"""Seeded synthetic scenes (host-side numpy), identical for the CUDA path and
+any checker.  Each builder returns a ``Scene``: parameters plus particle,
+constraint and body arrays in the layout of the C ABI.
+
+Randomness comes from splitmix64 streams keyed by the seed, so every
+consumer gets bit-identical inputs.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PHASE_FLUID, PHASE_GAS, PHASE_CLOTH, PHASE_SOLID, PHASE_RIGID = 0, 1, 2, 3, 4
+FLAG_TWOD = 1
+FLAG_KERNEL_UNITS = 1 << 4
+
+
+def splitmix64(seed: int, count: int) -> np.ndarray:
+    """count uint64 outputs of the splitmix64 generator started at seed."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + idx * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, shape, lo: float, hi: float) -> np.ndarray:
+    n = int(np.prod(shape))
+    u = (splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    return (lo + (hi - lo) * u).reshape(shape)
+
+
+def next_pow2(v: float) -> int:
+    return 1 << max(0, math.ceil(math.log2(max(1.0, v))))
+
+
+@dataclass
+class Scene:
+    name: str
+    params: dict
+    pos_w: np.ndarray                      # (N, 4) float32: xyz, inverse mass
+    phase: np.ndarray                      # (N,) int32
+    vel: np.ndarray | None = None          # (N, 4) float32
+    rest_density: np.ndarray | None = None  # (N,) float32
+    pairs: np.ndarray | None = None        # (M, 2) uint32
+    rest: np.ndarray | None = None         # (M,) float32
+    stiffness: np.ndarray | None = None    # (M,) float32
+    pins: np.ndarray | None = None         # (P,) uint32
+    pin_points: np.ndarray | None = None   # (P, 3) float32
+    bodies: list = field(default_factory=list)  # (first, count, stiffness)
+    dt: float = 1.0 / 60.0
+    info: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos_w.shape[0])
+
+
+def poly6_rest_density(spacing: float, h: float, mass: float = 1.0) -> float:
+    """Sum of poly6 over a cubic lattice (self included), FP64: the rest
+    density at which a perfect lattice of that spacing has C = 0."""
+    c = 315.0 / (64.0 * math.pi * h ** 9)
+    k = int(math.ceil(h / spacing)) + 1
+    rng = np.arange(-k, k + 1)
+    ox, oy, oz = np.meshgrid(rng, rng, rng, indexing="ij")
+    r2 = (ox ** 2 + oy ** 2 + oz ** 2).astype(np.float64) * spacing * spacing
+    r2 = r2[r2 < h * h]
+    return float(mass * np.sum(c * (h * h - r2) ** 3))
+
+
+def dam_break(nx: int = 128, ny: int = 128, nz: int = 64, h: float = 0.1, seed: int = 2024,
+              iterations: int = 4, xsph: float = 0.01) -> Scene:
+    """3-D PBF dam break: an nx*ny*nz fluid block, lattice spacing h/2,
+    jitter U(-0.01h, 0.01h), in the corner of a box four block-widths long
+    in x and twice the block height; cell size h, power-of-two grid.
+
+    Unit mass, rest density = the lattice's poly6 sum; s_corr k = 0.1,
+    n = 4, dq = 0.2 h and relaxation 1 in kernel-radius units
+    (FLAG_KERNEL_UNITS: 100 m^-2 at h = 0.1).  The reference's literal
+    relaxation 0.01 lets particles with few neighbours take lambda ~ 80
+    and the block explodes within one step at this length scale."""
+    s = 0.5 * h
+    r = 0.5 * s
+    ext = np.array([4 * nx * s, 2 * ny * s, nz * s])
+    grid = [next_pow2(ext[k] / h) for k in range(3)]
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    # particle order: x fastest, then y, then z (the reference's lattice loops)
+    lat = np.stack([ii.transpose(2, 1, 0).ravel(), jj.transpose(2, 1, 0).ravel(), kk.transpose(2, 1, 0).ravel()], 1)
+    pos = (lat + 0.5) * s + uniform(seed, lat.shape, -0.01 * h, 0.01 * h)
+    n = pos.shape[0]
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0
+    rho0 = poly6_rest_density(s, h)
+    params = dict(particle_radius=r, kernel_radius=h, cell_size=h, grid_size=grid,
+                  world_origin=[0.0, 0.0, 0.0], gravity=[0.0, -9.8, 0.0], box_min=[0.0, 0.0, 0.0],
+                  box_max=[float(v) for v in ext], iterations=iterations, relaxation=1.0, scorr_k=0.1,
+                  scorr_n=4.0, scorr_dq=0.2, xsph_c=xsph, max_dt=0.05, max_neighbors=500,
+                  flags=FLAG_KERNEL_UNITS)
+    return Scene("dam_break", params, pos_w, np.zeros(n, np.int32),
+                 rest_density=np.full(n, rho0, np.float32), dt=1.0 / 120.0,
+                 info=dict(nx=nx, ny=ny, nz=nz, spacing=s, rho0=rho0, seed=seed))
+
+
+def reference_scene_params(radius=0.25, grid=(64, 64, 64), min_bounds=(-50, 0, -50), max_bounds=(50, 200, 50),
+                           iterations=5) -> dict:
+    """The reference ParticleSystem constants (particleapp.cpp:23-38,
+    particlesystem.cpp:52-66, integration_kernel.cuh:20-42)."""
+    return dict(particle_radius=radius, kernel_radius=2.0, cell_size=2.0 * radius, grid_size=list(grid),
+                world_origin=[0.0, 0.0, 0.0], gravity=[0.0, -9.8, 0.0], box_min=[float(v) for v in min_bounds],
+                box_max=[float(v) for v in max_bounds], iterations=iterations, relaxation=0.01, scorr_k=0.1,
+                scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0, max_dt=0.05, max_neighbors=500,
+                contact_static_friction=0.005, contact_kinetic_friction=0.0002,
+                wall_static_friction=0.005, wall_kinetic_friction=0.0002)
+
+
+def reference_fluid(ll=(-4, 0, -4), ur=(4, 6, 4), radius=0.25, density=1.0, mass=1.0, seed=7,
+                    grid=(64, 64, 64), min_bounds=(-50, 0, -50), max_bounds=(50, 200, 50), jitter=0.01,
+                    iterations=5) -> Scene:
+    """The reference addFluid lattice (spacing 2.5 r, particlesystem.cpp:
+    357-405) with seeded jitter, reference constants (h = 2)."""
+    d = radius * 2.5
+    cnt = [int(float(int(math.ceil(ur[k] - ll[k]))) / d) for k in range(3)]
+    zz, yy, xx = np.meshgrid(np.arange(cnt[2]), np.arange(cnt[1]), np.arange(cnt[0]), indexing="ij")
+    lat = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1).astype(np.float64)
+    pos = np.array(ll, np.float64) + lat * d + uniform(seed, lat.shape, -1.0, 1.0) * (radius * jitter)
+    n = pos.shape[0]
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0 / mass
+    params = reference_scene_params(radius, grid, min_bounds, max_bounds, iterations)
+    return Scene("reference_fluid", params, pos_w, np.zeros(n, np.int32),
+                 rest_density=np.full(n, density, np.float32), dt=1.0 / 60.0)
+
+
+def reference_granular(ll=(-3, 0, -3), ur=(3, 8, 3), radius=0.25, mass=1.0, seed=11, jitter=0.05,
+                       grid=(64, 64, 64), min_bounds=(-50, 0, -50), max_bounds=(50, 200, 50),
+                       iterations=5, spacing_scale=1.95) -> Scene:
+    """A solid-particle stack (addParticleGrid, particlesystem.cpp:408-458)
+    packed slightly tighter than contact distance so contacts are active."""
+    d = radius * spacing_scale
+    cnt = [int(float(int(math.ceil(ur[k] - ll[k]))) / d) for k in range(3)]
+    zz, yy, xx = np.meshgrid(np.arange(cnt[2]), np.arange(cnt[1]), np.arange(cnt[0]), indexing="ij")
+    lat = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1).astype(np.float64)
+    pos = np.array(ll, np.float64) + lat * d + uniform(seed, lat.shape, -1.0, 1.0) * (radius * jitter)
+    pos[:, 1] += radius
+    n = pos.shape[0]
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0 / mass
+    params = reference_scene_params(radius, grid, min_bounds, max_bounds, iterations)
+    return Scene("reference_granular", params, pos_w, np.full(n, PHASE_SOLID, np.int32), dt=1.0 / 60.0)
+
+
+def rope_and_cloth(radius=0.25, seed=3, iterations=5, cloth=(12, 10), ropes=4, links=16) -> Scene:
+    """Ropes and a cloth as the reference builds them (addRope,
+    addHorizCloth; particlesystem.cpp:461-616): object phases RIGID + id,
+    axis distance constraints, pinned starts / one pinned cloth edge.  The
+    constrained particles come first so the reference's segment indexing
+    (solver.cu:227-230) is harmless and the reference can be compared."""
+    params = reference_scene_params(radius, iterations=iterations)
+    pos, ph, pairs, rest, pins, pts = [], [], [], [], [], []
+    obj = 0
+    n0 = 0
+    for r in range(ropes):
+        start = np.array([-6.0 + 3.0 * r, 20.0, 0.5 * r])
+        spacing = np.array([0.45, -0.12, 0.05 * (r + 1)])
+        for i in range(links + 1):
+            pos.append([*(start + i * spacing), 1.0])
+            ph.append(PHASE_RIGID + obj)
+            if i:
+                pairs.append([n0 + i - 1, n0 + i])
+                rest.append(0.4)
+        pins.append(n0)
+        pts.append(start)
+        n0 += links + 1
+        obj += 1
+    cx, cz = cloth
+    for z in range(cz):
+        for x in range(cx):
+            p = n0 + z * cx + x
+            pos.append([5.0 + 0.5 * x, 7.0, -3.0 + 0.5 * z, 1.0 / 3.0])
+            ph.append(PHASE_RIGID + obj)
+            if x > 0:
+                pairs.append([p - 1, p])
+                rest.append(0.3)
+            else:
+                pins.append(p)
+                pts.append(pos[-1][:3])
+            if z > 0:
+                pairs.append([p - cx, p])
+                rest.append(0.3)
+    pos_w = np.asarray(pos, np.float32)
+    jit = uniform(seed, (pos_w.shape[0], 3), -0.01, 0.01)
+    pos_w[:, :3] += jit.astype(np.float32)
+    pts = np.asarray(pts, np.float32)
+    pin_idx = np.asarray(pins, np.uint32)
+    pts = pos_w[pin_idx, :3].copy()
+    return Scene("rope_and_cloth", params, pos_w, np.asarray(ph, np.int32), pairs=np.asarray(pairs, np.uint32),
+                 rest=np.asarray(rest, np.float32), pins=pin_idx, pin_points=pts, dt=1.0 / 60.0)
+
+
+def random_quaternions(seed: int, count: int) -> np.ndarray:
+    """Uniform random unit quaternions (Shoemake's method), (count, 4) xyzw."""
+    u = uniform(seed, (count, 3), 0.0, 1.0)
+    a, b, c = u[:, 0], u[:, 1], u[:, 2]
+    q = np.stack([np.sqrt(1 - a) * np.sin(2 * np.pi * b), np.sqrt(1 - a) * np.cos(2 * np.pi * b),
+                  np.sqrt(a) * np.sin(2 * np.pi * c), np.sqrt(a) * np.cos(2 * np.pi * c)], 1)
+    return q
+
+
+def quat_rotate(q: np.ndarray, v: np.ndarray) -> np.ndarray:
+    x, y, z, w = q[..., 0:1], q[..., 1:2], q[..., 2:3], q[..., 3:4]
+    u = np.concatenate([x, y, z], -1)
+    t = 2.0 * np.cross(u, v)
+    return v + w * t + np.cross(u, t)
+
+
+def rigid_boxes(count=8, side=4, radius=0.25, seed=5, iterations=4, drop_height=6.0, stiffness=1.0) -> Scene:
+    """count shape-matched side^3 boxes at seeded random orientations above
+    the floor, as separate objects (phase RIGID + id)."""
+    params = reference_scene_params(radius, iterations=iterations)
+    d = 2.0 * radius
+    g = (np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3) - (side - 1) / 2.0) * d
+    qs = random_quaternions(seed, count)
+    centers = np.stack([(np.arange(count) % 4) * (side * d * 2.0) - 4.0,
+                        drop_height + (np.arange(count) // 4) * side * d * 2.0,
+                        uniform(seed + 1, (count,), -1.0, 1.0)], 1)
+    pos, ph, bodies = [], [], []
+    for b in range(count):
+        pts = quat_rotate(np.broadcast_to(qs[b], (g.shape[0], 4)), g) + centers[b]
+        bodies.append((len(pos), g.shape[0], stiffness))
+        for p in pts:
+            pos.append([*p, 1.0])
+            ph.append(PHASE_RIGID + b)
+    return Scene("rigid_boxes", params, np.asarray(pos, np.float32), np.asarray(ph, np.int32), bodies=bodies,
+                 dt=1.0 / 60.0)
+
+
+def apply_to(scene: Scene, system, params=None):
+    """Load a Scene into anything with the C ABI's add_* methods (the CUDA
+    ParticleSystem, or a checker with the same surface)."""
+    system.add_particles(scene.pos_w, scene.vel, scene.phase, scene.rest_density)
+    if scene.pairs is not None and len(scene.pairs):
+        system.add_distance_constraints(scene.pairs, scene.rest, scene.stiffness)
+    if scene.pins is not None and len(scene.pins):
+        system.add_point_constraints(scene.pins, scene.pin_points)
+    for first, count, st in scene.bodies:
+        system.add_rigid_body(first, count, st)
+    return system

@@ -1,0 +1,107 @@
+"""Generates the golden fixtures of tests/golden/ from the reference's own
+code: the reference GPU kernels and thrust functors compiled for the CPU
+(oracle/_ref/librefgpu.so, built from gpu/src/cuda/*.cuh in the reference
+tree).  Run where the reference sources exist:
+
+    python tests/golden/make_golden.py
+
+Each fixture holds the seeded inputs of one small scene and the reference's
+outputs after the grid build, each solver stage and full updates.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import refgpu  # noqa: E402
+from particlesolver_gb300 import workloads as W  # noqa: E402
+
+
+def ref_for(scene):
+    p = scene.params
+    r = refgpu.RefGPU(p["particle_radius"], p["grid_size"], [int(v) for v in p["box_min"]],
+                      [int(v) for v in p["box_max"]], p["iterations"])
+    r.add_particles(scene.pos_w, scene.vel, scene.phase, scene.rest_density)
+    if scene.pairs is not None:
+        r.add_distance_constraints(scene.pairs, scene.rest)
+    if scene.pins is not None:
+        r.add_point_constraints(scene.pins, scene.pin_points)
+    return r
+
+
+def scene_inputs(scene) -> dict:
+    d = dict(pos_w=scene.pos_w, phase=scene.phase, dt=np.float32(scene.dt),
+             iterations=np.int32(scene.params["iterations"]))
+    if scene.rest_density is not None:
+        d["rest_density"] = scene.rest_density
+    if scene.pairs is not None:
+        d.update(pairs=scene.pairs, rest=scene.rest)
+    if scene.pins is not None:
+        d.update(pins=scene.pins, pin_points=scene.pin_points)
+    return d
+
+
+def stage_outputs(scene) -> dict:
+    """Reference outputs of one iteration, stage by stage, starting from the
+    scene's positions (no prediction, so both sides share FP32 inputs)."""
+    r = ref_for(scene)
+    r.integrate(np.float32(1e-30))  # records x_old = start positions (no motion at dt ~ 0)
+    r.lib.refgpu_set_positions(r.s, np.ascontiguousarray(
+        np.where(np.arange(4) < 3, scene.pos_w, 1.0).astype(np.float32)).ctypes.data_as(
+        refgpu.ctypes.POINTER(refgpu.ctypes.c_float)))
+    out = {}
+    r.build_grid()
+    sh, si, cs, ce = r.grid()
+    out.update(grid_hash=sh, grid_index=si, cell_start=cs, cell_end=np.where(cs != 0xFFFFFFFF, ce, 0))
+    r.collide()
+    out["after_collide"] = r.positions()
+    r.solve_fluids()
+    out["after_fluids"] = r.positions()
+    out["lambda"] = r.lambdas()
+    r.collide_world()
+    out["after_world"] = r.positions()
+    r.solve_distances()
+    out["after_distance"] = r.positions()
+    r.solve_points()
+    out["after_points"] = r.positions()
+    return out
+
+
+def update_outputs(scene, steps: int) -> dict:
+    r = ref_for(scene)
+    out = {}
+    for k in range(steps):
+        r.update(np.float32(scene.dt))
+        out[f"update{k + 1}_pos"] = r.positions()
+        out[f"update{k + 1}_vel"] = r.velocities()
+    return out
+
+
+def scenes():
+    return {
+        "fluid": W.reference_fluid(ll=(-3, 0, -3), ur=(3, 5, 3), seed=21),
+        "granular": W.reference_granular(ll=(-2, 0, -2), ur=(2, 4, 2), seed=22),
+        "rope_cloth": W.rope_and_cloth(seed=23, cloth=(8, 6), ropes=3, links=10),
+    }
+
+
+def main():
+    if not refgpu.available():
+        raise SystemExit("reference sources not found")
+    for name, sc in scenes().items():
+        data = scene_inputs(sc)
+        data.update(stage_outputs(sc))
+        data.update(update_outputs(sc, 3))
+        path = HERE / f"ref_{name}.npz"
+        np.savez_compressed(path, **data)
+        print(path, path.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

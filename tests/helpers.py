@@ -1,0 +1,101 @@
+"""Shared helpers of the test suite (parameter structs, error metrics)."""
+from __future__ import annotations
+
+import numpy as np
+
+REF_BASE = dict(particle_radius=0.25, kernel_radius=2.0, cell_size=0.5, grid_size=[64, 64, 64],
+                world_origin=[0, 0, 0], gravity=[0, -9.8, 0], box_min=[-50, 0, -50], box_max=[50, 200, 50],
+                iterations=5, max_dt=0.05, relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0,
+                contact_static_friction=0.005, contact_kinetic_friction=0.0002, wall_static_friction=0.005,
+                wall_kinetic_friction=0.0002, max_neighbors=500, twod_z=0.0, flags=0)
+
+
+def params_nolib(d: dict | None = None):
+    """pbd_params filled without loading the CUDA library (CPU tests)."""
+    from particlesolver_gb300 import PbdParams
+
+    base = dict(REF_BASE)
+    base.update(d or {})
+    return PbdParams().update(**base)
+
+
+def norm_err(a, b) -> float:
+    """max_i |a_i - b_i| / max_i |b_i| over all components (vectors flattened)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = np.max(np.abs(b)) if b.size else 0.0
+    if scale == 0.0:
+        return float(np.max(np.abs(a - b))) if a.size else 0.0
+    return float(np.max(np.abs(a - b)) / scale)
+
+
+def displacement(after, before) -> np.ndarray:
+    return np.asarray(after, np.float64)[:, :3] - np.asarray(before, np.float64)[:, :3]
+
+
+def golden_scene(data):
+    """Rebuild the Scene stored in a golden fixture."""
+    from particlesolver_gb300 import workloads as W
+
+    pos_w = data["pos_w"]
+    params = dict(W.reference_scene_params(iterations=int(data["iterations"])))
+    return W.Scene("golden", params, pos_w, data["phase"],
+                   rest_density=data["rest_density"] if "rest_density" in data else None,
+                   pairs=data["pairs"] if "pairs" in data else None,
+                   rest=data["rest"] if "rest" in data else None,
+                   pins=data["pins"] if "pins" in data else None,
+                   pin_points=data["pin_points"] if "pin_points" in data else None,
+                   dt=float(data["dt"]))
+
+
+def run_stages(system) -> dict:
+    """One iteration stage by stage on a freshly loaded system (x_old = the
+    start positions), in the reference's order (particlesystem.cpp:171-232)."""
+    out = {}
+    system.build_grid()
+    sh, si, cs, ce = system.grid()
+    out.update(grid_hash=sh, grid_index=si, cell_start=cs, cell_end=ce)
+    system.collide()
+    out["after_collide"] = system.positions()
+    system.solve_fluids()
+    out["after_fluids"] = system.positions()
+    out["lambda"] = system.lambdas()
+    system.collide_world()
+    out["after_world"] = system.positions()
+    system.solve_distance_constraints()
+    out["after_distance"] = system.positions()
+    system.solve_point_constraints()
+    out["after_points"] = system.positions()
+    return out
+
+
+STAGE_KEYS = ["after_collide", "after_fluids", "after_world", "after_distance", "after_points"]
+
+
+def check_against_golden(out: dict, gold, start, tol: float = 5e-5):
+    """Compare stage outputs of a system with a golden fixture: grid
+    bit-exact, lambda and each stage's displacement within tol (normalised)."""
+    np.testing.assert_array_equal(out["grid_hash"], gold["grid_hash"])
+    np.testing.assert_array_equal(out["grid_index"], gold["grid_index"])
+    np.testing.assert_array_equal(out["cell_start"], gold["cell_start"])
+    np.testing.assert_array_equal(out["cell_end"], gold["cell_end"])
+    assert norm_err(out["lambda"], gold["lambda"]) < max(tol, 1e-5) or np.max(np.abs(gold["lambda"])) == 0
+    prev = start
+    for k in STAGE_KEYS:
+        d_out = displacement(out[k], prev)
+        d_gold = displacement(gold[k], prev)
+        if np.max(np.abs(d_gold)) > 0:
+            assert norm_err(d_out, d_gold) < tol, k
+        else:
+            assert np.max(np.abs(d_out)) < 1e-6, k
+        prev = gold[k]
+
+
+def check_trajectory(pos, gold_pos, start, pct_tol=1e-3):
+    """Invariant-style comparison of positions after full updates."""
+    d = displacement(pos, start)
+    g = displacement(gold_pos, start)
+    scale = np.max(np.abs(g))
+    per = np.linalg.norm(d - g, axis=1) / scale
+    assert np.percentile(per, 90) < pct_tol
+    assert np.max(np.abs(d.mean(0) - g.mean(0))) / scale < pct_tol

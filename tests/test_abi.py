@@ -1,0 +1,95 @@
+"""The C ABI library builds for sm_103a, loads and exports every symbol
+include/pbd.h declares; the ctypes mirror of pbd_params matches the C
+layout.  No GPU needed (nothing here launches work)."""
+import ctypes
+import subprocess
+import textwrap
+from pathlib import Path
+
+import pytest
+
+import particlesolver_gb300 as pbd
+from particlesolver_gb300 import _build
+
+
+def test_library_builds_and_loads():
+    path = _build.build()
+    assert path.exists()
+    lib = pbd.load_library()
+    assert lib.pbd_abi_version() == 1
+
+
+def test_every_header_symbol_is_exported():
+    lib = pbd.load_library()
+    names = pbd.header_functions()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the binding declares a signature for each
+    assert set(names) <= set(pbd._SIGNATURES), set(names) - set(pbd._SIGNATURES)
+
+
+def test_kernels_are_sm103a_only():
+    out = subprocess.run(["cuobjdump", "--list-elf", str(_build.lib_path())], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_params_layout_matches_c(tmp_path):
+    src = tmp_path / "layout.c"
+    fields = [f for f, _ in pbd.PbdParams._fields_]
+    body = "\n".join(f'printf("%zu\\n", offsetof(pbd_params, {f}));' for f in fields)
+    src.write_text(textwrap.dedent(f"""
+        #include <stddef.h>
+        #include <stdio.h>
+        #include "pbd.h"
+        int main(void) {{ printf("%zu\\n", sizeof(pbd_params)); {body} return 0; }}
+    """))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(_build.ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(pbd.PbdParams)
+    for (name, _), off in zip(pbd.PbdParams._fields_, vals[1:]):
+        assert getattr(pbd.PbdParams, name).offset == off, name
+
+
+def test_default_params_are_reference_values():
+    p = pbd.default_params()
+    assert p.particle_radius == 0.25 and p.kernel_radius == 2.0 and p.cell_size == 0.5
+    assert list(p.grid_size) == [64, 64, 64] and p.iterations == 5
+    assert abs(p.relaxation - 0.01) < 1e-9 and p.max_neighbors == 500
+    assert list(p.box_min) == [-50, 0, -50] and list(p.box_max) == [50, 200, 50]
+
+
+def test_create_without_gpu_fails_cleanly():
+    """pbd_create reports a CUDA error instead of exiting when no device
+    is present (skipped on a GPU machine)."""
+    from conftest import cuda_available
+
+    if cuda_available():
+        pytest.skip("GPU present")
+    lib = pbd.load_library()
+    h = ctypes.c_void_p()
+    rc = lib.pbd_create(ctypes.byref(pbd.default_params()), 16, ctypes.byref(h))
+    assert rc == 3  # PBD_ERR_CUDA
+    assert b"CUDA" in lib.pbd_last_error(None) or b"device" in lib.pbd_last_error(None)
+
+
+def test_cpp_drop_in_header_compiles(tmp_path):
+    """include/particle_system.hpp (the reference-shaped C++ class) compiles
+    against the C ABI."""
+    src = tmp_path / "use.cpp"
+    src.write_text(textwrap.dedent("""
+        #include "particle_system.hpp"
+        int main() {
+            pbd::ParticleSystem ps(0.25f, make_uint3(64, 64, 64), 15000, make_int3(-50, 0, -50),
+                                   make_int3(50, 200, 50), 5);
+            ps.addRope(make_float3(0, 20, 0), make_float3(0, -.5f, 0), .4f, 32, 1.f, true);
+            ps.update(1.f / 60);
+            return (int)ps.getNumParticles() == 33 ? 0 : 1;
+        }
+    """))
+    res = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(_build.ROOT / "include"),
+                          "-I", "/usr/local/cuda/include", str(src)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr

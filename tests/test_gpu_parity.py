@@ -1,0 +1,335 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+golden fixtures made from the reference's own kernels.
+
+Tolerances (written per test): grids, sorted indices and cell ranges are
+bit-exact; one projection of one iteration agrees with the FP64 oracle to
+1e-5 as max_i |d_gpu - d_64| / max_i |d_64| over the displacement the stage
+produces; several full steps are compared by invariants (90th percentile of
+the per-particle error and the centre-of-mass motion).
+"""
+import numpy as np
+import pytest
+
+from helpers import (check_against_golden, check_trajectory, displacement, golden_scene, norm_err, run_stages)
+from conftest import GOLDEN
+from oracle import Oracle
+from particlesolver_gb300 import (FLAG_DELTA_OVER_RHO0, FLAG_DENSITY_NEIGHBOR_MASS, FLAG_DISTANCE_MASS_WEIGHTED,
+                                  ParticleSystem, default_params)
+from particlesolver_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL_STAGE = 1e-5
+
+
+def make_pair(scene, **overrides):
+    d = dict(scene.params)
+    d.update(overrides)
+    p = default_params(**d)
+    g = ParticleSystem(p, scene.n)
+    W.apply_to(scene, g)
+    o = Oracle(p, scene.n)
+    W.apply_to(scene, o)
+    return g, o
+
+
+def sync_positions(g, o):
+    """Give the oracle the GPU's FP32 positions (so both sides start from
+    identical inputs and the FP32 grid / neighbour decisions coincide)."""
+    o.set_positions(g.positions().astype(np.float64))
+
+
+# ---------------------------------------------------------------- grid
+
+@pytest.mark.parametrize("builder", [W.reference_fluid, W.reference_granular, W.rope_and_cloth,
+                                     lambda: W.dam_break(24, 20, 12)])
+def test_grid_bit_exact(builder):
+    sc = builder()
+    g, o = make_pair(sc)
+    g.build_grid()
+    o.build_grid()
+    for a, b in zip(g.grid(), o.grid()):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_grid_wraps_and_aliases_like_reference():
+    # particles far outside a tiny power-of-two grid alias into its cells
+    sc = W.reference_fluid(ll=(-4, 0, -4), ur=(4, 4, 4), grid=(4, 8, 2))
+    pos = sc.pos_w.copy()
+    pos[::5, 0] += 37.0
+    pos[::7, 2] -= 23.0
+    sc.pos_w = pos
+    g, o = make_pair(sc)
+    g.build_grid()
+    o.build_grid()
+    for a, b in zip(g.grid(), o.grid()):
+        np.testing.assert_array_equal(a, b)
+    g.solve_fluids()
+    o.solve_fluids()
+    assert norm_err(g.lambdas(), o.lambdas()) < TOL_STAGE
+
+
+def test_empty_and_single_particle():
+    p = default_params()
+    g = ParticleSystem(p, 4)
+    g.update(1 / 60)  # no particles: a no-op
+    g.add_particles(np.array([[1.0, 5.0, 2.0, 1.0]], np.float32), phase=[3])
+    g.update(1 / 60)
+    x = g.positions()
+    assert np.isclose(x[0, 1], 5.0 - 9.8 / 60 / 60, atol=1e-5)
+
+
+# ----------------------------------------------------------------- PBF
+
+@pytest.mark.parametrize("flags", [0, FLAG_DENSITY_NEIGHBOR_MASS, FLAG_DELTA_OVER_RHO0,
+                                   FLAG_DENSITY_NEIGHBOR_MASS | FLAG_DELTA_OVER_RHO0])
+def test_pbf_lambda_and_delta_reference_constants(flags):
+    a = W.reference_fluid(ll=(-4, 0, -3), ur=(4, 3, 3), density=2.0, mass=1.0, seed=1)
+    b = W.reference_fluid(ll=(-4, 3, -3), ur=(4, 6, 3), density=3.0, mass=0.5, seed=2)
+    sc = W.Scene("two", a.params, np.concatenate([a.pos_w, b.pos_w]), np.concatenate([a.phase, b.phase]),
+                 rest_density=np.concatenate([a.rest_density, b.rest_density]))
+    g, o = make_pair(sc, flags=flags)
+    g.build_grid()
+    o.build_grid()
+    g.solve_fluids()
+    o.solve_fluids()
+    assert norm_err(g.lambdas(), o.lambdas()) < TOL_STAGE
+    d_g = displacement(g.positions(), sc.pos_w)
+    d_o = displacement(o.positions(), sc.pos_w)
+    assert norm_err(d_g, d_o) < TOL_STAGE
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 8), (40, 24, 20)])
+def test_pbf_dam_break_block_one_iteration(dims):
+    sc = W.dam_break(*dims)
+    g, o = make_pair(sc)
+    g.integrate(sc.dt)
+    o.integrate(sc.dt)
+    sync_positions(g, o)
+    g.build_grid()
+    o.build_grid()
+    for a, b in zip(g.grid(), o.grid()):
+        np.testing.assert_array_equal(a, b)
+    before = g.positions()
+    g.solve_fluids()
+    o.solve_fluids()
+    assert norm_err(g.lambdas(), o.lambdas()) < TOL_STAGE
+    assert norm_err(displacement(g.positions(), before), displacement(o.positions(), before)) < TOL_STAGE
+
+
+# ------------------------------------------------------------ contacts
+
+def test_contacts_with_friction_and_mass_scaling():
+    sc = W.reference_granular()
+    vel = np.zeros((sc.n, 4), np.float32)
+    vel[:, 0] = 0.3
+    sc.vel = vel
+    g, o = make_pair(sc)
+    g.integrate(sc.dt)
+    o.integrate(sc.dt)
+    sync_positions(g, o)
+    g.build_grid()
+    o.build_grid()
+    before = g.positions()
+    g.collide()
+    o.collide()
+    d_g, d_o = displacement(g.positions(), before), displacement(o.positions(), before)
+    assert np.max(np.abs(d_o)) > 1e-4
+    assert norm_err(d_g, d_o) < TOL_STAGE
+
+
+def test_contacts_between_objects_skip_same_object():
+    sc = W.rope_and_cloth()
+    g, o = make_pair(sc)
+    g.build_grid()
+    o.build_grid()
+    g.collide()
+    o.collide()
+    assert norm_err(displacement(g.positions(), sc.pos_w), displacement(o.positions(), sc.pos_w)) < TOL_STAGE
+
+
+# --------------------------------------------------------------- walls
+
+@pytest.mark.parametrize("twod", [False, True])
+def test_world_walls_with_jitter(twod):
+    from particlesolver_gb300 import FLAG_TWOD
+
+    sc = W.reference_granular(ll=(-3, 0, -3), ur=(3, 2, 3))
+    g, o = make_pair(sc, flags=FLAG_TWOD if twod else 0, twod_z=0.5)
+    jitter = [0.3, 0.7, 0.2, 0.9, 0.5, 0.1]
+    g.set_wall_jitter(jitter)
+    o.set_wall_jitter(jitter)
+    pos = sc.pos_w.copy()
+    pos[:, 0] += 0.01
+    pos[:, 1] -= 0.4
+    pos[::7, 0] = -50.3
+    pos[::11, 2] = 50.6
+    g.set_positions(pos)
+    o.set_positions(pos.astype(np.float64))
+    g.build_grid()
+    o.build_grid()
+    g.collide_world()
+    o.collide_world()
+    np.testing.assert_allclose(g.positions()[:, :3], o.positions()[:, :3], rtol=0, atol=2e-6)
+
+
+# ---------------------------------------------------- distance / pins
+
+@pytest.mark.parametrize("flags", [0, FLAG_DISTANCE_MASS_WEIGHTED])
+def test_distance_constraints_and_pins(flags):
+    sc = W.rope_and_cloth()
+    sc.stiffness = W.uniform(99, (len(sc.rest),), 0.2, 1.0).astype(np.float32)
+    g, o = make_pair(sc, flags=flags)
+    g.integrate(sc.dt)
+    o.integrate(sc.dt)
+    sync_positions(g, o)
+    before = g.positions()
+    g.solve_distance_constraints()
+    o.solve_distance_constraints()
+    d_g, d_o = displacement(g.positions(), before), displacement(o.positions(), before)
+    assert np.max(np.abs(d_o)) > 1e-3
+    assert norm_err(d_g, d_o) < TOL_STAGE
+    g.solve_point_constraints()
+    o.solve_point_constraints()
+    np.testing.assert_array_equal(g.positions()[sc.pins, :3], o.positions()[sc.pins, :3].astype(np.float32))
+
+
+def test_distance_constraints_any_particle_order():
+    """Constrained particles after unconstrained ones (the case the
+    reference's segment indexing got wrong, solver.cu:227-230)."""
+    fl = W.reference_fluid(ll=(-2, 0, -2), ur=(2, 2, 2))
+    rc = W.rope_and_cloth(ropes=2, cloth=(5, 4))
+    off = fl.n
+    sc = W.Scene("mix", fl.params, np.concatenate([fl.pos_w, rc.pos_w]), np.concatenate([fl.phase, rc.phase]),
+                 rest_density=np.concatenate([fl.rest_density, np.ones(rc.n, np.float32)]),
+                 pairs=rc.pairs + off, rest=rc.rest, pins=rc.pins + off, pin_points=rc.pin_points)
+    g, o = make_pair(sc)
+    g.integrate(sc.dt)
+    o.integrate(sc.dt)
+    sync_positions(g, o)
+    before = g.positions()
+    g.solve_distance_constraints()
+    o.solve_distance_constraints()
+    assert norm_err(displacement(g.positions(), before), displacement(o.positions(), before)) < TOL_STAGE
+
+
+# -------------------------------------------------------- shape matching
+
+def test_shape_matching_recovers_rotation():
+    sc = W.rigid_boxes(count=6)
+    g, o = make_pair(sc)
+    noise = W.uniform(77, (sc.n, 3), -0.05, 0.05).astype(np.float32)
+    pos = sc.pos_w.copy()
+    pos[:, :3] += noise
+    g.set_positions(pos)
+    o.set_positions(pos.astype(np.float64))
+    g.solve_shapes()
+    o.solve_shapes()
+    d_g, d_o = displacement(g.positions(), pos), displacement(o.positions(), pos)
+    assert norm_err(d_g, d_o) < 1e-5
+    # a rigid motion of the rest shape (random rotations about each centre)
+    # is a fixed point: the rotation extraction must find it from identity
+    g2, _ = make_pair(sc)
+    rot = sc.pos_w.astype(np.float64).copy()
+    qs = W.random_quaternions(1234, len(sc.bodies))
+    for b, (f, c, _) in enumerate(sc.bodies):
+        com = rot[f:f + c, :3].mean(0)
+        rot[f:f + c, :3] = W.quat_rotate(np.broadcast_to(qs[b], (c, 4)), rot[f:f + c, :3] - com) + com
+    rot = rot.astype(np.float32)
+    g2.set_positions(rot)
+    g2.solve_shapes()
+    assert np.max(np.abs(g2.positions()[:, :3] - rot[:, :3])) < 2e-5
+
+
+# ----------------------------------------------------- velocity / XSPH
+
+def test_velocity_and_xsph():
+    sc = W.dam_break(16, 16, 8)
+    g, o = make_pair(sc)
+    g.update(sc.dt)
+    o.set_positions(g.positions().astype(np.float64))
+    o.set_velocities(g.velocities().astype(np.float64))
+    # velocity from positions, then XSPH, from identical inputs
+    g.build_grid()
+    o.build_grid()
+    g.apply_xsph()
+    o.apply_xsph()
+    assert norm_err(g.velocities()[:, :3], o.velocities()[:, :3]) < TOL_STAGE
+
+
+# ---------------------------------------------------------- full steps
+
+@pytest.mark.parametrize("builder,steps", [(W.reference_fluid, 4), (W.reference_granular, 4),
+                                           (W.rope_and_cloth, 4), (lambda: W.rigid_boxes(count=8), 4),
+                                           (lambda: W.dam_break(16, 16, 8), 6)])
+def test_full_update_trajectory(builder, steps):
+    sc = builder()
+    g, o = make_pair(sc)
+    for _ in range(steps):
+        g.update(sc.dt)
+        o.update(sc.dt)
+    check_trajectory(g.positions(), o.positions(), sc.pos_w)
+
+
+def test_graph_replay_matches_eager_bitwise():
+    sc = W.dam_break(16, 16, 8)
+    a = ParticleSystem(default_params(**sc.params), sc.n)
+    b = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, a)
+    W.apply_to(sc, b)
+    for _ in range(5):
+        a.update(sc.dt)
+    b.update_graph(sc.dt, 5)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+
+
+def test_deterministic_runs():
+    sc = W.reference_granular()
+    runs = []
+    for _ in range(2):
+        g = ParticleSystem(default_params(**sc.params), sc.n)
+        W.apply_to(sc, g)
+        for _ in range(5):
+            g.update(sc.dt)
+        runs.append(g.positions())
+    np.testing.assert_array_equal(runs[0], runs[1])
+
+
+def test_save_load_state_roundtrip():
+    sc = W.rigid_boxes(count=3)
+    g = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, g)
+    g.update(sc.dt)
+    blob = g.save_state()
+    g.update(sc.dt)
+    after = g.positions()
+    g.load_state(blob)
+    g.update(sc.dt)
+    np.testing.assert_array_equal(g.positions(), after)
+
+
+# --------------------------------------------- golden (reference) fixtures
+
+FIXTURES = sorted(GOLDEN.glob("ref_*.npz"))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_stages_match_reference_golden(path):
+    data = np.load(path)
+    sc = golden_scene(data)
+    g = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, g)
+    out = run_stages(g)
+    check_against_golden(out, data, sc.pos_w)
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_updates_match_reference_golden(path):
+    data = np.load(path)
+    sc = golden_scene(data)
+    g = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, g)
+    for k in range(3):
+        g.update(sc.dt)
+        check_trajectory(g.positions(), data[f"update{k + 1}_pos"], sc.pos_w)
