@@ -208,10 +208,17 @@ def run_ours(args, world, rank, local_rank):
 
             dist.barrier()
 
-    # warm-up (captures the step graph on the first call)
+    # warm-up, then the lanes-per-particle choice (autotuned on the warmed-up
+    # state unless --tpp fixes it), then the step graph capture
     warm = max(3, args.warmup)
     for _ in range(warm):
-        sysm.update_graph(sc.dt, 1, sh)
+        sysm.update(sc.dt, sh)
+    if args.tpp:
+        sysm.set_threads_per_particle(args.tpp)
+    else:
+        sysm.autotune(sc.dt, 2, sh)
+    tpp = sysm.threads_per_particle
+    sysm.update_graph(sc.dt, 1, sh)
     torch.cuda.synchronize()
 
     # ---- timed region: K steps, L2 flushed before each, device events
@@ -252,11 +259,14 @@ def run_ours(args, world, rank, local_rank):
     prof = sysm.profile()
     sysm.set_profiling(False)
 
-    # ---- end to end through the public API with host buffers
-    pos_h = torch.from_numpy(sc.pos_w.copy()).pin_memory()
-    vel_h = torch.zeros((n, 4), dtype=torch.float32).pin_memory()
-    out_h = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    # ---- end to end through the public API with host buffers: the caller
+    # owns the state in pinned host memory; every step uploads positions and
+    # velocities, runs the update and downloads both
+    pos_h = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    vel_h = torch.empty((n, 4), dtype=torch.float32).pin_memory()
     lib = sysm.lib
+    sysm._check(lib.pbd_get_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
+    sysm._check(lib.pbd_get_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
     e2e_steps = max(3, min(args.steps, 20))
     torch.cuda.synchronize()
     barrier()
@@ -265,7 +275,8 @@ def run_ours(args, world, rank, local_rank):
         sysm._check(lib.pbd_set_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
         sysm._check(lib.pbd_set_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
         sysm.update_graph(sc.dt, 1, sh)
-        sysm._check(lib.pbd_get_positions(sysm.h, 0, n, out_h.data_ptr(), 0, sh))
+        sysm._check(lib.pbd_get_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
+        sysm._check(lib.pbd_get_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
     e2e_s = time.perf_counter() - t0
     if world > 1:
         import torch.distributed as dist
@@ -310,6 +321,7 @@ def run_ours(args, world, rank, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, splitmix64)",
         "config": {"workload": f"pbf_dam_break_{n}", "particles": n, "lattice": [args.nx, args.ny, args.nz],
                    "h": 0.1, "iterations": 4, "grid_rebuild": "every iteration", "xsph_c": 0.01,
+                   "threads_per_particle": tpp, "tpp_source": "fixed" if args.tpp else "autotuned",
                    "dt": sc.dt, "l2": "flushed before each timed step (256 MiB write)",
                    "timing": "per-step CUDA events on the launching stream, CUDA graph replay",
                    "particle_iterations_per_s": value * n * 4,
@@ -320,7 +332,7 @@ def run_ours(args, world, rank, local_rank):
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "stage_ms_per_step": {k: v / prof_steps for k, v in prof["stage_ms"].items()},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * n, "d2h_bytes_per_step": 16 * n,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * n, "d2h_bytes_per_step": 2 * 16 * n,
                 "steps": e2e_steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
@@ -339,6 +351,7 @@ def main():
     ap.add_argument("--ny", type=int, default=128)
     ap.add_argument("--nz", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tpp", type=int, default=0, help="lanes per particle (0 = autotune)")
     ap.add_argument("--ref-budget-s", type=float, default=120.0)
     args = ap.parse_args()
     world, rank, local_rank = dist_env()

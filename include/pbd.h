@@ -250,6 +250,25 @@ int pbd_check_finite(pbd_system *sys, void *stream);
 /* Blocks until the system's work on stream is done. */
 int pbd_synchronize(pbd_system *sys, void *stream);
 
+/* --------------------------------------------------------------- tuning */
+
+/* Launch shape of the neighbour passes (no counterpart in the reference,
+ * which launched one thread per particle, integration.cu:362,471).  Results
+ * do not depend on it beyond FP32 summation order. */
+typedef struct pbd_tuning {
+    uint32_t threads_per_particle; /* lanes sharing one particle's neighbour
+                                      walk: 1, 2, 4, 8, 16 or 32            */
+    uint32_t reserved[7];          /* zero                                  */
+} pbd_tuning;
+
+int pbd_set_tuning(pbd_system *sys, const pbd_tuning *tuning);
+int pbd_get_tuning(const pbd_system *sys, pbd_tuning *out);
+/* Times `steps` updates of the current scene for every threads_per_particle
+ * choice, starting each trial from a device snapshot of the state, then
+ * restores the state and keeps the fastest choice (written to *chosen if
+ * not NULL).  Synchronous. */
+int pbd_autotune(pbd_system *sys, float dt, uint32_t steps, void *stream, pbd_tuning *chosen);
+
 /* --------------------------------------------------------------- timing */
 
 /* Kernel groups of one step, for the per-stage device timing (no

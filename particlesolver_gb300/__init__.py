@@ -96,6 +96,10 @@ class PbdDeviceBuffers(ctypes.Structure):
 STAGES = ["predict", "grid", "lambda", "solve", "distance", "shapes", "velocity", "xsph"]
 
 
+class PbdTuning(ctypes.Structure):
+    _fields_ = [("threads_per_particle", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 7)]
+
+
 class PbdProfile(ctypes.Structure):
     _fields_ = [
         ("stage_ms", ctypes.c_double * 8),
@@ -164,6 +168,9 @@ _SIGNATURES = {
     "pbd_get_lambdas": ([_P, _PF], _I),
     "pbd_check_finite": ([_P, _P], _I),
     "pbd_synchronize": ([_P, _P], _I),
+    "pbd_set_tuning": ([_P, ctypes.POINTER(PbdTuning)], _I),
+    "pbd_get_tuning": ([_P, ctypes.POINTER(PbdTuning)], _I),
+    "pbd_autotune": ([_P, _F, _U32, _P, ctypes.POINTER(PbdTuning)], _I),
     "pbd_set_profiling": ([_P, _I], _I),
     "pbd_get_profile": ([_P, ctypes.POINTER(PbdProfile)], _I),
     "pbd_reset_profile": ([_P], _I),
@@ -418,6 +425,24 @@ class ParticleSystem:
         out = np.empty(self.num_particles, np.float32)
         self._check(self.lib.pbd_get_lambdas(self.h, out.ctypes.data_as(_PF)))
         return out
+
+    def set_threads_per_particle(self, tpp: int):
+        t = PbdTuning()
+        t.threads_per_particle = int(tpp)
+        self._check(self.lib.pbd_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, dt: float, steps: int = 2, stream: int | None = None) -> int:
+        """Pick the fastest lanes-per-particle for the current scene (state
+        is restored afterwards); returns the choice."""
+        t = PbdTuning()
+        self._check(self.lib.pbd_autotune(self.h, dt, steps, stream, ctypes.byref(t)))
+        return int(t.threads_per_particle)
+
+    @property
+    def threads_per_particle(self) -> int:
+        t = PbdTuning()
+        self._check(self.lib.pbd_get_tuning(self.h, ctypes.byref(t)))
+        return int(t.threads_per_particle)
 
     def set_profiling(self, enable: bool = True):
         self._check(self.lib.pbd_set_profiling(self.h, int(enable)))

@@ -207,6 +207,85 @@ __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uin
     sorted_x[i] = x[sorted_idx[i]];
 }
 
+// -------------------------------------------------------- group walking
+
+// A group of TPP consecutive lanes of a warp shares one particle: lane l
+// takes candidates b + l, b + l + TPP, ... of every stencil range, so each
+// step of the walk is one coalesced TPP x 16-byte load and TPP independent
+// neighbour tests.  Partial sums are combined with xor shuffles inside the
+// group.  TPP = 1 is the reference's thread-per-particle walk.
+template <int TPP>
+struct Group {
+    int lane;       // lane inside the group
+    int wl;         // lane inside the warp
+    unsigned mask;  // the group's lanes
+    __device__ __forceinline__ Group() {
+        wl = threadIdx.x & 31;
+        lane = wl & (TPP - 1);
+        mask = (TPP == 32) ? 0xffffffffu : (((1u << TPP) - 1u) << (wl & ~(TPP - 1)));
+    }
+    __device__ __forceinline__ float sum(float v) const {
+#pragma unroll
+        for (int o = TPP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+        return v;
+    }
+    __device__ __forceinline__ unsigned ballot(bool p) const {
+        return (TPP == 1) ? (p ? (1u << wl) : 0u) : (__ballot_sync(mask, p) & mask);
+    }
+};
+
+// Walks the (2 rad + 1)^3 stencil around cell g in the reference's order
+// (z outer, y, x inner, ascending sorted index; integration_kernel.cuh:
+// 388-398, 549-559).  accept(j) runs the neighbour test of this lane's
+// candidate; the first `cap` accepted candidates in visiting order are
+// passed to use(j) (the reference's neighbour cap, integration_kernel.cuh:
+// 344,508).  Returns the group's neighbour count (identical in every lane).
+// A stencil row whose cells do not wrap is one contiguous index range of
+// the dense cell offsets; a wrapping row is walked cell by cell, which also
+// repeats aliased cells as the reference does.
+template <int TPP, class Accept, class Use>
+__device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<TPP> &G, int3 g, int rad,
+                                               const uint32_t *__restrict__ cell_first, uint32_t cap,
+                                               Accept &&accept, Use &&use) {
+    uint32_t nb = 0;
+    auto range = [&](uint32_t b, uint32_t e) -> bool {
+        for (uint32_t base = b; base < e; base += TPP) {
+            const uint32_t j = base + (uint32_t)G.lane;
+            bool ok = (j < e) && accept(j);
+            const unsigned m = G.ballot(ok);
+            const uint32_t cnt = (uint32_t)__popc(m);
+            if (nb + cnt >= cap) {
+                const uint32_t keep = cap - nb;
+                ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < keep;
+                if (ok) use(j);
+                nb = cap;
+                return false;
+            }
+            if (ok) use(j);
+            nb += cnt;
+        }
+        return true;
+    };
+    for (int dz = -rad; dz <= rad; ++dz) {
+        const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
+        for (int dy = -rad; dy <= rad; ++dy) {
+            const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
+            const uint32_t row = (z * P.gy + y) * P.gx;
+            const int x0 = g.x - rad, x1 = g.x + rad;
+            if (x0 >= 0 && x1 < (int)P.gx) {
+                if (!range(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u)))
+                    return nb;
+            } else {
+                for (int dx = -rad; dx <= rad; ++dx) {
+                    const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
+                    if (!range(__ldg(cell_first + c), __ldg(cell_first + c + 1u))) return nb;
+                }
+            }
+        }
+    }
+    return nb;
+}
+
 // ----------------------------------------------------------------- lambda
 
 // findLambdasD + collideCellRadius (integration_kernel.cuh:481-593): for a
@@ -217,33 +296,38 @@ __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uin
 // lambda = -(rho / rho0 - 1) / (sum |grad_j|^2 + |sum grad_j|^2 + eps).
 // Non-fluid particles get lambda = 0 (the reference left their slots
 // unwritten and read whatever was there, integration_kernel.cuh:636).
+template <int TPP>
 __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
                                                    const float4 *__restrict__ sx,
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
                                                    float *__restrict__ lambda) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const Group<TPP> G;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
     const SortedAttr a = sattr[i];
     if (a.phase != kFluid) {
-        lambda[i] = 0.f;
+        if (G.lane == 0) lambda[i] = 0.f;
         return;
     }
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
     const float w = pi4.w;
     const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
-    uint32_t nb = 0;
+    const float inv_rho0 = 1.f / a.rho0;
     float ro = 0.f, denom = 0.f;
     float3 grad = make_float3(0.f, 0.f, 0.f);
-    const float inv_rho0 = 1.f / a.rho0;
-    for_each_candidate(P, grid_pos(P, pi), P.fluid_rad, cell_first, [&](uint32_t j) {
-        if (j == i) return true;
-        const float4 pj4 = sx[j];
-        const float d2 = dist2_exact(pi, f3(pj4));
-        if (d2 < P.h2) {
-            if (nb >= P.max_nb) return false;
-            ++nb;
+    float4 pj4;
+    float d2;
+    group_walk<TPP>(
+        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb,
+        [&](uint32_t j) {
+            if (j == i) return false;
+            pj4 = sx[j];
+            d2 = dist2_exact(pi, f3(pj4));
+            return d2 < P.h2;
+        },
+        [&](uint32_t) {
             const float3 r = pi - f3(pj4);
             const float rlen = sqrtf(d2);
             const float hm2 = P.h2 - d2;
@@ -256,12 +340,17 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
             sg = sg * inv_rho0;
             grad -= sg;
             denom += dot3(sg, sg);
-        }
-        return true;
-    });
-    ro += P.poly6_self / w;
-    denom += dot3(grad, grad);
-    lambda[i] = -(ro * inv_rho0 - 1.f) / (denom + P.relax);
+        });
+    ro = G.sum(ro);
+    denom = G.sum(denom);
+    grad.x = G.sum(grad.x);
+    grad.y = G.sum(grad.y);
+    grad.z = G.sum(grad.z);
+    if (G.lane == 0) {
+        ro += P.poly6_self / w;
+        denom += dot3(grad, grad);
+        lambda[i] = -(ro * inv_rho0 - 1.f) / (denom + P.relax);
+    }
 }
 
 // --------------------------------------------------------- fused particle
@@ -278,21 +367,26 @@ __device__ __forceinline__ float scorr_pow(const DevParams &P, float ratio) {
 // solveFluidsD (integration_kernel.cuh:596-642): same neighbour set as the
 // lambda pass; delta = sum (lambda_i + lambda_j + s_corr) spiky(r) with
 // s_corr = -k (W(r) / W(dq h))^n and the (0, EPS, 0) direction for r ~ 0;
-// divided by (rho0 + n) (or rho0 with PBD_FLAG_DELTA_OVER_RHO0).
-__device__ __forceinline__ float3 fluid_delta(const DevParams &P, uint32_t i, float3 pi,
+// divided by (rho0 + n) (or rho0 with PBD_FLAG_DELTA_OVER_RHO0).  Every
+// lane of the group returns the group's total.
+template <int TPP>
+__device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float3 pi,
                                               float rho0, const float4 *__restrict__ sx,
                                               const float *__restrict__ lambda,
                                               const uint32_t *__restrict__ cell_first) {
     const float lam_i = lambda[i];
-    uint32_t nb = 0;
     float3 delta = make_float3(0.f, 0.f, 0.f);
-    for_each_candidate(P, grid_pos(P, pi), P.fluid_rad, cell_first, [&](uint32_t j) {
-        if (j == i) return true;
-        const float3 pj = f3(sx[j]);
-        const float d2 = dist2_exact(pi, pj);
-        if (d2 < P.h2) {
-            if (nb >= P.max_nb) return false;
-            ++nb;
+    float3 pj;
+    float d2;
+    const uint32_t nb = group_walk<TPP>(
+        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb,
+        [&](uint32_t j) {
+            if (j == i) return false;
+            pj = f3(sx[j]);
+            d2 = dist2_exact(pi, pj);
+            return d2 < P.h2;
+        },
+        [&](uint32_t j) {
             const float3 r = pi - pj;
             const float rlen = sqrtf(d2);
             const float hm2 = P.h2 - d2;
@@ -302,17 +396,12 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, uint32_t i, fl
             const float ratio = P.poly6 * hm2 * hm2 * hm2 * P.scorr_inv_ref;
             const float corr = -P.scorr_k * scorr_pow(P, ratio);
             delta += (lam_i + lambda[j] + corr) * sg;
-        }
-        return true;
-    });
+        });
+    delta.x = G.sum(delta.x);
+    delta.y = G.sum(delta.y);
+    delta.z = G.sum(delta.z);
     const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
     return delta / div;
-}
-
-__device__ __forceinline__ bool contact_candidate(const DevParams &P, int ph, int phj, float3 pi,
-                                                  float3 pj) {
-    if (ph > kSolid && ph == phj) return false;
-    return dist2_exact(pi, pj) < P.collide2;
 }
 
 __device__ __forceinline__ float scaled_inv_mass(float w, float y) {
@@ -326,39 +415,34 @@ __device__ __forceinline__ float scaled_inv_mass(float w, float y) {
 // w e^y (both evaluated at this particle's y, as in the reference) and get
 // static/kinetic friction against the start-of-step positions.  Pairs with
 // zero total inverse mass or zero separation are skipped (the reference
-// produced NaN there).
-__device__ __forceinline__ float3 contact_delta(const DevParams &P, uint32_t i, float4 pi4, int ph,
-                                                uint32_t orig, const float4 *__restrict__ sx,
+// produced NaN there).  Two walks: the count, then the corrections.
+template <int TPP>
+__device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float4 pi4,
+                                                int ph, uint32_t orig, const float4 *__restrict__ sx,
                                                 const SortedAttr *__restrict__ sattr,
                                                 const uint32_t *__restrict__ sidx,
                                                 const uint32_t *__restrict__ cell_first,
                                                 const float4 *__restrict__ x_old) {
     const float3 pi = f3(pi4);
     const int3 g = grid_pos(P, pi);
-    uint32_t nb = 0;
-    for_each_candidate(P, g, 1, cell_first, [&](uint32_t j) {
-        if (j == i) return true;
-        if (contact_candidate(P, ph, sattr[j].phase, pi, f3(sx[j]))) {
-            if (nb >= P.max_nb) return false;
-            ++nb;
-        }
-        return true;
-    });
+    float4 pj4;
+    int phj;
+    auto accept = [&](uint32_t j) {
+        if (j == i) return false;
+        phj = sattr[j].phase;
+        if (ph > kSolid && ph == phj) return false;
+        pj4 = sx[j];
+        return dist2_exact(pi, f3(pj4)) < P.collide2;
+    };
+    const uint32_t nb = group_walk<TPP>(P, G, g, 1, cell_first, P.max_nb, accept, [](uint32_t) {});
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
     const float w = pi4.w;
     const float sw = scaled_inv_mass(w, pi.y);
     const float3 prev = f3(x_old[orig]);
     const float fnb = (float)nb;
-    uint32_t seen = 0;
-    for_each_candidate(P, g, 1, cell_first, [&](uint32_t j) {
-        if (j == i) return true;
-        const float4 pj4 = sx[j];
-        const int phj = sattr[j].phase;
+    group_walk<TPP>(P, G, g, 1, cell_first, nb, accept, [&](uint32_t j) {
         const float3 pj = f3(pj4);
-        if (!contact_candidate(P, ph, phj, pi, pj)) return true;
-        if (seen >= nb) return false;
-        ++seen;
         const float3 diff = pi - pj;
         const float dist = len3(diff);
         const float mag = dist - P.collide_dist;
@@ -368,23 +452,25 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, uint32_t i, 
             colw2 = scaled_inv_mass(pj4.w, pi.y);
         }
         const float wsum = colw + colw2;
-        if (wsum == 0.f || dist == 0.f) return true;
+        if (wsum == 0.f || dist == 0.f) return;
         const float scale = mag / wsum;
         const float3 dp = diff * (scale / dist);
         const float3 dp1 = (-colw * dp) / fnb;
         const float3 dp2 = (colw2 * dp) / fnb;
         delta += dp1;
-        if (ph < kSolid || phj < kSolid) return true;
+        if (ph < kSolid || phj < kSolid) return;
         const float3 prev2 = f3(x_old[sidx[j]]);
         const float3 nf = diff * rsqrtf(dot3(diff, diff));
         const float3 dprel = (pi + dp1 - prev) - (prev + dp2 - prev2);
         const float3 dpt = dprel - nf * dot3(dprel, nf);
         const float ldpt = len3(dpt);
-        if (ldpt < kEps) return true;
+        if (ldpt < kEps) return;
         if (ldpt < P.cs * dist) delta -= dpt * colw / wsum;
         else delta -= dpt * fminf(P.ck * dist / ldpt, 1.f);
-        return true;
     });
+    delta.x = G.sum(delta.x);
+    delta.y = G.sum(delta.y);
+    delta.z = G.sum(delta.z);
     return delta;
 }
 
@@ -438,11 +524,12 @@ __device__ __forceinline__ float3 world_collide(const DevParams &P, float3 e, in
     return e;
 }
 
-// One thread per sorted particle: the reference's collide, the delta half of
+// One group per sorted particle: the reference's collide, the delta half of
 // solveFluids and collideWorld, which touch disjoint particle sets and read
 // only the sorted start-of-iteration positions, fused into one pass with one
 // write per particle.  mask selects the stages (the stage entry points run
 // them one at a time).
+template <int TPP>
 __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint32_t mask,
                                                   const float4 *__restrict__ sx,
                                                   const SortedAttr *__restrict__ sattr,
@@ -451,7 +538,8 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
                                                   const float *__restrict__ lambda,
                                                   const float4 *__restrict__ x_old,
                                                   float4 *__restrict__ x) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const Group<TPP> G;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
     const SortedAttr a = sattr[i];
     const uint32_t orig = sidx[i];
@@ -459,12 +547,13 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
     float3 np = f3(pi4);
     bool touched = false;
     if ((mask & kDoFluid) && a.phase == kFluid) {
-        np = np + fluid_delta(P, i, np, a.rho0, sx, lambda, cell_first);
+        np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sx, lambda, cell_first);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
-        np = np + contact_delta(P, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
+        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
         touched = true;
     }
+    if (G.lane != 0) return;
     if (mask & kDoWorld) {
         if (!touched) np = f3(x[orig]);
         np = world_collide(P, np, a.phase, x_old, orig);
@@ -700,6 +789,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph_gather(uint32_t n, const uint32
 // dimensionless with the rest density: v_i += c sum_j m_j (v_j - v_i)
 // poly6(x_i - x_j) / rho0_i over fluid neighbours within h at the final
 // positions, candidates taken from the last grid.
+template <int TPP>
 __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const float4 *__restrict__ sx,
                                                  const SortedAttr *__restrict__ sattr,
                                                  const uint32_t *__restrict__ sidx,
@@ -707,7 +797,8 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
                                                  const float4 *__restrict__ xs,
                                                  const float4 *__restrict__ vs,
                                                  float4 *__restrict__ v) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const Group<TPP> G;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
     const SortedAttr a = sattr[i];
     if (a.phase != kFluid) return;
@@ -715,20 +806,25 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
     const float4 vi4 = vs[i];
     const float3 vi = f3(vi4);
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    uint32_t nb = 0;
-    for_each_candidate(P, grid_pos(P, f3(sx[i])), P.fluid_rad, cell_first, [&](uint32_t j) {
-        if (j == i || sattr[j].phase != kFluid) return true;
-        const float4 xj4 = xs[j];
-        const float d2 = dist2_exact(xi, f3(xj4));
-        if (d2 < P.h2) {
-            if (nb >= P.max_nb) return false;
-            ++nb;
+    float4 xj4;
+    float d2;
+    group_walk<TPP>(
+        P, G, grid_pos(P, f3(sx[i])), P.fluid_rad, cell_first, P.max_nb,
+        [&](uint32_t j) {
+            if (j == i || sattr[j].phase != kFluid) return false;
+            xj4 = xs[j];
+            d2 = dist2_exact(xi, f3(xj4));
+            return d2 < P.h2;
+        },
+        [&](uint32_t j) {
             const float hm2 = P.h2 - d2;
             const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
             acc += (f3(vs[j]) - vi) * wgt;
-        }
-        return true;
-    });
+        });
+    acc.x = G.sum(acc.x);
+    acc.y = G.sum(acc.y);
+    acc.z = G.sum(acc.z);
+    if (G.lane != 0) return;
     const float3 nv = vi + acc * (P.xsph_c / a.rho0);
     v[sidx[i]] = make_float4(nv.x, nv.y, nv.z, vi4.w);
 }
@@ -794,18 +890,29 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
     return cudaGetLastError();
 }
 
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float *lambda,
+// Dispatches a kernel template over the supported group sizes.
+#define PBD_TPP_DISPATCH(tpp, KERNEL, ...)                                             \
+    switch (tpp) {                                                                     \
+    case 1: KERNEL<1><<<blocks_for(n * 1u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 2: KERNEL<2><<<blocks_for(n * 2u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 4: KERNEL<4><<<blocks_for(n * 4u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 8: KERNEL<8><<<blocks_for(n * 8u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 16: KERNEL<16><<<blocks_for(n * 16u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
+    default: KERNEL<32><<<blocks_for(n * 32u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
+    }
+
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float *lambda, uint32_t tpp,
                           cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_lambda<<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, lambda);
+    PBD_TPP_DISPATCH(tpp, k_lambda, P, n, g.sorted_x, g.sorted_attr, g.cell_first, lambda);
     return cudaGetLastError();
 }
 
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
-                         const float *lambda, const float4 *x_old, float4 *x, cudaStream_t s) {
+                         const float *lambda, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_solve<<<blocks_for(n), kBlock, 0, s>>>(P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx,
-                                             g.cell_first, lambda, x_old, x);
+    PBD_TPP_DISPATCH(tpp, k_solve, P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, lambda,
+                     x_old, x);
     return cudaGetLastError();
 }
 
@@ -838,11 +945,10 @@ cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 
 }
 
 cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
-                        float4 *v, float4 *xs_final, float4 *vs, cudaStream_t s) {
+                        float4 *v, float4 *xs_final, float4 *vs, uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, x, v, xs_final, vs);
-    k_xsph<<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first,
-                                            xs_final, vs, v);
+    PBD_TPP_DISPATCH(tpp, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, xs_final, vs, v);
     return cudaGetLastError();
 }
 

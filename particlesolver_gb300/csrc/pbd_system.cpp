@@ -375,11 +375,11 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
         if (int rc = build_grid(s, st, it == 0)) return rc;
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
-            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->lambda, st));
+            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->lambda, s->tpp, st));
         }
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
-            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->lambda, s->x_old, s->x, st));
+            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->lambda, s->x_old, s->x, s->tpp, st));
         }
         if (dist_kernels) {
             Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
@@ -396,7 +396,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     }
     if (s->params.xsph_c != 0.f && s->n_fluid && s->params.iterations > 0) {
         Stage t(s, st, PBD_STAGE_XSPH, 2);
-        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->x, s->v, s->xs_final, s->vs, st));
+        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->x, s->v, s->xs_final, s->vs, s->tpp, st));
     }
     ++s->steps;
     return PBD_OK;
@@ -791,6 +791,98 @@ int pbd_update_graph(pbd_system *s, float dt, uint32_t nsteps, void *stream) {
     return PBD_OK;
 }
 
+int pbd_set_tuning(pbd_system *s, const pbd_tuning *t) {
+    if (int rc = check_sys(s)) return rc;
+    if (!t) return fail(s, PBD_ERR_INVALID_ARGUMENT, "tuning is NULL");
+    const uint32_t k = t->threads_per_particle;
+    if (!(k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32))
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "threads_per_particle must be 1, 2, 4, 8, 16 or 32");
+    s->tpp = k;
+    ++s->version;
+    return PBD_OK;
+}
+
+int pbd_get_tuning(const pbd_system *s, pbd_tuning *out) {
+    if (!s || !out) return PBD_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof *out);
+    out->threads_per_particle = s->tpp;
+    return PBD_OK;
+}
+
+int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuning *chosen) {
+    SYS_GUARD(s);
+    if (!(dt > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t n = s->n;
+    if (n == 0 || steps == 0) {
+        if (chosen) pbd_get_tuning(s, chosen);
+        return PBD_OK;
+    }
+    dt = clamp_dt(s, dt);
+    float4 *snap_x = nullptr, *snap_v = nullptr, *snap_q = nullptr;
+    const uint32_t nb = s->bodies.count;
+    auto release = [&]() {
+        dfree(snap_x);
+        dfree(snap_v);
+        dfree(snap_q);
+    };
+    if (dalloc(&snap_x, n) != cudaSuccess || dalloc(&snap_v, n) != cudaSuccess ||
+        (nb && dalloc(&snap_q, nb) != cudaSuccess)) {
+        release();
+        return fail(s, PBD_ERR_CUDA, "autotune: snapshot allocation failed");
+    }
+    auto copy = [&](bool save) -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(save ? snap_x : s->x, save ? s->x : snap_x, n * sizeof(float4),
+                                        cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(save ? snap_v : s->v, save ? s->v : snap_v, n * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess && nb)
+            e = cudaMemcpyAsync(save ? snap_q : s->bodies.quat, save ? s->bodies.quat : snap_q,
+                                nb * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+        return e;
+    };
+    cudaEvent_t a = nullptr, b = nullptr;
+    int rc = PBD_OK;
+    const uint32_t saved_tpp = s->tpp;
+    const bool saved_prof = s->profiling;
+    s->profiling = false;
+    uint32_t best = saved_tpp;
+    float best_ms = 0.f;
+    if (copy(true) != cudaSuccess || cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        rc = fail(s, PBD_ERR_CUDA, "autotune: setup failed");
+    }
+    const uint32_t choices[] = {1, 2, 4, 8, 16, 32};
+    for (uint32_t k = 0; rc == PBD_OK && k < 6; ++k) {
+        s->tpp = choices[k];
+        if (copy(false) != cudaSuccess || (rc = enqueue_update(s, dt, st)) != PBD_OK) break;  // untimed warm-up
+        if (copy(false) != cudaSuccess) break;
+        cudaEventRecord(a, st);
+        for (uint32_t i = 0; i < steps && rc == PBD_OK; ++i) rc = enqueue_update(s, dt, st);
+        cudaEventRecord(b, st);
+        float ms = 0.f;
+        if (rc || cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+            if (!rc) rc = fail(s, PBD_ERR_CUDA, "autotune: timing failed");
+            break;
+        }
+        if (k == 0 || ms < best_ms) {
+            best_ms = ms;
+            best = choices[k];
+        }
+    }
+    if (copy(false) != cudaSuccess && !rc) rc = fail(s, PBD_ERR_CUDA, "autotune: restore failed");
+    if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = fail(s, PBD_ERR_CUDA, "autotune: sync failed");
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    release();
+    s->profiling = saved_prof;
+    s->tpp = rc ? saved_tpp : best;
+    s->grid_valid = false;
+    ++s->version;
+    if (chosen) pbd_get_tuning(s, chosen);
+    return rc;
+}
+
 int pbd_set_profiling(pbd_system *s, int enable) {
     if (int rc = check_sys(s)) return rc;
     s->profiling = enable != 0;
@@ -841,7 +933,7 @@ int pbd_collide(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->lambda, s->x_old, s->x,
-                                  (cudaStream_t)stream));
+                                  s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
 }
@@ -850,8 +942,8 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->lambda, st));
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->lambda, s->x_old, s->x, st));
+    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->lambda, s->tpp, st));
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->lambda, s->x_old, s->x, s->tpp, st));
     s->launches += 2;
     return PBD_OK;
 }
@@ -860,7 +952,7 @@ int pbd_collide_world(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->lambda, s->x_old, s->x,
-                                  (cudaStream_t)stream));
+                                  s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
 }
@@ -895,7 +987,7 @@ int pbd_apply_xsph(pbd_system *s, void *stream) {
     if (int rc = need_grid(s)) return rc;
     if (!s->xs_final) return PBD_OK;  // no fluid
     CUDA_TRY(s, pbd::launch_xsph(s->dev, s->n, s->grid, s->x, s->v, s->xs_final, s->vs,
-                                 (cudaStream_t)stream));
+                                 s->tpp, (cudaStream_t)stream));
     return PBD_OK;
 }
 

@@ -43,6 +43,7 @@ struct pbd_system {
     // phase census for stage selection
     uint32_t n_fluid = 0, n_contact = 0;
 
+    uint32_t tpp = 8;     // lanes per particle in the neighbour passes
     int rigid_index = 0;  // next object id for the scene builders
     float rands[6] = {0, 0, 0, 0, 0, 0};
 

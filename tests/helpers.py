@@ -33,6 +33,24 @@ def displacement(after, before) -> np.ndarray:
     return np.asarray(after, np.float64)[:, :3] - np.asarray(before, np.float64)[:, :3]
 
 
+def assert_projection(after_gpu, after_64, before, rel: float = 1e-5):
+    """One projection of the FP32 path against the FP64 replay: every
+    component of the correction agrees to rel * max|correction| plus one
+    FP32 ulp of the stored coordinate (the FP32 result is a rounded
+    position; the replay's is exact)."""
+    d_g = displacement(after_gpu, before)
+    d_o = displacement(after_64, before)
+    coord = np.abs(np.asarray(after_64, np.float64)[:, :3]).astype(np.float32)
+    ulp = np.spacing(coord).astype(np.float64)
+    bound = rel * np.max(np.abs(d_o)) + ulp
+    excess = np.abs(d_g - d_o) - bound
+    worst = np.unravel_index(np.argmax(excess), excess.shape)
+    assert np.max(excess) <= 0.0, (
+        f"correction error {np.abs(d_g - d_o)[worst]:.3e} at {worst} exceeds {bound[worst]:.3e} "
+        f"(max correction {np.max(np.abs(d_o)):.3e}, normalised error {norm_err(d_g, d_o):.3e})")
+    return norm_err(d_g, d_o)
+
+
 def golden_scene(data):
     """Rebuild the Scene stored in a golden fixture."""
     from particlesolver_gb300 import workloads as W
