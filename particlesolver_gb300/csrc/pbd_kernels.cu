@@ -234,55 +234,77 @@ struct Group {
     }
 };
 
+// Accepted neighbours are not processed inside the candidate loop: each
+// lane appends their sorted indices to its own column of a shared-memory
+// buffer and runs the per-neighbour arithmetic as a dense loop whenever the
+// column fills and once at the end.  Only ~15 % of the stencil's candidates
+// are neighbours, so evaluating the heavy arithmetic inside the candidate
+// loop would run it under divergence on almost every step.
+constexpr int kNbBuf = 32;
+
+struct NbBuffer {
+    uint32_t *col;  // this thread's column, stride kBlock
+    __device__ __forceinline__ uint32_t get(uint32_t k) const { return col[k * kBlock]; }
+    __device__ __forceinline__ void put(uint32_t k, uint32_t j) const { col[k * kBlock] = j; }
+};
+
 // Walks the (2 rad + 1)^3 stencil around cell g in the reference's order
 // (z outer, y, x inner, ascending sorted index; integration_kernel.cuh:
 // 388-398, 549-559).  accept(j) runs the neighbour test of this lane's
-// candidate; the first `cap` accepted candidates in visiting order are
-// passed to use(j) (the reference's neighbour cap, integration_kernel.cuh:
-// 344,508).  Returns the group's neighbour count (identical in every lane).
-// A stencil row whose cells do not wrap is one contiguous index range of
-// the dense cell offsets; a wrapping row is walked cell by cell, which also
-// repeats aliased cells as the reference does.
-template <int TPP, class Accept, class Use>
+// candidate; the first `cap` accepted candidates of the group in visiting
+// order are buffered and handed to flush(count) (the reference's
+// neighbour cap, integration_kernel.cuh:344,508).  Returns the group's
+// neighbour count (identical in every lane of the group).  A stencil row
+// whose cells do not wrap is one contiguous index range of the dense cell
+// offsets; a wrapping row is walked cell by cell, which also repeats
+// aliased cells as the reference does.
+template <int TPP, class Accept, class Flush>
 __device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<TPP> &G, int3 g, int rad,
                                                const uint32_t *__restrict__ cell_first, uint32_t cap,
-                                               Accept &&accept, Use &&use) {
-    uint32_t nb = 0;
-    auto range = [&](uint32_t b, uint32_t e) -> bool {
+                                               const NbBuffer &buf, Accept &&accept, Flush &&flush) {
+    uint32_t nb = 0, cnt = 0;
+    bool open = true;
+    auto range = [&](uint32_t b, uint32_t e) {
         for (uint32_t base = b; base < e; base += TPP) {
             const uint32_t j = base + (uint32_t)G.lane;
             bool ok = (j < e) && accept(j);
             const unsigned m = G.ballot(ok);
-            const uint32_t cnt = (uint32_t)__popc(m);
-            if (nb + cnt >= cap) {
-                const uint32_t keep = cap - nb;
-                ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < keep;
-                if (ok) use(j);
-                nb = cap;
-                return false;
+            const uint32_t total = (uint32_t)__popc(m);
+            if (nb + total >= cap) {
+                ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < cap - nb;
+                open = false;
             }
-            if (ok) use(j);
-            nb += cnt;
+            if (ok) {
+                buf.put(cnt++, j);
+                if (cnt == kNbBuf) {
+                    flush(cnt);
+                    cnt = 0;
+                }
+            }
+            if (!open) {
+                nb = cap;
+                return;
+            }
+            nb += total;
         }
-        return true;
     };
-    for (int dz = -rad; dz <= rad; ++dz) {
+    for (int dz = -rad; dz <= rad && open; ++dz) {
         const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
-        for (int dy = -rad; dy <= rad; ++dy) {
+        for (int dy = -rad; dy <= rad && open; ++dy) {
             const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
             const uint32_t row = (z * P.gy + y) * P.gx;
             const int x0 = g.x - rad, x1 = g.x + rad;
             if (x0 >= 0 && x1 < (int)P.gx) {
-                if (!range(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u)))
-                    return nb;
+                range(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u));
             } else {
-                for (int dx = -rad; dx <= rad; ++dx) {
+                for (int dx = -rad; dx <= rad && open; ++dx) {
                     const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
-                    if (!range(__ldg(cell_first + c), __ldg(cell_first + c + 1u))) return nb;
+                    range(__ldg(cell_first + c), __ldg(cell_first + c + 1u));
                 }
             }
         }
     }
+    if (cnt) flush(cnt);
     return nb;
 }
 
@@ -302,6 +324,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
                                                    float *__restrict__ lambda) {
+    __shared__ uint32_t nbuf[kNbBuf * kBlock];
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -310,36 +333,34 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
         if (G.lane == 0) lambda[i] = 0.f;
         return;
     }
+    const NbBuffer buf{nbuf + threadIdx.x};
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
-    const float w = pi4.w;
     const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
+    const float inv_w = 1.f / pi4.w;
     const float inv_rho0 = 1.f / a.rho0;
+    const float spiky_r = -P.spiky * inv_rho0;  // spiky coefficient over rho0
     float ro = 0.f, denom = 0.f;
     float3 grad = make_float3(0.f, 0.f, 0.f);
-    float4 pj4;
-    float d2;
     group_walk<TPP>(
-        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb,
-        [&](uint32_t j) {
-            if (j == i) return false;
-            pj4 = sx[j];
-            d2 = dist2_exact(pi, f3(pj4));
-            return d2 < P.h2;
-        },
-        [&](uint32_t) {
-            const float3 r = pi - f3(pj4);
-            const float rlen = sqrtf(d2);
-            const float hm2 = P.h2 - d2;
-            const float hm = P.h - rlen;
-            const float wpoly = P.poly6 * hm2 * hm2 * hm2;
-            if (nb_mass) ro += (pj4.w > 0.f) ? wpoly / pj4.w : 0.f;
-            else ro += wpoly / w;
-            float3 sg = make_float3(0.f, 0.f, 0.f);
-            if (rlen >= kMinSpikyLen) sg = (r / rlen) * (-P.spiky * hm * hm);
-            sg = sg * inv_rho0;
-            grad -= sg;
-            denom += dot3(sg, sg);
+        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb, buf,
+        [&](uint32_t j) { return j != i && dist2_exact(pi, f3(sx[j])) < P.h2; },
+        [&](uint32_t cnt) {
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const float4 pj4 = sx[buf.get(k)];
+                const float3 r = pi - f3(pj4);
+                const float d2 = dist2_exact(pi, f3(pj4));
+                const float rlen = sqrtf(d2);
+                const float hm2 = P.h2 - d2;
+                const float hm = P.h - rlen;
+                const float wpoly = P.poly6 * hm2 * hm2 * hm2;
+                ro += nb_mass ? ((pj4.w > 0.f) ? wpoly / pj4.w : 0.f) : wpoly * inv_w;
+                if (rlen >= kMinSpikyLen) {
+                    const float3 sg = r * (spiky_r * hm * hm / rlen);
+                    grad -= sg;
+                    denom += dot3(sg, sg);
+                }
+            }
         });
     ro = G.sum(ro);
     denom = G.sum(denom);
@@ -347,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
     grad.y = G.sum(grad.y);
     grad.z = G.sum(grad.z);
     if (G.lane == 0) {
-        ro += P.poly6_self / w;
+        ro += P.poly6_self * inv_w;
         denom += dot3(grad, grad);
         lambda[i] = -(ro * inv_rho0 - 1.f) / (denom + P.relax);
     }
@@ -370,32 +391,30 @@ __device__ __forceinline__ float scorr_pow(const DevParams &P, float ratio) {
 // divided by (rho0 + n) (or rho0 with PBD_FLAG_DELTA_OVER_RHO0).  Every
 // lane of the group returns the group's total.
 template <int TPP>
-__device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float3 pi,
-                                              float rho0, const float4 *__restrict__ sx,
-                                              const float *__restrict__ lambda,
+__device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, const NbBuffer &buf,
+                                              uint32_t i, float3 pi, float rho0,
+                                              const float4 *__restrict__ sx, const float *__restrict__ lambda,
                                               const uint32_t *__restrict__ cell_first) {
     const float lam_i = lambda[i];
     float3 delta = make_float3(0.f, 0.f, 0.f);
-    float3 pj;
-    float d2;
     const uint32_t nb = group_walk<TPP>(
-        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb,
-        [&](uint32_t j) {
-            if (j == i) return false;
-            pj = f3(sx[j]);
-            d2 = dist2_exact(pi, pj);
-            return d2 < P.h2;
-        },
-        [&](uint32_t j) {
-            const float3 r = pi - pj;
-            const float rlen = sqrtf(d2);
-            const float hm2 = P.h2 - d2;
-            const float hm = P.h - rlen;
-            const float s = -P.spiky * hm * hm;
-            const float3 sg = (rlen < kMinSpikyLen) ? make_float3(0.f, kEps * s, 0.f) : (r / rlen) * s;
-            const float ratio = P.poly6 * hm2 * hm2 * hm2 * P.scorr_inv_ref;
-            const float corr = -P.scorr_k * scorr_pow(P, ratio);
-            delta += (lam_i + lambda[j] + corr) * sg;
+        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb, buf,
+        [&](uint32_t j) { return j != i && dist2_exact(pi, f3(sx[j])) < P.h2; },
+        [&](uint32_t cnt) {
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const uint32_t j = buf.get(k);
+                const float3 pj = f3(sx[j]);
+                const float3 r = pi - pj;
+                const float d2 = dist2_exact(pi, pj);
+                const float rlen = sqrtf(d2);
+                const float hm2 = P.h2 - d2;
+                const float hm = P.h - rlen;
+                const float s = -P.spiky * hm * hm;
+                const float3 sg = (rlen < kMinSpikyLen) ? make_float3(0.f, kEps * s, 0.f) : r * (s / rlen);
+                const float ratio = P.poly6 * hm2 * hm2 * hm2 * P.scorr_inv_ref;
+                const float corr = -P.scorr_k * scorr_pow(P, ratio);
+                delta += (lam_i + lambda[j] + corr) * sg;
+            }
         });
     delta.x = G.sum(delta.x);
     delta.y = G.sum(delta.y);
@@ -415,33 +434,40 @@ __device__ __forceinline__ float scaled_inv_mass(float w, float y) {
 // w e^y (both evaluated at this particle's y, as in the reference) and get
 // static/kinetic friction against the start-of-step positions.  Pairs with
 // zero total inverse mass or zero separation are skipped (the reference
-// produced NaN there).  Two walks: the count, then the corrections.
+// produced NaN there).  The corrections need the final contact count, so
+// the first walk only counts and buffers; when the count fits the buffer
+// the corrections run from it, otherwise a second walk revisits them.
 template <int TPP>
-__device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float4 pi4,
-                                                int ph, uint32_t orig, const float4 *__restrict__ sx,
+__device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, const NbBuffer &buf,
+                                                uint32_t i, float4 pi4, int ph, uint32_t orig,
+                                                const float4 *__restrict__ sx,
                                                 const SortedAttr *__restrict__ sattr,
                                                 const uint32_t *__restrict__ sidx,
                                                 const uint32_t *__restrict__ cell_first,
                                                 const float4 *__restrict__ x_old) {
     const float3 pi = f3(pi4);
     const int3 g = grid_pos(P, pi);
-    float4 pj4;
-    int phj;
     auto accept = [&](uint32_t j) {
         if (j == i) return false;
-        phj = sattr[j].phase;
+        const int phj = sattr[j].phase;
         if (ph > kSolid && ph == phj) return false;
-        pj4 = sx[j];
-        return dist2_exact(pi, f3(pj4)) < P.collide2;
+        return dist2_exact(pi, f3(sx[j])) < P.collide2;
     };
-    const uint32_t nb = group_walk<TPP>(P, G, g, 1, cell_first, P.max_nb, accept, [](uint32_t) {});
+    uint32_t kept = 0;
+    bool overflow = false;
+    const uint32_t nb = group_walk<TPP>(P, G, g, 1, cell_first, P.max_nb, buf, accept, [&](uint32_t cnt) {
+        if (cnt == (uint32_t)kNbBuf) overflow = true;
+        kept = cnt;
+    });
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
     const float w = pi4.w;
     const float sw = scaled_inv_mass(w, pi.y);
     const float3 prev = f3(x_old[orig]);
     const float fnb = (float)nb;
-    group_walk<TPP>(P, G, g, 1, cell_first, nb, accept, [&](uint32_t j) {
+    auto correct = [&](uint32_t j) {
+        const float4 pj4 = sx[j];
+        const int phj = sattr[j].phase;
         const float3 pj = f3(pj4);
         const float3 diff = pi - pj;
         const float dist = len3(diff);
@@ -467,7 +493,16 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
         if (ldpt < kEps) return;
         if (ldpt < P.cs * dist) delta -= dpt * colw / wsum;
         else delta -= dpt * fminf(P.ck * dist / ldpt, 1.f);
-    });
+    };
+    // the group agrees on whether any lane overflowed its column
+    const bool redo = G.ballot(overflow) != 0u;
+    if (!redo) {
+        for (uint32_t k = 0; k < kept; ++k) correct(buf.get(k));
+    } else {
+        group_walk<TPP>(P, G, g, 1, cell_first, nb, buf, accept, [&](uint32_t cnt) {
+            for (uint32_t k = 0; k < cnt; ++k) correct(buf.get(k));
+        });
+    }
     delta.x = G.sum(delta.x);
     delta.y = G.sum(delta.y);
     delta.z = G.sum(delta.z);
@@ -538,19 +573,21 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
                                                   const float *__restrict__ lambda,
                                                   const float4 *__restrict__ x_old,
                                                   float4 *__restrict__ x) {
+    __shared__ uint32_t nbuf[kNbBuf * kBlock];
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
+    const NbBuffer buf{nbuf + threadIdx.x};
     const SortedAttr a = sattr[i];
     const uint32_t orig = sidx[i];
     const float4 pi4 = sx[i];
     float3 np = f3(pi4);
     bool touched = false;
     if ((mask & kDoFluid) && a.phase == kFluid) {
-        np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sx, lambda, cell_first);
+        np = np + fluid_delta<TPP>(P, G, buf, i, np, a.rho0, sx, lambda, cell_first);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
-        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
+        np = np + contact_delta<TPP>(P, G, buf, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
         touched = true;
     }
     if (G.lane != 0) return;
@@ -712,20 +749,23 @@ __global__ void __launch_bounds__(kBlock) k_shapes(uint32_t bodies, const uint4 
     if (b >= bodies) return;
     const uint4 rg = range[b];
     const uint32_t first = rg.x, count = rg.y, roff = rg.z;
+    // centre of mass accumulated relative to the body's first particle, so
+    // the FP32 sums carry offsets of the body's size, not of its position
+    const float3 o = f3(x[first]);
     float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
     for (uint32_t k = lane; k < count; k += 32) {
         const float4 p = x[first + k];
         const float m = rest[roff + k].w;
-        sx += m * p.x;
-        sy += m * p.y;
-        sz += m * p.z;
+        sx += m * (p.x - o.x);
+        sy += m * (p.y - o.y);
+        sz += m * (p.z - o.z);
         sm += m;
     }
     sx = warp_sum(sx);
     sy = warp_sum(sy);
     sz = warp_sum(sz);
     sm = warp_sum(sm);
-    const float3 c = make_float3(sx / sm, sy / sm, sz / sm);
+    const float3 c = make_float3(o.x + sx / sm, o.y + sy / sm, o.z + sz / sm);
     float A[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     for (uint32_t k = lane; k < count; k += 32) {
         const float4 p = x[first + k];
@@ -749,12 +789,13 @@ __global__ void __launch_bounds__(kBlock) k_shapes(uint32_t bodies, const uint4 
     for (uint32_t k = lane; k < count; k += 32) {
         float4 p = x[first + k];
         const float4 r = rest[roff + k];
-        const float gx = c.x + R[0][0] * r.x + R[0][1] * r.y + R[0][2] * r.z;
-        const float gy = c.y + R[1][0] * r.x + R[1][1] * r.y + R[1][2] * r.z;
-        const float gz = c.z + R[2][0] * r.x + R[2][1] * r.y + R[2][2] * r.z;
-        p.x += (gx - p.x) * st;
-        p.y += (gy - p.y) * st;
-        p.z += (gz - p.z) * st;
+        // goal minus position formed from small terms: (c - x) + R q
+        const float gx = (c.x - p.x) + (R[0][0] * r.x + R[0][1] * r.y + R[0][2] * r.z);
+        const float gy = (c.y - p.y) + (R[1][0] * r.x + R[1][1] * r.y + R[1][2] * r.z);
+        const float gz = (c.z - p.z) + (R[2][0] * r.x + R[2][1] * r.y + R[2][2] * r.z);
+        p.x += gx * st;
+        p.y += gy * st;
+        p.z += gz * st;
         x[first + k] = p;
     }
 }
@@ -797,29 +838,28 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
                                                  const float4 *__restrict__ xs,
                                                  const float4 *__restrict__ vs,
                                                  float4 *__restrict__ v) {
+    __shared__ uint32_t nbuf[kNbBuf * kBlock];
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
     const SortedAttr a = sattr[i];
     if (a.phase != kFluid) return;
+    const NbBuffer buf{nbuf + threadIdx.x};
     const float3 xi = f3(xs[i]);
     const float4 vi4 = vs[i];
     const float3 vi = f3(vi4);
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    float4 xj4;
-    float d2;
     group_walk<TPP>(
-        P, G, grid_pos(P, f3(sx[i])), P.fluid_rad, cell_first, P.max_nb,
-        [&](uint32_t j) {
-            if (j == i || sattr[j].phase != kFluid) return false;
-            xj4 = xs[j];
-            d2 = dist2_exact(xi, f3(xj4));
-            return d2 < P.h2;
-        },
-        [&](uint32_t j) {
-            const float hm2 = P.h2 - d2;
-            const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
-            acc += (f3(vs[j]) - vi) * wgt;
+        P, G, grid_pos(P, f3(sx[i])), P.fluid_rad, cell_first, P.max_nb, buf,
+        [&](uint32_t j) { return j != i && sattr[j].phase == kFluid && dist2_exact(xi, f3(xs[j])) < P.h2; },
+        [&](uint32_t cnt) {
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const uint32_t j = buf.get(k);
+                const float4 xj4 = xs[j];
+                const float hm2 = P.h2 - dist2_exact(xi, f3(xj4));
+                const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
+                acc += (f3(vs[j]) - vi) * wgt;
+            }
         });
     acc.x = G.sum(acc.x);
     acc.y = G.sum(acc.y);
