@@ -194,7 +194,7 @@ def run_ours(args, world, rank, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    sc = W.dam_break(args.nx, args.ny, args.nz)
+    sc = W.dam_break(args.nx, args.ny, args.nz, cell_div=args.cell_div)
     n = sc.n
     sysm = ParticleSystem(default_params(**sc.params), n)
     W.apply_to(sc, sysm)
@@ -321,6 +321,7 @@ def run_ours(args, world, rank, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, splitmix64)",
         "config": {"workload": f"pbf_dam_break_{n}", "particles": n, "lattice": [args.nx, args.ny, args.nz],
                    "h": 0.1, "iterations": 4, "grid_rebuild": "every iteration", "xsph_c": 0.01,
+                   "cell_size": sc.params["cell_size"], "grid": sc.params["grid_size"],
                    "threads_per_particle": tpp, "tpp_source": "fixed" if args.tpp else "autotuned",
                    "dt": sc.dt, "l2": "flushed before each timed step (256 MiB write)",
                    "timing": "per-step CUDA events on the launching stream, CUDA graph replay",
@@ -352,6 +353,7 @@ def main():
     ap.add_argument("--nz", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tpp", type=int, default=0, help="lanes per particle (0 = autotune)")
+    ap.add_argument("--cell-div", type=int, default=1, help="grid cell size = h / cell_div")
     ap.add_argument("--ref-budget-s", type=float, default=120.0)
     args = ap.parse_args()
     world, rank, local_rank = dist_env()

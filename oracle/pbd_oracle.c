@@ -27,7 +27,7 @@
 #endif
 
 #define K_EPS 0.001            /* EPS, integration_kernel.cuh:20        */
-#define K_MIN_SPIKY 0.0001f    /* integration_kernel.cuh:580,625        */
+#define K_MIN_SPIKY2 1e-8f     /* |r| < 1e-4, integration_kernel.cuh:580,625, decided on |r|^2 */
 #define K_MIN_DIST 0.0001      /* solver_kernel.cuh:57                  */
 #define K_SHAPE_ITERS 24
 
@@ -389,8 +389,7 @@ static void compute_lambdas(orc_system *s) {
                 else ro += wpoly / w;
                 double sg[3] = {0, 0, 0};
                 /* the cut-off is decided on the FP32 length, as the kernel does */
-                float rl32 = sqrtf(dist2f(s->sx32 + 4 * i, s->sx32 + 4 * list[k]));
-                if (rl32 >= K_MIN_SPIKY)
+                if (dist2f(s->sx32 + 4 * i, s->sx32 + 4 * list[k]) >= K_MIN_SPIKY2)
                     for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * (-s->spiky * hm * hm);
                 for (int d = 0; d < 3; ++d) {
                     sg[d] /= rho0;
@@ -423,8 +422,7 @@ static void fluid_delta(const orc_system *s, uint32_t i, uint32_t *list, double 
         double hm2 = h2 - r2, hm = h - rlen;
         double sc = -s->spiky * hm * hm;
         double sg[3];
-        float rl32 = sqrtf(dist2f(s->sx32 + 4 * i, s->sx32 + 4 * j));
-        if (rl32 < K_MIN_SPIKY) {
+        if (dist2f(s->sx32 + 4 * i, s->sx32 + 4 * j) < K_MIN_SPIKY2) {
             sg[0] = 0; sg[1] = K_EPS * sc; sg[2] = 0;
         } else {
             for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * sc;

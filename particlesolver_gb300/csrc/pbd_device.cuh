@@ -29,7 +29,7 @@ enum : uint32_t { kDoContact = 1u, kDoFluid = 2u, kDoWorld = 4u };
 // 319, 580, 626; solver_kernel.cuh:57).
 constexpr float kEps = 0.001f;           // EPS
 constexpr float kCollideScale = 2.001f;  // collideDist = r * 2.001
-constexpr float kMinSpikyLen = 0.0001f;  // spiky gradient cut-off
+constexpr float kMinSpiky2 = 1e-8f;      // spiky gradient cut-off |r|^2 < (1e-4)^2
 constexpr float kMinDistLen = 0.0001f;   // distance constraint cut-off
 
 struct DevParams {

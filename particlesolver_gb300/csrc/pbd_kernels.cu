@@ -210,10 +210,9 @@ __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uin
 // -------------------------------------------------------- group walking
 
 // A group of TPP consecutive lanes of a warp shares one particle: lane l
-// takes candidates b + l, b + l + TPP, ... of every stencil range, so each
-// step of the walk is one coalesced TPP x 16-byte load and TPP independent
-// neighbour tests.  Partial sums are combined with xor shuffles inside the
-// group.  TPP = 1 is the reference's thread-per-particle walk.
+// takes candidates b + l, b + l + TPP, ... of every stencil range (one
+// coalesced TPP x 16-byte load per step), and partial sums meet in xor
+// shuffles.  TPP = 1 is the reference's thread-per-particle walk.
 template <int TPP>
 struct Group {
     int lane;       // lane inside the group
@@ -234,77 +233,109 @@ struct Group {
     }
 };
 
-// Accepted neighbours are not processed inside the candidate loop: each
-// lane appends their sorted indices to its own column of a shared-memory
-// buffer and runs the per-neighbour arithmetic as a dense loop whenever the
-// column fills and once at the end.  Only ~15 % of the stencil's candidates
-// are neighbours, so evaluating the heavy arithmetic inside the candidate
-// loop would run it under divergence on almost every step.
-constexpr int kNbBuf = 32;
+// Distance from coordinate p to the unwrapped cell k of one axis.
+__device__ __forceinline__ float slab_gap(float p, float origin, float cell, int k) {
+    const float lo = origin + (float)k * cell;
+    return fmaxf(fmaxf(lo - p, p - (lo + cell)), 0.f);
+}
 
-struct NbBuffer {
-    uint32_t *col;  // this thread's column, stride kBlock
-    __device__ __forceinline__ uint32_t get(uint32_t k) const { return col[k * kBlock]; }
-    __device__ __forceinline__ void put(uint32_t k, uint32_t j) const { col[k * kBlock] = j; }
-};
-
-// Walks the (2 rad + 1)^3 stencil around cell g in the reference's order
-// (z outer, y, x inner, ascending sorted index; integration_kernel.cuh:
-// 388-398, 549-559).  accept(j) runs the neighbour test of this lane's
-// candidate; the first `cap` accepted candidates of the group in visiting
-// order are buffered and handed to flush(count) (the reference's
-// neighbour cap, integration_kernel.cuh:344,508).  Returns the group's
-// neighbour count (identical in every lane of the group).  A stencil row
-// whose cells do not wrap is one contiguous index range of the dense cell
-// offsets; a wrapping row is walked cell by cell, which also repeats
-// aliased cells as the reference does.
-template <int TPP, class Accept, class Flush>
-__device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<TPP> &G, int3 g, int rad,
+// Walks the (2 rad + 1)^3 stencil around the cell of q in the reference's
+// order (z outer, y, x inner, ascending sorted index; integration_kernel.
+// cuh:388-398, 549-559).  Stencil rows and cells whose box lies farther
+// than the interaction reach from q (with a 1e-4 relative margin) are
+// skipped: they hold no neighbours, so the neighbour sequence -- and the
+// first-`cap` rule of the reference's neighbour cap (integration_kernel.cuh:
+// 344,508) -- is unchanged.  trim = false walks every stencil cell (for
+// passes whose candidate positions have left their cells).  A row whose
+// kept cells do not wrap is one contiguous range of the dense cell offsets;
+// a wrapping row is walked cell by cell, which also repeats aliased cells
+// as the reference does.  test(j, q_j, d2) decides a candidate (this lane's
+// candidate j with its position and squared distance); accepted ones within
+// the cap go to use(j, q_j, d2).  Returns the group's neighbour count.
+template <int TPP, class Test, class Use>
+__device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<TPP> &G, float3 q, int3 g,
+                                               int rad, float reach2, bool trim,
+                                               const float4 *__restrict__ pos,
                                                const uint32_t *__restrict__ cell_first, uint32_t cap,
-                                               const NbBuffer &buf, Accept &&accept, Flush &&flush) {
-    uint32_t nb = 0, cnt = 0;
+                                               Test &&test, Use &&use) {
+    const float lim = reach2 * 1.0001f + 1e-30f;
+    uint32_t nb = 0;
     bool open = true;
     auto range = [&](uint32_t b, uint32_t e) {
-        for (uint32_t base = b; base < e; base += TPP) {
-            const uint32_t j = base + (uint32_t)G.lane;
-            bool ok = (j < e) && accept(j);
-            const unsigned m = G.ballot(ok);
-            const uint32_t total = (uint32_t)__popc(m);
-            if (nb + total >= cap) {
-                ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < cap - nb;
-                open = false;
-            }
-            if (ok) {
-                buf.put(cnt++, j);
-                if (cnt == kNbBuf) {
-                    flush(cnt);
-                    cnt = 0;
+        if (TPP == 1) {
+            for (uint32_t j = b; j < e; ++j) {
+                const float4 pj = pos[j];
+                const float d2 = dist2_exact(q, f3(pj));
+                if (test(j, pj, d2)) {
+                    if (nb >= cap) {
+                        open = false;
+                        return;
+                    }
+                    ++nb;
+                    use(j, pj, d2);
                 }
             }
-            if (!open) {
-                nb = cap;
-                return;
+        } else {
+            for (uint32_t base = b; base < e; base += TPP) {
+                const uint32_t j = base + (uint32_t)G.lane;
+                float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+                float d2 = 0.f;
+                bool ok = false;
+                if (j < e) {
+                    pj = pos[j];
+                    d2 = dist2_exact(q, f3(pj));
+                    ok = test(j, pj, d2);
+                }
+                const unsigned m = G.ballot(ok);
+                const uint32_t total = (uint32_t)__popc(m);
+                if (nb + total >= cap) {
+                    ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < cap - nb;
+                    open = false;
+                }
+                if (ok) use(j, pj, d2);
+                if (!open) {
+                    nb = cap;
+                    return;
+                }
+                nb += total;
             }
-            nb += total;
         }
     };
     for (int dz = -rad; dz <= rad && open; ++dz) {
+        const float gz = trim ? slab_gap(q.z, P.origin.z, P.cell, g.z + dz) : 0.f;
+        const float gz2 = gz * gz;
+        if (gz2 > lim) continue;
         const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
         for (int dy = -rad; dy <= rad && open; ++dy) {
+            const float gy = trim ? slab_gap(q.y, P.origin.y, P.cell, g.y + dy) : 0.f;
+            const float gyz2 = gz2 + gy * gy;
+            if (gyz2 > lim) continue;
+            int xa = -rad, xb = rad;
+            if (trim) {
+                while (xa < 0) {
+                    const float gx = slab_gap(q.x, P.origin.x, P.cell, g.x + xa);
+                    if (gyz2 + gx * gx <= lim) break;
+                    ++xa;
+                }
+                while (xb > 0) {
+                    const float gx = slab_gap(q.x, P.origin.x, P.cell, g.x + xb);
+                    if (gyz2 + gx * gx <= lim) break;
+                    --xb;
+                }
+            }
             const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
             const uint32_t row = (z * P.gy + y) * P.gx;
-            const int x0 = g.x - rad, x1 = g.x + rad;
+            const int x0 = g.x + xa, x1 = g.x + xb;
             if (x0 >= 0 && x1 < (int)P.gx) {
                 range(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u));
             } else {
-                for (int dx = -rad; dx <= rad && open; ++dx) {
+                for (int dx = xa; dx <= xb && open; ++dx) {
                     const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
                     range(__ldg(cell_first + c), __ldg(cell_first + c + 1u));
                 }
             }
         }
     }
-    if (cnt) flush(cnt);
     return nb;
 }
 
@@ -318,13 +349,13 @@ __device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<T
 // lambda = -(rho / rho0 - 1) / (sum |grad_j|^2 + |sum grad_j|^2 + eps).
 // Non-fluid particles get lambda = 0 (the reference left their slots
 // unwritten and read whatever was there, integration_kernel.cuh:636).
+// Per neighbour: one reciprocal square root and no division.
 template <int TPP>
 __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
                                                    const float4 *__restrict__ sx,
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
                                                    float *__restrict__ lambda) {
-    __shared__ uint32_t nbuf[kNbBuf * kBlock];
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -333,7 +364,6 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
         if (G.lane == 0) lambda[i] = 0.f;
         return;
     }
-    const NbBuffer buf{nbuf + threadIdx.x};
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
     const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
@@ -343,23 +373,18 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
     float ro = 0.f, denom = 0.f;
     float3 grad = make_float3(0.f, 0.f, 0.f);
     group_walk<TPP>(
-        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb, buf,
-        [&](uint32_t j) { return j != i && dist2_exact(pi, f3(sx[j])) < P.h2; },
-        [&](uint32_t cnt) {
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const float4 pj4 = sx[buf.get(k)];
-                const float3 r = pi - f3(pj4);
-                const float d2 = dist2_exact(pi, f3(pj4));
-                const float rlen = sqrtf(d2);
-                const float hm2 = P.h2 - d2;
-                const float hm = P.h - rlen;
-                const float wpoly = P.poly6 * hm2 * hm2 * hm2;
-                ro += nb_mass ? ((pj4.w > 0.f) ? wpoly / pj4.w : 0.f) : wpoly * inv_w;
-                if (rlen >= kMinSpikyLen) {
-                    const float3 sg = r * (spiky_r * hm * hm / rlen);
-                    grad -= sg;
-                    denom += dot3(sg, sg);
-                }
+        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, true, sx, cell_first, P.max_nb,
+        [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+        [&](uint32_t, const float4 &pj4, float d2) {
+            const float hm2 = P.h2 - d2;
+            const float wpoly = P.poly6 * hm2 * hm2 * hm2;
+            ro += nb_mass ? ((pj4.w > 0.f) ? wpoly / pj4.w : 0.f) : wpoly * inv_w;
+            if (d2 >= kMinSpiky2) {
+                const float rs = rsqrtf(d2);
+                const float hm = P.h - d2 * rs;
+                const float3 sg = (pi - f3(pj4)) * (spiky_r * hm * hm * rs);
+                grad -= sg;
+                denom += dot3(sg, sg);
             }
         });
     ro = G.sum(ro);
@@ -391,29 +416,27 @@ __device__ __forceinline__ float scorr_pow(const DevParams &P, float ratio) {
 // divided by (rho0 + n) (or rho0 with PBD_FLAG_DELTA_OVER_RHO0).  Every
 // lane of the group returns the group's total.
 template <int TPP>
-__device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, const NbBuffer &buf,
-                                              uint32_t i, float3 pi, float rho0,
-                                              const float4 *__restrict__ sx, const float *__restrict__ lambda,
+__device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float3 pi,
+                                              float rho0, const float4 *__restrict__ sx,
+                                              const float *__restrict__ lambda,
                                               const uint32_t *__restrict__ cell_first) {
     const float lam_i = lambda[i];
     float3 delta = make_float3(0.f, 0.f, 0.f);
+    const float poly6_ref = P.poly6 * P.scorr_inv_ref;
     const uint32_t nb = group_walk<TPP>(
-        P, G, grid_pos(P, pi), P.fluid_rad, cell_first, P.max_nb, buf,
-        [&](uint32_t j) { return j != i && dist2_exact(pi, f3(sx[j])) < P.h2; },
-        [&](uint32_t cnt) {
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const uint32_t j = buf.get(k);
-                const float3 pj = f3(sx[j]);
-                const float3 r = pi - pj;
-                const float d2 = dist2_exact(pi, pj);
-                const float rlen = sqrtf(d2);
-                const float hm2 = P.h2 - d2;
-                const float hm = P.h - rlen;
-                const float s = -P.spiky * hm * hm;
-                const float3 sg = (rlen < kMinSpikyLen) ? make_float3(0.f, kEps * s, 0.f) : r * (s / rlen);
-                const float ratio = P.poly6 * hm2 * hm2 * hm2 * P.scorr_inv_ref;
-                const float corr = -P.scorr_k * scorr_pow(P, ratio);
-                delta += (lam_i + lambda[j] + corr) * sg;
+        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, true, sx, cell_first, P.max_nb,
+        [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+        [&](uint32_t j, const float4 &pj4, float d2) {
+            const float hm2 = P.h2 - d2;
+            const float ratio = poly6_ref * hm2 * hm2 * hm2;
+            const float coef = lam_i + lambda[j] - P.scorr_k * scorr_pow(P, ratio);
+            if (d2 >= kMinSpiky2) {
+                const float rs = rsqrtf(d2);
+                const float hm = P.h - d2 * rs;
+                delta += (pi - f3(pj4)) * (coef * -P.spiky * hm * hm * rs);
+            } else {
+                const float hm = P.h - sqrtf(d2);
+                delta.y += coef * (-P.spiky * hm * hm * kEps);  // the reference's (0, EPS, 0) direction
             }
         });
     delta.x = G.sum(delta.x);
@@ -434,39 +457,31 @@ __device__ __forceinline__ float scaled_inv_mass(float w, float y) {
 // w e^y (both evaluated at this particle's y, as in the reference) and get
 // static/kinetic friction against the start-of-step positions.  Pairs with
 // zero total inverse mass or zero separation are skipped (the reference
-// produced NaN there).  The corrections need the final contact count, so
-// the first walk only counts and buffers; when the count fits the buffer
-// the corrections run from it, otherwise a second walk revisits them.
+// produced NaN there).  Two walks: the count, then the corrections.
 template <int TPP>
-__device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, const NbBuffer &buf,
-                                                uint32_t i, float4 pi4, int ph, uint32_t orig,
-                                                const float4 *__restrict__ sx,
+__device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float4 pi4,
+                                                int ph, uint32_t orig, const float4 *__restrict__ sx,
                                                 const SortedAttr *__restrict__ sattr,
                                                 const uint32_t *__restrict__ sidx,
                                                 const uint32_t *__restrict__ cell_first,
                                                 const float4 *__restrict__ x_old) {
     const float3 pi = f3(pi4);
     const int3 g = grid_pos(P, pi);
-    auto accept = [&](uint32_t j) {
-        if (j == i) return false;
+    auto test = [&](uint32_t j, const float4 &, float d2) {
+        if (j == i || !(d2 < P.collide2)) return false;
         const int phj = sattr[j].phase;
-        if (ph > kSolid && ph == phj) return false;
-        return dist2_exact(pi, f3(sx[j])) < P.collide2;
+        return !(ph > kSolid && ph == phj);
     };
-    uint32_t kept = 0;
-    bool overflow = false;
-    const uint32_t nb = group_walk<TPP>(P, G, g, 1, cell_first, P.max_nb, buf, accept, [&](uint32_t cnt) {
-        if (cnt == (uint32_t)kNbBuf) overflow = true;
-        kept = cnt;
-    });
+    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, P.collide2, true, sx, cell_first, P.max_nb, test,
+                                        [](uint32_t, const float4 &, float) {});
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
     const float w = pi4.w;
     const float sw = scaled_inv_mass(w, pi.y);
     const float3 prev = f3(x_old[orig]);
     const float fnb = (float)nb;
-    auto correct = [&](uint32_t j) {
-        const float4 pj4 = sx[j];
+    group_walk<TPP>(P, G, pi, g, 1, P.collide2, true, sx, cell_first, nb, test,
+                    [&](uint32_t j, const float4 &pj4, float) {
         const int phj = sattr[j].phase;
         const float3 pj = f3(pj4);
         const float3 diff = pi - pj;
@@ -493,16 +508,7 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
         if (ldpt < kEps) return;
         if (ldpt < P.cs * dist) delta -= dpt * colw / wsum;
         else delta -= dpt * fminf(P.ck * dist / ldpt, 1.f);
-    };
-    // the group agrees on whether any lane overflowed its column
-    const bool redo = G.ballot(overflow) != 0u;
-    if (!redo) {
-        for (uint32_t k = 0; k < kept; ++k) correct(buf.get(k));
-    } else {
-        group_walk<TPP>(P, G, g, 1, cell_first, nb, buf, accept, [&](uint32_t cnt) {
-            for (uint32_t k = 0; k < cnt; ++k) correct(buf.get(k));
-        });
-    }
+    });
     delta.x = G.sum(delta.x);
     delta.y = G.sum(delta.y);
     delta.z = G.sum(delta.z);
@@ -573,21 +579,19 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
                                                   const float *__restrict__ lambda,
                                                   const float4 *__restrict__ x_old,
                                                   float4 *__restrict__ x) {
-    __shared__ uint32_t nbuf[kNbBuf * kBlock];
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
-    const NbBuffer buf{nbuf + threadIdx.x};
     const SortedAttr a = sattr[i];
     const uint32_t orig = sidx[i];
     const float4 pi4 = sx[i];
     float3 np = f3(pi4);
     bool touched = false;
     if ((mask & kDoFluid) && a.phase == kFluid) {
-        np = np + fluid_delta<TPP>(P, G, buf, i, np, a.rho0, sx, lambda, cell_first);
+        np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sx, lambda, cell_first);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
-        np = np + contact_delta<TPP>(P, G, buf, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
+        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
         touched = true;
     }
     if (G.lane != 0) return;
@@ -838,28 +842,24 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
                                                  const float4 *__restrict__ xs,
                                                  const float4 *__restrict__ vs,
                                                  float4 *__restrict__ v) {
-    __shared__ uint32_t nbuf[kNbBuf * kBlock];
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
     const SortedAttr a = sattr[i];
     if (a.phase != kFluid) return;
-    const NbBuffer buf{nbuf + threadIdx.x};
     const float3 xi = f3(xs[i]);
     const float4 vi4 = vs[i];
     const float3 vi = f3(vi4);
     float3 acc = make_float3(0.f, 0.f, 0.f);
+    // candidates come from the last grid but are tested at their final
+    // positions, which may have left their cells: no stencil trimming
     group_walk<TPP>(
-        P, G, grid_pos(P, f3(sx[i])), P.fluid_rad, cell_first, P.max_nb, buf,
-        [&](uint32_t j) { return j != i && sattr[j].phase == kFluid && dist2_exact(xi, f3(xs[j])) < P.h2; },
-        [&](uint32_t cnt) {
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const uint32_t j = buf.get(k);
-                const float4 xj4 = xs[j];
-                const float hm2 = P.h2 - dist2_exact(xi, f3(xj4));
-                const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
-                acc += (f3(vs[j]) - vi) * wgt;
-            }
+        P, G, xi, grid_pos(P, f3(sx[i])), P.fluid_rad, P.h2, false, xs, cell_first, P.max_nb,
+        [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2 && sattr[j].phase == kFluid; },
+        [&](uint32_t j, const float4 &xj4, float d2) {
+            const float hm2 = P.h2 - d2;
+            const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
+            acc += (f3(vs[j]) - vi) * wgt;
         });
     acc.x = G.sum(acc.x);
     acc.y = G.sum(acc.y);

@@ -72,10 +72,11 @@ def poly6_rest_density(spacing: float, h: float, mass: float = 1.0) -> float:
 
 
 def dam_break(nx: int = 128, ny: int = 128, nz: int = 64, h: float = 0.1, seed: int = 2024,
-              iterations: int = 4, xsph: float = 0.01) -> Scene:
+              iterations: int = 4, xsph: float = 0.01, cell_div: int = 1) -> Scene:
     """3-D PBF dam break: an nx*ny*nz fluid block, lattice spacing h/2,
     jitter U(-0.01h, 0.01h), in the corner of a box four block-widths long
-    in x and twice the block height; cell size h, power-of-two grid.
+    in x and twice the block height; cell size h / cell_div, power-of-two
+    grid covering the box.
 
     Unit mass, rest density = the lattice's poly6 sum; s_corr k = 0.1,
     n = 4, dq = 0.2 h and relaxation 1 in kernel-radius units
@@ -85,7 +86,8 @@ def dam_break(nx: int = 128, ny: int = 128, nz: int = 64, h: float = 0.1, seed: 
     s = 0.5 * h
     r = 0.5 * s
     ext = np.array([4 * nx * s, 2 * ny * s, nz * s])
-    grid = [next_pow2(ext[k] / h) for k in range(3)]
+    cell = h / cell_div
+    grid = [next_pow2(ext[k] / cell) for k in range(3)]
     ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
     # particle order: x fastest, then y, then z (the reference's lattice loops)
     lat = np.stack([ii.transpose(2, 1, 0).ravel(), jj.transpose(2, 1, 0).ravel(), kk.transpose(2, 1, 0).ravel()], 1)
@@ -95,7 +97,7 @@ def dam_break(nx: int = 128, ny: int = 128, nz: int = 64, h: float = 0.1, seed: 
     pos_w[:, :3] = pos
     pos_w[:, 3] = 1.0
     rho0 = poly6_rest_density(s, h)
-    params = dict(particle_radius=r, kernel_radius=h, cell_size=h, grid_size=grid,
+    params = dict(particle_radius=r, kernel_radius=h, cell_size=cell, grid_size=grid,
                   world_origin=[0.0, 0.0, 0.0], gravity=[0.0, -9.8, 0.0], box_min=[0.0, 0.0, 0.0],
                   box_max=[float(v) for v in ext], iterations=iterations, relaxation=1.0, scorr_k=0.1,
                   scorr_n=4.0, scorr_dq=0.2, xsph_c=xsph, max_dt=0.05, max_neighbors=500,

@@ -98,9 +98,10 @@ def test_pbf_lambda_and_delta_reference_constants(flags):
     assert_projection(g.positions(), o.positions(), sc.pos_w, TOL_STAGE)
 
 
-@pytest.mark.parametrize("dims", [(16, 16, 8), (40, 24, 20)])
-def test_pbf_dam_break_block_one_iteration(dims):
-    sc = W.dam_break(*dims)
+@pytest.mark.parametrize("dims,cell_div", [((16, 16, 8), 1), ((40, 24, 20), 1), ((24, 20, 12), 2),
+                                           ((20, 16, 12), 3)])
+def test_pbf_dam_break_block_one_iteration(dims, cell_div):
+    sc = W.dam_break(*dims, cell_div=cell_div)
     g, o = make_pair(sc)
     g.integrate(sc.dt)
     o.integrate(sc.dt)
