@@ -53,6 +53,9 @@ struct DevParams {
     float ws, wk;        // sqrt of wall static / kinetic friction
     float collide_dist, collide2;
     int fluid_rad;       // ceil(h / cell)
+    // Stencil trimming is exact only when no two cells of a stencil alias
+    // to one grid cell: 2 rad + 1 <= every grid dimension.
+    bool trim_fluid, trim_contact;
     uint32_t max_nb;
     float twod_z;
     uint32_t flags;

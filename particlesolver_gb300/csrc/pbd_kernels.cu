@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
     float ro = 0.f, denom = 0.f;
     float3 grad = make_float3(0.f, 0.f, 0.f);
     group_walk<TPP>(
-        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, true, sx, cell_first, P.max_nb,
+        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
         [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
         [&](uint32_t, const float4 &pj4, float d2) {
             const float hm2 = P.h2 - d2;
@@ -424,7 +424,7 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
     float3 delta = make_float3(0.f, 0.f, 0.f);
     const float poly6_ref = P.poly6 * P.scorr_inv_ref;
     const uint32_t nb = group_walk<TPP>(
-        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, true, sx, cell_first, P.max_nb,
+        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
         [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
         [&](uint32_t j, const float4 &pj4, float d2) {
             const float hm2 = P.h2 - d2;
@@ -472,7 +472,7 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
         const int phj = sattr[j].phase;
         return !(ph > kSolid && ph == phj);
     };
-    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, P.collide2, true, sx, cell_first, P.max_nb, test,
+    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, P.max_nb, test,
                                         [](uint32_t, const float4 &, float) {});
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
@@ -480,7 +480,7 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
     const float sw = scaled_inv_mass(w, pi.y);
     const float3 prev = f3(x_old[orig]);
     const float fnb = (float)nb;
-    group_walk<TPP>(P, G, pi, g, 1, P.collide2, true, sx, cell_first, nb, test,
+    group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, nb, test,
                     [&](uint32_t j, const float4 &pj4, float) {
         const int phj = sattr[j].phase;
         const float3 pj = f3(pj4);

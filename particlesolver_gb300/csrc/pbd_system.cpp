@@ -92,6 +92,9 @@ pbd::DevParams make_dev(const pbd_params &p, const float rands[6]) {
     d.collide_dist = p.particle_radius * pbd::kCollideScale;
     d.collide2 = d.collide_dist * d.collide_dist;
     d.fluid_rad = (int)std::ceil(p.kernel_radius / p.cell_size);
+    const uint32_t gmin = std::min(d.gx, std::min(d.gy, d.gz));
+    d.trim_fluid = (uint32_t)(2 * d.fluid_rad + 1) <= gmin;
+    d.trim_contact = 3u <= gmin;
     d.max_nb = p.max_neighbors;
     d.twod_z = p.twod_z;
     d.flags = p.flags;
