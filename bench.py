@@ -211,11 +211,11 @@ def run_ours(args, world, rank, local_rank):
     # warm-up, then the lanes-per-particle choice (autotuned on the warmed-up
     # state unless --tpp fixes it), then the step graph capture
     warm = max(3, args.warmup)
-    for _ in range(warm):
-        sysm.update(sc.dt, sh)
     if args.tpp:
         sysm.set_threads_per_particle(args.tpp)
-    else:
+    for _ in range(warm):
+        sysm.update(sc.dt, sh)
+    if not args.tpp:
         sysm.autotune(sc.dt, 2, sh)
     tpp = sysm.threads_per_particle
     sysm.update_graph(sc.dt, 1, sh)

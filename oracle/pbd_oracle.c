@@ -741,21 +741,21 @@ void orc_calc_velocity(orc_system *s, double dt) {
 }
 
 /* XSPH (Macklin & Mueller 2013, eq. 17), normalised by the rest density:
- * v_i += c sum_j m_j (v_j - v_i) poly6(x_i - x_j) / rho0_i over fluid
- * neighbours within h at the final positions; candidates from the last grid
- * (stencil around the particle's grid position), as the CUDA k_xsph. */
+ * v_i += c sum_j m_j (v_j - v_i) poly6(x_i - x_j) / rho0_i over the fluid
+ * neighbours of the last solver iteration -- found and weighted at the
+ * positions that iteration's grid was built from -- with the step's final
+ * velocities (the CUDA k_xsph). */
 typedef struct {
     const orc_system *s;
     uint32_t i, nb;
-    const float *xi32;
-    const float *xs32;
     uint32_t *list;
 } xs_ctx;
 
 static int xsph_visit(void *vctx, uint32_t j) {
     xs_ctx *c = (xs_ctx *)vctx;
-    if (j == c->i || c->s->sphase[j] != PBD_PHASE_FLUID) return 0;
-    if (dist2f(c->xi32, c->xs32 + 4 * j) < c->s->h2f) {
+    if (j == c->i) return 0;
+    if (dist2f(c->s->sx32 + 4 * c->i, c->s->sx32 + 4 * j) < c->s->h2f &&
+        c->s->sphase[j] == PBD_PHASE_FLUID) {
         if (c->nb >= c->s->p.max_neighbors) return 1;
         c->list[c->nb++] = j;
     }
@@ -764,12 +764,7 @@ static int xsph_visit(void *vctx, uint32_t j) {
 
 void orc_apply_xsph(orc_system *s) {
     const uint32_t n = s->n;
-    float *xs32 = (float *)malloc(4ull * (n ? n : 1) * sizeof(float));
     double *vnew = (double *)malloc(3ull * (n ? n : 1) * sizeof(double));
-    for (uint32_t i = 0; i < n; ++i) {
-        uint32_t o = s->sorted_idx[i];
-        for (int d = 0; d < 4; ++d) xs32[4 * i + d] = (float)s->x[4 * o + d];
-    }
     const double h2 = (double)s->p.kernel_radius * (double)s->p.kernel_radius;
     set_threads();
 #pragma omp parallel
@@ -780,15 +775,15 @@ void orc_apply_xsph(orc_system *s) {
             uint32_t i = (uint32_t)ii, o = s->sorted_idx[i];
             for (int d = 0; d < 3; ++d) vnew[3 * i + d] = s->v[4 * o + d];
             if (s->sphase[i] != PBD_PHASE_FLUID) continue;
-            xs_ctx c = {s, i, 0, xs32 + 4 * i, xs32, list};
+            xs_ctx c = {s, i, 0, list};
             int g[3];
             grid_cell(s, s->sx32 + 4 * i, g);
             for_each_candidate(s, g, s->fluid_rad, xsph_visit, &c);
-            const double *xi = s->x + 4 * o, *vi = s->v + 4 * o;
+            const double *xi = s->sx + 4 * i, *vi = s->v + 4 * o;
             double acc[3] = {0, 0, 0};
             for (uint32_t k = 0; k < c.nb; ++k) {
-                uint32_t oj = s->sorted_idx[list[k]];
-                const double *xj = s->x + 4 * oj, *vj = s->v + 4 * oj;
+                const uint32_t j = list[k];
+                const double *xj = s->sx + 4 * j, *vj = s->v + 4 * s->sorted_idx[j];
                 double r2 = 0;
                 for (int d = 0; d < 3; ++d) r2 += (xi[d] - xj[d]) * (xi[d] - xj[d]);
                 double hm2 = h2 - r2;
@@ -803,7 +798,6 @@ void orc_apply_xsph(orc_system *s) {
         uint32_t o = s->sorted_idx[i];
         for (int d = 0; d < 3; ++d) s->v[4 * o + d] = vnew[3 * i + d];
     }
-    free(xs32);
     free(vnew);
 }
 

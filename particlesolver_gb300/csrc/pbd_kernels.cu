@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uin
 // A group of TPP consecutive lanes of a warp shares one particle: lane l
 // takes candidates b + l, b + l + TPP, ... of every stencil range (one
 // coalesced TPP x 16-byte load per step), and partial sums meet in xor
-// shuffles.  TPP = 1 is the reference's thread-per-particle walk.
+// shuffles.  TPP = 1 runs a particle per thread with branch-free inner
+// loops.
 template <int TPP>
 struct Group {
     int lane;       // lane inside the group
@@ -239,107 +240,119 @@ __device__ __forceinline__ float slab_gap(float p, float origin, float cell, int
     return fmaxf(fmaxf(lo - p, p - (lo + cell)), 0.f);
 }
 
-// Walks the (2 rad + 1)^3 stencil around the cell of q in the reference's
-// order (z outer, y, x inner, ascending sorted index; integration_kernel.
-// cuh:388-398, 549-559).  Stencil rows and cells whose box lies farther
-// than the interaction reach from q (with a 1e-4 relative margin) are
-// skipped: they hold no neighbours, so the neighbour sequence -- and the
-// first-`cap` rule of the reference's neighbour cap (integration_kernel.cuh:
-// 344,508) -- is unchanged.  trim = false walks every stencil cell (for
-// passes whose candidate positions have left their cells).  A row whose
-// kept cells do not wrap is one contiguous range of the dense cell offsets;
-// a wrapping row is walked cell by cell, which also repeats aliased cells
-// as the reference does.  test(j, q_j, d2) decides a candidate (this lane's
-// candidate j with its position and squared distance); accepted ones within
-// the cap go to use(j, q_j, d2).  Returns the group's neighbour count.
+// Calls f(b, e) for the sorted-index ranges of the (2 rad + 1)^3 stencil
+// around cell g in the reference's order (z outer, y, x inner;
+// integration_kernel.cuh:388-398, 549-559); f returns false to stop.
+// With trim, stencil rows and cells whose box lies farther than the reach
+// from q (1e-4 relative margin) are skipped -- they hold no neighbours, so
+// the neighbour sequence, and with it the reference's first-`cap` neighbour
+// rule (integration_kernel.cuh:344,508), is unchanged; exact only when no
+// two stencil cells alias (DevParams::trim_*).  A row whose kept cells do
+// not wrap is one contiguous range of the dense cell offsets; a wrapping
+// row goes cell by cell, repeating aliased cells as the reference does.
+template <class F>
+__device__ __forceinline__ void stencil_ranges(const DevParams &P, float3 q, int3 g, int rad, float reach2,
+                                               bool trim, const uint32_t *__restrict__ cell_first, F &&f) {
+    const float lim = reach2 * 1.0001f + 1e-30f;
+    const float inv_cell = 1.f / P.cell;
+    for (int dz = -rad; dz <= rad; ++dz) {
+        float gz2 = 0.f;
+        if (trim) {
+            const float t = slab_gap(q.z, P.origin.z, P.cell, g.z + dz);
+            gz2 = t * t;
+            if (gz2 > lim) continue;
+        }
+        const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
+        for (int dy = -rad; dy <= rad; ++dy) {
+            float gyz2 = gz2;
+            if (trim) {
+                const float t = slab_gap(q.y, P.origin.y, P.cell, g.y + dy);
+                gyz2 += t * t;
+                if (gyz2 > lim) continue;
+            }
+            int xa = -rad, xb = rad;
+            if (trim) {
+                // cells met by the sphere's slice |x - q.x| <= w, widened
+                // by a small margin against rounding
+                const float w = sqrtf(lim - gyz2);
+                xa = max(xa, __float2int_rd((q.x - w - P.origin.x) * inv_cell - 1e-3f) - g.x);
+                xb = min(xb, __float2int_rd((q.x + w - P.origin.x) * inv_cell + 1e-3f) - g.x);
+            }
+            const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
+            const uint32_t row = (z * P.gy + y) * P.gx;
+            const int x0 = g.x + xa, x1 = g.x + xb;
+            if (x0 >= 0 && x1 < (int)P.gx) {
+                if (x0 <= x1 &&
+                    !f(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u)))
+                    return;
+            } else {
+                for (int dx = xa; dx <= xb; ++dx) {
+                    const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
+                    if (!f(__ldg(cell_first + c), __ldg(cell_first + c + 1u))) return;
+                }
+            }
+        }
+    }
+}
+
+// Group walk with the exact neighbour cap: test(j, q_j, d2) decides this
+// lane's candidate; the first `cap` accepted candidates of the group in
+// visiting order go to use(j, q_j, d2).  Returns the group's count.
 template <int TPP, class Test, class Use>
 __device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<TPP> &G, float3 q, int3 g,
                                                int rad, float reach2, bool trim,
                                                const float4 *__restrict__ pos,
                                                const uint32_t *__restrict__ cell_first, uint32_t cap,
                                                Test &&test, Use &&use) {
-    const float lim = reach2 * 1.0001f + 1e-30f;
     uint32_t nb = 0;
-    bool open = true;
-    auto range = [&](uint32_t b, uint32_t e) {
-        if (TPP == 1) {
-            for (uint32_t j = b; j < e; ++j) {
-                const float4 pj = pos[j];
-                const float d2 = dist2_exact(q, f3(pj));
-                if (test(j, pj, d2)) {
-                    if (nb >= cap) {
-                        open = false;
-                        return;
-                    }
-                    ++nb;
-                    use(j, pj, d2);
-                }
+    stencil_ranges(P, q, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
+        for (uint32_t base = b; base < e; base += TPP) {
+            const uint32_t j = base + (uint32_t)G.lane;
+            float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+            float d2 = 0.f;
+            bool ok = false;
+            if (j < e) {
+                pj = pos[j];
+                d2 = dist2_exact(q, f3(pj));
+                ok = test(j, pj, d2);
             }
-        } else {
-            for (uint32_t base = b; base < e; base += TPP) {
-                const uint32_t j = base + (uint32_t)G.lane;
-                float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
-                float d2 = 0.f;
-                bool ok = false;
-                if (j < e) {
-                    pj = pos[j];
-                    d2 = dist2_exact(q, f3(pj));
-                    ok = test(j, pj, d2);
-                }
-                const unsigned m = G.ballot(ok);
-                const uint32_t total = (uint32_t)__popc(m);
-                if (nb + total >= cap) {
-                    ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < cap - nb;
-                    open = false;
-                }
+            const unsigned m = G.ballot(ok);
+            const uint32_t total = (uint32_t)__popc(m);
+            if (nb + total >= cap) {
+                ok = ok && (uint32_t)__popc(m & ((1u << G.wl) - 1u)) < cap - nb;
                 if (ok) use(j, pj, d2);
-                if (!open) {
-                    nb = cap;
-                    return;
-                }
-                nb += total;
+                nb = cap;
+                return false;
             }
+            if (ok) use(j, pj, d2);
+            nb += total;
         }
-    };
-    for (int dz = -rad; dz <= rad && open; ++dz) {
-        const float gz = trim ? slab_gap(q.z, P.origin.z, P.cell, g.z + dz) : 0.f;
-        const float gz2 = gz * gz;
-        if (gz2 > lim) continue;
-        const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
-        for (int dy = -rad; dy <= rad && open; ++dy) {
-            const float gy = trim ? slab_gap(q.y, P.origin.y, P.cell, g.y + dy) : 0.f;
-            const float gyz2 = gz2 + gy * gy;
-            if (gyz2 > lim) continue;
-            int xa = -rad, xb = rad;
-            if (trim) {
-                while (xa < 0) {
-                    const float gx = slab_gap(q.x, P.origin.x, P.cell, g.x + xa);
-                    if (gyz2 + gx * gx <= lim) break;
-                    ++xa;
-                }
-                while (xb > 0) {
-                    const float gx = slab_gap(q.x, P.origin.x, P.cell, g.x + xb);
-                    if (gyz2 + gx * gx <= lim) break;
-                    --xb;
-                }
-            }
-            const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
-            const uint32_t row = (z * P.gy + y) * P.gx;
-            const int x0 = g.x + xa, x1 = g.x + xb;
-            if (x0 >= 0 && x1 < (int)P.gx) {
-                range(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u));
-            } else {
-                for (int dx = xa; dx <= xb && open; ++dx) {
-                    const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
-                    range(__ldg(cell_first + c), __ldg(cell_first + c + 1u));
-                }
-            }
-        }
-    }
+        return true;
+    });
     return nb;
 }
 
 // ----------------------------------------------------------------- lambda
+
+// Per-neighbour terms of findLambdasD (integration_kernel.cuh:561-589),
+// evaluated under the neighbour mask `ok` so the candidate loop has no
+// data-dependent branch: poly6 weight, and the spiky gradient over rho0
+// (zero below the reference's 1e-4 length cut-off).
+struct LambdaAcc {
+    float ro, denom;
+    float3 grad;
+    __device__ __forceinline__ void add(const DevParams &P, bool ok, float d2, float3 dr, float mass_factor,
+                                        float spiky_r) {
+        const float hm2 = P.h2 - d2;
+        ro += ok ? P.poly6 * hm2 * hm2 * hm2 * mass_factor : 0.f;
+        const float rs = rsqrtf(fmaxf(d2, kMinSpiky2));
+        const float hm = P.h - d2 * rs;
+        const float sc = (ok && d2 >= kMinSpiky2) ? spiky_r * hm * hm * rs : 0.f;
+        const float3 sg = dr * sc;
+        grad -= sg;
+        denom += dot3(sg, sg);
+    }
+};
 
 // findLambdasD + collideCellRadius (integration_kernel.cuh:481-593): for a
 // fluid particle, neighbours are all particles with |r|^2 < h^2 in the
@@ -349,59 +362,76 @@ __device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<T
 // lambda = -(rho / rho0 - 1) / (sum |grad_j|^2 + |sum grad_j|^2 + eps).
 // Non-fluid particles get lambda = 0 (the reference left their slots
 // unwritten and read whatever was there, integration_kernel.cuh:636).
-// Per neighbour: one reciprocal square root and no division.
+// Output: (position, lambda) per sorted slot, the delta pass's one load.
 template <int TPP>
 __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
                                                    const float4 *__restrict__ sx,
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
-                                                   float *__restrict__ lambda) {
+                                                   float4 *__restrict__ sxl) {
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
     const SortedAttr a = sattr[i];
-    if (a.phase != kFluid) {
-        if (G.lane == 0) lambda[i] = 0.f;
-        return;
-    }
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
+    if (a.phase != kFluid) {
+        if (G.lane == 0) sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
+        return;
+    }
     const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
     const float inv_w = 1.f / pi4.w;
     const float inv_rho0 = 1.f / a.rho0;
     const float spiky_r = -P.spiky * inv_rho0;  // spiky coefficient over rho0
-    float ro = 0.f, denom = 0.f;
-    float3 grad = make_float3(0.f, 0.f, 0.f);
-    group_walk<TPP>(
-        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-        [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
-        [&](uint32_t, const float4 &pj4, float d2) {
-            const float hm2 = P.h2 - d2;
-            const float wpoly = P.poly6 * hm2 * hm2 * hm2;
-            ro += nb_mass ? ((pj4.w > 0.f) ? wpoly / pj4.w : 0.f) : wpoly * inv_w;
-            if (d2 >= kMinSpiky2) {
-                const float rs = rsqrtf(d2);
-                const float hm = P.h - d2 * rs;
-                const float3 sg = (pi - f3(pj4)) * (spiky_r * hm * hm * rs);
-                grad -= sg;
-                denom += dot3(sg, sg);
+    const int3 g = grid_pos(P, pi);
+    LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
+    bool capped = (TPP != 1);
+    if (TPP == 1) {
+        uint32_t nb = 0;
+        stencil_ranges(P, pi, g, P.fluid_rad, P.h2, P.trim_fluid, cell_first, [&](uint32_t b, uint32_t e) {
+            for (uint32_t j = b; j < e; ++j) {
+                const float4 pj = sx[j];
+                const float d2 = dist2_exact(pi, f3(pj));
+                const bool ok = d2 < P.h2 && j != i;
+                nb += ok ? 1u : 0u;
+                const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
+                acc.add(P, ok, d2, pi - f3(pj), mf, spiky_r);
             }
+            return true;
         });
-    ro = G.sum(ro);
-    denom = G.sum(denom);
-    grad.x = G.sum(grad.x);
-    grad.y = G.sum(grad.y);
-    grad.z = G.sum(grad.z);
+        if (nb > P.max_nb) {  // only past the neighbour cap: redo with the exact cap
+            acc = LambdaAcc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
+            capped = true;
+        }
+    }
+    if (capped) {
+        group_walk<TPP>(
+            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+            [&](uint32_t, const float4 &pj, float d2) {
+                const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
+                acc.add(P, true, d2, pi - f3(pj), mf, spiky_r);
+            });
+        acc.ro = G.sum(acc.ro);
+        acc.denom = G.sum(acc.denom);
+        acc.grad.x = G.sum(acc.grad.x);
+        acc.grad.y = G.sum(acc.grad.y);
+        acc.grad.z = G.sum(acc.grad.z);
+    }
     if (G.lane == 0) {
-        ro += P.poly6_self * inv_w;
-        denom += dot3(grad, grad);
-        lambda[i] = -(ro * inv_rho0 - 1.f) / (denom + P.relax);
+        const float ro = acc.ro + P.poly6_self * inv_w;
+        const float denom = acc.denom + dot3(acc.grad, acc.grad);
+        sxl[i] = make_float4(pi.x, pi.y, pi.z, -(ro * inv_rho0 - 1.f) / (denom + P.relax));
     }
 }
 
 // --------------------------------------------------------- fused particle
 
 __device__ __forceinline__ float scorr_pow(const DevParams &P, float ratio) {
+    if (P.scorr_n_int == 4) {
+        const float r2 = ratio * ratio;
+        return r2 * r2;
+    }
     if (P.scorr_n_int > 0) {
         float r = ratio;
         for (int k = 1; k < P.scorr_n_int; ++k) r *= ratio;
@@ -410,38 +440,65 @@ __device__ __forceinline__ float scorr_pow(const DevParams &P, float ratio) {
     return powf(ratio, P.scorr_n);
 }
 
+// Per-neighbour term of solveFluidsD (integration_kernel.cuh:615-637):
+// (lambda_i + lambda_j + s_corr) * spiky gradient, with the reference's
+// (0, EPS, 0) direction below the 1e-4 length cut-off.
+__device__ __forceinline__ void delta_add(const DevParams &P, float3 &delta, bool ok, float d2, float3 dr,
+                                          float lam_sum, float poly6_ref) {
+    const float hm2 = P.h2 - d2;
+    const float coef = lam_sum - P.scorr_k * scorr_pow(P, poly6_ref * hm2 * hm2 * hm2);
+    const float rs = rsqrtf(fmaxf(d2, kMinSpiky2));
+    const float hm = P.h - d2 * rs;
+    const bool far = d2 >= kMinSpiky2;
+    const float sc = (ok && far) ? coef * -P.spiky * hm * hm * rs : 0.f;
+    delta += dr * sc;
+    if (ok && !far) {
+        const float hz = P.h - sqrtf(d2);
+        delta.y += coef * (-P.spiky * hz * hz * kEps);
+    }
+}
+
 // solveFluidsD (integration_kernel.cuh:596-642): same neighbour set as the
 // lambda pass; delta = sum (lambda_i + lambda_j + s_corr) spiky(r) with
-// s_corr = -k (W(r) / W(dq h))^n and the (0, EPS, 0) direction for r ~ 0;
-// divided by (rho0 + n) (or rho0 with PBD_FLAG_DELTA_OVER_RHO0).  Every
-// lane of the group returns the group's total.
+// s_corr = -k (W(r) / W(dq h))^n; divided by (rho0 + n) (or rho0 with
+// PBD_FLAG_DELTA_OVER_RHO0).  Every lane of the group returns the total.
 template <int TPP>
 __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float3 pi,
-                                              float rho0, const float4 *__restrict__ sx,
-                                              const float *__restrict__ lambda,
+                                              float rho0, const float4 *__restrict__ sxl,
                                               const uint32_t *__restrict__ cell_first) {
-    const float lam_i = lambda[i];
-    float3 delta = make_float3(0.f, 0.f, 0.f);
+    const float lam_i = sxl[i].w;
     const float poly6_ref = P.poly6 * P.scorr_inv_ref;
-    const uint32_t nb = group_walk<TPP>(
-        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-        [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
-        [&](uint32_t j, const float4 &pj4, float d2) {
-            const float hm2 = P.h2 - d2;
-            const float ratio = poly6_ref * hm2 * hm2 * hm2;
-            const float coef = lam_i + lambda[j] - P.scorr_k * scorr_pow(P, ratio);
-            if (d2 >= kMinSpiky2) {
-                const float rs = rsqrtf(d2);
-                const float hm = P.h - d2 * rs;
-                delta += (pi - f3(pj4)) * (coef * -P.spiky * hm * hm * rs);
-            } else {
-                const float hm = P.h - sqrtf(d2);
-                delta.y += coef * (-P.spiky * hm * hm * kEps);  // the reference's (0, EPS, 0) direction
+    const int3 g = grid_pos(P, pi);
+    float3 delta = make_float3(0.f, 0.f, 0.f);
+    uint32_t nb = 0;
+    bool capped = (TPP != 1);
+    if (TPP == 1) {
+        stencil_ranges(P, pi, g, P.fluid_rad, P.h2, P.trim_fluid, cell_first, [&](uint32_t b, uint32_t e) {
+            for (uint32_t j = b; j < e; ++j) {
+                const float4 pl = sxl[j];
+                const float d2 = dist2_exact(pi, f3(pl));
+                const bool ok = d2 < P.h2 && j != i;
+                nb += ok ? 1u : 0u;
+                delta_add(P, delta, ok, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
             }
+            return true;
         });
-    delta.x = G.sum(delta.x);
-    delta.y = G.sum(delta.y);
-    delta.z = G.sum(delta.z);
+        if (nb > P.max_nb) {
+            delta = make_float3(0.f, 0.f, 0.f);
+            capped = true;
+        }
+    }
+    if (capped) {
+        nb = group_walk<TPP>(
+            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sxl, cell_first, P.max_nb,
+            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+            [&](uint32_t, const float4 &pl, float d2) {
+                delta_add(P, delta, true, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
+            });
+        delta.x = G.sum(delta.x);
+        delta.y = G.sum(delta.y);
+        delta.z = G.sum(delta.z);
+    }
     const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
     return delta / div;
 }
@@ -472,8 +529,8 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
         const int phj = sattr[j].phase;
         return !(ph > kSolid && ph == phj);
     };
-    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, P.max_nb, test,
-                                        [](uint32_t, const float4 &, float) {});
+    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, P.max_nb,
+                                        test, [](uint32_t, const float4 &, float) {});
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
     const float w = pi4.w;
@@ -576,7 +633,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
                                                   const SortedAttr *__restrict__ sattr,
                                                   const uint32_t *__restrict__ sidx,
                                                   const uint32_t *__restrict__ cell_first,
-                                                  const float *__restrict__ lambda,
+                                                  const float4 *__restrict__ sxl,
                                                   const float4 *__restrict__ x_old,
                                                   float4 *__restrict__ x) {
     const Group<TPP> G;
@@ -588,7 +645,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
     float3 np = f3(pi4);
     bool touched = false;
     if ((mask & kDoFluid) && a.phase == kFluid) {
-        np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sx, lambda, cell_first);
+        np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
         np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
@@ -820,26 +877,22 @@ __global__ void __launch_bounds__(kBlock) k_velocity(uint32_t n, float dt, const
 // ------------------------------------------------------------------- XSPH
 
 __global__ void __launch_bounds__(kBlock) k_xsph_gather(uint32_t n, const uint32_t *__restrict__ sidx,
-                                                        const float4 *__restrict__ x,
-                                                        const float4 *__restrict__ v,
-                                                        float4 *__restrict__ xs, float4 *__restrict__ vs) {
+                                                        const float4 *__restrict__ v, float4 *__restrict__ vs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t o = sidx[i];
-    xs[i] = x[o];
-    vs[i] = v[o];
+    vs[i] = v[sidx[i]];
 }
 
 // XSPH viscosity (Macklin & Mueller 2013, eq. 17) on fluid particles, made
 // dimensionless with the rest density: v_i += c sum_j m_j (v_j - v_i)
-// poly6(x_i - x_j) / rho0_i over fluid neighbours within h at the final
-// positions, candidates taken from the last grid.
+// poly6(x_i - x_j) / rho0_i over the fluid neighbours of the last solver
+// iteration (the positions its grid was built from), with the step's final
+// velocities.
 template <int TPP>
 __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const float4 *__restrict__ sx,
                                                  const SortedAttr *__restrict__ sattr,
                                                  const uint32_t *__restrict__ sidx,
                                                  const uint32_t *__restrict__ cell_first,
-                                                 const float4 *__restrict__ xs,
                                                  const float4 *__restrict__ vs,
                                                  float4 *__restrict__ v) {
     const Group<TPP> G;
@@ -847,14 +900,12 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
     if (i >= n) return;
     const SortedAttr a = sattr[i];
     if (a.phase != kFluid) return;
-    const float3 xi = f3(xs[i]);
+    const float3 xi = f3(sx[i]);
     const float4 vi4 = vs[i];
     const float3 vi = f3(vi4);
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    // candidates come from the last grid but are tested at their final
-    // positions, which may have left their cells: no stencil trimming
     group_walk<TPP>(
-        P, G, xi, grid_pos(P, f3(sx[i])), P.fluid_rad, P.h2, false, xs, cell_first, P.max_nb,
+        P, G, xi, grid_pos(P, xi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
         [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2 && sattr[j].phase == kFluid; },
         [&](uint32_t j, const float4 &xj4, float d2) {
             const float hm2 = P.h2 - d2;
@@ -941,17 +992,17 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
     default: KERNEL<32><<<blocks_for(n * 32u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
     }
 
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float *lambda, uint32_t tpp,
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, uint32_t tpp,
                           cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    PBD_TPP_DISPATCH(tpp, k_lambda, P, n, g.sorted_x, g.sorted_attr, g.cell_first, lambda);
+    PBD_TPP_DISPATCH(tpp, k_lambda, P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
     return cudaGetLastError();
 }
 
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
-                         const float *lambda, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s) {
+                         const float4 *sxl, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    PBD_TPP_DISPATCH(tpp, k_solve, P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, lambda,
+    PBD_TPP_DISPATCH(tpp, k_solve, P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, sxl,
                      x_old, x);
     return cudaGetLastError();
 }
@@ -984,11 +1035,11 @@ cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 
     return cudaGetLastError();
 }
 
-cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
-                        float4 *v, float4 *xs_final, float4 *vs, uint32_t tpp, cudaStream_t s) {
+cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs, uint32_t tpp,
+                        cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, x, v, xs_final, vs);
-    PBD_TPP_DISPATCH(tpp, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, xs_final, vs, v);
+    k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, v, vs);
+    PBD_TPP_DISPATCH(tpp, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v);
     return cudaGetLastError();
 }
 

@@ -59,17 +59,20 @@ cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers
 cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4 *x,
                                   cudaStream_t s);
 // tpp: lanes sharing one particle's neighbour walk (1, 2, 4, 8, 16, 32).
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float *lambda, uint32_t tpp,
+// sxl: per sorted slot (position xyz, lambda) -- written by the lambda pass,
+// read by the solve pass.
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, uint32_t tpp,
                           cudaStream_t s);
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
-                         const float *lambda, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s);
+                         const float4 *sxl, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s);
 cudaError_t launch_distance(const DevParams &P, const ConstraintBuffers &c, float4 *x,
                             bool apply_distance, bool apply_pins, cudaStream_t s);
 cudaError_t launch_shapes(const BodyBuffers &b, float4 *x, cudaStream_t s);
 cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 *x_old, float4 *v,
                             cudaStream_t s);
-cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
-                        float4 *v, float4 *xs_final, float4 *vs, uint32_t tpp, cudaStream_t s);
+// vs: scratch for the velocities in sorted order.
+cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs, uint32_t tpp,
+                        cudaStream_t s);
 cudaError_t launch_finite_check(uint32_t n, const float4 *x, const float4 *v, uint32_t *flag,
                                 cudaStream_t s);
 

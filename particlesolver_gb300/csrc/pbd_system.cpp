@@ -378,11 +378,11 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
         if (int rc = build_grid(s, st, it == 0)) return rc;
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
-            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->lambda, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->sxl, s->tpp, st));
         }
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
-            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->lambda, s->x_old, s->x, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->sxl, s->x_old, s->x, s->tpp, st));
         }
         if (dist_kernels) {
             Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
@@ -399,7 +399,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     }
     if (s->params.xsph_c != 0.f && s->n_fluid && s->params.iterations > 0) {
         Stage t(s, st, PBD_STAGE_XSPH, 2);
-        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->x, s->v, s->xs_final, s->vs, s->tpp, st));
+        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, s->tpp, st));
     }
     ++s->steps;
     return PBD_OK;
@@ -480,7 +480,7 @@ int pbd_create(const pbd_params *params, uint32_t max_particles, pbd_system **ou
     ALLOC(s->x_old, c);
     ALLOC(s->phase, c);
     ALLOC(s->rho0, c);
-    ALLOC(s->lambda, c);
+    ALLOC(s->sxl, c);
     ALLOC(s->flag, 1);
     ALLOC(s->grid.hash, c);
     ALLOC(s->grid.slot, c);
@@ -509,8 +509,7 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->x_old);
     dfree(s->phase);
     dfree(s->rho0);
-    dfree(s->lambda);
-    dfree(s->xs_final);
+    dfree(s->sxl);
     dfree(s->vs);
     dfree(s->flag);
     dfree(s->grid.hash);
@@ -603,8 +602,7 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
     s->n += n;
     s->n_fluid += nf;
     s->n_contact += nc;
-    if (s->n_fluid && !s->xs_final) {
-        CUDA_TRY(s, dalloc(&s->xs_final, s->cap));
+    if (s->n_fluid && !s->vs) {
         CUDA_TRY(s, dalloc(&s->vs, s->cap));
     }
     s->grid_valid = false;
@@ -935,7 +933,7 @@ int pbd_build_grid(pbd_system *s, void *stream) {
 int pbd_collide(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->lambda, s->x_old, s->x,
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->sxl, s->x_old, s->x,
                                   s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
@@ -945,8 +943,8 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->lambda, s->tpp, st));
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->lambda, s->x_old, s->x, s->tpp, st));
+    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->sxl, s->tpp, st));
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->sxl, s->x_old, s->x, s->tpp, st));
     s->launches += 2;
     return PBD_OK;
 }
@@ -954,7 +952,7 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
 int pbd_collide_world(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->lambda, s->x_old, s->x,
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->sxl, s->x_old, s->x,
                                   s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
@@ -988,9 +986,8 @@ int pbd_calc_velocity(pbd_system *s, float dt, void *stream) {
 int pbd_apply_xsph(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    if (!s->xs_final) return PBD_OK;  // no fluid
-    CUDA_TRY(s, pbd::launch_xsph(s->dev, s->n, s->grid, s->x, s->v, s->xs_final, s->vs,
-                                 s->tpp, (cudaStream_t)stream));
+    if (!s->vs) return PBD_OK;  // no fluid
+    CUDA_TRY(s, pbd::launch_xsph(s->dev, s->n, s->grid, s->v, s->vs, s->tpp, (cudaStream_t)stream));
     return PBD_OK;
 }
 
@@ -1028,10 +1025,10 @@ int pbd_get_lambdas(pbd_system *s, float *dst) {
     const uint32_t n = s->n;
     if (!n) return PBD_OK;
     std::vector<uint32_t> idx(n);
-    std::vector<float> lam(n);
+    std::vector<float4> sl(n);
     CUDA_TRY(s, cudaMemcpy(idx.data(), s->grid.sorted_idx, n * 4ull, cudaMemcpyDeviceToHost));
-    CUDA_TRY(s, cudaMemcpy(lam.data(), s->lambda, n * 4ull, cudaMemcpyDeviceToHost));
-    for (uint32_t p = 0; p < n; ++p) dst[idx[p]] = lam[p];
+    CUDA_TRY(s, cudaMemcpy(sl.data(), s->sxl, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t p = 0; p < n; ++p) dst[idx[p]] = sl[p].w;
     return PBD_OK;
 }
 

@@ -19,8 +19,8 @@ struct pbd_system {
     float4 *x = nullptr, *v = nullptr, *x_old = nullptr;
     int *phase = nullptr;
     float *rho0 = nullptr;
-    float *lambda = nullptr;  // sorted order
-    float4 *xs_final = nullptr, *vs = nullptr;  // XSPH scratch, sorted order
+    float4 *sxl = nullptr;  // sorted order: position xyz, PBF lambda w
+    float4 *vs = nullptr;   // XSPH scratch: velocities in sorted order
     uint32_t *flag = nullptr;  // finite check
 
     pbd::GridBuffers grid{};
@@ -43,7 +43,7 @@ struct pbd_system {
     // phase census for stage selection
     uint32_t n_fluid = 0, n_contact = 0;
 
-    uint32_t tpp = 8;     // lanes per particle in the neighbour passes
+    uint32_t tpp = 1;     // lanes per particle in the neighbour passes
     int rigid_index = 0;  // next object id for the scene builders
     float rands[6] = {0, 0, 0, 0, 0, 0};
 
