@@ -258,7 +258,12 @@ int pbd_synchronize(pbd_system *sys, void *stream);
 typedef struct pbd_tuning {
     uint32_t threads_per_particle; /* lanes sharing one particle's neighbour
                                       walk: 1, 2, 4, 8, 16 or 32            */
-    uint32_t reserved[7];          /* zero                                  */
+    uint32_t neighbor_list_capacity; /* with threads_per_particle == 1: fluid
+                                      neighbours recorded per particle and
+                                      iteration (multiple of 4, 0 = no list,
+                                      default 64); particles with more fall
+                                      back to the stencil walk              */
+    uint32_t reserved[6];          /* zero                                  */
 } pbd_tuning;
 
 int pbd_set_tuning(pbd_system *sys, const pbd_tuning *tuning);

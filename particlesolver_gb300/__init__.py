@@ -97,7 +97,8 @@ STAGES = ["predict", "grid", "lambda", "solve", "distance", "shapes", "velocity"
 
 
 class PbdTuning(ctypes.Structure):
-    _fields_ = [("threads_per_particle", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 7)]
+    _fields_ = [("threads_per_particle", ctypes.c_uint32), ("neighbor_list_capacity", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 6)]
 
 
 class PbdProfile(ctypes.Structure):
@@ -426,10 +427,21 @@ class ParticleSystem:
         self._check(self.lib.pbd_get_lambdas(self.h, out.ctypes.data_as(_PF)))
         return out
 
-    def set_threads_per_particle(self, tpp: int):
+    def tuning(self) -> PbdTuning:
         t = PbdTuning()
-        t.threads_per_particle = int(tpp)
+        self._check(self.lib.pbd_get_tuning(self.h, ctypes.byref(t)))
+        return t
+
+    def set_tuning(self, threads_per_particle: int | None = None, neighbor_list_capacity: int | None = None):
+        t = self.tuning()
+        if threads_per_particle is not None:
+            t.threads_per_particle = int(threads_per_particle)
+        if neighbor_list_capacity is not None:
+            t.neighbor_list_capacity = int(neighbor_list_capacity)
         self._check(self.lib.pbd_set_tuning(self.h, ctypes.byref(t)))
+
+    def set_threads_per_particle(self, tpp: int):
+        self.set_tuning(threads_per_particle=tpp)
 
     def autotune(self, dt: float, steps: int = 2, stream: int | None = None) -> int:
         """Pick the fastest lanes-per-particle for the current scene (state

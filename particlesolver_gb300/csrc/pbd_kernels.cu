@@ -572,6 +572,117 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
     return delta;
 }
 
+// ------------------------------------------------------- neighbour lists
+
+// Per-iteration neighbour list, one thread per particle: the lambda pass
+// walks the stencil once, testing candidates only, and records every
+// neighbour's sorted index in visiting order (four to a uint4, slot-major
+// so that reading slot q of 32 consecutive particles is one coalesced
+// 512-byte load); the per-neighbour arithmetic of lambda, delta and XSPH
+// then runs over the list.  Particles with more neighbours than the list
+// holds (or than the reference's cap) use the exact stencil walk instead.
+
+__device__ __forceinline__ bool list_usable(const DevParams &P, const NbList &L, uint32_t cnt) {
+    return cnt <= L.capacity && cnt <= P.max_nb;
+}
+
+// Calls f(j) for the cnt listed neighbours of particle i.
+template <class F>
+__device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uint32_t cnt, F &&f) {
+    for (uint32_t q = 0; 4u * q < cnt; ++q) {
+        const uint4 e = L.slot[q * L.stride + i];
+        const uint32_t left = cnt - 4u * q;
+        f(e.x);
+        if (left > 1u) f(e.y);
+        if (left > 2u) f(e.z);
+        if (left > 3u) f(e.w);
+    }
+}
+
+// findLambdasD (integration_kernel.cuh:481-593) with the list build: the
+// walk records the neighbours (|r|^2 < h^2, any phase, visiting order) and
+// lambda is summed over the list.  Output as k_lambda.
+__global__ void __launch_bounds__(kBlock) k_lambda_list(DevParams P, uint32_t n, const float4 *__restrict__ sx,
+                                                        const SortedAttr *__restrict__ sattr,
+                                                        const uint32_t *__restrict__ cell_first,
+                                                        float4 *__restrict__ sxl, NbList L) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SortedAttr a = sattr[i];
+    const float4 pi4 = sx[i];
+    const float3 pi = f3(pi4);
+    if (a.phase != kFluid) {
+        sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
+        L.count[i] = 0u;
+        return;
+    }
+    const int3 g = grid_pos(P, pi);
+    uint32_t cnt = 0;
+    uint4 pend = make_uint4(0u, 0u, 0u, 0u);
+    stencil_ranges(P, pi, g, P.fluid_rad, P.h2, P.trim_fluid, cell_first, [&](uint32_t b, uint32_t e) {
+        for (uint32_t j = b; j < e; ++j) {
+            if (dist2_exact(pi, f3(sx[j])) < P.h2 && j != i) {
+                if (cnt < L.capacity) {
+                    switch (cnt & 3u) {
+                    case 0: pend.x = j; break;
+                    case 1: pend.y = j; break;
+                    case 2: pend.z = j; break;
+                    default: pend.w = j; L.slot[(cnt >> 2) * L.stride + i] = pend; break;
+                    }
+                }
+                ++cnt;
+            }
+        }
+        return true;
+    });
+    if (cnt < L.capacity && (cnt & 3u)) L.slot[(cnt >> 2) * L.stride + i] = pend;
+    L.count[i] = cnt;
+    const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
+    const float inv_w = 1.f / pi4.w;
+    const float inv_rho0 = 1.f / a.rho0;
+    const float spiky_r = -P.spiky * inv_rho0;
+    LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
+    auto add = [&](const float4 &pj, float d2) {
+        const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
+        acc.add(P, true, d2, pi - f3(pj), mf, spiky_r);
+    };
+    if (list_usable(P, L, cnt)) {
+        for_each_listed(L, i, cnt, [&](uint32_t j) {
+            const float4 pj = sx[j];
+            add(pj, dist2_exact(pi, f3(pj)));
+        });
+    } else {
+        const Group<1> G;
+        group_walk<1>(
+            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+            [&](uint32_t, const float4 &pj, float d2) { add(pj, d2); });
+    }
+    const float ro = acc.ro + P.poly6_self * inv_w;
+    const float denom = acc.denom + dot3(acc.grad, acc.grad);
+    sxl[i] = make_float4(pi.x, pi.y, pi.z, -(ro * inv_rho0 - 1.f) / (denom + P.relax));
+}
+
+// solveFluidsD (integration_kernel.cuh:596-642) over the lambda pass's list.
+__device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t i, float3 pi, float rho0,
+                                                   const float4 *__restrict__ sxl,
+                                                   const uint32_t *__restrict__ cell_first, const NbList &L) {
+    const uint32_t cnt = L.count[i];
+    if (!list_usable(P, L, cnt)) {
+        const Group<1> G;
+        return fluid_delta<1>(P, G, i, pi, rho0, sxl, cell_first);
+    }
+    const float lam_i = sxl[i].w;
+    const float poly6_ref = P.poly6 * P.scorr_inv_ref;
+    float3 delta = make_float3(0.f, 0.f, 0.f);
+    for_each_listed(L, i, cnt, [&](uint32_t j) {
+        const float4 pl = sxl[j];
+        delta_add(P, delta, true, dist2_exact(pi, f3(pl)), pi - f3(pl), lam_i + pl.w, poly6_ref);
+    });
+    const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)cnt;
+    return delta / div;
+}
+
 // collide_world_functor (integration_kernel.cuh:57-157): clamp into the box
 // shrunk by r with the jitter uniforms, then boundary friction against the
 // start-of-step position for phases >= CLOTH.
@@ -635,7 +746,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
                                                   const uint32_t *__restrict__ cell_first,
                                                   const float4 *__restrict__ sxl,
                                                   const float4 *__restrict__ x_old,
-                                                  float4 *__restrict__ x) {
+                                                  float4 *__restrict__ x, NbList L, bool use_list) {
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -645,7 +756,8 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
     float3 np = f3(pi4);
     bool touched = false;
     if ((mask & kDoFluid) && a.phase == kFluid) {
-        np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
+        if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, cell_first, L);
+        else np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
         np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
@@ -894,7 +1006,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
                                                  const uint32_t *__restrict__ sidx,
                                                  const uint32_t *__restrict__ cell_first,
                                                  const float4 *__restrict__ vs,
-                                                 float4 *__restrict__ v) {
+                                                 float4 *__restrict__ v, NbList L, bool use_list) {
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -904,14 +1016,25 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
     const float4 vi4 = vs[i];
     const float3 vi = f3(vi4);
     float3 acc = make_float3(0.f, 0.f, 0.f);
-    group_walk<TPP>(
-        P, G, xi, grid_pos(P, xi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-        [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2 && sattr[j].phase == kFluid; },
-        [&](uint32_t j, const float4 &xj4, float d2) {
-            const float hm2 = P.h2 - d2;
-            const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
-            acc += (f3(vs[j]) - vi) * wgt;
+    auto add = [&](uint32_t j, const float4 &xj4, float d2) {
+        const float hm2 = P.h2 - d2;
+        const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
+        acc += (f3(vs[j]) - vi) * wgt;
+    };
+    const uint32_t cnt = (TPP == 1 && use_list) ? L.count[i] : 0u;
+    if (TPP == 1 && use_list && list_usable(P, L, cnt)) {
+        // the last lambda pass listed every neighbour of any phase
+        for_each_listed(L, i, cnt, [&](uint32_t j) {
+            if (sattr[j].phase != kFluid) return;
+            const float4 xj4 = sx[j];
+            add(j, xj4, dist2_exact(xi, f3(xj4)));
         });
+    } else {
+        group_walk<TPP>(
+            P, G, xi, grid_pos(P, xi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2 && sattr[j].phase == kFluid; },
+            add);
+    }
     acc.x = G.sum(acc.x);
     acc.y = G.sum(acc.y);
     acc.z = G.sum(acc.z);
@@ -992,18 +1115,24 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
     default: KERNEL<32><<<blocks_for(n * 32u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
     }
 
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, uint32_t tpp,
-                          cudaStream_t s) {
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, const NbList &L,
+                          uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    if (tpp == 1 && L.slot) {
+        k_lambda_list<<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+        return cudaGetLastError();
+    }
     PBD_TPP_DISPATCH(tpp, k_lambda, P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
     return cudaGetLastError();
 }
 
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
-                         const float4 *sxl, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s) {
+                         const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
+                         uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    use_list = use_list && L.slot != nullptr;
     PBD_TPP_DISPATCH(tpp, k_solve, P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, sxl,
-                     x_old, x);
+                     x_old, x, L, use_list);
     return cudaGetLastError();
 }
 
@@ -1035,11 +1164,12 @@ cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 
     return cudaGetLastError();
 }
 
-cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs, uint32_t tpp,
-                        cudaStream_t s) {
+cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs,
+                        const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    use_list = use_list && L.slot != nullptr;
     k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, v, vs);
-    PBD_TPP_DISPATCH(tpp, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v);
+    PBD_TPP_DISPATCH(tpp, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L, use_list);
     return cudaGetLastError();
 }
 

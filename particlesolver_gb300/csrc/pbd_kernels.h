@@ -22,6 +22,15 @@ struct GridBuffers {
     SortedAttr *sorted_attr;  // [cap] phase and rest density, sorted
 };
 
+// Per-iteration fluid neighbour lists (sorted indices in the reference's
+// visiting order, four per uint4, slot-major).
+struct NbList {
+    uint4 *slot;        // [capacity / 4][stride]
+    uint32_t *count;    // [stride] neighbours found (may exceed capacity)
+    uint32_t capacity;  // neighbours per particle, a multiple of 4
+    uint32_t stride;    // particles per slot row
+};
+
 struct ConstraintBuffers {
     uint32_t count;        // constrained particles
     uint32_t *particle;    // [count] particle index
@@ -61,18 +70,21 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
 // tpp: lanes sharing one particle's neighbour walk (1, 2, 4, 8, 16, 32).
 // sxl: per sorted slot (position xyz, lambda) -- written by the lambda pass,
 // read by the solve pass.
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, uint32_t tpp,
-                          cudaStream_t s);
+// With tpp == 1 and a list allocated, the lambda pass also records the
+// neighbour list that the solve and XSPH passes then use (use_list).
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, const NbList &L,
+                          uint32_t tpp, cudaStream_t s);
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
-                         const float4 *sxl, const float4 *x_old, float4 *x, uint32_t tpp, cudaStream_t s);
+                         const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
+                         uint32_t tpp, cudaStream_t s);
 cudaError_t launch_distance(const DevParams &P, const ConstraintBuffers &c, float4 *x,
                             bool apply_distance, bool apply_pins, cudaStream_t s);
 cudaError_t launch_shapes(const BodyBuffers &b, float4 *x, cudaStream_t s);
 cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 *x_old, float4 *v,
                             cudaStream_t s);
 // vs: scratch for the velocities in sorted order.
-cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs, uint32_t tpp,
-                        cudaStream_t s);
+cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs,
+                        const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s);
 cudaError_t launch_finite_check(uint32_t n, const float4 *x, const float4 *v, uint32_t *flag,
                                 cudaStream_t s);
 

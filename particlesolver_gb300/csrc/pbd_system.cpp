@@ -142,6 +142,13 @@ void free_grid(pbd_system *s) {
     s->grid_cells = 0;
 }
 
+void free_list(pbd_system *s) {
+    dfree(s->nbl.slot);
+    dfree(s->nbl.count);
+    s->nbl.capacity = 0;
+    s->list_valid = false;
+}
+
 void drop_graph(pbd_system *s) {
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->graph_exec = nullptr;
@@ -347,6 +354,7 @@ int build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict) {
     }
     CUDA_TRY(s, pbd::launch_grid_finish(P, s->n, s->grid, s->x, s->phase, s->rho0, st));
     s->grid_valid = true;
+    s->list_valid = false;
     return PBD_OK;
 }
 
@@ -378,11 +386,13 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
         if (int rc = build_grid(s, st, it == 0)) return rc;
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
-            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->sxl, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->sxl, s->nbl, s->tpp, st));
+            s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
         }
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
-            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->sxl, s->x_old, s->x, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->sxl, s->x_old, s->x, s->nbl, s->list_valid,
+                                          s->tpp, st));
         }
         if (dist_kernels) {
             Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
@@ -399,7 +409,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     }
     if (s->params.xsph_c != 0.f && s->n_fluid && s->params.iterations > 0) {
         Stage t(s, st, PBD_STAGE_XSPH, 2);
-        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, s->tpp, st));
+        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, s->nbl, s->list_valid, s->tpp, st));
     }
     ++s->steps;
     return PBD_OK;
@@ -510,6 +520,7 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->phase);
     dfree(s->rho0);
     dfree(s->sxl);
+    free_list(s);
     dfree(s->vs);
     dfree(s->flag);
     dfree(s->grid.hash);
@@ -602,8 +613,12 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
     s->n += n;
     s->n_fluid += nf;
     s->n_contact += nc;
-    if (s->n_fluid && !s->vs) {
-        CUDA_TRY(s, dalloc(&s->vs, s->cap));
+    if (s->n_fluid && !s->vs) CUDA_TRY(s, dalloc(&s->vs, s->cap));
+    if (s->n_fluid && !s->nbl.slot && s->list_capacity) {
+        CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
+        CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
+        s->nbl.capacity = s->list_capacity;
+        s->nbl.stride = s->cap;
     }
     s->grid_valid = false;
     ++s->version;
@@ -798,7 +813,21 @@ int pbd_set_tuning(pbd_system *s, const pbd_tuning *t) {
     const uint32_t k = t->threads_per_particle;
     if (!(k == 1 || k == 2 || k == 4 || k == 8 || k == 16 || k == 32))
         return fail(s, PBD_ERR_INVALID_ARGUMENT, "threads_per_particle must be 1, 2, 4, 8, 16 or 32");
+    const uint32_t cap = t->neighbor_list_capacity;
+    if (cap % 4u || cap > 1024u)
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "neighbor_list_capacity must be a multiple of 4, at most 1024");
     s->tpp = k;
+    if (cap != s->list_capacity) {
+        free_list(s);
+        s->list_capacity = cap;
+        if (s->n_fluid && cap) {
+            CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(cap / 4u) * s->cap));
+            CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
+            s->nbl.capacity = cap;
+            s->nbl.stride = s->cap;
+        }
+    }
+    s->list_valid = false;
     ++s->version;
     return PBD_OK;
 }
@@ -807,6 +836,7 @@ int pbd_get_tuning(const pbd_system *s, pbd_tuning *out) {
     if (!s || !out) return PBD_ERR_INVALID_ARGUMENT;
     std::memset(out, 0, sizeof *out);
     out->threads_per_particle = s->tpp;
+    out->neighbor_list_capacity = s->list_capacity;
     return PBD_OK;
 }
 
@@ -933,8 +963,8 @@ int pbd_build_grid(pbd_system *s, void *stream) {
 int pbd_collide(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->sxl, s->x_old, s->x,
-                                  s->tpp, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+                                  false, s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
 }
@@ -943,8 +973,10 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->sxl, s->tpp, st));
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->sxl, s->x_old, s->x, s->tpp, st));
+    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->sxl, s->nbl, s->tpp, st));
+    s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+                                  s->list_valid, s->tpp, st));
     s->launches += 2;
     return PBD_OK;
 }
@@ -952,8 +984,8 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
 int pbd_collide_world(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->sxl, s->x_old, s->x,
-                                  s->tpp, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+                                  false, s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
 }
@@ -987,7 +1019,8 @@ int pbd_apply_xsph(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     if (!s->vs) return PBD_OK;  // no fluid
-    CUDA_TRY(s, pbd::launch_xsph(s->dev, s->n, s->grid, s->v, s->vs, s->tpp, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_xsph(s->dev, s->n, s->grid, s->v, s->vs, s->nbl, s->list_valid, s->tpp,
+                                 (cudaStream_t)stream));
     return PBD_OK;
 }
 

@@ -44,6 +44,9 @@ struct pbd_system {
     uint32_t n_fluid = 0, n_contact = 0;
 
     uint32_t tpp = 1;     // lanes per particle in the neighbour passes
+    pbd::NbList nbl{};    // per-iteration fluid neighbour lists
+    uint32_t list_capacity = 64;
+    bool list_valid = false;  // nbl matches the current grid
     int rigid_index = 0;  // next object id for the scene builders
     float rands[6] = {0, 0, 0, 0, 0, 0};
 

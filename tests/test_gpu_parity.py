@@ -381,3 +381,27 @@ def test_autotune_restores_state():
     assert chosen in (1, 2, 4, 8, 16, 32)
     np.testing.assert_array_equal(a.positions(), b.positions())
     np.testing.assert_array_equal(a.velocities(), b.velocities())
+
+
+@pytest.mark.parametrize("capacity", [0, 4, 16, 64])
+def test_neighbor_list_capacity_and_fallback(capacity):
+    """Small list capacities force the exact stencil-walk fallback for some
+    or all particles; every capacity gives the oracle's result."""
+    sc = W.dam_break(20, 16, 12, cell_div=2)
+    g, o = make_pair(sc)
+    g.set_tuning(threads_per_particle=1, neighbor_list_capacity=capacity)
+    g.integrate(sc.dt)
+    o.integrate(sc.dt)
+    sync_positions(g, o)
+    g.build_grid()
+    o.build_grid()
+    before = g.positions()
+    g.solve_fluids()
+    o.solve_fluids()
+    assert norm_err(g.lambdas(), o.lambdas()) < TOL_STAGE
+    assert_projection(g.positions(), o.positions(), before, TOL_STAGE)
+    g.calc_velocity(sc.dt)
+    o.calc_velocity(sc.dt)
+    g.apply_xsph()
+    o.apply_xsph()
+    assert norm_err(g.velocities()[:, :3], o.velocities()[:, :3]) < TOL_STAGE
