@@ -599,10 +599,69 @@ __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uin
     }
 }
 
+// Stencil ranges with the radius fixed at compile time (RAD > 0; RAD = 0
+// defers to the runtime version): rows unroll, the per-axis slab gaps are
+// computed once, and the x extent of each kept row comes from a reciprocal
+// square root (its rounding is covered by the 1e-3-cell widening).  Same
+// visiting order and the same exactness conditions as stencil_ranges.
+template <int RAD, class F>
+__device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 q, int3 g, float reach2, bool trim,
+                                                     const uint32_t *__restrict__ cell_first, F &&f) {
+    if (RAD == 0) {
+        stencil_ranges(P, q, g, P.fluid_rad, reach2, trim, cell_first, f);
+        return;
+    }
+    constexpr int W = 2 * RAD + 1;
+    const float lim = reach2 * 1.0001f + 1e-30f;
+    const float inv_cell = 1.f / P.cell;
+    float gz2[W], gy2[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        const float tz = trim ? slab_gap(q.z, P.origin.z, P.cell, g.z + k - RAD) : 0.f;
+        const float ty = trim ? slab_gap(q.y, P.origin.y, P.cell, g.y + k - RAD) : 0.f;
+        gz2[k] = tz * tz;
+        gy2[k] = ty * ty;
+    }
+    const float qx = (q.x - P.origin.x) * inv_cell;
+#pragma unroll
+    for (int kz = 0; kz < W; ++kz) {
+        if (gz2[kz] > lim) continue;
+        const uint32_t z = (uint32_t)(g.z + kz - RAD) & (P.gz - 1u);
+#pragma unroll
+        for (int ky = 0; ky < W; ++ky) {
+            const float gyz2 = gz2[kz] + gy2[ky];
+            if (gyz2 > lim) continue;
+            int xa = -RAD, xb = RAD;
+            if (trim) {
+                const float r2 = lim - gyz2;
+                const float wc = r2 * rsqrtf(fmaxf(r2, 1e-30f)) * inv_cell;  // slice half-width in cells
+                xa = max(xa, __float2int_rd(qx - wc - 1e-3f) - g.x);
+                xb = min(xb, __float2int_rd(qx + wc + 1e-3f) - g.x);
+            }
+            const uint32_t y = (uint32_t)(g.y + ky - RAD) & (P.gy - 1u);
+            const uint32_t row = (z * P.gy + y) * P.gx;
+            const int x0 = g.x + xa, x1 = g.x + xb;
+            if (x0 >= 0 && x1 < (int)P.gx) {
+                if (x0 <= x1 &&
+                    !f(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u)))
+                    return;
+            } else {
+                for (int dx = xa; dx <= xb; ++dx) {
+                    const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
+                    if (!f(__ldg(cell_first + c), __ldg(cell_first + c + 1u))) return;
+                }
+            }
+        }
+    }
+}
+
 // findLambdasD (integration_kernel.cuh:481-593) with the list build: the
 // walk records the neighbours (|r|^2 < h^2, any phase, visiting order) and
-// lambda is summed over the list.  Output as k_lambda.
-__global__ void __launch_bounds__(kBlock) k_lambda_list(DevParams P, uint32_t n, const float4 *__restrict__ sx,
+// lambda is summed over the list.  The candidate loop is branch-free: the
+// neighbour test drives predicated register inserts and a predicated
+// 16-byte store per four neighbours.  Output as k_lambda.
+template <int RAD>
+__global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P, uint32_t n, const float4 *__restrict__ sx,
                                                         const SortedAttr *__restrict__ sattr,
                                                         const uint32_t *__restrict__ cell_first,
                                                         float4 *__restrict__ sxl, NbList L) {
@@ -619,23 +678,25 @@ __global__ void __launch_bounds__(kBlock) k_lambda_list(DevParams P, uint32_t n,
     const int3 g = grid_pos(P, pi);
     uint32_t cnt = 0;
     uint4 pend = make_uint4(0u, 0u, 0u, 0u);
-    stencil_ranges(P, pi, g, P.fluid_rad, P.h2, P.trim_fluid, cell_first, [&](uint32_t b, uint32_t e) {
+    uint4 *const row_base = L.slot + i;
+    const uint32_t cap = L.capacity;
+    const float h2 = P.h2;
+    stencil_ranges_fixed<RAD>(P, pi, g, h2, P.trim_fluid, cell_first, [&](uint32_t b, uint32_t e) {
+#pragma unroll 2
         for (uint32_t j = b; j < e; ++j) {
-            if (dist2_exact(pi, f3(sx[j])) < P.h2 && j != i) {
-                if (cnt < L.capacity) {
-                    switch (cnt & 3u) {
-                    case 0: pend.x = j; break;
-                    case 1: pend.y = j; break;
-                    case 2: pend.z = j; break;
-                    default: pend.w = j; L.slot[(cnt >> 2) * L.stride + i] = pend; break;
-                    }
-                }
-                ++cnt;
-            }
+            const float4 q = __ldg(sx + j);
+            const bool ok = dist2_exact(pi, f3(q)) < h2 && j != i;
+            const uint32_t s4 = cnt & 3u;
+            pend.x = (ok && s4 == 0u) ? j : pend.x;
+            pend.y = (ok && s4 == 1u) ? j : pend.y;
+            pend.z = (ok && s4 == 2u) ? j : pend.z;
+            pend.w = (ok && s4 == 3u) ? j : pend.w;
+            if (ok && s4 == 3u && cnt < cap) row_base[(cnt >> 2) * L.stride] = pend;
+            cnt += ok ? 1u : 0u;
         }
         return true;
     });
-    if (cnt < L.capacity && (cnt & 3u)) L.slot[(cnt >> 2) * L.stride + i] = pend;
+    if (cnt < cap && (cnt & 3u)) row_base[(cnt >> 2) * L.stride] = pend;
     L.count[i] = cnt;
     const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
     const float inv_w = 1.f / pi4.w;
@@ -648,7 +709,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda_list(DevParams P, uint32_t n,
     };
     if (list_usable(P, L, cnt)) {
         for_each_listed(L, i, cnt, [&](uint32_t j) {
-            const float4 pj = sx[j];
+            const float4 pj = __ldg(sx + j);
             add(pj, dist2_exact(pi, f3(pj)));
         });
     } else {
@@ -1119,7 +1180,13 @@ cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, 
                           uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if (tpp == 1 && L.slot) {
-        k_lambda_list<<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+        const unsigned nb = blocks_for(n);
+        if (P.fluid_rad == 1)
+            k_lambda_list<1><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+        else if (P.fluid_rad == 2)
+            k_lambda_list<2><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+        else
+            k_lambda_list<0><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
         return cudaGetLastError();
     }
     PBD_TPP_DISPATCH(tpp, k_lambda, P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
