@@ -1181,10 +1181,11 @@ cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, 
     if (n == 0) return cudaSuccess;
     if (tpp == 1 && L.slot) {
         const unsigned nb = blocks_for(n);
+        // the 9-row stencil unrolls; wider ones stay loops (fully unrolled
+        // 25-row code measured slower: instruction-cache stalls, lower
+        // occupancy)
         if (P.fluid_rad == 1)
             k_lambda_list<1><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
-        else if (P.fluid_rad == 2)
-            k_lambda_list<2><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
         else
             k_lambda_list<0><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
         return cudaGetLastError();
