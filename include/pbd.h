@@ -245,6 +245,28 @@ int pbd_get_grid(pbd_system *sys, uint32_t *sorted_hash, uint32_t *sorted_index,
 /* PBF lambda of every particle from the last solve, in particle order. */
 int pbd_get_lambdas(pbd_system *sys, float *dst);
 uint32_t pbd_num_cells(const pbd_system *sys);
+
+/* Neighbour-grid build that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc where they need a
+ * grid -- inside stream capture or a real-time loop, or when every device
+ * buffer belongs to the caller's own allocator.  Same result as
+ * pbd_build_grid + pbd_get_grid on the same positions: particles sorted by
+ * (cell hash, index) and the cell start / end of the reference layout.
+ * Inputs and outputs are device pointers the caller owns: positions
+ * float4[n] (x, y, z, w), sorted_index uint32[n], cell_start and cell_end
+ * uint32[grid cells].  Scratch comes from one fixed device array inside the
+ * library (~7 MiB per device, held until the process exits), so n is at
+ * most PBD_NOALLOC_MAX_PARTICLES and the grid at most
+ * PBD_NOALLOC_MAX_CELLS cells; larger requests return
+ * PBD_ERR_INVALID_ARGUMENT.  The first call on a device looks up that
+ * array's device address, so make it before any stream capture.  Every
+ * call shares the array: calls that overlap on the GPU race.  Errors are
+ * reported through pbd_last_error(NULL). */
+#define PBD_NOALLOC_MAX_PARTICLES (1u << 18)
+#define PBD_NOALLOC_MAX_CELLS (1u << 20)
+int pbd_build_grid_noalloc(const pbd_params *params, const float *positions, uint32_t n,
+                           uint32_t *sorted_index, uint32_t *cell_start, uint32_t *cell_end, void *stream);
+
 /* Returns PBD_ERR_NONFINITE if a position or velocity is NaN/Inf. */
 int pbd_check_finite(pbd_system *sys, void *stream);
 /* Blocks until the system's work on stream is done. */

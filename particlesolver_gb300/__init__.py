@@ -175,6 +175,7 @@ _SIGNATURES = {
     "pbd_set_profiling": ([_P, _I], _I),
     "pbd_get_profile": ([_P, ctypes.POINTER(PbdProfile)], _I),
     "pbd_reset_profile": ([_P], _I),
+    "pbd_build_grid_noalloc": ([ctypes.POINTER(PbdParams), _P, _U32, _P, _P, _P, _P], _I),
     "pbd_state_size": ([_P], ctypes.c_uint64),
     "pbd_save_state": ([_P, _P, ctypes.c_uint64], _I),
     "pbd_load_state": ([_P, _P, ctypes.c_uint64], _I),

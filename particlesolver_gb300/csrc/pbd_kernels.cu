@@ -199,6 +199,33 @@ __global__ void __launch_bounds__(kBlock) k_rank_reorder(uint32_t n, const uint3
     sorted_attr[p] = a;
 }
 
+// Stable in-cell rank only (k_rank_reorder without the data gather).
+__global__ void __launch_bounds__(kBlock) k_rank_only(uint32_t n, const uint32_t *__restrict__ hash,
+                                                      const uint32_t *__restrict__ cell_first,
+                                                      const uint32_t *__restrict__ tmp,
+                                                      uint32_t *__restrict__ sorted_idx) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t h = hash[i];
+    const uint32_t b = cell_first[h], e = cell_first[h + 1];
+    uint32_t rank = 0;
+    for (uint32_t k = b; k < e; ++k) rank += (tmp[k] < i) ? 1u : 0u;
+    sorted_idx[b + rank] = i;
+}
+
+// Dense offsets to the reference's cellStart / cellEnd layout
+// (integration_kernel.cuh:274-285): empty cells get start 0xffffffff and
+// end 0.
+__global__ void __launch_bounds__(kBlock) k_cell_ranges(uint32_t cells, const uint32_t *__restrict__ cell_first,
+                                                        uint32_t *__restrict__ cell_start,
+                                                        uint32_t *__restrict__ cell_end) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    const uint32_t b = cell_first[c], e = cell_first[c + 1];
+    cell_start[c] = (e > b) ? b : 0xffffffffu;
+    cell_end[c] = (e > b) ? e : 0u;
+}
+
 __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uint32_t *__restrict__ sorted_idx,
                                                            const float4 *__restrict__ x,
                                                            float4 *__restrict__ sorted_x) {
@@ -1155,6 +1182,24 @@ cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers
     k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.slot, g.cell_first, g.tmp);
     k_rank_reorder<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.cell_first, g.tmp, x, phase, rho0,
                                                     g.sorted_idx, g.sorted_x, g.sorted_attr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_into_cells(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash, uint32_t *slot,
+                                   uint32_t *cell_first, uint32_t *partials, uint32_t *tmp, uint32_t *sorted_idx,
+                                   uint32_t *cell_start, uint32_t *cell_end, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(cell_first, 0, ((size_t)P.num_cells + 1u) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    if (n) {
+        k_hash_count<<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, cell_first);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = launch_exclusive_scan(cell_first, P.num_cells + 1u, partials, s)) != cudaSuccess) return e;
+    if (n) {
+        k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, hash, slot, cell_first, tmp);
+        k_rank_only<<<blocks_for(n), kBlock, 0, s>>>(n, hash, cell_first, tmp, sorted_idx);
+    }
+    k_cell_ranges<<<blocks_for(P.num_cells), kBlock, 0, s>>>(P.num_cells, cell_first, cell_start, cell_end);
     return cudaGetLastError();
 }
 

@@ -65,6 +65,13 @@ cudaError_t launch_exclusive_scan(uint32_t *data, uint32_t elements, uint32_t *p
 cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers &g,
                                const float4 *x, const int *phase, const float *rho0,
                                cudaStream_t s);
+// The whole grid build into caller buffers: cell hashes, counting sort in
+// (hash, index) order, and the reference's cellStart / cellEnd layout.
+// hash, slot, tmp: [n]; cell_first: [cells + 1]; partials:
+// [scan_partial_count(cells + 1)]; sorted_idx: [n]; cell_start/end: [cells].
+cudaError_t launch_sort_into_cells(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash, uint32_t *slot,
+                                   uint32_t *cell_first, uint32_t *partials, uint32_t *tmp, uint32_t *sorted_idx,
+                                   uint32_t *cell_start, uint32_t *cell_end, cudaStream_t s);
 cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4 *x,
                                   cudaStream_t s);
 // tpp: lanes sharing one particle's neighbour walk (1, 2, 4, 8, 16, 32).

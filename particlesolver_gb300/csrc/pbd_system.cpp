@@ -419,6 +419,20 @@ float clamp_dt(const pbd_system *s, float dt) { return std::min(dt, s->params.ma
 
 }  // namespace
 
+int pbd_internal_device_params(const pbd_params *params, pbd::DevParams *out, std::string *why) {
+    std::string w;
+    const int rc = validate_params(params, w);
+    if (rc) {
+        if (why) *why = w;
+        return rc;
+    }
+    const float zero[6] = {0, 0, 0, 0, 0, 0};
+    *out = make_dev(*params, zero);
+    return PBD_OK;
+}
+
+void pbd_internal_set_thread_error(const std::string &msg) { g_create_error = msg; }
+
 // =================================================================== ABI
 
 extern "C" {

@@ -74,3 +74,8 @@ struct pbd_system {
 
     std::string err;
 };
+
+// Shared by the C ABI translation units: parameter validation into device
+// constants, and the calling thread's error text for calls without a handle.
+int pbd_internal_device_params(const pbd_params *params, pbd::DevParams *out, std::string *why);
+void pbd_internal_set_thread_error(const std::string &msg);
