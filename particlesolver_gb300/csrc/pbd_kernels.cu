@@ -261,6 +261,8 @@ struct Group {
     }
 };
 
+__device__ __forceinline__ float sq(float v) { return v * v; }
+
 // Distance from coordinate p to the unwrapped cell k of one axis.
 __device__ __forceinline__ float slab_gap(float p, float origin, float cell, int k) {
     const float lo = origin + (float)k * cell;
@@ -627,10 +629,13 @@ __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uin
 }
 
 // Stencil ranges with the radius fixed at compile time (RAD > 0; RAD = 0
-// defers to the runtime version): rows unroll, the per-axis slab gaps are
-// computed once, and the x extent of each kept row comes from a reciprocal
-// square root (its rounding is covered by the 1e-3-cell widening).  Same
-// visiting order and the same exactness conditions as stencil_ranges.
+// defers to the runtime version).  The per-axis slab gaps are computed once
+// and, per z slab, all 2 RAD + 1 row ranges are fetched before any of them
+// is walked, so their cell-offset loads overlap instead of each row waiting
+// for its own.  The x extent of a kept row comes from a reciprocal square
+// root (its rounding is covered by the 1e-3-cell widening).  Same visiting
+// order and the same exactness conditions as stencil_ranges; a slab with a
+// wrapping row is walked row by row, cell by cell where it wraps.
 template <int RAD, class F>
 __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 q, int3 g, float reach2, bool trim,
                                                      const uint32_t *__restrict__ cell_first, F &&f) {
@@ -641,41 +646,74 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
     constexpr int W = 2 * RAD + 1;
     const float lim = reach2 * 1.0001f + 1e-30f;
     const float inv_cell = 1.f / P.cell;
-    float gz2[W], gy2[W];
+    const float qx = (q.x - P.origin.x) * inv_cell;
+    float gy2[W];
 #pragma unroll
     for (int k = 0; k < W; ++k) {
-        const float tz = trim ? slab_gap(q.z, P.origin.z, P.cell, g.z + k - RAD) : 0.f;
-        const float ty = trim ? slab_gap(q.y, P.origin.y, P.cell, g.y + k - RAD) : 0.f;
-        gz2[k] = tz * tz;
-        gy2[k] = ty * ty;
+        const float t = trim ? slab_gap(q.y, P.origin.y, P.cell, g.y + k - RAD) : 0.f;
+        gy2[k] = t * t;
     }
-    const float qx = (q.x - P.origin.x) * inv_cell;
-#pragma unroll
+#pragma unroll 1
     for (int kz = 0; kz < W; ++kz) {
-        if (gz2[kz] > lim) continue;
-        const uint32_t z = (uint32_t)(g.z + kz - RAD) & (P.gz - 1u);
+        const float tz = trim ? slab_gap(q.z, P.origin.z, P.cell, g.z + kz - RAD) : 0.f;
+        const float gz2 = tz * tz;
+        if (gz2 > lim) continue;
+        const uint32_t zrow = ((uint32_t)(g.z + kz - RAD) & (P.gz - 1u)) * P.gy;
+        uint32_t rb[W], re[W];
+        bool wraps = false;
 #pragma unroll
         for (int ky = 0; ky < W; ++ky) {
-            const float gyz2 = gz2[kz] + gy2[ky];
-            if (gyz2 > lim) continue;
-            int xa = -RAD, xb = RAD;
-            if (trim) {
-                const float r2 = lim - gyz2;
-                const float wc = r2 * rsqrtf(fmaxf(r2, 1e-30f)) * inv_cell;  // slice half-width in cells
-                xa = max(xa, __float2int_rd(qx - wc - 1e-3f) - g.x);
-                xb = min(xb, __float2int_rd(qx + wc + 1e-3f) - g.x);
+            rb[ky] = re[ky] = 0u;  // empty unless kept
+            const float gyz2 = gz2 + gy2[ky];
+            if (gyz2 <= lim) {
+                int a = -RAD, b = RAD;
+                if (trim) {
+                    const float r2 = lim - gyz2;
+                    const float wc = r2 * rsqrtf(fmaxf(r2, 1e-30f)) * inv_cell;
+                    a = max(a, __float2int_rd(qx - wc - 1e-3f) - g.x);
+                    b = min(b, __float2int_rd(qx + wc + 1e-3f) - g.x);
+                }
+                const int x0 = g.x + a, x1 = g.x + b;
+                if (x0 >= 0 && x1 < (int)P.gx) {
+                    if (x0 <= x1) {
+                        const uint32_t row = (zrow + ((uint32_t)(g.y + ky - RAD) & (P.gy - 1u))) * P.gx;
+                        rb[ky] = __ldg(cell_first + row + (uint32_t)x0);
+                        re[ky] = __ldg(cell_first + row + (uint32_t)x1 + 1u);
+                    }
+                } else if (a <= b) {
+                    wraps = true;
+                }
             }
-            const uint32_t y = (uint32_t)(g.y + ky - RAD) & (P.gy - 1u);
-            const uint32_t row = (z * P.gy + y) * P.gx;
-            const int x0 = g.x + xa, x1 = g.x + xb;
-            if (x0 >= 0 && x1 < (int)P.gx) {
-                if (x0 <= x1 &&
-                    !f(__ldg(cell_first + row + (uint32_t)x0), __ldg(cell_first + row + (uint32_t)x1 + 1u)))
-                    return;
-            } else {
-                for (int dx = xa; dx <= xb; ++dx) {
-                    const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
-                    if (!f(__ldg(cell_first + c), __ldg(cell_first + c + 1u))) return;
+        }
+        if (!wraps) {
+#pragma unroll
+            for (int ky = 0; ky < W; ++ky)
+                if (rb[ky] < re[ky] && !f(rb[ky], re[ky])) return;
+        } else {
+            // rare: recompute each row (no indexed arrays, which would live
+            // in local memory) and walk wrapping rows cell by cell
+#pragma unroll 1
+            for (int ky = 0; ky < W; ++ky) {
+                const float gyz2 = gz2 + (trim ? sq(slab_gap(q.y, P.origin.y, P.cell, g.y + ky - RAD)) : 0.f);
+                if (gyz2 > lim) continue;
+                int a = -RAD, b = RAD;
+                if (trim) {
+                    const float r2 = lim - gyz2;
+                    const float wc = r2 * rsqrtf(fmaxf(r2, 1e-30f)) * inv_cell;
+                    a = max(a, __float2int_rd(qx - wc - 1e-3f) - g.x);
+                    b = min(b, __float2int_rd(qx + wc + 1e-3f) - g.x);
+                }
+                const uint32_t row = (zrow + ((uint32_t)(g.y + ky - RAD) & (P.gy - 1u))) * P.gx;
+                const int x0 = g.x + a, x1 = g.x + b;
+                if (x0 >= 0 && x1 < (int)P.gx) {
+                    if (x0 <= x1 && !f(__ldg(cell_first + row + (uint32_t)x0),
+                                       __ldg(cell_first + row + (uint32_t)x1 + 1u)))
+                        return;
+                } else {
+                    for (int dx = a; dx <= b; ++dx) {
+                        const uint32_t c = row + ((uint32_t)(g.x + dx) & (P.gx - 1u));
+                        if (!f(__ldg(cell_first + c), __ldg(cell_first + c + 1u))) return;
+                    }
                 }
             }
         }
@@ -1226,11 +1264,10 @@ cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, 
     if (n == 0) return cudaSuccess;
     if (tpp == 1 && L.slot) {
         const unsigned nb = blocks_for(n);
-        // the 9-row stencil unrolls; wider ones stay loops (fully unrolled
-        // 25-row code measured slower: instruction-cache stalls, lower
-        // occupancy)
         if (P.fluid_rad == 1)
             k_lambda_list<1><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+        else if (P.fluid_rad == 2)
+            k_lambda_list<2><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
         else
             k_lambda_list<0><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
         return cudaGetLastError();

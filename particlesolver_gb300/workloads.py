@@ -76,7 +76,7 @@ def dam_break(nx: int = 128, ny: int = 128, nz: int = 64, h: float = 0.1, seed: 
     """3-D PBF dam break: an nx*ny*nz fluid block, lattice spacing h/2,
     jitter U(-0.01h, 0.01h), in the corner of a box four block-widths long
     in x and twice the block height; cell size h / cell_div, power-of-two
-    grid covering the box.
+    grid covering the box's length and depth and the block's height.
 
     Unit mass, rest density = the lattice's poly6 sum; s_corr k = 0.1,
     n = 4, dq = 0.2 h and relaxation 1 in kernel-radius units
@@ -87,7 +87,10 @@ def dam_break(nx: int = 128, ny: int = 128, nz: int = 64, h: float = 0.1, seed: 
     r = 0.5 * s
     ext = np.array([4 * nx * s, 2 * ny * s, nz * s])
     cell = h / cell_div
-    grid = [next_pow2(ext[k] / cell) for k in range(3)]
+    # the grid spans the box in x and z and the block's height in y; rare
+    # particles splashing higher wrap onto lower cells (the reference's
+    # power-of-two wrap), where the distance test rejects them
+    grid = [next_pow2(ext[0] / cell), next_pow2(ny * s / cell), next_pow2(ext[2] / cell)]
     ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
     # particle order: x fastest, then y, then z (the reference's lattice loops)
     lat = np.stack([ii.transpose(2, 1, 0).ravel(), jj.transpose(2, 1, 0).ravel(), kk.transpose(2, 1, 0).ravel()], 1)
