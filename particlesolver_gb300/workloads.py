@@ -256,3 +256,91 @@ def apply_to(scene: Scene, system, params=None):
     for first, count, st in scene.bodies:
         system.add_rigid_body(first, count, st)
     return system
+
+
+def mixed_scene(cloth: int = 256, ropes: int = 2000, rope_particles: int = 64, bodies: int = 10000,
+                side: int = 4, radius: float = 0.25, seed: int = 77, iterations: int = 4,
+                rope_lift: float = 3.0, layer_gap: float = 1.0, body_lift: float | None = None) -> Scene:
+    """Mixed rigid/rope/cloth scene: a cloth x cloth sheet with stretch
+    (axis neighbours), shear (diagonals) and bend (skip-one) distance
+    constraints and pinned edges; `ropes` free ropes of `rope_particles`
+    particles in layers above it; and `bodies` shape-matched side^3 boxes at
+    seeded uniform-random orientations above the ropes.  Spacing 2 r;
+    every object has its own phase (RIGID + id), so no self-collisions.
+    Heights: cloth at 10, the first rope layer rope_lift above it, rope
+    layers layer_gap apart, box centres from body_lift (default 2 side r)
+    above the last rope layer, box layers 4 side r apart.
+    The defaults give 65,536 + 128,000 + 640,000 = 833,536 particles."""
+    d = 2.0 * radius
+    ext = cloth * d  # sheet edge length
+    pos, phase, pairs, rest, pins = [], [], [], [], []
+    obj = 0
+    # cloth, particle (x, z) at index x + cloth * z, height 10
+    cx, cz = np.meshgrid(np.arange(cloth), np.arange(cloth), indexing="xy")
+    cloth_pos = np.stack([cx.ravel() * d, np.full(cloth * cloth, 10.0), cz.ravel() * d], 1)
+    pos.append(cloth_pos)
+    phase.append(np.full(cloth * cloth, PHASE_RIGID + obj, np.int32))
+    obj += 1
+    idx = np.arange(cloth * cloth).reshape(cloth, cloth)  # [z, x]
+    for (a, b, rl) in ((idx[:, :-1], idx[:, 1:], d), (idx[:-1, :], idx[1:, :], d),            # stretch
+                       (idx[:-1, :-1], idx[1:, 1:], d * math.sqrt(2)), (idx[:-1, 1:], idx[1:, :-1], d * math.sqrt(2)),  # shear
+                       (idx[:, :-2], idx[:, 2:], 2 * d), (idx[:-2, :], idx[2:, :], 2 * d)):     # bend
+        pairs.append(np.stack([a.ravel(), b.ravel()], 1))
+        rest.append(np.full(a.size, rl))
+    edge = np.unique(np.concatenate([idx[0, :], idx[-1, :], idx[:, 0], idx[:, -1]]))
+    pins.append(edge)
+    n0 = cloth * cloth
+    # ropes along x in layers above the sheet
+    per_row = max(1, int(ext // (rope_particles * d)))
+    rows_per_layer = max(1, int(ext // 1.0))
+    for r in range(ropes):
+        layer, rr = divmod(r, per_row * rows_per_layer)
+        row, k = divmod(rr, per_row)
+        start = np.array([k * rope_particles * d, 10.0 + rope_lift + layer_gap * layer,
+                          (row + 0.5) * (ext / rows_per_layer)])
+        rp = start + np.arange(rope_particles)[:, None] * np.array([d, 0.0, 0.0])
+        pos.append(rp)
+        phase.append(np.full(rope_particles, PHASE_RIGID + obj, np.int32))
+        obj += 1
+        ids = n0 + np.arange(rope_particles)
+        pairs.append(np.stack([ids[:-1], ids[1:]], 1))
+        rest.append(np.full(rope_particles - 1, d))
+        n0 += rope_particles
+    rope_layers = -(-ropes // (per_row * rows_per_layer))
+    top = 10.0 + rope_lift + layer_gap * max(0, rope_layers - 1) + (side * d if body_lift is None else body_lift)
+    # boxes above, on a lattice of 2 side spacing, random orientations
+    g = (np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3) - (side - 1) / 2.0) * d
+    qs = random_quaternions(seed, bodies)
+    pitch = 2.0 * side * d
+    per_axis = max(1, int(ext // pitch))
+    body_list = []
+    for b in range(bodies):
+        layer, rr = divmod(b, per_axis * per_axis)
+        ix, iz = divmod(rr, per_axis)
+        c = np.array([(ix + 0.5) * pitch, top + layer * pitch, (iz + 0.5) * pitch])
+        pts = quat_rotate(np.broadcast_to(qs[b], (g.shape[0], 4)), g) + c
+        body_list.append((n0, g.shape[0], 1.0))
+        pos.append(pts)
+        phase.append(np.full(g.shape[0], PHASE_RIGID + obj, np.int32))
+        obj += 1
+        n0 += g.shape[0]
+    pos = np.concatenate(pos)
+    n = pos.shape[0]
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos + uniform(seed + 1, (n, 3), -0.01 * radius, 0.01 * radius)
+    pos_w[:, 3] = 1.0
+    pins = np.concatenate(pins).astype(np.uint32)
+    height = float(top + (bodies // (per_axis * per_axis) + 1) * pitch + 2.0)
+    cell = 2.002 * radius
+    # the wrapping hash lets x and z spill a few cells past the grid's span
+    grid = [next_pow2(ext / cell), next_pow2(height / cell), next_pow2(ext / cell)]
+    params = dict(particle_radius=radius, kernel_radius=2.0 * radius, cell_size=cell, grid_size=grid,
+                  world_origin=[-1.0, 0.0, -1.0], gravity=[0.0, -9.8, 0.0], box_min=[-1.0, 0.0, -1.0],
+                  box_max=[ext + 1.0, height, ext + 1.0], iterations=iterations, relaxation=0.01, scorr_k=0.1,
+                  scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0, max_dt=0.05, max_neighbors=500,
+                  contact_static_friction=0.005, contact_kinetic_friction=0.0002,
+                  wall_static_friction=0.005, wall_kinetic_friction=0.0002)
+    return Scene("mixed", params, pos_w, np.concatenate(phase), pairs=np.concatenate(pairs).astype(np.uint32),
+                 rest=np.concatenate(rest).astype(np.float32), pins=pins, pin_points=pos_w[pins, :3].copy(),
+                 bodies=body_list, dt=1.0 / 60.0,
+                 info=dict(cloth=cloth, ropes=ropes, bodies=bodies, constraints=int(sum(len(r) for r in rest))))

@@ -271,6 +271,64 @@ def test_full_update_trajectory(builder, steps):
     check_trajectory(g.positions(), o.positions(), sc.pos_w)
 
 
+def _small_mixed():
+    return W.mixed_scene(cloth=24, ropes=12, rope_particles=16, bodies=24, rope_lift=0.55, layer_gap=0.55,
+                         body_lift=1.4)
+
+
+def test_mixed_scene_stages():
+    """Cloth (stretch/shear/bend), ropes and shape-matched boxes pressed
+    together: every projector of one iteration against the FP64 oracle."""
+    sc = _small_mixed()
+    g, o = make_pair(sc)
+    pos = sc.pos_w.copy()
+    pos[:, 1] = 10.0 + (pos[:, 1] - 10.0) * 0.6  # overlap rope and box layers
+    g.set_positions(pos)
+    o.set_positions(pos.astype(np.float64))
+    g.build_grid()
+    o.build_grid()
+    for stage in ("collide", "collide_world", "solve_distance_constraints", "solve_point_constraints",
+                  "solve_shapes"):
+        before = g.positions()
+        getattr(g, stage)()
+        getattr(o, stage)()
+        assert_projection(g.positions(), o.positions(), before, TOL_STAGE)
+        sync_positions(g, o)
+
+
+def test_mixed_scene_trajectory_invariants():
+    """Ropes fall onto the pinned cloth and boxes onto the ropes: positions
+    by invariants, plus the distance-constraint residual and the rigid
+    bodies' RMS deviation from their rest shape, against the oracle."""
+    sc = _small_mixed()
+    g, o = make_pair(sc)
+    for _ in range(12):
+        g.update(sc.dt)
+        o.update(sc.dt)
+    pg, po = g.positions().astype(np.float64), o.positions()
+    check_trajectory(pg, po, sc.pos_w)
+    a, b = sc.pairs[:, 0], sc.pairs[:, 1]
+
+    def residual(p):
+        return np.abs(np.linalg.norm(p[a, :3] - p[b, :3], axis=1) - sc.rest)
+
+    assert abs(residual(pg).mean() - residual(po).mean()) <= 1e-3 * sc.rest.mean()
+
+    def rigid_rms(p):
+        dev = []
+        for f, c, _ in sc.bodies:
+            x = p[f:f + c, :3] - p[f:f + c, :3].mean(0)
+            r = sc.pos_w[f:f + c, :3].astype(np.float64)
+            r = r - r.mean(0)
+            u, _, vt = np.linalg.svd(x.T @ r)
+            rot = u @ np.diag([1.0, 1.0, np.sign(np.linalg.det(u @ vt))]) @ vt
+            dev.append(np.mean(np.sum((x - r @ rot.T) ** 2, 1)))
+        return np.sqrt(np.mean(dev))
+
+    assert abs(rigid_rms(pg) - rigid_rms(po)) <= 1e-3 * 2 * sc.params["particle_radius"]
+    np.testing.assert_array_equal(g.positions()[sc.pins, :3], sc.pin_points)
+
+
 def test_graph_replay_matches_eager_bitwise():
     sc = W.dam_break(16, 16, 8)
     a = ParticleSystem(default_params(**sc.params), sc.n)
