@@ -177,6 +177,104 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def load_scenes(scenes, max_particles=None):
+    """All scenes in one system, scene k from slot sum(n_0 .. n_(k-1))."""
+    from particlesolver_gb300 import ParticleSystem, default_params
+    from particlesolver_gb300 import workloads as W
+
+    total = sum(sc.n for sc in scenes)
+    sysm = ParticleSystem(default_params(**scenes[0].params), max_particles or total)
+    for k, sc in enumerate(scenes):
+        if k:
+            sysm.begin_scene(default_params(**sc.params))
+        first = sysm.num_particles
+        W.apply_to(W.Scene(sc.name, sc.params, sc.pos_w, sc.phase, vel=sc.vel, rest_density=sc.rest_density,
+                           pairs=None if sc.pairs is None else sc.pairs + first, rest=sc.rest,
+                           stiffness=sc.stiffness, pins=None if sc.pins is None else sc.pins + first,
+                           pin_points=sc.pin_points, bodies=[(f + first, c, st) for f, c, st in sc.bodies]), sysm)
+    return sysm
+
+
+def run_batched(args, dev, stream, flush):
+    """Batched scenes (512 PBF blocks / granular columns, log-uniform 1k-64k
+    particles): one system stepping every scene with one launch per stage,
+    replayed from a CUDA graph, against the plain per-scene solver (one
+    system per scene, stepped one after another on the same stream)."""
+    import torch
+
+    from particlesolver_gb300 import ParticleSystem, default_params
+    from particlesolver_gb300 import workloads as W
+
+    scenes = W.batched_scenes(args.batch_scenes)
+    S = len(scenes)
+    total = sum(sc.n for sc in scenes)
+    dt = 1.0 / 60.0
+    sh = stream.cuda_stream
+    batch = load_scenes(scenes)
+    for _ in range(3):
+        batch.update(dt, sh)
+    batch.autotune(dt, 2, sh)
+    batch.update_graph(dt, 1, sh)
+    torch.cuda.synchronize()
+    K = args.batch_steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    batch.reset_profile()
+    with torch.cuda.stream(stream):
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            batch.update_graph(dt, 1, sh)
+            b.record(stream)
+    torch.cuda.synchronize()
+    t_batch = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    launches = batch.profile()["kernel_launches"]
+    batch.check_finite(sh)
+    del batch
+
+    singles = []
+    for sc in scenes:
+        sy = ParticleSystem(default_params(**sc.params), sc.n)
+        W.apply_to(sc, sy)
+        singles.append(sy)
+    for sy in singles:
+        sy.update(dt, sh)
+
+    def per_scene(graph: bool, steps: int):
+        for sy in singles:  # warm (and capture)
+            sy.update_graph(dt, 1, sh) if graph else sy.update(dt, sh)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a.record(stream)
+            for _ in range(steps):
+                for sy in singles:
+                    sy.update_graph(dt, 1, sh) if graph else sy.update(dt, sh)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    k_single = max(1, min(K, args.batch_single_steps))
+    t_eager = per_scene(False, k_single)
+    t_graph = per_scene(True, k_single)
+    for sy in singles:
+        sy.close()
+    kinds = [sc.name for sc in scenes]
+    v_batch = S * K / t_batch
+    v_eager = S * k_single / t_eager
+    v_graph = S * k_single / t_graph
+    return {"unit": "scenes*steps/s", "value": v_batch, "scenes": S, "particles": total,
+            "pbf_blocks": kinds.count("pbf_block"), "granular_columns": kinds.count("granular_column"),
+            "steps": K, "ms_per_step": 1e3 * t_batch / K, "gpu_launches": launches,
+            "per_scene_plain": {"value": v_eager, "steps": k_single, "ms_per_step": 1e3 * t_eager / k_single,
+                                "how": "one system per scene, pbd_update each, same stream"},
+            "per_scene_graph": {"value": v_graph, "steps": k_single, "ms_per_step": 1e3 * t_graph / k_single,
+                                "how": "one system per scene, its own captured step graph"},
+            "speedup_vs_plain": v_batch / v_eager, "speedup_vs_per_scene_graph": v_batch / v_graph,
+            "dt": dt, "workload": f"{S} scenes, counts round(exp(U(ln 1024, ln 65536))), PBF block or 2-D "
+                                  f"granular column by coin flip (seeded)"}
+
+
 def _param_defaults():
     return dict(particle_radius=0.25, kernel_radius=2.0, cell_size=0.5, grid_size=[64, 64, 64],
                 world_origin=[0, 0, 0], gravity=[0, -9.8, 0], box_min=[-50, 0, -50], box_max=[50, 200, 50],
@@ -286,6 +384,10 @@ def run_ours(args, world, rank, local_rank):
         e2e_s = float(t.item())
     e2e_value = world * e2e_steps / e2e_s
     sysm.check_finite(sh)
+    batched = None
+    if args.batch_scenes:
+        sysm.close()
+        batched = run_batched(args, dev, stream, flush)
 
     if rank != 0:
         return
@@ -338,6 +440,7 @@ def run_ours(args, world, rank, local_rank):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
 
@@ -355,6 +458,9 @@ def main():
     ap.add_argument("--tpp", type=int, default=0, help="lanes per particle (0 = autotune)")
     ap.add_argument("--cell-div", type=int, default=1, help="grid cell size = h / cell_div")
     ap.add_argument("--ref-budget-s", type=float, default=120.0)
+    ap.add_argument("--batch-scenes", type=int, default=512, help="batched-scenes measurement (0 = skip)")
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-single-steps", type=int, default=3)
     args = ap.parse_args()
     world, rank, local_rank = dist_env()
     if args.impl == "reference":

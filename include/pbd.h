@@ -133,12 +133,34 @@ int pbd_destroy(pbd_system *sys);
 /* Last error text of sys; sys == NULL gives the calling thread's last
  * pbd_create failure. */
 const char *pbd_last_error(const pbd_system *sys);
-/* Replaces setParameters (integration.cu:96-100). */
+/* Replaces setParameters (integration.cu:96-100).  With several scenes
+ * these act on scene 0. */
 int pbd_set_params(pbd_system *sys, const pbd_params *params);
 int pbd_get_params(const pbd_system *sys, pbd_params *out);
 /* Replaces getNumParticles (particlesystem.h:48). */
 uint32_t pbd_num_particles(const pbd_system *sys);
 uint32_t pbd_capacity(const pbd_system *sys);
+
+/* ---------------------------------------------------------------- scenes
+ *
+ * A system holds one or more independent scenes (the reference has one
+ * ParticleSystem per scene; particlesystem.cpp:36-69).  pbd_create makes
+ * scene 0 with its params; pbd_begin_scene opens the next scene with its
+ * own params, and every later pbd_add_* call fills the newest scene.  A
+ * scene's particles are the slots [first, first + count) in add order;
+ * distance constraints and rigid bodies must stay inside one scene.  Scenes
+ * never interact: each has its own grid, box, constants, iteration count
+ * and dt clamp (max_dt).  pbd_update advances every scene by one step with
+ * the same launches (one per stage over all scenes); a scene with K
+ * iterations runs in the last K of the batch's iterations and gives the
+ * result it would give alone.  The stage entry points act on every scene
+ * with iterations > 0. */
+#define PBD_MAX_SCENES 65535u
+int pbd_begin_scene(pbd_system *sys, const pbd_params *params, uint32_t *scene_index);
+uint32_t pbd_num_scenes(const pbd_system *sys);
+/* first / count / params may be NULL. */
+int pbd_get_scene(const pbd_system *sys, uint32_t scene, uint32_t *first, uint32_t *count, pbd_params *params);
+int pbd_set_scene_params(pbd_system *sys, uint32_t scene, const pbd_params *params);
 
 /* --------------------------------------------------------- scene content */
 

@@ -134,6 +134,10 @@ _SIGNATURES = {
     "pbd_last_error": ([_P], ctypes.c_char_p),
     "pbd_set_params": ([_P, ctypes.POINTER(PbdParams)], _I),
     "pbd_get_params": ([_P, ctypes.POINTER(PbdParams)], _I),
+    "pbd_begin_scene": ([_P, ctypes.POINTER(PbdParams), _PU], _I),
+    "pbd_num_scenes": ([_P], _U32),
+    "pbd_get_scene": ([_P, _U32, _PU, _PU, ctypes.POINTER(PbdParams)], _I),
+    "pbd_set_scene_params": ([_P, _U32, ctypes.POINTER(PbdParams)], _I),
     "pbd_num_particles": ([_P], _U32),
     "pbd_capacity": ([_P], _U32),
     "pbd_num_cells": ([_P], _U32),
@@ -311,6 +315,26 @@ class ParticleSystem:
     def set_params(self, params: PbdParams):
         self._check(self.lib.pbd_set_params(self.h, ctypes.byref(params)))
         self.params = params
+
+    # -- scenes ---------------------------------------------------------
+    def begin_scene(self, params: PbdParams) -> int:
+        """Open the next independent scene; later add_* calls fill it."""
+        k = ctypes.c_uint32()
+        self._check(self.lib.pbd_begin_scene(self.h, ctypes.byref(params), ctypes.byref(k)))
+        return k.value
+
+    @property
+    def num_scenes(self) -> int:
+        return int(self.lib.pbd_num_scenes(self.h))
+
+    def scene(self, k: int):
+        """(first slot, particle count, params) of scene k."""
+        first, count, p = ctypes.c_uint32(), ctypes.c_uint32(), PbdParams()
+        self._check(self.lib.pbd_get_scene(self.h, k, ctypes.byref(first), ctypes.byref(count), ctypes.byref(p)))
+        return first.value, count.value, p
+
+    def set_scene_params(self, k: int, params: PbdParams):
+        self._check(self.lib.pbd_set_scene_params(self.h, k, ctypes.byref(params)))
 
     # reference scene builders
     def add_fluid(self, ll, ur, mass, density, seed=1):

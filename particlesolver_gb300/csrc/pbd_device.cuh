@@ -60,6 +60,17 @@ struct DevParams {
     float twod_z;
     uint32_t flags;
     float rands[6];      // wall jitter uniforms
+    uint32_t iterations; // solver iterations per step
+    float max_dt;        // step length clamp
+    // First cell of this scene in the cell space shared by every scene of a
+    // system (0 for a system with one scene): each scene hashes into its own
+    // block of cells, so one counting sort keeps scenes apart and contiguous.
+    uint32_t cell_base;
+    // Batched launches only (nullptr otherwise): the parameter block of every
+    // scene and the scene of every particle slot.  A scene's particles
+    // occupy the same slot range in original and in sorted order.
+    const DevParams *table;
+    const uint16_t *scene_of;
 };
 
 #if defined(__CUDACC__)
@@ -99,7 +110,7 @@ __device__ __forceinline__ uint32_t grid_hash(const DevParams &P, int3 g) {
     uint32_t x = (uint32_t)g.x & (P.gx - 1u);
     uint32_t y = (uint32_t)g.y & (P.gy - 1u);
     uint32_t z = (uint32_t)g.z & (P.gz - 1u);
-    return (z * P.gy + y) * P.gx + x;
+    return P.cell_base + (z * P.gy + y) * P.gx + x;
 }
 
 // Visits the candidate particles of the (2 rad + 1)^3 cell stencil around
@@ -117,7 +128,7 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &P, int3 g, i
         const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
         for (int dy = -rad; dy <= rad; ++dy) {
             const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
-            const uint32_t row = (z * P.gy + y) * P.gx;
+            const uint32_t row = P.cell_base + (z * P.gy + y) * P.gx;
             const int x0 = g.x - rad, x1 = g.x + rad;
             if (x0 >= 0 && x1 < (int)P.gx) {
                 const uint32_t b = __ldg(cell_first + row + (uint32_t)x0);
@@ -134,6 +145,23 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &P, int3 g, i
             }
         }
     }
+}
+
+// Parameters of the scene that slot i belongs to: the launch's own block
+// for a single scene, the scene table's entry in a batched launch.
+template <bool B>
+__device__ __forceinline__ DevParams scene_params(const DevParams &P0, uint32_t i) {
+    if constexpr (B) return P0.table[P0.scene_of[i]];
+    else return P0;
+}
+
+// Iterations run right-aligned in a batch: a scene with K iterations is
+// active in the last K of the batch's, so its last iteration (whose grid
+// and neighbour lists XSPH reuses) is everyone's last.  iter_left counts
+// the batch iterations still to come after the current one.
+template <bool B>
+__device__ __forceinline__ bool scene_active(const DevParams &P, uint32_t iter_left) {
+    return !B || iter_left < P.iterations;
 }
 
 #endif  // __CUDACC__

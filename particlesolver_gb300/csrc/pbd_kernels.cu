@@ -25,8 +25,10 @@ inline unsigned blocks_for(uint32_t n, int per_block = kBlock) {
 // reference does not store v'; neither do we (the velocity is recomputed
 // from positions at the end of the step).  When counts is given, the cell
 // hash of the predicted position is computed and counted here too, which is
-// the first grid build's calcHashD (integration_kernel.cuh:206-225).
-__global__ void __launch_bounds__(kBlock) k_predict(DevParams P, uint32_t n, float dt,
+// the first grid build's calcHashD (integration_kernel.cuh:206-225).  The
+// step is min(dt, max_dt) of the particle's scene.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_predict(DevParams P0, uint32_t n, float dt_in,
                                                     float4 *__restrict__ x,
                                                     const float4 *__restrict__ v,
                                                     float4 *__restrict__ x_old,
@@ -35,6 +37,8 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevParams P, uint32_t n, flo
                                                     uint32_t *__restrict__ counts) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    const float dt = fminf(dt_in, P.max_dt);
     float4 p = x[i];
     const float4 vel = v[i];
     x_old[i] = p;
@@ -53,13 +57,15 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevParams P, uint32_t n, flo
 // calcHashD (integration_kernel.cuh:206-225) plus the per-cell count of the
 // counting sort.  The arrival slot is only used to bucket indices; the final
 // order inside a cell is fixed by original index in k_rank_reorder.
-__global__ void __launch_bounds__(kBlock) k_hash_count(DevParams P, uint32_t n,
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_hash_count(DevParams P0, uint32_t n,
                                                        const float4 *__restrict__ x,
                                                        uint32_t *__restrict__ hash,
                                                        uint32_t *__restrict__ slot,
                                                        uint32_t *__restrict__ counts) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
     const uint32_t h = grid_hash(P, grid_pos(P, f3(x[i])));
     hash[i] = h;
     slot[i] = atomicAdd(counts + h, 1u);
@@ -308,7 +314,7 @@ __device__ __forceinline__ void stencil_ranges(const DevParams &P, float3 q, int
                 xb = min(xb, __float2int_rd((q.x + w - P.origin.x) * inv_cell + 1e-3f) - g.x);
             }
             const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);
-            const uint32_t row = (z * P.gy + y) * P.gx;
+            const uint32_t row = P.cell_base + (z * P.gy + y) * P.gx;
             const int x0 = g.x + xa, x1 = g.x + xb;
             if (x0 >= 0 && x1 < (int)P.gx) {
                 if (x0 <= x1 &&
@@ -392,8 +398,8 @@ struct LambdaAcc {
 // Non-fluid particles get lambda = 0 (the reference left their slots
 // unwritten and read whatever was there, integration_kernel.cuh:636).
 // Output: (position, lambda) per sorted slot, the delta pass's one load.
-template <int TPP>
-__global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
+template <int TPP, bool B>
+__global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uint32_t iter_left,
                                                    const float4 *__restrict__ sx,
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
@@ -401,6 +407,8 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P, uint32_t n,
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    if (!scene_active<B>(P, iter_left)) return;
     const SortedAttr a = sattr[i];
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
@@ -532,18 +540,19 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
     return delta / div;
 }
 
-__device__ __forceinline__ float scaled_inv_mass(float w, float y) {
-    return (w != 0.f) ? (1.f / ((1.f / w) * expf(-y))) : w;
-}
-
 // collideD + collideCell (integration_kernel.cuh:303-462): contacts of a
 // non-fluid particle with every particle closer than 2.001 r in the 27-cell
 // stencil (same-object pairs skipped, capped at max_nb), each averaged over
-// the contact count; solid-solid pairs use the height-scaled inverse mass
-// w e^y (both evaluated at this particle's y, as in the reference) and get
-// static/kinetic friction against the start-of-step positions.  Pairs with
-// zero total inverse mass or zero separation are skipped (the reference
-// produced NaN there).  Two walks: the count, then the corrections.
+// the contact count; solid-solid pairs get static/kinetic friction against
+// the start-of-step positions.  The reference scales both inverse masses of
+// a solid-solid pair by the same e^y (y of this particle,
+// integration_kernel.cuh:403,422-426); the factor cancels in w_i / (w_i + w_j),
+// the only way the masses enter, so it is left out -- exact in real
+// arithmetic, and free of the FP32 overflow above y ~ 88 where the
+// reference's w e^y became inf and the correction inf * 0 = NaN.  Pairs
+// with zero total inverse mass or zero separation are skipped (the
+// reference produced NaN there).  Two walks: the count, then the
+// corrections.
 template <int TPP>
 __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float4 pi4,
                                                 int ph, uint32_t orig, const float4 *__restrict__ sx,
@@ -563,7 +572,6 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
     const float w = pi4.w;
-    const float sw = scaled_inv_mass(w, pi.y);
     const float3 prev = f3(x_old[orig]);
     const float fnb = (float)nb;
     group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, nb, test,
@@ -573,11 +581,7 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
         const float3 diff = pi - pj;
         const float dist = len3(diff);
         const float mag = dist - P.collide_dist;
-        float colw = w, colw2 = pj4.w;
-        if (ph >= kSolid && phj >= kSolid) {
-            colw = sw;
-            colw2 = scaled_inv_mass(pj4.w, pi.y);
-        }
+        const float colw = w, colw2 = pj4.w;
         const float wsum = colw + colw2;
         if (wsum == 0.f || dist == 0.f) return;
         const float scale = mag / wsum;
@@ -676,7 +680,8 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
                 const int x0 = g.x + a, x1 = g.x + b;
                 if (x0 >= 0 && x1 < (int)P.gx) {
                     if (x0 <= x1) {
-                        const uint32_t row = (zrow + ((uint32_t)(g.y + ky - RAD) & (P.gy - 1u))) * P.gx;
+                        const uint32_t row =
+                            P.cell_base + (zrow + ((uint32_t)(g.y + ky - RAD) & (P.gy - 1u))) * P.gx;
                         rb[ky] = __ldg(cell_first + row + (uint32_t)x0);
                         re[ky] = __ldg(cell_first + row + (uint32_t)x1 + 1u);
                     }
@@ -703,7 +708,7 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
                     a = max(a, __float2int_rd(qx - wc - 1e-3f) - g.x);
                     b = min(b, __float2int_rd(qx + wc + 1e-3f) - g.x);
                 }
-                const uint32_t row = (zrow + ((uint32_t)(g.y + ky - RAD) & (P.gy - 1u))) * P.gx;
+                const uint32_t row = P.cell_base + (zrow + ((uint32_t)(g.y + ky - RAD) & (P.gy - 1u))) * P.gx;
                 const int x0 = g.x + a, x1 = g.x + b;
                 if (x0 >= 0 && x1 < (int)P.gx) {
                     if (x0 <= x1 && !f(__ldg(cell_first + row + (uint32_t)x0),
@@ -725,13 +730,16 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
 // lambda is summed over the list.  The candidate loop is branch-free: the
 // neighbour test drives predicated register inserts and a predicated
 // 16-byte store per four neighbours.  Output as k_lambda.
-template <int RAD>
-__global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P, uint32_t n, const float4 *__restrict__ sx,
+template <int RAD, bool B>
+__global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                        const float4 *__restrict__ sx,
                                                         const SortedAttr *__restrict__ sattr,
                                                         const uint32_t *__restrict__ cell_first,
                                                         float4 *__restrict__ sxl, NbList L) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    if (!scene_active<B>(P, iter_left)) return;
     const SortedAttr a = sattr[i];
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
@@ -864,8 +872,8 @@ __device__ __forceinline__ float3 world_collide(const DevParams &P, float3 e, in
 // only the sorted start-of-iteration positions, fused into one pass with one
 // write per particle.  mask selects the stages (the stage entry points run
 // them one at a time).
-template <int TPP>
-__global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint32_t mask,
+template <int TPP, bool B>
+__global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint32_t mask, uint32_t iter_left,
                                                   const float4 *__restrict__ sx,
                                                   const SortedAttr *__restrict__ sattr,
                                                   const uint32_t *__restrict__ sidx,
@@ -876,6 +884,8 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    if (!scene_active<B>(P, iter_left)) return;
     const SortedAttr a = sattr[i];
     const uint32_t orig = sidx[i];
     const float4 pi4 = sx[i];
@@ -909,7 +919,8 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P, uint32_t n, uint3
 // second), and divides by its constraint count.  The reference applied the
 // k-th reduced segment to particle k (solver.cu:227-230); here each sum goes
 // to its own particle.
-__global__ void __launch_bounds__(kBlock) k_distance_gather(DevParams P, uint32_t count,
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_distance_gather(DevParams P0, uint32_t count, uint32_t iter_left,
                                                             const uint32_t *__restrict__ particle,
                                                             const uint32_t *__restrict__ row,
                                                             const uint32_t *__restrict__ other,
@@ -921,6 +932,8 @@ __global__ void __launch_bounds__(kBlock) k_distance_gather(DevParams P, uint32_
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= count) return;
     const uint32_t k = particle[s];
+    const DevParams P = scene_params<B>(P0, k);
+    if (!scene_active<B>(P, iter_left)) return;
     const float4 xk4 = x[k];
     const float3 xk = f3(xk4);
     const bool mass_weighted = (P.flags & kFlagDistanceMassWeighted) != 0u;
@@ -947,7 +960,8 @@ __global__ void __launch_bounds__(kBlock) k_distance_gather(DevParams P, uint32_
 
 // Writes the gathered positions back and applies pins last
 // (point_constraint_functor, solver_kernel.cuh:10-25).
-__global__ void __launch_bounds__(kBlock) k_distance_apply(uint32_t count,
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_distance_apply(DevParams P0, uint32_t count, uint32_t iter_left,
                                                            const uint32_t *__restrict__ particle,
                                                            const float4 *__restrict__ tmp,
                                                            const float4 *__restrict__ pin,
@@ -956,6 +970,7 @@ __global__ void __launch_bounds__(kBlock) k_distance_apply(uint32_t count,
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= count) return;
     const uint32_t k = particle[s];
+    if (!scene_active<B>(scene_params<B>(P0, k), iter_left)) return;
     const bool pinned = apply_pins && pin[s].w != 0.f;
     if (!apply_distance && !pinned) return;
     float4 p = apply_distance ? tmp[s] : x[k];
@@ -1038,7 +1053,9 @@ __device__ __forceinline__ float warp_sum(float v) {
 // TotalShapeConstraint::project with Body::updateCOM
 // (cpu/src/constraint/totalshapeconstraint.cpp:14-24,
 // cpu/src/solver/particle.cpp:15-57).
-__global__ void __launch_bounds__(kBlock) k_shapes(uint32_t bodies, const uint4 *__restrict__ range,
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_shapes(DevParams P0, uint32_t iter_left, uint32_t bodies,
+                                                   const uint4 *__restrict__ range,
                                                    const float *__restrict__ stiff,
                                                    const float4 *__restrict__ rest,
                                                    float4 *__restrict__ quat,
@@ -1048,6 +1065,7 @@ __global__ void __launch_bounds__(kBlock) k_shapes(uint32_t bodies, const uint4 
     if (b >= bodies) return;
     const uint4 rg = range[b];
     const uint32_t first = rg.x, count = rg.y, roff = rg.z;
+    if (!scene_active<B>(scene_params<B>(P0, first), iter_left)) return;
     // centre of mass accumulated relative to the body's first particle, so
     // the FP32 sums carry offsets of the body's size, not of its position
     const float3 o = f3(x[first]);
@@ -1101,14 +1119,17 @@ __global__ void __launch_bounds__(kBlock) k_shapes(uint32_t bodies, const uint4 
 
 // --------------------------------------------------------------- velocity
 
-// subtract_functor (integration_kernel.cuh:465-475): v = (x_old - x) / -dt.
-__global__ void __launch_bounds__(kBlock) k_velocity(uint32_t n, float dt, const float4 *__restrict__ x,
+// subtract_functor (integration_kernel.cuh:465-475): v = (x_old - x) / -dt,
+// dt = min(dt, max_dt) of the particle's scene.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_velocity(DevParams P0, uint32_t n, float dt,
+                                                     const float4 *__restrict__ x,
                                                      const float4 *__restrict__ x_old,
                                                      float4 *__restrict__ v) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = x[i], o = x_old[i];
-    const float nd = -dt;
+    const float nd = -fminf(dt, scene_params<B>(P0, i).max_dt);
     v[i] = make_float4((o.x - p.x) / nd, (o.y - p.y) / nd, (o.z - p.z) / nd, 0.f);
 }
 
@@ -1126,8 +1147,8 @@ __global__ void __launch_bounds__(kBlock) k_xsph_gather(uint32_t n, const uint32
 // poly6(x_i - x_j) / rho0_i over the fluid neighbours of the last solver
 // iteration (the positions its grid was built from), with the step's final
 // velocities.
-template <int TPP>
-__global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const float4 *__restrict__ sx,
+template <int TPP, bool B>
+__global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const float4 *__restrict__ sx,
                                                  const SortedAttr *__restrict__ sattr,
                                                  const uint32_t *__restrict__ sidx,
                                                  const uint32_t *__restrict__ cell_first,
@@ -1136,6 +1157,8 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P, uint32_t n, const 
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    if (B && (P.xsph_c == 0.f || P.iterations == 0u)) return;
     const SortedAttr a = sattr[i];
     if (a.phase != kFluid) return;
     const float3 xi = f3(sx[i]);
@@ -1192,14 +1215,16 @@ cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, 
                            float4 *x_old, uint32_t *hash, uint32_t *slot, uint32_t *counts,
                            cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_predict<<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts);
+    if (P.table) k_predict<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts);
+    else k_predict<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts);
     return cudaGetLastError();
 }
 
 cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash,
                               uint32_t *slot, uint32_t *counts, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_hash_count<<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts);
+    if (P.table) k_hash_count<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts);
+    else k_hash_count<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts);
     return cudaGetLastError();
 }
 
@@ -1228,10 +1253,7 @@ cudaError_t launch_sort_into_cells(const DevParams &P, uint32_t n, const float4 
                                    uint32_t *cell_start, uint32_t *cell_end, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(cell_first, 0, ((size_t)P.num_cells + 1u) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    if (n) {
-        k_hash_count<<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, cell_first);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
+    if ((e = launch_hash_count(P, n, x, hash, slot, cell_first, s)) != cudaSuccess) return e;
     if ((e = launch_exclusive_scan(cell_first, P.num_cells + 1u, partials, s)) != cudaSuccess) return e;
     if (n) {
         k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, hash, slot, cell_first, tmp);
@@ -1248,69 +1270,95 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
     return cudaGetLastError();
 }
 
-// Dispatches a kernel template over the supported group sizes.
-#define PBD_TPP_DISPATCH(tpp, KERNEL, ...)                                             \
-    switch (tpp) {                                                                     \
-    case 1: KERNEL<1><<<blocks_for(n * 1u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 2: KERNEL<2><<<blocks_for(n * 2u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 4: KERNEL<4><<<blocks_for(n * 4u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 8: KERNEL<8><<<blocks_for(n * 8u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 16: KERNEL<16><<<blocks_for(n * 16u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
-    default: KERNEL<32><<<blocks_for(n * 32u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
+// Dispatches a kernel template over the supported group sizes (B: batched).
+#define PBD_TPP_DISPATCH(tpp, B, KERNEL, ...)                                             \
+    switch (tpp) {                                                                        \
+    case 1: KERNEL<1, B><<<blocks_for(n * 1u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 2: KERNEL<2, B><<<blocks_for(n * 2u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 4: KERNEL<4, B><<<blocks_for(n * 4u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 8: KERNEL<8, B><<<blocks_for(n * 8u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
+    case 16: KERNEL<16, B><<<blocks_for(n * 16u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
+    default: KERNEL<32, B><<<blocks_for(n * 32u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
     }
 
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, const NbList &L,
-                          uint32_t tpp, cudaStream_t s) {
+template <bool B>
+void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
+                          const NbList &L, cudaStream_t s) {
+    const unsigned nb = blocks_for(n);
+    if (P.fluid_rad == 1)
+        k_lambda_list<1, B><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+    else if (P.fluid_rad == 2)
+        k_lambda_list<2, B><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+    else
+        k_lambda_list<0, B><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+}
+
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
+                          const NbList &L, uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if (tpp == 1 && L.slot) {
-        const unsigned nb = blocks_for(n);
-        if (P.fluid_rad == 1)
-            k_lambda_list<1><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
-        else if (P.fluid_rad == 2)
-            k_lambda_list<2><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
-        else
-            k_lambda_list<0><<<nb, kBlock, 0, s>>>(P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+        if (P.table) lambda_list_dispatch<true>(P, n, iter_left, g, sxl, L, s);
+        else lambda_list_dispatch<false>(P, n, iter_left, g, sxl, L, s);
         return cudaGetLastError();
     }
-    PBD_TPP_DISPATCH(tpp, k_lambda, P, n, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
+    if (P.table) {
+        PBD_TPP_DISPATCH(tpp, true, k_lambda, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
+    } else {
+        PBD_TPP_DISPATCH(tpp, false, k_lambda, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
+cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t iter_left, const GridBuffers &g,
                          const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
                          uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
-    PBD_TPP_DISPATCH(tpp, k_solve, P, n, mask, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, sxl,
-                     x_old, x, L, use_list);
+    if (P.table) {
+        PBD_TPP_DISPATCH(tpp, true, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
+                         g.cell_first, sxl, x_old, x, L, use_list);
+    } else {
+        PBD_TPP_DISPATCH(tpp, false, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
+                         g.cell_first, sxl, x_old, x, L, use_list);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_distance(const DevParams &P, const ConstraintBuffers &c, float4 *x,
+cudaError_t launch_distance(const DevParams &P, uint32_t iter_left, const ConstraintBuffers &c, float4 *x,
                             bool apply_distance, bool apply_pins, cudaStream_t s) {
     if (c.count == 0) return cudaSuccess;
     apply_distance = apply_distance && c.any_distance;
     apply_pins = apply_pins && c.any_pin;
     if (!apply_distance && !apply_pins) return cudaSuccess;
-    if (apply_distance)
-        k_distance_gather<<<blocks_for(c.count), kBlock, 0, s>>>(P, c.count, c.particle, c.row, c.other,
-                                                                 c.rest, c.stiff, c.occ, x, c.tmp);
-    k_distance_apply<<<blocks_for(c.count), kBlock, 0, s>>>(c.count, c.particle, c.tmp, c.pin,
-                                                            apply_distance ? 1 : 0, apply_pins ? 1 : 0, x);
+    const unsigned nb = blocks_for(c.count);
+    const int ad = apply_distance ? 1 : 0, ap = apply_pins ? 1 : 0;
+    if (P.table) {
+        if (apply_distance)
+            k_distance_gather<true><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.row, c.other, c.rest,
+                                                          c.stiff, c.occ, x, c.tmp);
+        k_distance_apply<true><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.tmp, c.pin, ad, ap, x);
+    } else {
+        if (apply_distance)
+            k_distance_gather<false><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.row, c.other, c.rest,
+                                                           c.stiff, c.occ, x, c.tmp);
+        k_distance_apply<false><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.tmp, c.pin, ad, ap, x);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_shapes(const BodyBuffers &b, float4 *x, cudaStream_t s) {
+cudaError_t launch_shapes(const DevParams &P, uint32_t iter_left, const BodyBuffers &b, float4 *x, cudaStream_t s) {
     if (b.count == 0) return cudaSuccess;
-    const uint32_t threads = b.count * 32u;
-    k_shapes<<<blocks_for(threads), kBlock, 0, s>>>(b.count, b.range, b.stiff, b.rest, b.quat, x);
+    const unsigned nb = blocks_for(b.count * 32u);
+    if (P.table) k_shapes<true><<<nb, kBlock, 0, s>>>(P, iter_left, b.count, b.range, b.stiff, b.rest, b.quat, x);
+    else k_shapes<false><<<nb, kBlock, 0, s>>>(P, iter_left, b.count, b.range, b.stiff, b.rest, b.quat, x);
     return cudaGetLastError();
 }
 
-cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 *x_old, float4 *v,
-                            cudaStream_t s) {
+cudaError_t launch_velocity(const DevParams &P, uint32_t n, float dt, const float4 *x, const float4 *x_old,
+                            float4 *v, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_velocity<<<blocks_for(n), kBlock, 0, s>>>(n, dt, x, x_old, v);
+    if (P.table) k_velocity<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, x_old, v);
+    else k_velocity<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, x_old, v);
     return cudaGetLastError();
 }
 
@@ -1319,7 +1367,13 @@ cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, fl
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
     k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, v, vs);
-    PBD_TPP_DISPATCH(tpp, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L, use_list);
+    if (P.table) {
+        PBD_TPP_DISPATCH(tpp, true, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L,
+                         use_list);
+    } else {
+        PBD_TPP_DISPATCH(tpp, false, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L,
+                         use_list);
+    }
     return cudaGetLastError();
 }
 

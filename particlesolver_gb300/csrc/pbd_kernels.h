@@ -79,16 +79,22 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
 // read by the solve pass.
 // With tpp == 1 and a list allocated, the lambda pass also records the
 // neighbour list that the solve and XSPH passes then use (use_list).
-cudaError_t launch_lambda(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *sxl, const NbList &L,
-                          uint32_t tpp, cudaStream_t s);
-cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, const GridBuffers &g,
+//
+// P.table set: a batched launch over every scene of a system, each slot
+// taking its scene's parameters.  iter_left: solver iterations still to come
+// in the step after this one (a scene with K iterations is active while
+// iter_left < K); the single-stage entry points pass 0.
+cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
+                          const NbList &L, uint32_t tpp, cudaStream_t s);
+cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t iter_left, const GridBuffers &g,
                          const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
                          uint32_t tpp, cudaStream_t s);
-cudaError_t launch_distance(const DevParams &P, const ConstraintBuffers &c, float4 *x,
+cudaError_t launch_distance(const DevParams &P, uint32_t iter_left, const ConstraintBuffers &c, float4 *x,
                             bool apply_distance, bool apply_pins, cudaStream_t s);
-cudaError_t launch_shapes(const BodyBuffers &b, float4 *x, cudaStream_t s);
-cudaError_t launch_velocity(uint32_t n, float dt, const float4 *x, const float4 *x_old, float4 *v,
-                            cudaStream_t s);
+cudaError_t launch_shapes(const DevParams &P, uint32_t iter_left, const BodyBuffers &b, float4 *x, cudaStream_t s);
+// dt is clamped to each scene's max_dt on the device (predict and velocity).
+cudaError_t launch_velocity(const DevParams &P, uint32_t n, float dt, const float4 *x, const float4 *x_old,
+                            float4 *v, cudaStream_t s);
 // vs: scratch for the velocities in sorted order.
 cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs,
                         const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s);

@@ -28,7 +28,7 @@ int lattice_count(int lo, int hi, float spacing) {
     return (int)((float)(int)std::ceil((float)(hi - lo)) / spacing);
 }
 
-bool is_twod(const pbd_system *s) { return (s->params.flags & PBD_FLAG_TWOD) != 0u; }
+bool is_twod(const pbd_system *s) { return (s->cur_params().flags & PBD_FLAG_TWOD) != 0u; }
 
 int add_block(pbd_system *s, const int32_t ll[3], const int32_t ur[3], float distance, float jitter,
               float w, float ro, int phase, uint64_t seed) {
@@ -47,7 +47,7 @@ int add_block(pbd_system *s, const int32_t ll[3], const int32_t ur[3], float dis
             for (int x = 0; x < cx; ++x, ++k) {
                 pos[4 * k + 0] = ll[0] + x * distance + rng.sym() * jitter;
                 pos[4 * k + 1] = ll[1] + y * distance + rng.sym() * jitter;
-                pos[4 * k + 2] = is_twod(s) ? s->params.twod_z : ll[2] + z * distance + rng.sym() * jitter;
+                pos[4 * k + 2] = is_twod(s) ? s->cur_params().twod_z : ll[2] + z * distance + rng.sym() * jitter;
                 pos[4 * k + 3] = w;
             }
     uint32_t first;
@@ -62,7 +62,7 @@ int pbd_add_fluid(pbd_system *s, const int32_t ll[3], const int32_t ur[3], float
                   uint64_t seed) {
     if (!s) return PBD_ERR_INVALID_ARGUMENT;
     if (!(mass > 0.f) || !(density > 0.f)) return PBD_ERR_INVALID_ARGUMENT;
-    const float r = s->params.particle_radius;
+    const float r = s->cur_params().particle_radius;
     return add_block(s, ll, ur, r * 2.5f, r * 0.01f, 1.f / mass, density, PBD_PHASE_FLUID, seed);
 }
 
@@ -70,7 +70,7 @@ int pbd_add_particle_grid(pbd_system *s, const int32_t ll[3], const int32_t ur[3
                           uint64_t seed) {
     if (!s) return PBD_ERR_INVALID_ARGUMENT;
     if (!(mass > 0.f)) return PBD_ERR_INVALID_ARGUMENT;
-    const float r = s->params.particle_radius;
+    const float r = s->cur_params().particle_radius;
     return add_block(s, ll, ur, r * 2.002f, jitter ? r * 0.01f : 0.f, 1.f / mass, 1.f, PBD_PHASE_SOLID, seed);
 }
 
@@ -91,7 +91,7 @@ int pbd_add_horiz_cloth(pbd_system *s, const int32_t ll[2], const int32_t ur[2],
         for (int x = 0; x < cx; ++x, ++k) {
             pos[4 * k + 0] = ll[0] + x * spacing[0];
             pos[4 * k + 1] = spacing[1];
-            pos[4 * k + 2] = is_twod(s) ? s->params.twod_z : ll[1] + z * spacing[2];
+            pos[4 * k + 2] = is_twod(s) ? s->cur_params().twod_z : ll[1] + z * spacing[2];
             pos[4 * k + 3] = 1.f / mass;
             const uint32_t pidx = start + (uint32_t)(z * cx + x);
             auto add_pin = [&]() {
@@ -169,7 +169,7 @@ int pbd_add_static_sphere(pbd_system *s, const int32_t ll[3], const int32_t ur[3
         for (int y = 0; y < cy; ++y)
             for (int x = 0; x < cx; ++x) {
                 const float p[3] = {ll[0] + x * spacing, ll[1] + y * spacing,
-                                    is_twod(s) ? s->params.twod_z : ll[2] + z * spacing};
+                                    is_twod(s) ? s->cur_params().twod_z : ll[2] + z * spacing};
                 const float dx = p[0] - c[0], dy = p[1] - c[1], dz = p[2] - c[2];
                 if (std::sqrt(dx * dx + dy * dy + dz * dz) < radius) {
                     pos.insert(pos.end(), {p[0], p[1], p[2], .01f});  // W = .01 (particlesystem.cpp:675)

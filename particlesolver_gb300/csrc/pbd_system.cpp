@@ -99,6 +99,11 @@ pbd::DevParams make_dev(const pbd_params &p, const float rands[6]) {
     d.twod_z = p.twod_z;
     d.flags = p.flags;
     for (int k = 0; k < 6; ++k) d.rands[k] = rands[k];
+    d.iterations = p.iterations;
+    d.max_dt = p.max_dt;
+    d.cell_base = 0;
+    d.table = nullptr;
+    d.scene_of = nullptr;
     return d;
 }
 
@@ -163,6 +168,64 @@ int alloc_grid(pbd_system *s) {
     s->grid_cells = cells;
     s->grid_valid = false;
     return PBD_OK;
+}
+
+// Recomputes every scene's parameter block (cells numbered scene after
+// scene) and the launch parameters; with several scenes, uploads the scene
+// table.  The launch block of a batch carries the total cell count, the
+// largest iteration count and the stencil radius shared by every scene with
+// fluid (0 when they differ: the kernels then read each scene's own).
+int refresh_scenes(pbd_system *s) {
+    uint64_t base = 0;
+    uint32_t iters = 0;
+    int rad = -1;
+    for (pbd_scene &sc : s->scenes) {
+        sc.dev = make_dev(sc.params, s->rands);
+        sc.dev.cell_base = (uint32_t)base;
+        base += sc.dev.num_cells;
+        if (base >= (1ull << 31))
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "the scenes' grids hold too many cells in total (limit 2^31 - 1)");
+        iters = std::max(iters, sc.params.iterations);
+        if (sc.n_fluid) rad = (rad < 0 || rad == sc.dev.fluid_rad) ? sc.dev.fluid_rad : 0;
+    }
+    if (!s->batched()) {
+        s->dev = s->scenes[0].dev;
+        return alloc_grid(s);
+    }
+    const uint32_t S = (uint32_t)s->scenes.size();
+    if (S > s->table_cap) {
+        dfree(s->d_table);
+        const uint32_t want = std::max<uint32_t>(S, 2u * s->table_cap);
+        CUDA_TRY(s, dalloc(&s->d_table, want));
+        s->table_cap = want;
+    }
+    std::vector<pbd::DevParams> tab(S);
+    for (uint32_t k = 0; k < S; ++k) tab[k] = s->scenes[k].dev;
+    CUDA_TRY(s, cudaMemcpy(s->d_table, tab.data(), S * sizeof(pbd::DevParams), cudaMemcpyHostToDevice));
+    s->dev = s->scenes[0].dev;
+    s->dev.num_cells = (uint32_t)base;
+    s->dev.iterations = iters;
+    s->dev.fluid_rad = rad < 0 ? 1 : rad;
+    s->dev.table = s->d_table;
+    s->dev.scene_of = s->d_scene_of;
+    return alloc_grid(s);
+}
+
+// Scene holding particle slot i.
+uint32_t scene_of_slot(const pbd_system *s, uint32_t i) {
+    uint32_t lo = 0, hi = (uint32_t)s->scenes.size();
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (s->scenes[mid].first <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+bool any_xsph(const pbd_system *s) {
+    for (const pbd_scene &sc : s->scenes)
+        if (sc.params.xsph_c != 0.f && sc.n_fluid && sc.params.iterations > 0) return true;
+    return false;
 }
 
 // Rebuilds the device CSR of distance constraints and pins from the host
@@ -368,7 +431,10 @@ uint32_t solve_mask(const pbd_system *s) {
 // The step in the reference's order (particlesystem.cpp:144-246): predict,
 // then every iteration rebuilds the grid from the current positions and
 // runs contacts + PBF + walls (one fused pass), distance constraints with
-// pins, and shape matching; finally the velocity update and XSPH.
+// pins, and shape matching; finally the velocity update and XSPH.  With
+// several scenes every launch covers all of them; a scene with fewer
+// iterations than the batch's most sits out the first ones (its particles
+// keep their predicted positions, so the grids it skips change nothing).
 int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     const pbd::DevParams &P = s->dev;
     const uint32_t n = s->n;
@@ -382,32 +448,34 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     const uint32_t mask = solve_mask(s);
     const uint32_t dist_kernels =
         s->cons.count ? (s->cons.any_distance ? 2u : (s->cons.any_pin ? 1u : 0u)) : 0u;
-    for (uint32_t it = 0; it < s->params.iterations; ++it) {
+    const uint32_t iters = P.iterations;
+    for (uint32_t it = 0; it < iters; ++it) {
+        const uint32_t left = iters - 1u - it;
         if (int rc = build_grid(s, st, it == 0)) return rc;
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
-            CUDA_TRY(s, pbd::launch_lambda(P, n, s->grid, s->sxl, s->nbl, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, s->nbl, s->tpp, st));
             s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
         }
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
-            CUDA_TRY(s, pbd::launch_solve(P, n, mask, s->grid, s->sxl, s->x_old, s->x, s->nbl, s->list_valid,
-                                          s->tpp, st));
+            CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+                                          s->list_valid, s->tpp, st));
         }
         if (dist_kernels) {
             Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
-            CUDA_TRY(s, pbd::launch_distance(P, s->cons, s->x, true, true, st));
+            CUDA_TRY(s, pbd::launch_distance(P, left, s->cons, s->x, true, true, st));
         }
         if (s->bodies.count) {
             Stage t(s, st, PBD_STAGE_SHAPES, 1);
-            CUDA_TRY(s, pbd::launch_shapes(s->bodies, s->x, st));
+            CUDA_TRY(s, pbd::launch_shapes(P, left, s->bodies, s->x, st));
         }
     }
     {
         Stage t(s, st, PBD_STAGE_VELOCITY, 1);
-        CUDA_TRY(s, pbd::launch_velocity(n, dt, s->x, s->x_old, s->v, st));
+        CUDA_TRY(s, pbd::launch_velocity(P, n, dt, s->x, s->x_old, s->v, st));
     }
-    if (s->params.xsph_c != 0.f && s->n_fluid && s->params.iterations > 0) {
+    if (any_xsph(s)) {
         Stage t(s, st, PBD_STAGE_XSPH, 2);
         CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, s->nbl, s->list_valid, s->tpp, st));
     }
@@ -415,7 +483,11 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     return PBD_OK;
 }
 
-float clamp_dt(const pbd_system *s, float dt) { return std::min(dt, s->params.max_dt); }
+// One scene: the step is clamped here.  Several: each scene's own clamp is
+// applied on the device.
+float clamp_dt(const pbd_system *s, float dt) {
+    return s->batched() ? dt : std::min(dt, s->scenes[0].params.max_dt);
+}
 
 }  // namespace
 
@@ -477,9 +549,10 @@ int pbd_create(const pbd_params *params, uint32_t max_particles, pbd_system **ou
     if (max_particles == 0 || max_particles >= (1u << 31))
         return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "max_particles must be in [1, 2^31)");
     pbd_system *s = new pbd_system();
-    s->params = *params;
+    s->scenes.emplace_back();
+    s->scenes[0].params = *params;
     s->cap = max_particles;
-    s->dev = make_dev(s->params, s->rands);
+    s->dev = make_dev(*params, s->rands);
     int rc = PBD_OK;
     auto bail = [&](int code) {
         g_create_error = s->err;
@@ -513,7 +586,7 @@ int pbd_create(const pbd_params *params, uint32_t max_particles, pbd_system **ou
     ALLOC(s->grid.sorted_x, c);
     ALLOC(s->grid.sorted_attr, c);
 #undef ALLOC
-    if ((rc = alloc_grid(s))) return bail(rc);
+    if ((rc = refresh_scenes(s))) return bail(rc);
     *out = s;
     return PBD_OK;
 }
@@ -543,6 +616,8 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->grid.sorted_idx);
     dfree(s->grid.sorted_x);
     dfree(s->grid.sorted_attr);
+    dfree(s->d_table);
+    dfree(s->d_scene_of);
     free_grid(s);
     free_constraints(s);
     free_bodies(s);
@@ -554,17 +629,78 @@ int pbd_set_params(pbd_system *s, const pbd_params *params) {
     SYS_GUARD(s);
     std::string why;
     if (validate_params(params, why)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "%s", why.c_str());
-    s->params = *params;
-    s->dev = make_dev(s->params, s->rands);
-    if (int rc = alloc_grid(s)) return rc;
+    const pbd_params old = s->scenes[0].params;
+    s->scenes[0].params = *params;
+    if (int rc = refresh_scenes(s)) {
+        s->scenes[0].params = old;
+        refresh_scenes(s);
+        return rc;
+    }
     s->grid_valid = false;
+    s->list_valid = false;
     ++s->version;
     return PBD_OK;
 }
 
 int pbd_get_params(const pbd_system *s, pbd_params *out) {
     if (!s || !out) return PBD_ERR_INVALID_ARGUMENT;
-    *out = s->params;
+    *out = s->scenes[0].params;
+    return PBD_OK;
+}
+
+int pbd_begin_scene(pbd_system *s, const pbd_params *params, uint32_t *scene_index) {
+    SYS_GUARD(s);
+    std::string why;
+    if (validate_params(params, why)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "%s", why.c_str());
+    if (s->scenes.size() >= PBD_MAX_SCENES)
+        return fail(s, PBD_ERR_CAPACITY, "a system holds at most %u scenes", (unsigned)PBD_MAX_SCENES);
+    if (!s->d_scene_of) {
+        CUDA_TRY(s, dalloc(&s->d_scene_of, s->cap));
+        CUDA_TRY(s, cudaMemset(s->d_scene_of, 0, (size_t)s->cap * sizeof(uint16_t)));  // all in scene 0
+    }
+    pbd_scene sc;
+    sc.params = *params;
+    sc.first = s->n;
+    s->scenes.push_back(sc);
+    if (int rc = refresh_scenes(s)) {
+        s->scenes.pop_back();
+        refresh_scenes(s);
+        return rc;
+    }
+    s->grid_valid = false;
+    s->list_valid = false;
+    ++s->version;
+    if (scene_index) *scene_index = (uint32_t)s->scenes.size() - 1u;
+    return PBD_OK;
+}
+
+uint32_t pbd_num_scenes(const pbd_system *s) { return s ? (uint32_t)s->scenes.size() : 0u; }
+
+int pbd_get_scene(const pbd_system *s, uint32_t scene, uint32_t *first, uint32_t *count, pbd_params *params) {
+    if (!s) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "system handle is NULL");
+    if (scene >= s->scenes.size()) return PBD_ERR_INVALID_ARGUMENT;
+    const pbd_scene &sc = s->scenes[scene];
+    if (first) *first = sc.first;
+    if (count) *count = sc.count;
+    if (params) *params = sc.params;
+    return PBD_OK;
+}
+
+int pbd_set_scene_params(pbd_system *s, uint32_t scene, const pbd_params *params) {
+    SYS_GUARD(s);
+    if (scene >= s->scenes.size()) return fail(s, PBD_ERR_INVALID_ARGUMENT, "no scene %u", scene);
+    std::string why;
+    if (validate_params(params, why)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "%s", why.c_str());
+    const pbd_params old = s->scenes[scene].params;
+    s->scenes[scene].params = *params;
+    if (int rc = refresh_scenes(s)) {
+        s->scenes[scene].params = old;
+        refresh_scenes(s);
+        return rc;
+    }
+    s->grid_valid = false;
+    s->list_valid = false;
+    ++s->version;
     return PBD_OK;
 }
 
@@ -578,8 +714,8 @@ int pbd_set_wall_jitter(pbd_system *s, const float rands[6]) {
     for (int k = 0; k < 6; ++k) {
         if (!std::isfinite(rands[k])) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rands must be finite");
         s->rands[k] = rands[k];
-        s->dev.rands[k] = rands[k];
     }
+    if (int rc = refresh_scenes(s)) return rc;
     ++s->version;
     return PBD_OK;
 }
@@ -624,9 +760,19 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
     if (rest_density) std::copy(rest_density, rest_density + n, ro.begin());
     CUDA_TRY(s, cudaMemcpy(s->rho0 + off, ro.data(), n * 4ull, cudaMemcpyHostToDevice));
     CUDA_TRY(s, cudaMemcpy(s->x_old + off, pos_w, n * sizeof(float4), cudaMemcpyHostToDevice));
+    if (s->batched()) {
+        const std::vector<uint16_t> tag(n, (uint16_t)(s->scenes.size() - 1u));
+        CUDA_TRY(s, cudaMemcpy(s->d_scene_of + off, tag.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
     s->n += n;
     s->n_fluid += nf;
     s->n_contact += nc;
+    pbd_scene &cur = s->scenes.back();
+    cur.count += n;
+    cur.n_fluid += nf;
+    cur.n_contact += nc;
+    if (nf && cur.n_fluid == nf)
+        if (int rc = refresh_scenes(s)) return rc;  // the shared stencil radius may change
     if (s->n_fluid && !s->vs) CUDA_TRY(s, dalloc(&s->vs, s->cap));
     if (s->n_fluid && !s->nbl.slot && s->list_capacity) {
         CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
@@ -651,6 +797,8 @@ int pbd_add_distance_constraints(pbd_system *s, uint32_t m, const uint32_t *pair
             return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u references a particle >= %u", c, s->n);
         if (pairs[2 * c] == pairs[2 * c + 1])
             return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u joins a particle to itself", c);
+        if (s->batched() && scene_of_slot(s, pairs[2 * c]) != scene_of_slot(s, pairs[2 * c + 1]))
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u joins particles of different scenes", c);
         if (!std::isfinite(rest[c]) || rest[c] < 0.f)
             return fail(s, PBD_ERR_INVALID_ARGUMENT, "constraint %u has an invalid rest length", c);
         if (stiffness && !(stiffness[c] >= 0.f && stiffness[c] <= 1.f))
@@ -688,6 +836,8 @@ int pbd_add_rigid_body(pbd_system *s, uint32_t first, uint32_t count, float stif
     SYS_GUARD(s);
     if (count < 2) return fail(s, PBD_ERR_INVALID_ARGUMENT, "a rigid body needs at least 2 particles");
     if ((uint64_t)first + count > s->n) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rigid body range exceeds the particle count");
+    if (s->batched() && scene_of_slot(s, first) != scene_of_slot(s, first + count - 1u))
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "rigid body spans several scenes");
     if (!(stiffness >= 0.f && stiffness <= 1.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "stiffness must be in [0, 1]");
     for (const uint4 &r : s->body_range)
         if (first < r.x + r.y && r.x < first + count)
@@ -977,7 +1127,7 @@ int pbd_build_grid(pbd_system *s, void *stream) {
 int pbd_collide(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, 0u, s->grid, s->sxl, s->x_old, s->x, s->nbl,
                                   false, s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
@@ -987,9 +1137,9 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, s->grid, s->sxl, s->nbl, s->tpp, st));
+    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, 0u, s->grid, s->sxl, s->nbl, s->tpp, st));
     s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, 0u, s->grid, s->sxl, s->x_old, s->x, s->nbl,
                                   s->list_valid, s->tpp, st));
     s->launches += 2;
     return PBD_OK;
@@ -998,7 +1148,7 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
 int pbd_collide_world(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
-    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+    CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoWorld, 0u, s->grid, s->sxl, s->x_old, s->x, s->nbl,
                                   false, s->tpp, (cudaStream_t)stream));
     s->launches += 1;
     return PBD_OK;
@@ -1006,26 +1156,26 @@ int pbd_collide_world(pbd_system *s, void *stream) {
 
 int pbd_solve_distance_constraints(pbd_system *s, void *stream) {
     SYS_GUARD(s);
-    CUDA_TRY(s, pbd::launch_distance(s->dev, s->cons, s->x, true, false, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_distance(s->dev, 0u, s->cons, s->x, true, false, (cudaStream_t)stream));
     return PBD_OK;
 }
 
 int pbd_solve_point_constraints(pbd_system *s, void *stream) {
     SYS_GUARD(s);
-    CUDA_TRY(s, pbd::launch_distance(s->dev, s->cons, s->x, false, true, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_distance(s->dev, 0u, s->cons, s->x, false, true, (cudaStream_t)stream));
     return PBD_OK;
 }
 
 int pbd_solve_shapes(pbd_system *s, void *stream) {
     SYS_GUARD(s);
-    CUDA_TRY(s, pbd::launch_shapes(s->bodies, s->x, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_shapes(s->dev, 0u, s->bodies, s->x, (cudaStream_t)stream));
     return PBD_OK;
 }
 
 int pbd_calc_velocity(pbd_system *s, float dt, void *stream) {
     SYS_GUARD(s);
     if (!(dt > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
-    CUDA_TRY(s, pbd::launch_velocity(s->n, clamp_dt(s, dt), s->x, s->x_old, s->v, (cudaStream_t)stream));
+    CUDA_TRY(s, pbd::launch_velocity(s->dev, s->n, clamp_dt(s, dt), s->x, s->x_old, s->v, (cudaStream_t)stream));
     return PBD_OK;
 }
 

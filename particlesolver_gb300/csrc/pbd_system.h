@@ -8,9 +8,25 @@
 #include "../../include/pbd.h"
 #include "pbd_kernels.h"
 
-struct pbd_system {
+// One scene of a system: its parameters, particle range and phase census.
+// Scenes are filled in order, so scene k's particles are the slots
+// [first, first + count), directly after scene k - 1's.
+struct pbd_scene {
     pbd_params params{};
+    pbd::DevParams dev{};  // parameter block (cell_base set, no table)
+    uint32_t first = 0, count = 0;
+    uint32_t n_fluid = 0, n_contact = 0;
+};
+
+struct pbd_system {
+    std::vector<pbd_scene> scenes;  // at least one; particles go to the last
+    // Launch parameters: scene 0's block for a single scene; for several,
+    // the batch's totals (cell count, most iterations, common stencil
+    // radius) with the scene table and the slot -> scene map attached.
     pbd::DevParams dev{};
+    pbd::DevParams *d_table = nullptr;  // [scenes] device copy of each scene's block
+    uint16_t *d_scene_of = nullptr;     // [cap] scene of each slot (several scenes only)
+    uint32_t table_cap = 0;             // entries d_table holds
     uint32_t cap = 0;  // max particles
     uint32_t n = 0;    // live particles
     int device = 0;
@@ -40,8 +56,9 @@ struct pbd_system {
     std::vector<float4> body_rest;
     pbd::BodyBuffers bodies{};
 
-    // phase census for stage selection
+    // phase census for stage selection (all scenes)
     uint32_t n_fluid = 0, n_contact = 0;
+    bool any_xsph = false;  // some scene with fluid, xsph_c != 0 and iterations > 0
 
     uint32_t tpp = 1;     // lanes per particle in the neighbour passes
     pbd::NbList nbl{};    // per-iteration fluid neighbour lists
@@ -73,6 +90,9 @@ struct pbd_system {
     uint64_t version = 1;  // bumped whenever a captured graph would go stale
 
     std::string err;
+
+    bool batched() const { return scenes.size() > 1; }
+    const pbd_params &cur_params() const { return scenes.back().params; }
 };
 
 // Shared by the C ABI translation units: parameter validation into device

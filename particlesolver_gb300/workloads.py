@@ -344,3 +344,89 @@ def mixed_scene(cloth: int = 256, ropes: int = 2000, rope_particles: int = 64, b
                  rest=np.concatenate(rest).astype(np.float32), pins=pins, pin_points=pos_w[pins, :3].copy(),
                  bodies=body_list, dt=1.0 / 60.0,
                  info=dict(cloth=cloth, ropes=ropes, bodies=bodies, constraints=int(sum(len(r) for r in rest))))
+
+
+_RHO0_CACHE: dict = {}
+
+
+def pbf_block(count: int, h: float = 0.1, seed: int = 2024, iterations: int = 4, xsph: float = 0.01,
+              cell_div: int = 1, max_dt: float = 1.0 / 120.0) -> Scene:
+    """A PBF block of exactly `count` fluid particles on the dam-break
+    lattice (spacing h/2, jitter U(-0.01h, 0.01h)): footprint nx = 2 nz
+    columns, filled from the floor up (x fastest, then z, then y; the top
+    layer may be partial), in the corner of a box four block-widths long
+    and twice the block height.  Parameters as dam_break; max_dt = 1/120
+    so that a 1/60 step of a mixed batch gives the dam break's 1/120."""
+    s = 0.5 * h
+    nz = max(1, int(round((count / 4.0) ** (1.0 / 3.0))))
+    nx = 2 * nz
+    ny = -(-count // (nx * nz))
+    k = np.arange(count)
+    lat = np.stack([k % nx, k // (nx * nz), (k // nx) % nz], 1)
+    pos = (lat + 0.5) * s + uniform(seed, lat.shape, -0.01 * h, 0.01 * h)
+    ext = np.array([4 * nx * s, 2 * ny * s, nz * s])
+    cell = h / cell_div
+    grid = [next_pow2(ext[0] / cell), next_pow2(ny * s / cell), next_pow2(ext[2] / cell)]
+    pos_w = np.empty((count, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0
+    key = (s, h)
+    if key not in _RHO0_CACHE:
+        _RHO0_CACHE[key] = poly6_rest_density(s, h)
+    rho0 = _RHO0_CACHE[key]
+    params = dict(particle_radius=0.5 * s, kernel_radius=h, cell_size=cell, grid_size=grid,
+                  world_origin=[0.0, 0.0, 0.0], gravity=[0.0, -9.8, 0.0], box_min=[0.0, 0.0, 0.0],
+                  box_max=[float(v) for v in ext], iterations=iterations, relaxation=1.0, scorr_k=0.1,
+                  scorr_n=4.0, scorr_dq=0.2, xsph_c=xsph, max_dt=max_dt, max_neighbors=500,
+                  flags=FLAG_KERNEL_UNITS)
+    return Scene("pbf_block", params, pos_w, np.zeros(count, np.int32),
+                 rest_density=np.full(count, rho0, np.float32), dt=1.0 / 120.0,
+                 info=dict(nx=nx, ny=ny, nz=nz, rho0=rho0, seed=seed))
+
+
+def granular_column(count: int = 1600, width: int | None = None, radius: float = 0.25, seed: int = 1600,
+                    iterations: int = 3, static_friction: float = 0.5, kinetic_friction: float = 0.3) -> Scene:
+    """2-D granular column collapse: `count` solid particles (unit inverse
+    mass) on a lattice of spacing 2r, `width` columns (default round(sqrt
+    (count)), 40 for 1,600), rows from y = r up, the top row possibly
+    partial, jitter U(-0.01r, 0.01r) in x and y; centred in a box as wide as
+    twice the column, friction mu_s / mu_k on contacts and walls, z pinned
+    to 0 (FLAG_TWOD), 3 iterations, dt = 1/60.  Cell 2r as the reference;
+    the grid covers the box's width and the column's height and has four
+    cells in z (the stencil must not alias there)."""
+    d = 2.0 * radius
+    width = int(width or max(1, round(math.sqrt(count))))
+    rows = -(-count // width)
+    k = np.arange(count)
+    pos = np.zeros((count, 3))
+    pos[:, 0] = (k % width - (width - 1) / 2.0) * d
+    pos[:, 1] = radius + (k // width) * d
+    pos[:, :2] += uniform(seed, (count, 2), -0.01 * radius, 0.01 * radius)
+    half = width * d
+    height = rows * d
+    cell = d
+    grid = [next_pow2(2 * half / cell), next_pow2(height / cell), 4]
+    pos_w = np.empty((count, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0
+    params = dict(particle_radius=radius, kernel_radius=2.0 * d, cell_size=cell, grid_size=grid,
+                  world_origin=[-half, 0.0, -2.0 * cell], gravity=[0.0, -9.8, 0.0],
+                  box_min=[-half, 0.0, -1.0], box_max=[half, 2.0 * height + 10.0, 1.0], iterations=iterations,
+                  relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0, max_dt=1.0 / 60.0,
+                  max_neighbors=500, contact_static_friction=static_friction,
+                  contact_kinetic_friction=kinetic_friction, wall_static_friction=static_friction,
+                  wall_kinetic_friction=kinetic_friction, twod_z=0.0, flags=FLAG_TWOD)
+    return Scene("granular_column", params, pos_w, np.full(count, PHASE_SOLID, np.int32), dt=1.0 / 60.0,
+                 info=dict(width=width, rows=rows, seed=seed))
+
+
+def batched_scenes(count: int = 512, seed: int = 512, lo: int = 1024, hi: int = 65536) -> list:
+    """`count` independent scenes with particle counts round(exp(U(ln lo,
+    ln hi))), each a PBF block or a granular column by a seeded coin flip."""
+    sizes = np.rint(np.exp(uniform(seed, (count,), math.log(lo), math.log(hi)))).astype(np.int64)
+    coin = uniform(seed + 1, (count,), 0.0, 1.0) < 0.5
+    out = []
+    for k in range(count):
+        n = int(sizes[k])
+        out.append(pbf_block(n, seed=seed * 1000 + k) if coin[k] else granular_column(n, seed=seed * 1000 + k))
+    return out

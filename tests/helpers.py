@@ -117,3 +117,17 @@ def check_trajectory(pos, gold_pos, start, pct_tol=1e-3):
     per = np.linalg.norm(d - g, axis=1) / scale
     assert np.percentile(per, 90) < pct_tol
     assert np.max(np.abs(d.mean(0) - g.mean(0))) / scale < pct_tol
+
+
+def check_granular(pos, gold_pos, rel: float):
+    """Invariants of a granular pile, whose particle trajectories are
+    chaotic (contacts switch at the 2.001 r threshold, friction switches
+    static / kinetic): the mean height and the horizontal spread agree to
+    rel, and every particle is finite."""
+    p = np.asarray(pos, np.float64)[:, :3]
+    g = np.asarray(gold_pos, np.float64)[:, :3]
+    assert np.all(np.isfinite(p))
+    mean_y, gmean_y = p[:, 1].mean(), g[:, 1].mean()
+    assert abs(mean_y - gmean_y) <= rel * abs(gmean_y), (mean_y, gmean_y)
+    sx, gsx = p[:, 0].std(), g[:, 0].std()
+    assert abs(sx - gsx) <= rel * gsx, (sx, gsx)

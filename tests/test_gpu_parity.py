@@ -261,7 +261,8 @@ def test_velocity_and_xsph():
 
 @pytest.mark.parametrize("builder,steps", [(W.reference_fluid, 4), (W.reference_granular, 4),
                                            (W.rope_and_cloth, 4), (lambda: W.rigid_boxes(count=8), 4),
-                                           (lambda: W.dam_break(16, 16, 8), 6)])
+                                           (lambda: W.dam_break(16, 16, 8), 6),
+                                           (lambda: W.pbf_block(2000), 4)])
 def test_full_update_trajectory(builder, steps):
     sc = builder()
     g, o = make_pair(sc)
@@ -269,6 +270,35 @@ def test_full_update_trajectory(builder, steps):
         g.update(sc.dt)
         o.update(sc.dt)
     check_trajectory(g.positions(), o.positions(), sc.pos_w)
+
+
+def test_granular_column_collapse():
+    """The 2-D granular column (1,600 particles, 40 x 40, spacing 2r, mu_s
+    0.5, mu_k 0.3, 3 iterations, dt 1/60).  Its lattice sits at the contact
+    threshold, so trajectories are chaotic: each step is checked from a
+    common state (the oracle restarted from the GPU's positions and
+    velocities), and 60 free-running steps by pile invariants."""
+    from helpers import check_granular
+
+    sc = W.granular_column()
+    g, o = make_pair(sc)
+    for step in range(12):
+        o.set_positions(g.positions().astype(np.float64))
+        o.set_velocities(g.velocities().astype(np.float64))
+        start = g.positions()
+        g.update(sc.dt)
+        o.update(sc.dt)
+        d_g, d_o = displacement(g.positions(), start), displacement(o.positions(), start)
+        # per particle: 1e-4 of the step's largest move plus 4 FP32 ulps of
+        # the coordinate; a minority may switch contacts at the threshold
+        ulp = np.spacing(np.abs(o.positions()[:, :3]).astype(np.float32)).astype(np.float64).max(1)
+        excess = np.linalg.norm(d_g - d_o, axis=1) - (1e-4 * np.max(np.abs(d_o)) + 4.0 * ulp)
+        assert np.mean(excess > 0) < 0.1, (step, np.mean(excess > 0))
+    g2, o2 = make_pair(sc)
+    for _ in range(60):
+        g2.update(sc.dt)
+        o2.update(sc.dt)
+    check_granular(g2.positions(), o2.positions(), 0.05)
 
 
 def _small_mixed():
