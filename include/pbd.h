@@ -41,7 +41,8 @@ typedef enum pbd_status {
                                      particlesystem.cpp:311-312,335-336)     */
     PBD_ERR_CUDA = 3,             /* a CUDA runtime call failed              */
     PBD_ERR_STATE = 4,            /* call not valid in the current state    */
-    PBD_ERR_NONFINITE = 5         /* NaN/Inf found by pbd_check_finite       */
+    PBD_ERR_NONFINITE = 5,        /* NaN/Inf found by pbd_check_finite       */
+    PBD_ERR_UNSUPPORTED = 6       /* feature not available for this scene   */
 } pbd_status;
 
 /* Particle phases (gpu/src/cuda/shared_variables.cuh:4-9).  Rigid objects,
@@ -355,6 +356,37 @@ int pbd_reset_profile(pbd_system *sys);
 uint64_t pbd_state_size(const pbd_system *sys);
 int pbd_save_state(pbd_system *sys, void *dst, uint64_t size);
 int pbd_load_state(pbd_system *sys, const void *src, uint64_t size);
+
+/* ------------------------------------------------------- differentiation
+ *
+ * Reverse-mode gradients of a rollout (no counterpart in the reference).
+ * Covered: prediction and the velocity update, contacts with friction, the
+ * world walls (with their friction), distance constraints (including the
+ * gradient of each constraint's stiffness) and pins; a system with fluid
+ * particles or rigid bodies returns PBD_ERR_UNSUPPORTED.  Contact pairs,
+ * friction modes, wall clamps and cut-offs are those of the forward pass,
+ * held fixed (the gradient of the piecewise-smooth step where it is
+ * smooth).  Works on batched systems (every scene at once). */
+
+/* Replaces the stiffness of every distance constraint, in add order
+ * (count = number of constraints; values in [0, 1]; host or device array). */
+int pbd_set_distance_stiffness(pbd_system *sys, uint32_t count, const float *stiffness, int on_device,
+                               void *stream);
+uint32_t pbd_num_distance_constraints(const pbd_system *sys);
+/* Runs `steps` updates of dt from the current state (as pbd_update) and
+ * keeps the state every `checkpoint_every` steps in device memory for
+ * pbd_backward.  Memory: 32 bytes per particle per checkpoint. */
+int pbd_rollout(pbd_system *sys, float dt, uint32_t steps, uint32_t checkpoint_every, void *stream);
+/* Gradients of a loss L(x_T, v_T) of the last rollout's final state.
+ * Device arrays: dL_dx, dL_dv float4[n] (w ignored; NULL = zero);
+ * outputs dL_dx0, dL_dv0 float4[n] (w = 0) with respect to the rollout's
+ * initial positions and velocities, dL_dstiffness float[m] (add order);
+ * any output may be NULL.  Recomputes each checkpoint segment with the
+ * forward kernels (working memory (1 + 2 iterations) x checkpoint_every x
+ * 16 bytes per particle) and leaves the system in the rollout's final
+ * state.  Returns PBD_ERR_STATE if the scene changed since the rollout. */
+int pbd_backward(pbd_system *sys, const float *dL_dx, const float *dL_dv, float *dL_dx0, float *dL_dv0,
+                 float *dL_dstiffness, void *stream);
 
 #ifdef __cplusplus
 }

@@ -110,6 +110,10 @@ class PbdProfile(ctypes.Structure):
     ]
 
 
+PBD_OK, PBD_ERR_INVALID_ARGUMENT, PBD_ERR_CAPACITY, PBD_ERR_CUDA, PBD_ERR_STATE, PBD_ERR_NONFINITE, \
+    PBD_ERR_UNSUPPORTED = range(7)
+
+
 class PbdError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"pbd error {code}: {message}")
@@ -182,6 +186,10 @@ _SIGNATURES = {
     "pbd_build_grid_noalloc": ([ctypes.POINTER(PbdParams), _P, _U32, _P, _P, _P, _P], _I),
     "pbd_state_size": ([_P], ctypes.c_uint64),
     "pbd_save_state": ([_P, _P, ctypes.c_uint64], _I),
+    "pbd_set_distance_stiffness": ([_P, _U32, _P, _I, _P], _I),
+    "pbd_rollout": ([_P, _F, _U32, _U32, _P], _I),
+    "pbd_num_distance_constraints": ([_P], _U32),
+    "pbd_backward": ([_P, _P, _P, _P, _P, _P, _P], _I),
     "pbd_load_state": ([_P, _P, ctypes.c_uint64], _I),
 }
 
@@ -296,6 +304,7 @@ class ParticleSystem:
         st = None if stiffness is None else _f32(stiffness).reshape(-1)
         self._check(self.lib.pbd_add_distance_constraints(self.h, pairs.shape[0], pairs.ctypes.data_as(_PU),
                                                           _fptr(rest), _fptr(st)))
+
 
     def add_point_constraints(self, index, points):
         index = np.ascontiguousarray(index, dtype=np.uint32).reshape(-1)
@@ -493,6 +502,31 @@ class ParticleSystem:
 
     def reset_profile(self):
         self._check(self.lib.pbd_reset_profile(self.h))
+
+    # -- differentiation ---------------------------------------------------
+    @property
+    def num_distance_constraints(self) -> int:
+        return int(self.lib.pbd_num_distance_constraints(self.h))
+
+    def set_distance_stiffness(self, stiffness, device_ptr: int | None = None, stream=None):
+        """Stiffness of every distance constraint (add order): a host array,
+        or `device_ptr` to `num_distance_constraints` device floats."""
+        if device_ptr is not None:
+            self._check(self.lib.pbd_set_distance_stiffness(self.h, self.num_distance_constraints, device_ptr, 1,
+                                                            stream))
+            return
+        a = _f32(stiffness).reshape(-1)
+        self._check(self.lib.pbd_set_distance_stiffness(self.h, a.shape[0], a.ctypes.data, 0, stream))
+
+    def rollout(self, dt: float, steps: int, checkpoint_every: int = 10, stream=None):
+        """`steps` updates with checkpoints every `checkpoint_every` steps
+        (the forward pass of pbd_backward)."""
+        self._check(self.lib.pbd_rollout(self.h, dt, steps, checkpoint_every, stream))
+
+    def backward_device(self, dL_dx: int | None, dL_dv: int | None, dL_dx0: int | None, dL_dv0: int | None,
+                        dL_dstiffness: int | None, stream=None):
+        """pbd_backward on raw device pointers (float4[n] / float[m])."""
+        self._check(self.lib.pbd_backward(self.h, dL_dx, dL_dv, dL_dx0, dL_dv0, dL_dstiffness, stream))
 
     def save_state(self) -> bytes:
         size = int(self.lib.pbd_state_size(self.h))

@@ -1,0 +1,557 @@
+// Differentiation of the PBD step: rollouts with checkpoints, and a
+// backward pass of hand-written adjoint kernels for the integrator (predict
+// and velocity), contacts with friction, the world walls, distance
+// constraints (with the gradient of every constraint's stiffness) and pins.
+//
+// pbd_rollout runs `steps` updates and keeps (x, v) every `every` steps in
+// device memory.  pbd_backward walks the checkpoint segments from last to
+// first: it restores a segment's checkpoint, recomputes the segment with
+// the forward kernels while recording the positions each projector read
+// (the start of every iteration, after the contact / wall pass), then runs
+// the adjoint kernels in reverse.  The recomputed grids and neighbour sets
+// are those of the forward pass (same kernels, same inputs), so the
+// neighbour lists the forward pass used are the ones held fixed.
+//
+// Every adjoint is a gather: a particle sums what it receives from its own
+// neighbours and constraint incidences (the contact relation and the
+// constraint CSR are symmetric), so there are no atomics and results are
+// deterministic.  The per-pair Jacobian blocks come from the
+// scalar-generic projector formulas in pbd_dual.cuh evaluated on dual
+// numbers.
+#include <cmath>
+#include <cstdio>
+
+#include "pbd_dual.cuh"
+#include "pbd_system.h"
+
+namespace pbd {
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned blocks_for(uint32_t n) { return (n + kBlock - 1u) / kBlock; }
+
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+
+// ------------------------------------------------------------ integrator
+
+// After the last iteration: v = (x - x_old) / dt.  Given the adjoints of x
+// and v after the step, the adjoint of the final positions (gfin) and the
+// first part of the adjoint of x_old.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_velocity(DevParams P0, uint32_t n, float dt,
+                                                         const float4 *__restrict__ gx_next,
+                                                         const float4 *__restrict__ gv_next,
+                                                         float4 *__restrict__ gfin, float4 *__restrict__ gxo) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float h = fminf(dt, scene_params<B>(P0, i).max_dt);
+    const float4 gx = gx_next[i];
+    const float4 gv = gv_next ? gv_next[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    gfin[i] = make_float4(gx.x + gv.x / h, gx.y + gv.y / h, gx.z + gv.z / h, 0.f);
+    gxo[i] = make_float4(-gv.x / h, -gv.y / h, -gv.z / h, 0.f);
+}
+
+// Predict: x_old = x, x* = x + (v + g dt) dt.  gx_out = gx* + gx_old,
+// gv_out = gx* dt.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_predict(DevParams P0, uint32_t n, float dt,
+                                                        const float4 *__restrict__ gpred,
+                                                        const float4 *__restrict__ gxo,
+                                                        float4 *__restrict__ gx_out, float4 *__restrict__ gv_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float h = fminf(dt, scene_params<B>(P0, i).max_dt);
+    const float4 g = gpred[i], o = gxo[i];
+    gx_out[i] = make_float4(g.x + o.x, g.y + o.y, g.z + o.z, 0.f);
+    gv_out[i] = make_float4(g.x * h, g.y * h, g.z * h, 0.f);
+}
+
+// ---------------------------------------------------- distance and pins
+
+// Pins set the position: the adjoint of what the distance pass wrote is
+// zero for pinned particles of active scenes.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_pins(DevParams P0, uint32_t count, uint32_t iter_left,
+                                                     const uint32_t *__restrict__ particle,
+                                                     const float4 *__restrict__ pin, float4 *__restrict__ gt) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= count) return;
+    const uint32_t k = particle[s];
+    if (!scene_active<B>(scene_params<B>(P0, k), iter_left)) return;
+    if (pin[s].w != 0.f) gt[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// t_k = y_k + sum_e d(y_k, y_o, s_e) / occ_k over k's incidences.  The
+// adjoint of y_k gathers k's own terms and, through the same constraints
+// seen from the other end, the terms of each partner o.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_distance(DevParams P0, uint32_t count, uint32_t iter_left,
+                                                         const uint32_t *__restrict__ particle,
+                                                         const uint32_t *__restrict__ row,
+                                                         const uint32_t *__restrict__ other,
+                                                         const float *__restrict__ rest,
+                                                         const float *__restrict__ stiff,
+                                                         const float *__restrict__ occ_of,
+                                                         const float4 *__restrict__ y,
+                                                         const float4 *__restrict__ gt, float4 *__restrict__ gy) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= count) return;
+    const uint32_t k = particle[s];
+    const DevParams P = scene_params<B>(P0, k);
+    if (!scene_active<B>(P, iter_left)) return;
+    const float4 yk4 = y[k];
+    const float4 gk4 = gt[k];
+    const float3 gk = make_float3(gk4.x, gk4.y, gk4.z);
+    const float occ_k = occ_of[k];
+    float3 acc = gk;
+    const uint32_t e1 = row[s + 1];
+    for (uint32_t e = row[s]; e < e1; ++e) {
+        const uint32_t o = other[e];
+        const float4 yo4 = y[o];
+        // own term: d(y_k, y_o) / occ_k, derivative in y_k
+        const V3<Dual<3>> dk = distance_term<Dual<3>>(P, seed<3>(f3(yk4), 0), yk4.w, lift<Dual<3>>(f3(yo4)), yo4.w,
+                                                       rest[e], cst<Dual<3>>(stiff[e]));
+        acc = add3(acc, contract(dk, make_float3(gk.x / occ_k, gk.y / occ_k, gk.z / occ_k), 0));
+        // partner's term: d(y_o, y_k) / occ_o, derivative in y_k
+        const float4 go4 = gt[o];
+        const float occ_o = occ_of[o];
+        const V3<Dual<3>> dn = distance_term<Dual<3>>(P, lift<Dual<3>>(f3(yo4)), yo4.w, seed<3>(f3(yk4), 0), yk4.w,
+                                                       rest[e], cst<Dual<3>>(stiff[e]));
+        acc = add3(acc, contract(dn, make_float3(go4.x / occ_o, go4.y / occ_o, go4.z / occ_o), 0));
+    }
+    gy[k] = make_float4(acc.x, acc.y, acc.z, 0.f);
+}
+
+// d L / d stiffness_e += gt_a . d(d_a)/ds / occ_a + gt_b . d(d_b)/ds / occ_b.
+// One thread per constraint accumulates over the whole backward pass.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_stiffness(DevParams P0, uint32_t m, uint32_t iter_left,
+                                                          const uint32_t *__restrict__ ca,
+                                                          const uint32_t *__restrict__ cb,
+                                                          const float *__restrict__ crest,
+                                                          const float *__restrict__ cstiff,
+                                                          const float *__restrict__ occ_of,
+                                                          const float4 *__restrict__ y,
+                                                          const float4 *__restrict__ gt, float *__restrict__ gs) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    const uint32_t a = ca[c], b = cb[c];
+    const DevParams P = scene_params<B>(P0, a);
+    if (!scene_active<B>(P, iter_left)) return;
+    const float4 ya = y[a], yb = y[b];
+    Dual<1> st = dconst<1>(cstiff[c]);
+    st.d[0] = 1.f;
+    const V3<Dual<1>> da = distance_term<Dual<1>>(P, lift<Dual<1>>(f3(ya)), ya.w, lift<Dual<1>>(f3(yb)), yb.w,
+                                                  crest[c], st);
+    const V3<Dual<1>> db = distance_term<Dual<1>>(P, lift<Dual<1>>(f3(yb)), yb.w, lift<Dual<1>>(f3(ya)), ya.w,
+                                                  crest[c], st);
+    const float4 ga = gt[a], gb = gt[b];
+    const float va = (ga.x * da.x.d[0] + ga.y * da.y.d[0] + ga.z * da.z.d[0]) / occ_of[a];
+    const float vb = (gb.x * db.x.d[0] + gb.y * db.y.d[0] + gb.z * db.z.d[0]) / occ_of[b];
+    gs[c] += va + vb;
+}
+
+// Per-constraint stiffness into the per-incidence copy the forward reads.
+__global__ void __launch_bounds__(kBlock) k_scatter_stiffness(uint32_t incidences, const uint32_t *__restrict__ inc_con,
+                                                              const float *__restrict__ cstiff,
+                                                              float *__restrict__ stiff) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= incidences) return;
+    stiff[e] = cstiff[inc_con[e]];
+}
+
+// ------------------------------------------------------ contacts + walls
+
+__device__ __forceinline__ bool contact_test(const DevParams &P, uint32_t i, uint32_t j, int phi, int phj, float d2) {
+    return j != i && d2 < P.collide2 && !(phi > kSolid && phi == phj);
+}
+
+// Walks the 27-cell contact stencil of sorted particle i (the forward
+// kernel's candidate order), calling f(j) for every contact partner.
+template <class F>
+__device__ __forceinline__ void for_each_contact(const DevParams &P, uint32_t i, float3 pi, int phi,
+                                                 const float4 *__restrict__ sx, const SortedAttr *__restrict__ sattr,
+                                                 const uint32_t *__restrict__ cell_first, F &&f) {
+    for_each_candidate(P, grid_pos(P, pi), 1, cell_first, [&](uint32_t j) {
+        const float d2 = dist2_exact(pi, f3(sx[j]));
+        if (contact_test(P, i, j, phi, sattr[j].phase, d2)) f(j);
+        return true;
+    });
+}
+
+// Forward of the fused pass for sorted particle i: u = x_i + sum of its
+// contact terms (phases >= CLOTH), then walls.  The adjoint of u from the
+// adjoint gy of the written position, and the walls' part of the adjoint
+// of x_old; stores u's adjoint and i's contact count for the gather.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_solve_prep(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                           bool contacts, const float4 *__restrict__ sx,
+                                                           const SortedAttr *__restrict__ sattr,
+                                                           const uint32_t *__restrict__ sidx,
+                                                           const uint32_t *__restrict__ cell_first,
+                                                           const float4 *__restrict__ x_old,
+                                                           const float4 *__restrict__ gy,
+                                                           float4 *__restrict__ gu, uint32_t *__restrict__ cnt,
+                                                           float4 *__restrict__ gxo) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    const uint32_t orig = sidx[i];
+    const float4 g4 = gy[orig];
+    if (!scene_active<B>(P, iter_left)) {
+        gu[i] = g4;
+        cnt[i] = 0u;
+        return;
+    }
+    const float4 pi4 = sx[i];
+    const float3 pi = f3(pi4);
+    const int phi = sattr[i].phase;
+    const float3 prev = f3(x_old[orig]);
+    float3 u = pi;
+    uint32_t nb = 0;
+    if (contacts && phi >= kCloth) {
+        for_each_contact(P, i, pi, phi, sx, sattr, cell_first, [&](uint32_t) { ++nb; });
+        if (nb) {
+            V3<float> acc = lift<float>(make_float3(0.f, 0.f, 0.f));
+            const float fnb = (float)nb;
+            for_each_contact(P, i, pi, phi, sx, sattr, cell_first, [&](uint32_t j) {
+                const float4 pj4 = sx[j];
+                acc = acc + contact_pair<float>(P, lift<float>(pi), pi4.w, phi, lift<float>(prev), lift<float>(f3(pj4)),
+                                                pj4.w, sattr[j].phase, lift<float>(f3(x_old[sidx[j]])), fnb);
+            });
+            u = make_float3(pi.x + acc.x, pi.y + acc.y, pi.z + acc.z);
+        }
+    }
+    cnt[i] = nb;
+    const V3<Dual<6>> w = world_generic<Dual<6>>(P, seed<6>(u, 0), phi, seed<6>(prev, 3));
+    const float3 g = make_float3(g4.x, g4.y, g4.z);
+    const float3 gu3 = contract(w, g, 0);
+    const float3 go3 = contract(w, g, 3);
+    gu[i] = make_float4(gu3.x, gu3.y, gu3.z, 0.f);
+    const float4 o = gxo[orig];
+    gxo[orig] = make_float4(o.x + go3.x, o.y + go3.y, o.z + go3.z, 0.f);
+}
+
+// Gather for sorted particle j: the adjoint of its start-of-iteration
+// position (identity plus its own contact terms, plus every partner i's
+// terms through x_j) and the contact terms' part of the adjoint of
+// x_old_j.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                             bool contacts, const float4 *__restrict__ sx,
+                                                             const SortedAttr *__restrict__ sattr,
+                                                             const uint32_t *__restrict__ sidx,
+                                                             const uint32_t *__restrict__ cell_first,
+                                                             const float4 *__restrict__ x_old,
+                                                             const float4 *__restrict__ gu,
+                                                             const uint32_t *__restrict__ cnt,
+                                                             float4 *__restrict__ gstart, float4 *__restrict__ gxo) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const DevParams P = scene_params<B>(P0, j);
+    const uint32_t orig = sidx[j];
+    const float4 guj4 = gu[j];
+    const float3 guj = make_float3(guj4.x, guj4.y, guj4.z);
+    if (!scene_active<B>(P, iter_left) || !contacts) {
+        gstart[orig] = make_float4(guj.x, guj.y, guj.z, 0.f);
+        return;
+    }
+    const float4 pj4 = sx[j];
+    const float3 pj = f3(pj4);
+    const int phj = sattr[j].phase;
+    const float3 prevj = f3(x_old[orig]);
+    const uint32_t nj = cnt[j];
+    float3 gx = guj, go = make_float3(0.f, 0.f, 0.f);
+    for_each_contact(P, j, pj, phj, sx, sattr, cell_first, [&](uint32_t i) {
+        const float4 pi4 = sx[i];
+        const int phi = sattr[i].phase;
+        const float3 previ = f3(x_old[sidx[i]]);
+        if (phj >= kCloth && nj) {  // j's own term c_ji, in x_j and x_old_j
+            const V3<Dual<6>> c = contact_pair<Dual<6>>(P, seed<6>(pj, 0), pj4.w, phj, seed<6>(prevj, 3),
+                                                        lift<Dual<6>>(f3(pi4)), pi4.w, phi, lift<Dual<6>>(previ),
+                                                        (float)nj);
+            gx = add3(gx, contract(c, guj, 0));
+            go = add3(go, contract(c, guj, 3));
+        }
+        const uint32_t ni = cnt[i];
+        if (phi >= kCloth && ni) {  // partner's term c_ij, in x_j and x_old_j
+            const float4 gui4 = gu[i];
+            const float3 gui = make_float3(gui4.x, gui4.y, gui4.z);
+            const V3<Dual<6>> c = contact_pair<Dual<6>>(P, lift<Dual<6>>(f3(pi4)), pi4.w, phi, lift<Dual<6>>(previ),
+                                                        seed<6>(pj, 0), pj4.w, phj, seed<6>(prevj, 3), (float)ni);
+            gx = add3(gx, contract(c, gui, 0));
+            go = add3(go, contract(c, gui, 3));
+        }
+    });
+    gstart[orig] = make_float4(gx.x, gx.y, gx.z, 0.f);
+    const float4 o = gxo[orig];
+    gxo[orig] = make_float4(o.x + go.x, o.y + go.y, o.z + go.z, 0.f);
+}
+
+// ------------------------------------------------------------ host side
+
+#define ADJ_TRY(s, call)                                                                              \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return pbd_internal_fail((s), PBD_ERR_CUDA, std::string(#call " failed: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+cudaError_t grow(T **p, size_t &have, size_t want) {
+    if (have >= want && *p) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    have = 0;
+    cudaError_t e = cudaMalloc((void **)p, want * sizeof(T));
+    if (e == cudaSuccess) have = want;
+    return e;
+}
+
+int differentiable(pbd_system *s) {
+    if (s->n_fluid)
+        return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED,
+                                 "differentiation covers contacts, walls, distance constraints, pins and the "
+                                 "integrator; this system has fluid particles");
+    if (s->bodies.count)
+        return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED,
+                                 "differentiation covers contacts, walls, distance constraints, pins and the "
+                                 "integrator; this system has rigid bodies");
+    return PBD_OK;
+}
+
+// The forward step with the positions the projectors read recorded:
+// rec[0] = x at the start (x_old), then per iteration the position at the
+// iteration start and after the contact / wall pass.  The same launches in
+// the same order as enqueue_update for a system without fluid or bodies.
+int record_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec) {
+    const DevParams &P = s->dev;
+    const uint32_t n = s->n;
+    const size_t bytes = (size_t)n * sizeof(float4);
+    ADJ_TRY(s, cudaMemcpyAsync(rec, s->x, bytes, cudaMemcpyDeviceToDevice, st));
+    ADJ_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
+    ADJ_TRY(s, launch_predict(P, n, dt, s->x, s->v, s->x_old, s->grid.hash, s->grid.slot, s->grid.cell_first, st));
+    uint32_t mask = kDoWorld;
+    if (s->n_contact) mask |= kDoContact;
+    const uint32_t iters = P.iterations;
+    for (uint32_t it = 0; it < iters; ++it) {
+        const uint32_t left = iters - 1u - it;
+        if (int rc = pbd_internal_build_grid(s, st, it == 0)) return rc;
+        ADJ_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 2 * it) * n, s->x, bytes, cudaMemcpyDeviceToDevice, st));
+        ADJ_TRY(s, launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, s->nbl, false, s->tpp, st));
+        ADJ_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 2 * it) * n, s->x, bytes, cudaMemcpyDeviceToDevice, st));
+        if (s->cons.count) ADJ_TRY(s, launch_distance(P, left, s->cons, s->x, true, true, st));
+    }
+    ADJ_TRY(s, launch_velocity(P, n, dt, s->x, s->x_old, s->v, st));
+    return PBD_OK;
+}
+
+}  // namespace
+}  // namespace pbd
+
+using namespace pbd;
+
+void pbd_internal_free_adjoint(pbd_system *s) {
+    auto &a = s->adj;
+    for (float4 **p : {&a.ckpt_x, &a.ckpt_v, &a.rec, &a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu, &a.save_x, &a.save_v,
+                       &a.save_xo}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    if (a.cnt) cudaFree(a.cnt);
+    if (a.gstiff) cudaFree(a.gstiff);
+    a.cnt = nullptr;
+    a.gstiff = nullptr;
+    a.ckpt_cap = a.rec_cap = 0;
+    a.work_cap = a.stiff_cap = 0;
+    a.recorded = false;
+}
+
+extern "C" {
+
+int pbd_set_distance_stiffness(pbd_system *s, uint32_t count, const float *stiffness, int on_device, void *stream) {
+    if (int rc = pbd_internal_guard(s)) return rc;
+    const uint32_t m = (uint32_t)s->dist_a.size();
+    if (count != m) return pbd_internal_fail(s, PBD_ERR_INVALID_ARGUMENT, "stiffness count must equal the number of distance constraints");
+    if (m == 0) return PBD_OK;
+    if (!stiffness) return pbd_internal_fail(s, PBD_ERR_INVALID_ARGUMENT, "stiffness is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<float> host(m);
+    if (on_device) {
+        ADJ_TRY(s, cudaMemcpyAsync(host.data(), stiffness, m * 4ull, cudaMemcpyDeviceToHost, st));
+        ADJ_TRY(s, cudaStreamSynchronize(st));
+    } else {
+        std::copy(stiffness, stiffness + m, host.begin());
+    }
+    for (uint32_t c = 0; c < m; ++c)
+        if (!(host[c] >= 0.f && host[c] <= 1.f))
+            return pbd_internal_fail(s, PBD_ERR_INVALID_ARGUMENT, "stiffness must be in [0, 1]");
+    s->dist_stiff = host;
+    ++s->version;
+    const ConstraintBuffers &c = s->cons;
+    ADJ_TRY(s, cudaMemcpyAsync(c.con_stiff, host.data(), m * 4ull, cudaMemcpyHostToDevice, st));
+    uint32_t E = 0;
+    ADJ_TRY(s, cudaMemcpyAsync(&E, c.row + c.count, 4, cudaMemcpyDeviceToHost, st));
+    ADJ_TRY(s, cudaStreamSynchronize(st));
+    if (E) k_scatter_stiffness<<<blocks_for(E), kBlock, 0, st>>>(E, c.inc_con, c.con_stiff, c.stiff);
+    ADJ_TRY(s, cudaGetLastError());
+    ADJ_TRY(s, cudaStreamSynchronize(st));
+    return PBD_OK;
+}
+
+uint32_t pbd_num_distance_constraints(const pbd_system *s) { return s ? (uint32_t)s->dist_a.size() : 0u; }
+
+int pbd_rollout(pbd_system *s, float dt, uint32_t steps, uint32_t every, void *stream) {
+    if (int rc = pbd_internal_guard(s)) return rc;
+    if (!(dt > 0.f) || !std::isfinite(dt)) return pbd_internal_fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
+    if (steps == 0 || every == 0) return pbd_internal_fail(s, PBD_ERR_INVALID_ARGUMENT, "steps and every must be > 0");
+    if (int rc = differentiable(s)) return rc;
+    auto &a = s->adj;
+    a.recorded = false;
+    const uint32_t n = s->n;
+    const uint32_t nck = (steps + every - 1u) / every;
+    const size_t want = (size_t)nck * n;
+    if (a.ckpt_cap < want || !a.ckpt_x || !a.ckpt_v) {
+        if (a.ckpt_x) cudaFree(a.ckpt_x);
+        if (a.ckpt_v) cudaFree(a.ckpt_v);
+        a.ckpt_x = a.ckpt_v = nullptr;
+        a.ckpt_cap = 0;
+        ADJ_TRY(s, cudaMalloc((void **)&a.ckpt_x, want * sizeof(float4)));
+        ADJ_TRY(s, cudaMalloc((void **)&a.ckpt_v, want * sizeof(float4)));
+        a.ckpt_cap = want;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    dt = pbd_internal_clamp_dt(s, dt);
+    const size_t bytes = (size_t)n * sizeof(float4);
+    for (uint32_t t = 0; t < steps; ++t) {
+        if (t % every == 0) {
+            const size_t off = (size_t)(t / every) * n;
+            ADJ_TRY(s, cudaMemcpyAsync(a.ckpt_x + off, s->x, bytes, cudaMemcpyDeviceToDevice, st));
+            ADJ_TRY(s, cudaMemcpyAsync(a.ckpt_v + off, s->v, bytes, cudaMemcpyDeviceToDevice, st));
+        }
+        if (int rc = pbd_internal_enqueue_update(s, dt, st)) return rc;
+    }
+    a.recorded = true;
+    a.version = s->version;
+    a.dt = dt;
+    a.steps = steps;
+    a.every = every;
+    a.nckpt = nck;
+    return PBD_OK;
+}
+
+int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *dL_dx0, float *dL_dv0,
+                 float *dL_dstiffness, void *stream) {
+    if (int rc = pbd_internal_guard(s)) return rc;
+    auto &a = s->adj;
+    if (!a.recorded || a.version != s->version)
+        return pbd_internal_fail(s, PBD_ERR_STATE, "no rollout to differentiate: call pbd_rollout after the last change of the scene");
+    if (int rc = differentiable(s)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t n = s->n;
+    const DevParams &P = s->dev;
+    const bool batched = P.table != nullptr;
+    const uint32_t iters = P.iterations;
+    const size_t bytes = (size_t)n * sizeof(float4);
+    const size_t per_step = 1u + 2u * iters;
+    // work arrays
+    size_t rec_have = a.rec_cap;
+    ADJ_TRY(s, grow(&a.rec, rec_have, per_step * a.every * (size_t)n));
+    a.rec_cap = rec_have;
+    if (a.work_cap < s->cap) {
+        for (float4 **p : {&a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu, &a.save_x, &a.save_v, &a.save_xo}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+            ADJ_TRY(s, cudaMalloc((void **)p, (size_t)s->cap * sizeof(float4)));
+        }
+        if (a.cnt) cudaFree(a.cnt);
+        a.cnt = nullptr;
+        ADJ_TRY(s, cudaMalloc((void **)&a.cnt, (size_t)s->cap * sizeof(uint32_t)));
+        a.work_cap = s->cap;
+    }
+    const uint32_t m = s->cons.m;
+    if (m && a.stiff_cap < m) {
+        if (a.gstiff) cudaFree(a.gstiff);
+        a.gstiff = nullptr;
+        ADJ_TRY(s, cudaMalloc((void **)&a.gstiff, (size_t)m * sizeof(float)));
+        a.stiff_cap = m;
+    }
+    if (m) ADJ_TRY(s, cudaMemsetAsync(a.gstiff, 0, (size_t)m * sizeof(float), st));
+    // the state after the rollout, restored at the end
+    ADJ_TRY(s, cudaMemcpyAsync(a.save_x, s->x, bytes, cudaMemcpyDeviceToDevice, st));
+    ADJ_TRY(s, cudaMemcpyAsync(a.save_v, s->v, bytes, cudaMemcpyDeviceToDevice, st));
+    ADJ_TRY(s, cudaMemcpyAsync(a.save_xo, s->x_old, bytes, cudaMemcpyDeviceToDevice, st));
+    // incoming adjoints
+    if (dL_dx) ADJ_TRY(s, cudaMemcpyAsync(a.gx, dL_dx, bytes, cudaMemcpyDeviceToDevice, st));
+    else ADJ_TRY(s, cudaMemsetAsync(a.gx, 0, bytes, st));
+    if (dL_dv) ADJ_TRY(s, cudaMemcpyAsync(a.gv, dL_dv, bytes, cudaMemcpyDeviceToDevice, st));
+    else ADJ_TRY(s, cudaMemsetAsync(a.gv, 0, bytes, st));
+    const bool contacts = s->n_contact != 0;
+    const ConstraintBuffers &c = s->cons;
+    const unsigned nb = blocks_for(n);
+    const float dt = a.dt;
+#define ADJ_LAUNCH(KERNEL, GRID, ...)                                                     \
+    do {                                                                                  \
+        if (batched) KERNEL<true><<<(GRID), kBlock, 0, st>>>(__VA_ARGS__);                \
+        else KERNEL<false><<<(GRID), kBlock, 0, st>>>(__VA_ARGS__);                       \
+        ADJ_TRY(s, cudaGetLastError());                                                   \
+    } while (0)
+    for (int seg = (int)a.nckpt - 1; seg >= 0; --seg) {
+        const uint32_t t0 = (uint32_t)seg * a.every;
+        const uint32_t t1 = std::min(a.steps, t0 + a.every);
+        // recompute the segment from its checkpoint, recording
+        ADJ_TRY(s, cudaMemcpyAsync(s->x, a.ckpt_x + (size_t)seg * n, bytes, cudaMemcpyDeviceToDevice, st));
+        ADJ_TRY(s, cudaMemcpyAsync(s->v, a.ckpt_v + (size_t)seg * n, bytes, cudaMemcpyDeviceToDevice, st));
+        for (uint32_t t = t0; t < t1; ++t)
+            if (int rc = record_update(s, dt, st, a.rec + (t - t0) * per_step * n)) return rc;
+        // reverse over its steps
+        for (int t = (int)t1 - 1; t >= (int)t0; --t) {
+            float4 *rec = a.rec + (size_t)(t - (int)t0) * per_step * n;
+            // x_old of this step for the friction and wall terms
+            ADJ_TRY(s, cudaMemcpyAsync(s->x_old, rec, bytes, cudaMemcpyDeviceToDevice, st));
+            // gy <- adjoint of the final positions, gxo <- -gv / dt
+            ADJ_LAUNCH(k_adj_velocity, nb, P, n, dt, a.gx, a.gv, a.gy, a.gxo);
+            for (int it = (int)iters - 1; it >= 0; --it) {
+                const uint32_t left = iters - 1u - (uint32_t)it;
+                const float4 *xstart = rec + (size_t)(1 + 2 * it) * n;
+                const float4 *ysolve = rec + (size_t)(2 + 2 * it) * n;
+                // pins and distance constraints: gy (after pins) -> gt -> gy
+                if (c.count) {
+                    ADJ_TRY(s, cudaMemcpyAsync(a.gt, a.gy, bytes, cudaMemcpyDeviceToDevice, st));
+                    const unsigned cb = blocks_for(c.count);
+                    if (c.any_pin) ADJ_LAUNCH(k_adj_pins, cb, P, c.count, left, c.particle, c.pin, a.gt);
+                    ADJ_TRY(s, cudaMemcpyAsync(a.gy, a.gt, bytes, cudaMemcpyDeviceToDevice, st));
+                    if (c.any_distance) {
+                        ADJ_LAUNCH(k_adj_distance, cb, P, c.count, left, c.particle, c.row, c.other, c.rest, c.stiff,
+                                   c.occ_of, ysolve, a.gt, a.gy);
+                        ADJ_LAUNCH(k_adj_stiffness, blocks_for(m), P, m, left, c.con_a, c.con_b, c.con_rest,
+                                   c.con_stiff, c.occ_of, ysolve, a.gt, a.gstiff);
+                    }
+                }
+                // contacts and walls: rebuild this iteration's grid, then
+                // prep (walls, u's adjoint, counts) and gather
+                ADJ_TRY(s, cudaMemcpyAsync(s->x, xstart, bytes, cudaMemcpyDeviceToDevice, st));
+                if (int rc = pbd_internal_build_grid(s, st, false)) return rc;
+                ADJ_LAUNCH(k_adj_solve_prep, nb, P, n, left, contacts, s->grid.sorted_x, s->grid.sorted_attr,
+                           s->grid.sorted_idx, s->grid.cell_first, s->x_old, a.gy, a.gu, a.cnt, a.gxo);
+                ADJ_LAUNCH(k_adj_solve_gather, nb, P, n, left, contacts, s->grid.sorted_x, s->grid.sorted_attr,
+                           s->grid.sorted_idx, s->grid.cell_first, s->x_old, a.gu, a.cnt, a.gy, a.gxo);
+            }
+            // predict: gy is now the adjoint of the predicted positions
+            ADJ_LAUNCH(k_adj_predict, nb, P, n, dt, a.gy, a.gxo, a.gx, a.gv);
+        }
+    }
+#undef ADJ_LAUNCH
+    if (dL_dx0) ADJ_TRY(s, cudaMemcpyAsync(dL_dx0, a.gx, bytes, cudaMemcpyDeviceToDevice, st));
+    if (dL_dv0) ADJ_TRY(s, cudaMemcpyAsync(dL_dv0, a.gv, bytes, cudaMemcpyDeviceToDevice, st));
+    if (dL_dstiffness && m)
+        ADJ_TRY(s, cudaMemcpyAsync(dL_dstiffness, a.gstiff, (size_t)m * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    ADJ_TRY(s, cudaMemcpyAsync(s->x, a.save_x, bytes, cudaMemcpyDeviceToDevice, st));
+    ADJ_TRY(s, cudaMemcpyAsync(s->v, a.save_v, bytes, cudaMemcpyDeviceToDevice, st));
+    ADJ_TRY(s, cudaMemcpyAsync(s->x_old, a.save_xo, bytes, cudaMemcpyDeviceToDevice, st));
+    s->grid_valid = false;
+    return PBD_OK;
+}
+
+}  // extern "C"

@@ -42,6 +42,12 @@ struct ConstraintBuffers {
     float4 *pin;           // [count] pin point, w = 1 when pinned
     float4 *tmp;           // [count] new positions
     bool any_distance, any_pin;
+    // per distance constraint, in add order (stiffness updates, adjoint)
+    uint32_t m;            // constraints
+    uint32_t *con_a, *con_b;  // [m] endpoints
+    float *con_rest, *con_stiff;  // [m]
+    uint32_t *inc_con;     // [incidences] constraint of each incidence
+    float *occ_of;         // [particles] constraint count of each particle (0: none)
 };
 
 struct BodyBuffers {

@@ -129,7 +129,14 @@ void free_constraints(pbd_system *s) {
     dfree(s->cons.occ);
     dfree(s->cons.pin);
     dfree(s->cons.tmp);
+    dfree(s->cons.con_a);
+    dfree(s->cons.con_b);
+    dfree(s->cons.con_rest);
+    dfree(s->cons.con_stiff);
+    dfree(s->cons.inc_con);
+    dfree(s->cons.occ_of);
     s->cons.count = 0;
+    s->cons.m = 0;
     s->cons.any_distance = s->cons.any_pin = false;
 }
 
@@ -263,7 +270,7 @@ int upload_constraints(pbd_system *s) {
         row[sidx + 1] = row[sidx] + first_cnt[k] + second_cnt[k];
     }
     const uint32_t E = row[C];
-    std::vector<uint32_t> other(E), fill_first(C, 0), fill_second(C, 0);
+    std::vector<uint32_t> other(E), fill_first(C, 0), fill_second(C, 0), inc_con(E);
     std::vector<float> rest(E), stiff(E);
     for (size_t c = 0; c < m; ++c) {
         const uint32_t a = s->dist_a[c], b = s->dist_b[c];
@@ -272,6 +279,7 @@ int upload_constraints(pbd_system *s) {
         other[ea] = b;
         rest[ea] = s->dist_rest[c];
         stiff[ea] = s->dist_stiff[c];
+        inc_con[ea] = (uint32_t)c;
     }
     for (size_t c = 0; c < m; ++c) {
         const uint32_t a = s->dist_a[c], b = s->dist_b[c];
@@ -280,6 +288,7 @@ int upload_constraints(pbd_system *s) {
         other[eb] = a;
         rest[eb] = s->dist_rest[c];
         stiff[eb] = s->dist_stiff[c];
+        inc_con[eb] = (uint32_t)c;
     }
     std::vector<float> occf(C);
     std::vector<float4> pin(C, make_float4(0.f, 0.f, 0.f, 0.f));
@@ -309,6 +318,23 @@ int upload_constraints(pbd_system *s) {
     }
     CUDA_TRY(s, cudaMemcpy(cb.occ, occf.data(), C * 4ull, cudaMemcpyHostToDevice));
     CUDA_TRY(s, cudaMemcpy(cb.pin, pin.data(), C * sizeof(float4), cudaMemcpyHostToDevice));
+    std::vector<float> occ_of(n);
+    for (uint32_t k = 0; k < n; ++k) occ_of[k] = (float)occ[k];
+    CUDA_TRY(s, dalloc(&cb.occ_of, n));
+    CUDA_TRY(s, cudaMemcpy(cb.occ_of, occ_of.data(), n * 4ull, cudaMemcpyHostToDevice));
+    if (m) {
+        CUDA_TRY(s, dalloc(&cb.con_a, m));
+        CUDA_TRY(s, dalloc(&cb.con_b, m));
+        CUDA_TRY(s, dalloc(&cb.con_rest, m));
+        CUDA_TRY(s, dalloc(&cb.con_stiff, m));
+        CUDA_TRY(s, dalloc(&cb.inc_con, E));
+        CUDA_TRY(s, cudaMemcpy(cb.con_a, s->dist_a.data(), m * 4ull, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(cb.con_b, s->dist_b.data(), m * 4ull, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(cb.con_rest, s->dist_rest.data(), m * 4ull, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(cb.con_stiff, s->dist_stiff.data(), m * 4ull, cudaMemcpyHostToDevice));
+        CUDA_TRY(s, cudaMemcpy(cb.inc_con, inc_con.data(), E * 4ull, cudaMemcpyHostToDevice));
+    }
+    cb.m = (uint32_t)m;
     cb.count = C;
     cb.any_distance = m > 0;
     cb.any_pin = !s->pin_idx.empty();
@@ -491,6 +517,17 @@ float clamp_dt(const pbd_system *s, float dt) {
 
 }  // namespace
 
+int pbd_internal_fail(pbd_system *s, int code, const std::string &msg) { return fail(s, code, "%s", msg.c_str()); }
+int pbd_internal_guard(pbd_system *s) {
+    if (int rc = check_sys(s)) return rc;
+    return use_device(s);
+}
+int pbd_internal_build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict) {
+    return build_grid(s, st, hashed_in_predict);
+}
+int pbd_internal_enqueue_update(pbd_system *s, float dt, cudaStream_t st) { return enqueue_update(s, dt, st); }
+float pbd_internal_clamp_dt(const pbd_system *s, float dt) { return clamp_dt(s, dt); }
+
 int pbd_internal_device_params(const pbd_params *params, pbd::DevParams *out, std::string *why) {
     std::string w;
     const int rc = validate_params(params, w);
@@ -618,6 +655,7 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->grid.sorted_attr);
     dfree(s->d_table);
     dfree(s->d_scene_of);
+    pbd_internal_free_adjoint(s);
     free_grid(s);
     free_constraints(s);
     free_bodies(s);

@@ -89,6 +89,24 @@ struct pbd_system {
     uint64_t graph_version = 0;
     uint64_t version = 1;  // bumped whenever a captured graph would go stale
 
+    // differentiation: checkpoints of the last pbd_rollout and the
+    // backward pass's work arrays (pbd_adjoint.cu)
+    struct Adjoint {
+        bool recorded = false;
+        uint64_t version = 0;   // system version the rollout ran on
+        float dt = 0.f;
+        uint32_t steps = 0, every = 0, nckpt = 0;
+        float4 *ckpt_x = nullptr, *ckpt_v = nullptr;  // [nckpt][cap]
+        size_t ckpt_cap = 0;                          // states allocated
+        float4 *rec = nullptr;                        // segment recording
+        size_t rec_cap = 0;                           // states allocated
+        float4 *gx = nullptr, *gv = nullptr, *gxo = nullptr, *gt = nullptr, *gy = nullptr, *gu = nullptr;
+        float4 *save_x = nullptr, *save_v = nullptr, *save_xo = nullptr;
+        uint32_t *cnt = nullptr;
+        float *gstiff = nullptr;
+        uint32_t work_cap = 0, stiff_cap = 0;
+    } adj;
+
     std::string err;
 
     bool batched() const { return scenes.size() > 1; }
@@ -99,3 +117,10 @@ struct pbd_system {
 // constants, and the calling thread's error text for calls without a handle.
 int pbd_internal_device_params(const pbd_params *params, pbd::DevParams *out, std::string *why);
 void pbd_internal_set_thread_error(const std::string &msg);
+// Step internals used by the adjoint (pbd_adjoint.cu).
+int pbd_internal_fail(pbd_system *s, int code, const std::string &msg);
+int pbd_internal_guard(pbd_system *s);  // handle check + its device current
+int pbd_internal_build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict);
+int pbd_internal_enqueue_update(pbd_system *s, float dt, cudaStream_t st);
+float pbd_internal_clamp_dt(const pbd_system *s, float dt);
+void pbd_internal_free_adjoint(pbd_system *s);

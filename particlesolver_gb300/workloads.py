@@ -430,3 +430,70 @@ def batched_scenes(count: int = 512, seed: int = 512, lo: int = 1024, hi: int = 
         n = int(sizes[k])
         out.append(pbf_block(n, seed=seed * 1000 + k) if coin[k] else granular_column(n, seed=seed * 1000 + k))
     return out
+
+
+def cloth_ropes_grains(cloth: int = 64, ropes: int = 8, rope_particles: int = 32, grains: int = 200,
+                       radius: float = 0.25, seed: int = 5, iterations: int = 4, drop: float = 3.0,
+                       stiffness_seed: int | None = None) -> Scene:
+    """A cloth x cloth sheet (spacing 2r, stretch constraints between axis
+    neighbours, the two edges x = 0 and x = max pinned) at height 6; `ropes`
+    ropes of `rope_particles` particles lying across it 0.6 above (first
+    particle pinned); `grains` solid grains seeded uniformly in a slab
+    `drop` above the sheet with downward velocities U(-2, -1) and small
+    sideways ones.  Stiffness U(0.2, 1) per constraint when stiffness_seed
+    is given (else 1).  The defaults give 4,096 + 256 + 200 = 4,552
+    particles."""
+    d = 2.0 * radius
+    ext = cloth * d
+    pos, vel, phase, pairs, pins = [], [], [], [], []
+    obj = 0
+    cx, cz = np.meshgrid(np.arange(cloth), np.arange(cloth), indexing="xy")
+    pos.append(np.stack([cx.ravel() * d, np.full(cloth * cloth, 6.0), cz.ravel() * d], 1))
+    phase.append(np.full(cloth * cloth, PHASE_RIGID + obj, np.int32))
+    obj += 1
+    idx = np.arange(cloth * cloth).reshape(cloth, cloth)  # [z, x]
+    pairs += [np.stack([idx[:, :-1].ravel(), idx[:, 1:].ravel()], 1),
+              np.stack([idx[:-1, :].ravel(), idx[1:, :].ravel()], 1)]
+    pins.append(np.concatenate([idx[:, 0], idx[:, -1]]))
+    n0 = cloth * cloth
+    for r in range(ropes):
+        z = (r + 0.5) * ext / ropes
+        rp = np.stack([0.5 * d + np.arange(rope_particles) * d * min(1.0, (cloth - 1) / rope_particles),
+                       np.full(rope_particles, 6.6), np.full(rope_particles, z)], 1)
+        pos.append(rp)
+        phase.append(np.full(rope_particles, PHASE_RIGID + obj, np.int32))
+        obj += 1
+        ids = n0 + np.arange(rope_particles)
+        pairs.append(np.stack([ids[:-1], ids[1:]], 1))
+        pins.append(ids[:1])
+        n0 += rope_particles
+    g = np.stack([uniform(seed, (grains,), 0.1 * ext, 0.9 * ext), uniform(seed + 1, (grains,), 7.2, 7.2 + drop),
+                  uniform(seed + 2, (grains,), 0.1 * ext, 0.9 * ext)], 1)
+    pos.append(g)
+    phase.append(np.full(grains, PHASE_SOLID, np.int32))
+    pos = np.concatenate(pos)
+    n = pos.shape[0]
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0
+    vel = np.zeros((n, 4), np.float32)
+    vel[n - grains:, 0] = uniform(seed + 3, (grains,), -0.3, 0.3)
+    vel[n - grains:, 1] = uniform(seed + 4, (grains,), -2.0, -1.0)
+    vel[n - grains:, 2] = uniform(seed + 5, (grains,), -0.3, 0.3)
+    pairs = np.concatenate(pairs).astype(np.uint32)
+    rest = np.linalg.norm(pos_w[pairs[:, 0], :3].astype(np.float64) - pos_w[pairs[:, 1], :3], axis=1)
+    stiff = (np.ones(len(pairs), np.float32) if stiffness_seed is None
+             else uniform(stiffness_seed, (len(pairs),), 0.2, 1.0).astype(np.float32))
+    pins = np.concatenate(pins).astype(np.uint32)
+    cell = 2.002 * radius
+    height = 7.2 + drop + 2.0
+    grid = [next_pow2(ext / cell), next_pow2(height / cell), next_pow2(ext / cell)]
+    params = dict(particle_radius=radius, kernel_radius=2.0 * radius, cell_size=cell, grid_size=grid,
+                  world_origin=[-1.0, 0.0, -1.0], gravity=[0.0, -9.8, 0.0], box_min=[-1.0, 0.0, -1.0],
+                  box_max=[ext + 1.0, 60.0, ext + 1.0], iterations=iterations, relaxation=0.01, scorr_k=0.1,
+                  scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0, max_dt=1.0 / 60.0, max_neighbors=500,
+                  contact_static_friction=0.1, contact_kinetic_friction=0.05,
+                  wall_static_friction=0.1, wall_kinetic_friction=0.05)
+    return Scene("cloth_ropes_grains", params, pos_w, np.concatenate(phase), vel=vel, pairs=pairs,
+                 rest=rest.astype(np.float32), stiffness=stiff, pins=pins, pin_points=pos_w[pins, :3].copy(),
+                 dt=1.0 / 60.0, info=dict(cloth=cloth, ropes=ropes, grains=grains))

@@ -1,0 +1,206 @@
+"""Adjoint (reverse-mode) gradients of rollouts, through the C ABI and the
+torch.autograd bridge, against central finite differences of the FP64
+oracle.
+
+Loss L = sum_i c_i . x_T,i with fixed random c.  The FP32 adjoint's
+directional derivative along a random direction in (stiffness, x0, v0)
+must match the oracle's (L(p + eps d) - L(p - eps d)) / (2 eps) to 1e-3
+relative; eps = 1e-5 is far inside the range where the oracle's central
+difference has converged and no contact switches on or off."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import Oracle  # noqa: E402
+from particlesolver_gb300 import PBD_ERR_UNSUPPORTED, ParticleSystem, PbdError, default_params  # noqa: E402
+from particlesolver_gb300 import workloads as W  # noqa: E402
+from particlesolver_gb300.autograd import rollout  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-3
+
+
+def small_scene(seed=5, stiffness_seed=9):
+    return W.cloth_ropes_grains(cloth=8, ropes=2, rope_particles=8, grains=12, drop=0.8, seed=seed,
+                                stiffness_seed=stiffness_seed)
+
+
+def sliding_grains():
+    """Grains sliding on the floor into a side wall: wall clamps and wall
+    friction (static and kinetic), no particle contacts."""
+    sc = W.granular_column(16, width=4, seed=3)
+    sc.params.update(contact_static_friction=0.3, contact_kinetic_friction=0.2, wall_static_friction=0.3,
+                     wall_kinetic_friction=0.2, flags=0, box_min=[-2.0, 0.0, -2.0], box_max=[2.0, 40.0, 2.0],
+                     grid_size=[16, 32, 16], world_origin=[-2.0, 0.0, -2.0])
+    pos = sc.pos_w.copy()
+    pos[:, 0] *= 1.3  # spacing 0.65: no contacts
+    pos[:, 1] = 0.3 + 0.65 * (np.arange(16) // 4) * 0.0
+    pos[:, 2] = np.repeat(np.arange(4), 4) * 0.65 - 1.0
+    sc.pos_w = pos
+    vel = np.zeros((16, 4), np.float32)
+    vel[:, 0] = 1.5
+    vel[:, 1] = -0.5
+    vel[:, 2] = np.linspace(-0.4, 0.4, 16)
+    sc.vel = vel
+    return sc
+
+
+def gpu_gradients(sc, stiffness, steps, every, c):
+    sys = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, sys)
+    dev = torch.device("cuda", 0)
+    st = torch.tensor(stiffness if stiffness is not None else np.zeros(0), dtype=torch.float32, device=dev,
+                      requires_grad=True)
+    x0 = torch.tensor(sc.pos_w, device=dev, requires_grad=True)
+    v0 = torch.tensor(sc.vel if sc.vel is not None else np.zeros((sc.n, 4), np.float32), device=dev,
+                      requires_grad=True)
+    xT, _ = rollout(sys, st, x0, v0, sc.dt, steps, every)
+    loss = (xT[:, :3] * torch.tensor(c, dtype=torch.float32, device=dev)).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    gs = st.grad.cpu().numpy() if st.grad is not None else np.zeros(0)
+    return gs, x0.grad.cpu().numpy()[:, :3], v0.grad.cpu().numpy()[:, :3], xT.detach().cpu().numpy()
+
+
+def oracle_loss(sc, stiffness, x0, v0, steps, c):
+    o = Oracle(default_params(**sc.params), sc.n)
+    pos = np.asarray(sc.pos_w, np.float64).copy()
+    pos[:, :3] = x0
+    vel = np.zeros((sc.n, 4))
+    vel[:, :3] = v0
+    o.add_particles(pos, vel, sc.phase, sc.rest_density)
+    if sc.pairs is not None and len(sc.pairs):
+        o.add_distance_constraints(sc.pairs, sc.rest, stiffness)
+    if sc.pins is not None and len(sc.pins):
+        o.add_point_constraints(sc.pins, sc.pin_points)
+    for _ in range(steps):
+        o.update(sc.dt)
+    return float(np.sum(o.positions()[:, :3] * c))
+
+
+def check_directional(sc, steps, every, seed, eps=1e-5):
+    rng = np.random.default_rng(seed)
+    c = rng.standard_normal((sc.n, 3))
+    m = 0 if sc.pairs is None else len(sc.pairs)
+    stiff = None if not m else (sc.stiffness if sc.stiffness is not None else np.ones(m, np.float32))
+    gs, gx, gv, _ = gpu_gradients(sc, stiff, steps, every, c)
+    ds = rng.uniform(-1, 1, m)
+    dx = rng.standard_normal((sc.n, 3)) * 0.1
+    dv = rng.standard_normal((sc.n, 3))
+    ad = float(np.dot(gs, ds) + np.sum(gx * dx) + np.sum(gv * dv))
+    s0 = None if not m else np.asarray(stiff, np.float64)
+    x0 = np.asarray(sc.pos_w[:, :3], np.float64)
+    v0 = np.zeros((sc.n, 3)) if sc.vel is None else np.asarray(sc.vel[:, :3], np.float64)
+    lp = oracle_loss(sc, None if s0 is None else s0 + eps * ds, x0 + eps * dx, v0 + eps * dv, steps, c)
+    lm = oracle_loss(sc, None if s0 is None else s0 - eps * ds, x0 - eps * dx, v0 - eps * dv, steps, c)
+    fd = (lp - lm) / (2 * eps)
+    assert abs(ad - fd) <= TOL * abs(fd), (ad, fd)
+    return ad, fd
+
+
+@pytest.mark.parametrize("steps,every", [(6, 6), (12, 5)])
+def test_cloth_ropes_grains_gradient_matches_fd(steps, every):
+    """Distance constraints with per-constraint stiffness, pins, contacts
+    with friction between grains and cloth / ropes, the integrator."""
+    check_directional(small_scene(), steps, every, seed=steps)
+
+
+def test_each_parameter_block_matches_fd():
+    """Stiffness, x0 and v0 directions checked one at a time."""
+    sc = small_scene(seed=6, stiffness_seed=10)
+    steps, every = 10, 4
+    rng = np.random.default_rng(1)
+    c = rng.standard_normal((sc.n, 3))
+    gs, gx, gv, _ = gpu_gradients(sc, sc.stiffness, steps, every, c)
+    eps = 1e-5
+    s0 = sc.stiffness.astype(np.float64)
+    x0 = sc.pos_w[:, :3].astype(np.float64)
+    v0 = sc.vel[:, :3].astype(np.float64)
+    for which in ("stiffness", "x0", "v0"):
+        ds = rng.uniform(-1, 1, len(s0)) if which == "stiffness" else np.zeros(len(s0))
+        dx = rng.standard_normal(x0.shape) * 0.1 if which == "x0" else np.zeros_like(x0)
+        dv = rng.standard_normal(v0.shape) if which == "v0" else np.zeros_like(v0)
+        ad = float(np.dot(gs, ds) + np.sum(gx * dx) + np.sum(gv * dv))
+        fd = (oracle_loss(sc, s0 + eps * ds, x0 + eps * dx, v0 + eps * dv, steps, c)
+              - oracle_loss(sc, s0 - eps * ds, x0 - eps * dx, v0 - eps * dv, steps, c)) / (2 * eps)
+        assert abs(ad - fd) <= TOL * abs(fd), (which, ad, fd)
+
+
+def test_wall_clamps_and_friction_gradient():
+    check_directional(sliding_grains(), 8, 3, seed=4)
+
+
+def test_gradient_independent_of_checkpoint_interval():
+    """The backward pass recomputes segments from checkpoints; any
+    interval gives the same result bit for bit."""
+    sc = small_scene()
+    c = np.random.default_rng(2).standard_normal((sc.n, 3))
+    ref = gpu_gradients(sc, sc.stiffness, 9, 9, c)
+    for every in (1, 2, 4):
+        got = gpu_gradients(sc, sc.stiffness, 9, every, c)
+        for a, b in zip(ref, got):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_batched_gradients_equal_each_scene_alone():
+    scenes = [small_scene(seed=5, stiffness_seed=9), small_scene(seed=8, stiffness_seed=11)]
+    rng = np.random.default_rng(3)
+    cs = [rng.standard_normal((sc.n, 3)) for sc in scenes]
+    alone = [gpu_gradients(sc, sc.stiffness, 8, 3, c) for sc, c in zip(scenes, cs)]
+    total = sum(sc.n for sc in scenes)
+    sys = ParticleSystem(default_params(**scenes[0].params), total)
+    off = [0, scenes[0].n]
+    for k, sc in enumerate(scenes):
+        if k:
+            sys.begin_scene(default_params(**sc.params))
+        W.apply_to(W.Scene(sc.name, sc.params, sc.pos_w, sc.phase, vel=sc.vel, pairs=sc.pairs + off[k],
+                           rest=sc.rest, stiffness=sc.stiffness, pins=sc.pins + off[k], pin_points=sc.pin_points),
+                   sys)
+    dev = torch.device("cuda", 0)
+    st = torch.tensor(np.concatenate([sc.stiffness for sc in scenes]), device=dev, requires_grad=True)
+    x0 = torch.tensor(np.concatenate([sc.pos_w for sc in scenes]), device=dev, requires_grad=True)
+    v0 = torch.tensor(np.concatenate([sc.vel for sc in scenes]), device=dev, requires_grad=True)
+    xT, _ = rollout(sys, st, x0, v0, 1.0 / 60.0, 8, 3)
+    (xT[:, :3] * torch.tensor(np.concatenate(cs), dtype=torch.float32, device=dev)).sum().backward()
+    m0 = len(scenes[0].pairs)
+    gs, gx, gv = st.grad.cpu().numpy(), x0.grad.cpu().numpy()[:, :3], v0.grad.cpu().numpy()[:, :3]
+    for k, sc in enumerate(scenes):
+        sl = slice(off[k], off[k] + sc.n)
+        ss = slice(0, m0) if k == 0 else slice(m0, None)
+        for a, b in ((gs[ss], alone[k][0]), (gx[sl], alone[k][1]), (gv[sl], alone[k][2])):
+            np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-5 * np.max(np.abs(b)))
+
+
+def test_backward_is_deterministic_and_restores_state():
+    sc = small_scene()
+    sys = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, sys)
+    sys.rollout(sc.dt, 7, 3)
+    end = sys.positions()
+    dev = torch.device("cuda", 0)
+    g = torch.randn((sc.n, 4), device=dev)
+    outs = []
+    for _ in range(2):
+        dx0 = torch.empty((sc.n, 4), device=dev)
+        dv0 = torch.empty((sc.n, 4), device=dev)
+        ds = torch.empty(len(sc.pairs), device=dev)
+        sys.backward_device(g.data_ptr(), None, dx0.data_ptr(), dv0.data_ptr(), ds.data_ptr())
+        torch.cuda.synchronize()
+        outs.append((dx0.cpu().numpy(), dv0.cpu().numpy(), ds.cpu().numpy()))
+        np.testing.assert_array_equal(sys.positions(), end)
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_unsupported_scenes_are_rejected():
+    sc = W.dam_break(8, 8, 4)
+    sys = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, sys)
+    with pytest.raises(PbdError) as e:
+        sys.rollout(sc.dt, 2, 1)
+    assert e.value.code == PBD_ERR_UNSUPPORTED
+    sys2 = ParticleSystem(default_params(**small_scene().params), 10)
+    with pytest.raises(PbdError):
+        sys2.backward_device(None, None, None, None, None)  # no rollout yet
