@@ -1,0 +1,97 @@
+// Headless driver of the reference's 2-D CPU solver (cpu/src/simulation.cpp,
+// built in place from the reference tree with the stand-ins of include/):
+// builds a scene of solid particles in a box and ticks it, single-threaded
+// as the reference is written.  Test infrastructure: timed CPU baseline and
+// invariant comparison for the 2-D granular column.
+//
+// The scene is assembled through Simulation's own members (access opened
+// below) instead of one of its built-in init* scenes, so that the column
+// of the benchmark (its lattice, jitter, friction and box) can be loaded.
+// Every header outside the reference tree first, so that opening access
+// below touches only the reference's own classes.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+#include <QHash>
+#include <QList>
+#include <QSet>
+#include <qgl.h>
+#include <GL/glu.h>
+#define GLM_FORCE_RADIANS
+#include <glm/vec2.hpp>
+#include <glm.hpp>
+#include <glm/gtx/rotate_vector.hpp>
+
+#define private public
+#include "simulation.h"
+#undef private
+
+#include <cstdint>
+
+extern "C" {
+
+void *refcpu_create(double xmin, double xmax, double ymin, double ymax, double gx, double gy) {
+    Simulation *s = new Simulation();  // builds the reference's default scene
+    s->clear();                        // ... which is dropped here
+    s->m_counts = nullptr;
+    s->m_xBoundaries = glm::dvec2(xmin, xmax);
+    s->m_yBoundaries = glm::dvec2(ymin, ymax);
+    s->m_gravity = glm::dvec2(gx, gy);
+    return s;
+}
+
+// n solid particles: xy, v as 2n doubles (v may be NULL), unit phase SOLID.
+void refcpu_add_particles(void *h, int n, const double *xy, const double *v, double mass, double s_friction,
+                          double k_friction) {
+    Simulation *s = static_cast<Simulation *>(h);
+    for (int i = 0; i < n; ++i) {
+        Particle *p = new Particle(glm::dvec2(xy[2 * i], xy[2 * i + 1]), mass, SOLID);
+        if (v) p->v = glm::dvec2(v[2 * i], v[2 * i + 1]);
+        p->sFriction = s_friction;
+        p->kFriction = k_friction;
+        s->m_particles.append(p);
+    }
+}
+
+// After the last add: the tail of Simulation::init (simulation.cpp:105-108).
+void refcpu_finalize(void *h) {
+    Simulation *s = static_cast<Simulation *>(h);
+    s->m_standardSolver.setupM(&s->m_particles);
+    delete[] s->m_counts;
+    s->m_counts = new int[s->m_particles.size()];
+}
+
+void refcpu_tick(void *h, double seconds, int steps) {
+    Simulation *s = static_cast<Simulation *>(h);
+    for (int k = 0; k < steps; ++k) s->tick(seconds);
+}
+
+int refcpu_num(void *h) { return static_cast<Simulation *>(h)->m_particles.size(); }
+
+// xy, v: 2n doubles each (either may be NULL).
+void refcpu_get(void *h, double *xy, double *v) {
+    Simulation *s = static_cast<Simulation *>(h);
+    for (int i = 0; i < s->m_particles.size(); ++i) {
+        const Particle *p = s->m_particles.at(i);
+        if (xy) {
+            xy[2 * i] = p->p.x;
+            xy[2 * i + 1] = p->p.y;
+        }
+        if (v) {
+            v[2 * i] = p->v.x;
+            v[2 * i + 1] = p->v.y;
+        }
+    }
+}
+
+void refcpu_destroy(void *h) { delete static_cast<Simulation *>(h); }
+
+}  // extern "C"

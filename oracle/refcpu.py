@@ -1,0 +1,82 @@
+"""ctypes wrapper of oracle/_ref/librefcpu.so: the reference's own 2-D CPU
+solver (cpu/src, built headless by oracle/ref_build.py where the reference
+tree exists).  Test infrastructure only: a timed CPU baseline and an
+invariant comparison for the 2-D granular column.  The reference's
+sources do not travel to machines without the tree, so it is absent
+there and callers skip."""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+LIB = Path(__file__).resolve().parent / "_ref" / "librefcpu.so"
+_lib = None
+
+
+def available() -> bool:
+    if not LIB.exists():
+        return False
+    try:
+        load()
+        return True
+    except OSError:
+        return False
+
+
+def load():
+    global _lib
+    if _lib is None:
+        lib = ctypes.CDLL(str(LIB))
+        D, P, I = ctypes.c_double, ctypes.c_void_p, ctypes.c_int
+        PD = ctypes.POINTER(ctypes.c_double)
+        lib.refcpu_create.argtypes = [D, D, D, D, D, D]
+        lib.refcpu_create.restype = P
+        lib.refcpu_add_particles.argtypes = [P, I, PD, PD, D, D, D]
+        lib.refcpu_finalize.argtypes = [P]
+        lib.refcpu_tick.argtypes = [P, D, I]
+        lib.refcpu_num.argtypes = [P]
+        lib.refcpu_num.restype = I
+        lib.refcpu_get.argtypes = [P, PD, PD]
+        lib.refcpu_destroy.argtypes = [P]
+        _lib = lib
+    return _lib
+
+
+class RefCPU:
+    """The reference's Simulation with a scene of solid particles (x, y);
+    particle radius fixed at 0.25 and 3 solver iterations, as compiled."""
+
+    def __init__(self, xy, v=None, mass=1.0, s_friction=0.5, k_friction=0.3, x_bounds=(-20.0, 20.0),
+                 y_bounds=(0.0, 1e6), gravity=(0.0, -9.8)):
+        self.lib = load()
+        self.h = self.lib.refcpu_create(x_bounds[0], x_bounds[1], y_bounds[0], y_bounds[1], *gravity)
+        xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+        vv = None if v is None else np.ascontiguousarray(v, np.float64).reshape(-1, 2)
+        pd = ctypes.POINTER(ctypes.c_double)
+        self.lib.refcpu_add_particles(self.h, xy.shape[0], xy.ctypes.data_as(pd),
+                                      None if vv is None else vv.ctypes.data_as(pd), mass, s_friction, k_friction)
+        self.lib.refcpu_finalize(self.h)
+
+    def tick(self, dt: float, steps: int = 1):
+        self.lib.refcpu_tick(self.h, dt, steps)
+
+    def state(self):
+        n = self.lib.refcpu_num(self.h)
+        xy = np.empty((n, 2))
+        v = np.empty((n, 2))
+        pd = ctypes.POINTER(ctypes.c_double)
+        self.lib.refcpu_get(self.h, xy.ctypes.data_as(pd), v.ctypes.data_as(pd))
+        return xy, v
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.refcpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -62,3 +62,29 @@ def rollout(system, stiffness: torch.Tensor, x0: torch.Tensor, v0: torch.Tensor,
             checkpoint_every: int = 10):
     """(x_T, v_T) after `steps` updates, differentiable in stiffness, x0, v0."""
     return _Rollout.apply(stiffness, x0, v0, system, float(dt), int(steps), int(checkpoint_every))
+
+
+def fit(system, x0: torch.Tensor, target: torch.Tensor, stiffness0: torch.Tensor, v0_init: torch.Tensor, dt: float,
+        steps: int, checkpoint_every: int, iterations: int, lr_stiffness: float = 0.05, lr_velocity: float = 0.1,
+        stiffness_range=(0.2, 1.0), callback=None):
+    """Recovers distance-constraint stiffness and initial velocities from
+    final positions: Adam on L = mean |x_T - target|^2 through rollout(),
+    stiffness projected to stiffness_range after each update.  Returns
+    (stiffness, v0, losses)."""
+    st = stiffness0.detach().clone().requires_grad_(True)
+    v0 = v0_init.detach().clone().requires_grad_(True)
+    opt = torch.optim.Adam([{"params": [st], "lr": lr_stiffness}, {"params": [v0], "lr": lr_velocity}])
+    losses = []
+    for it in range(iterations):
+        opt.zero_grad()
+        xT, _ = rollout(system, st, x0, v0, dt, steps, checkpoint_every)
+        loss = ((xT[:, :3] - target[:, :3]) ** 2).sum(1).mean()
+        loss.backward()
+        losses.append(float(loss.detach()))
+        opt.step()
+        with torch.no_grad():
+            st.clamp_(*stiffness_range)
+            v0[:, 3] = 0.0
+        if callback:
+            callback(it, losses[-1])
+    return st.detach(), v0.detach(), losses

@@ -497,3 +497,10 @@ def cloth_ropes_grains(cloth: int = 64, ropes: int = 8, rope_particles: int = 32
     return Scene("cloth_ropes_grains", params, pos_w, np.concatenate(phase), vel=vel, pairs=pairs,
                  rest=rest.astype(np.float32), stiffness=stiff, pins=pins, pin_points=pos_w[pins, :3].copy(),
                  dt=1.0 / 60.0, info=dict(cloth=cloth, ropes=ropes, grains=grains))
+
+
+def differentiation_scenes(count: int = 64, seed: int = 64, **kw) -> list:
+    """`count` cloth / rope / grain scenes (cloth_ropes_grains), each with
+    its own grain cloud and hidden per-constraint stiffness U(0.2, 1)."""
+    return [cloth_ropes_grains(seed=seed * 1000 + 10 * k, stiffness_seed=seed * 1000 + 10 * k + 7, **kw)
+            for k in range(count)]
