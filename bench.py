@@ -377,6 +377,7 @@ def run_ours(args, world, rank, local_rank):
     if not args.tpp:
         sysm.autotune(sc.dt, 2, sh)
     tpp = sysm.threads_per_particle
+    tuning = sysm.tuning()
     sysm.update_graph(sc.dt, 1, sh)
     torch.cuda.synchronize()
 
@@ -445,6 +446,7 @@ def run_ours(args, world, rank, local_rank):
         e2e_s = float(t.item())
     e2e_value = world * e2e_steps / e2e_s
     sysm.check_finite(sh)
+    reuses = sysm.list_reuses()
     batched = None
     if args.batch_scenes:
         sysm.close()
@@ -487,6 +489,9 @@ def run_ours(args, world, rank, local_rank):
                    "h": 0.1, "iterations": 4, "grid_rebuild": "every iteration", "xsph_c": 0.01,
                    "cell_size": sc.params["cell_size"], "grid": sc.params["grid_size"],
                    "threads_per_particle": tpp, "tpp_source": "fixed" if args.tpp else "autotuned",
+                   "neighbor_skin": float(tuning.neighbor_skin),
+                   "neighbor_list_capacity": int(tuning.neighbor_list_capacity),
+                   "list_reuses_last_step": reuses,
                    "dt": sc.dt, "l2": "flushed before each timed step (256 MiB write)",
                    "timing": "per-step CUDA events on the launching stream, CUDA graph replay",
                    "particle_iterations_per_s": value * n * 4,

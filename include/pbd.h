@@ -308,11 +308,25 @@ typedef struct pbd_tuning {
                                       iteration (multiple of 4, 0 = no list,
                                       default 64); particles with more fall
                                       back to the stencil walk              */
-    uint32_t reserved[6];          /* zero                                  */
+    float neighbor_skin;           /* with a list: its radius is (1 + skin) h
+                                      and it is reused by the later
+                                      iterations of a step while no particle
+                                      has moved more than 0.49 skin h since
+                                      it was built (checked on the device
+                                      each iteration; else the grid and the
+                                      list are rebuilt).  Neighbour sets stay
+                                      exact (every use filters |r| < h); only
+                                      the summation order differs.  0 = off
+                                      (grid and list rebuilt every
+                                      iteration, the reference's schedule)  */
+    uint32_t reserved[5];          /* zero                                  */
 } pbd_tuning;
 
 int pbd_set_tuning(pbd_system *sys, const pbd_tuning *tuning);
 int pbd_get_tuning(const pbd_system *sys, pbd_tuning *out);
+/* Iterations of the last step that reused a skin list (0 without one).
+ * Synchronous. */
+int pbd_list_reuses(pbd_system *sys, uint32_t *count);
 /* Times `steps` updates of the current scene for every threads_per_particle
  * choice, starting each trial from a device snapshot of the state, then
  * restores the state and keeps the fastest choice (written to *chosen if

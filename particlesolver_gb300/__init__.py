@@ -98,7 +98,7 @@ STAGES = ["predict", "grid", "lambda", "solve", "distance", "shapes", "velocity"
 
 class PbdTuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_uint32), ("neighbor_list_capacity", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 6)]
+                ("neighbor_skin", ctypes.c_float), ("reserved", ctypes.c_uint32 * 5)]
 
 
 class PbdProfile(ctypes.Structure):
@@ -188,6 +188,7 @@ _SIGNATURES = {
     "pbd_save_state": ([_P, _P, ctypes.c_uint64], _I),
     "pbd_set_distance_stiffness": ([_P, _U32, _P, _I, _P], _I),
     "pbd_rollout": ([_P, _F, _U32, _U32, _P], _I),
+    "pbd_list_reuses": ([_P, _PU], _I),
     "pbd_num_distance_constraints": ([_P], _U32),
     "pbd_backward": ([_P, _P, _P, _P, _P, _P, _P], _I),
     "pbd_load_state": ([_P, _P, ctypes.c_uint64], _I),
@@ -466,20 +467,30 @@ class ParticleSystem:
         self._check(self.lib.pbd_get_tuning(self.h, ctypes.byref(t)))
         return t
 
-    def set_tuning(self, threads_per_particle: int | None = None, neighbor_list_capacity: int | None = None):
+    def set_tuning(self, threads_per_particle: int | None = None, neighbor_list_capacity: int | None = None,
+                   neighbor_skin: float | None = None):
         t = self.tuning()
         if threads_per_particle is not None:
             t.threads_per_particle = int(threads_per_particle)
         if neighbor_list_capacity is not None:
             t.neighbor_list_capacity = int(neighbor_list_capacity)
+        if neighbor_skin is not None:
+            t.neighbor_skin = float(neighbor_skin)
         self._check(self.lib.pbd_set_tuning(self.h, ctypes.byref(t)))
+
+    def list_reuses(self) -> int:
+        """Iterations of the last step that reused a skin list."""
+        c = ctypes.c_uint32()
+        self._check(self.lib.pbd_list_reuses(self.h, ctypes.byref(c)))
+        return c.value
 
     def set_threads_per_particle(self, tpp: int):
         self.set_tuning(threads_per_particle=tpp)
 
     def autotune(self, dt: float, steps: int = 2, stream: int | None = None) -> int:
-        """Pick the fastest lanes-per-particle for the current scene (state
-        is restored afterwards); returns the choice."""
+        """Pick the fastest launch shape / list schedule (lanes per
+        particle, skin) for the current scene (state is restored
+        afterwards); returns the lanes per particle chosen."""
         t = PbdTuning()
         self._check(self.lib.pbd_autotune(self.h, dt, steps, stream, ctypes.byref(t)))
         return int(t.threads_per_particle)

@@ -65,7 +65,7 @@ def rollout(system, stiffness: torch.Tensor, x0: torch.Tensor, v0: torch.Tensor,
 
 
 def fit(system, x0: torch.Tensor, target: torch.Tensor, stiffness0: torch.Tensor, v0_init: torch.Tensor, dt: float,
-        steps: int, checkpoint_every: int, iterations: int, lr_stiffness: float = 0.05, lr_velocity: float = 0.1,
+        steps: int, checkpoint_every: int, iterations: int, lr_stiffness: float = 0.01, lr_velocity: float = 0.01,
         stiffness_range=(0.2, 1.0), callback=None):
     """Recovers distance-constraint stiffness and initial velocities from
     final positions: Adam on L = mean |x_T - target|^2 through rollout(),

@@ -7,6 +7,7 @@
 #include "pbd_kernels.h"
 
 #include <cfloat>
+#include <cmath>
 
 namespace pbd {
 
@@ -62,9 +63,10 @@ __global__ void __launch_bounds__(kBlock) k_hash_count(DevParams P0, uint32_t n,
                                                        const float4 *__restrict__ x,
                                                        uint32_t *__restrict__ hash,
                                                        uint32_t *__restrict__ slot,
-                                                       uint32_t *__restrict__ counts) {
+                                                       uint32_t *__restrict__ counts,
+                                                       const uint32_t *__restrict__ skip) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (skip && *skip)) return;
     const DevParams P = scene_params<B>(P0, i);
     const uint32_t h = grid_hash(P, grid_pos(P, f3(x[i])));
     hash[i] = h;
@@ -107,7 +109,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__restrict__ data,
                                                               uint32_t elements,
-                                                              uint32_t *__restrict__ partials) {
+                                                              uint32_t *__restrict__ partials,
+                                                              const uint32_t *__restrict__ skip) {
+    if (skip && *skip) return;
     __shared__ uint32_t smem[32];
     const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t s = 0;
@@ -120,7 +124,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t *__restrict__ partials,
-                                                                uint32_t count) {
+                                                                uint32_t count,
+                                                                const uint32_t *__restrict__ skip) {
+    if (skip && *skip) return;
     __shared__ uint32_t smem[32];
     uint32_t carry = 0;
     for (uint32_t chunk = 0; chunk < count; chunk += kScanTile) {
@@ -144,7 +150,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t *__rest
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint32_t *__restrict__ data,
                                                              uint32_t elements,
-                                                             const uint32_t *__restrict__ partials) {
+                                                             const uint32_t *__restrict__ partials,
+                                                             const uint32_t *__restrict__ skip) {
+    if (skip && *skip) return;
     __shared__ uint32_t smem[32];
     const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems], s = 0;
@@ -167,9 +175,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint32_t *__restric
 __global__ void __launch_bounds__(kBlock) k_bucket(uint32_t n, const uint32_t *__restrict__ hash,
                                                    const uint32_t *__restrict__ slot,
                                                    const uint32_t *__restrict__ cell_first,
-                                                   uint32_t *__restrict__ tmp) {
+                                                   uint32_t *__restrict__ tmp, const uint32_t *__restrict__ skip) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (skip && *skip)) return;
     tmp[cell_first[hash[i]] + slot[i]] = i;
 }
 
@@ -189,9 +197,10 @@ __global__ void __launch_bounds__(kBlock) k_rank_reorder(uint32_t n, const uint3
                                                          const float *__restrict__ rho0,
                                                          uint32_t *__restrict__ sorted_idx,
                                                          float4 *__restrict__ sorted_x,
-                                                         SortedAttr *__restrict__ sorted_attr) {
+                                                         SortedAttr *__restrict__ sorted_attr,
+                                                         const uint32_t *__restrict__ skip) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (skip && *skip)) return;
     const uint32_t h = hash[i];
     const uint32_t b = cell_first[h], e = cell_first[h + 1];
     uint32_t rank = 0;
@@ -238,6 +247,48 @@ __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uin
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     sorted_x[i] = x[sorted_idx[i]];
+}
+
+// Cell counts cleared (the memset of a grid build), unless *skip.
+__global__ void __launch_bounds__(kBlock) k_clear_counts(uint32_t elements, uint32_t *__restrict__ counts,
+                                                         const uint32_t *__restrict__ skip) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= elements || *skip) return;
+    counts[c] = 0u;
+}
+
+// Skin-list check: the sorted positions refreshed from x in the sorted
+// order of the list's grid, and the largest |x - x_at_build| / h over all
+// particles into words[2 + iter] (non-negative floats order like their
+// bit patterns, so an integer max).
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_skin_check(DevParams P0, uint32_t n, const uint32_t *__restrict__ sidx,
+                                                       const float4 *__restrict__ x,
+                                                       const float4 *__restrict__ sref,
+                                                       float4 *__restrict__ sorted_x, uint32_t *__restrict__ word) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d = 0.f;
+    if (i < n) {
+        const float4 p = x[sidx[i]];
+        sorted_x[i] = p;
+        const float4 r = sref[i];
+        const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
+        d = sqrtf(dx * dx + dy * dy + dz * dz) / scene_params<B>(P0, i).h;
+        if (!(d <= 3.0e38f)) d = 3.0e38f;  // NaN or inf: never reuse
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(word, __float_as_uint(d));
+}
+
+// One thread: reuse the list this iteration iff every particle stayed
+// within 0.49 skin h of where it was when the list was built and no list
+// overflowed; otherwise clear the overflow mark for the rebuild.
+__global__ void k_skin_decide(uint32_t *__restrict__ words, uint32_t iter, float limit) {
+    const bool reuse = __uint_as_float(words[2 + iter]) <= limit && words[1] == 0u;
+    words[0] = reuse ? 1u : 0u;
+    if (!reuse) words[1] = 0u;
+    else words[kSkinWords - 1] += 1u;  // reuses in this step
 }
 
 // -------------------------------------------------------- group walking
@@ -641,10 +692,10 @@ __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uin
 // order and the same exactness conditions as stencil_ranges; a slab with a
 // wrapping row is walked row by row, cell by cell where it wraps.
 template <int RAD, class F>
-__device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 q, int3 g, float reach2, bool trim,
-                                                     const uint32_t *__restrict__ cell_first, F &&f) {
+__device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 q, int3 g, int rad, float reach2,
+                                                     bool trim, const uint32_t *__restrict__ cell_first, F &&f) {
     if (RAD == 0) {
-        stencil_ranges(P, q, g, P.fluid_rad, reach2, trim, cell_first, f);
+        stencil_ranges(P, q, g, rad, reach2, trim, cell_first, f);
         return;
     }
     constexpr int W = 2 * RAD + 1;
@@ -725,12 +776,23 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
     }
 }
 
+// Stencil radius and trimming of a list build: the list radius is
+// (1 + skin) h (h without a skin).
+__device__ __forceinline__ int list_rad(const DevParams &P, float skin) {
+    if (skin <= 0.f) return P.fluid_rad;
+    return (int)ceilf(P.h * (1.f + skin) / P.cell * 1.000001f);
+}
+
 // findLambdasD (integration_kernel.cuh:481-593) with the list build: the
-// walk records the neighbours (|r|^2 < h^2, any phase, visiting order) and
-// lambda is summed over the list.  The candidate loop is branch-free: the
-// neighbour test drives predicated register inserts and a predicated
-// 16-byte store per four neighbours.  Output as k_lambda.
-template <int RAD, bool B>
+// walk records the neighbours (|r| below the list radius, any phase,
+// visiting order) and lambda is summed over the listed particles closer
+// than h.  The candidate loop is branch-free: the neighbour test drives
+// predicated register inserts and a predicated 16-byte store per four
+// neighbours.  SKIN: the list has a skin (radius (1 + skin) h, build
+// positions kept in L.sref), and when it is reused (*L.reuse) there is no
+// walk: the old list is filtered at the refreshed positions.  Output as
+// k_lambda.
+template <int RAD, bool B, bool SKIN>
 __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_t n, uint32_t iter_left,
                                                         const float4 *__restrict__ sx,
                                                         const SortedAttr *__restrict__ sattr,
@@ -739,38 +801,21 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DevParams P = scene_params<B>(P0, i);
-    if (!scene_active<B>(P, iter_left)) return;
+    const bool reuse = SKIN && L.reuse && *L.reuse;
+    // A scene sitting out this iteration needs nothing -- except when a skin
+    // list is built: every scene's list must exist for the later
+    // iterations that reuse it.
+    if (!scene_active<B>(P, iter_left) && (reuse || !SKIN)) return;
     const SortedAttr a = sattr[i];
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
+    if (SKIN && !reuse) L.sref[i] = pi4;
     if (a.phase != kFluid) {
         sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
-        L.count[i] = 0u;
+        if (!reuse) L.count[i] = 0u;
         return;
     }
-    const int3 g = grid_pos(P, pi);
-    uint32_t cnt = 0;
-    uint4 pend = make_uint4(0u, 0u, 0u, 0u);
-    uint4 *const row_base = L.slot + i;
-    const uint32_t cap = L.capacity;
     const float h2 = P.h2;
-    stencil_ranges_fixed<RAD>(P, pi, g, h2, P.trim_fluid, cell_first, [&](uint32_t b, uint32_t e) {
-#pragma unroll 2
-        for (uint32_t j = b; j < e; ++j) {
-            const float4 q = __ldg(sx + j);
-            const bool ok = dist2_exact(pi, f3(q)) < h2 && j != i;
-            const uint32_t s4 = cnt & 3u;
-            pend.x = (ok && s4 == 0u) ? j : pend.x;
-            pend.y = (ok && s4 == 1u) ? j : pend.y;
-            pend.z = (ok && s4 == 2u) ? j : pend.z;
-            pend.w = (ok && s4 == 3u) ? j : pend.w;
-            if (ok && s4 == 3u && cnt < cap) row_base[(cnt >> 2) * L.stride] = pend;
-            cnt += ok ? 1u : 0u;
-        }
-        return true;
-    });
-    if (cnt < cap && (cnt & 3u)) row_base[(cnt >> 2) * L.stride] = pend;
-    L.count[i] = cnt;
     const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
     const float inv_w = 1.f / pi4.w;
     const float inv_rho0 = 1.f / a.rho0;
@@ -780,17 +825,65 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
         const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
         acc.add(P, true, d2, pi - f3(pj), mf, spiky_r);
     };
-    if (list_usable(P, L, cnt)) {
-        for_each_listed(L, i, cnt, [&](uint32_t j) {
+    if (reuse) {
+        for_each_listed(L, i, L.count[i], [&](uint32_t j) {
             const float4 pj = __ldg(sx + j);
-            add(pj, dist2_exact(pi, f3(pj)));
+            const float d2 = dist2_exact(pi, f3(pj));
+            if (d2 < h2) add(pj, d2);
         });
     } else {
-        const Group<1> G;
-        group_walk<1>(
-            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
-            [&](uint32_t, const float4 &pj, float d2) { add(pj, d2); });
+        const int3 g = grid_pos(P, pi);
+        uint32_t cnt = 0;
+        uint4 pend = make_uint4(0u, 0u, 0u, 0u);
+        uint4 *const row_base = L.slot + i;
+        const uint32_t cap = L.capacity;
+        int rad = P.fluid_rad;
+        float reach2 = h2;
+        bool trim = P.trim_fluid;
+        if (SKIN) {
+            const int r = list_rad(P, L.skin);
+            if ((uint32_t)(2 * r + 1) <= min(P.gx, min(P.gy, P.gz))) {
+                const float lr = P.h * (1.f + L.skin);
+                rad = r;
+                reach2 = lr * lr;
+                trim = true;
+            } else {
+                // the skin's stencil would alias on this grid (cells seen
+                // twice): a plain list, and no reuse this step
+                atomicOr(L.ovf, 1u);
+            }
+        }
+        stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
+#pragma unroll 2
+            for (uint32_t j = b; j < e; ++j) {
+                const float4 q = __ldg(sx + j);
+                const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
+                const uint32_t s4 = cnt & 3u;
+                pend.x = (ok && s4 == 0u) ? j : pend.x;
+                pend.y = (ok && s4 == 1u) ? j : pend.y;
+                pend.z = (ok && s4 == 2u) ? j : pend.z;
+                pend.w = (ok && s4 == 3u) ? j : pend.w;
+                if (ok && s4 == 3u && cnt < cap) row_base[(cnt >> 2) * L.stride] = pend;
+                cnt += ok ? 1u : 0u;
+            }
+            return true;
+        });
+        if (cnt < cap && (cnt & 3u)) row_base[(cnt >> 2) * L.stride] = pend;
+        L.count[i] = cnt;
+        if (list_usable(P, L, cnt)) {
+            for_each_listed(L, i, cnt, [&](uint32_t j) {
+                const float4 pj = __ldg(sx + j);
+                const float d2 = dist2_exact(pi, f3(pj));
+                if (!SKIN || d2 < h2) add(pj, d2);
+            });
+        } else {
+            if (SKIN) atomicOr(L.ovf, 1u);  // this list cannot be reused
+            const Group<1> G;
+            group_walk<1>(
+                P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+                [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+                [&](uint32_t, const float4 &pj, float d2) { add(pj, d2); });
+        }
     }
     const float ro = acc.ro + P.poly6_self * inv_w;
     const float denom = acc.denom + dot3(acc.grad, acc.grad);
@@ -808,12 +901,18 @@ __device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t 
     }
     const float lam_i = sxl[i].w;
     const float poly6_ref = P.poly6 * P.scorr_inv_ref;
+    const float h2 = P.h2;
     float3 delta = make_float3(0.f, 0.f, 0.f);
+    uint32_t nb = 0;
     for_each_listed(L, i, cnt, [&](uint32_t j) {
         const float4 pl = sxl[j];
-        delta_add(P, delta, true, dist2_exact(pi, f3(pl)), pi - f3(pl), lam_i + pl.w, poly6_ref);
+        const float d2 = dist2_exact(pi, f3(pl));
+        if (d2 < h2) {  // all of a plain list; a skin list holds more
+            delta_add(P, delta, true, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
+            ++nb;
+        }
     });
-    const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)cnt;
+    const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
     return delta / div;
 }
 
@@ -1176,7 +1275,8 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
         for_each_listed(L, i, cnt, [&](uint32_t j) {
             if (sattr[j].phase != kFluid) return;
             const float4 xj4 = sx[j];
-            add(j, xj4, dist2_exact(xi, f3(xj4)));
+            const float d2 = dist2_exact(xi, f3(xj4));
+            if (d2 < P.h2) add(j, xj4, d2);
         });
     } else {
         group_walk<TPP>(
@@ -1223,28 +1323,51 @@ cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, 
 cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash,
                               uint32_t *slot, uint32_t *counts, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (P.table) k_hash_count<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts);
-    else k_hash_count<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts);
+    if (P.table) k_hash_count<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, nullptr);
+    else k_hash_count<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_begin(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash, uint32_t *slot,
+                              uint32_t *counts, const uint32_t *skip, cudaStream_t s) {
+    const uint32_t elements = P.num_cells + 1u;
+    k_clear_counts<<<blocks_for(elements), kBlock, 0, s>>>(elements, counts, skip);
+    if (n) {
+        if (P.table) k_hash_count<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, skip);
+        else k_hash_count<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, skip);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_skin_check(const DevParams &P, uint32_t n, uint32_t iter, float skin, const GridBuffers &g,
+                              const float4 *x, const float4 *sref, uint32_t *words, cudaStream_t s) {
+    if (n) {
+        if (P.table)
+            k_skin_check<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_idx, x, sref, g.sorted_x, words + 2 + iter);
+        else
+            k_skin_check<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, g.sorted_idx, x, sref, g.sorted_x, words + 2 + iter);
+    }
+    k_skin_decide<<<1, 1, 0, s>>>(words, iter, 0.49f * skin);
     return cudaGetLastError();
 }
 
 cudaError_t launch_exclusive_scan(uint32_t *data, uint32_t elements, uint32_t *partials,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, const uint32_t *skip) {
     const uint32_t tiles = (uint32_t)scan_partial_count(elements);
-    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(data, elements, partials);
-    k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, tiles);
-    k_scan_apply<<<tiles, kScanThreads, 0, s>>>(data, elements, partials);
+    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(data, elements, partials, skip);
+    k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, tiles, skip);
+    k_scan_apply<<<tiles, kScanThreads, 0, s>>>(data, elements, partials, skip);
     return cudaGetLastError();
 }
 
 cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers &g,
                                const float4 *x, const int *phase, const float *rho0,
-                               cudaStream_t s) {
-    cudaError_t e = launch_exclusive_scan(g.cell_first, P.num_cells + 1u, g.scan_part, s);
+                               cudaStream_t s, const uint32_t *skip) {
+    cudaError_t e = launch_exclusive_scan(g.cell_first, P.num_cells + 1u, g.scan_part, s, skip);
     if (e != cudaSuccess || n == 0) return e;
-    k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.slot, g.cell_first, g.tmp);
+    k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.slot, g.cell_first, g.tmp, skip);
     k_rank_reorder<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.cell_first, g.tmp, x, phase, rho0,
-                                                    g.sorted_idx, g.sorted_x, g.sorted_attr);
+                                                    g.sorted_idx, g.sorted_x, g.sorted_attr, skip);
     return cudaGetLastError();
 }
 
@@ -1256,7 +1379,7 @@ cudaError_t launch_sort_into_cells(const DevParams &P, uint32_t n, const float4 
     if ((e = launch_hash_count(P, n, x, hash, slot, cell_first, s)) != cudaSuccess) return e;
     if ((e = launch_exclusive_scan(cell_first, P.num_cells + 1u, partials, s)) != cudaSuccess) return e;
     if (n) {
-        k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, hash, slot, cell_first, tmp);
+        k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, hash, slot, cell_first, tmp, nullptr);
         k_rank_only<<<blocks_for(n), kBlock, 0, s>>>(n, hash, cell_first, tmp, sorted_idx);
     }
     k_cell_ranges<<<blocks_for(P.num_cells), kBlock, 0, s>>>(P.num_cells, cell_first, cell_start, cell_end);
@@ -1285,12 +1408,26 @@ template <bool B>
 void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
                           const NbList &L, cudaStream_t s) {
     const unsigned nb = blocks_for(n);
-    if (P.fluid_rad == 1)
-        k_lambda_list<1, B><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
-    else if (P.fluid_rad == 2)
-        k_lambda_list<2, B><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
-    else
-        k_lambda_list<0, B><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L);
+    // the list radius's stencil; a batch whose fluid scenes differ, and any
+    // batch with a skin, runs the runtime-radius walk (rad 0)
+    int rad = P.fluid_rad;
+    if (L.sref) {
+        // (the same single-precision expression as list_rad on the device;
+        // the host enables a skin only where its stencil does not alias)
+        rad = P.table ? 0 : (int)std::ceil(P.h * (1.f + L.skin) / P.cell * 1.000001f);
+    }
+#define PBD_LIST(R, S) \
+    k_lambda_list<R, B, S><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L)
+    if (L.sref) {
+        if (rad == 1) PBD_LIST(1, true);
+        else if (rad == 2) PBD_LIST(2, true);
+        else PBD_LIST(0, true);
+    } else {
+        if (rad == 1) PBD_LIST(1, false);
+        else if (rad == 2) PBD_LIST(2, false);
+        else PBD_LIST(0, false);
+    }
+#undef PBD_LIST
 }
 
 cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,

@@ -29,7 +29,21 @@ struct NbList {
     uint32_t *count;    // [stride] neighbours found (may exceed capacity)
     uint32_t capacity;  // neighbours per particle, a multiple of 4
     uint32_t stride;    // particles per slot row
+    // Skin lists (reused by later iterations; all null / 0 when off): the
+    // list radius is (1 + skin) h; sref holds the sorted positions it was
+    // built from; *reuse (set on the device each iteration) selects
+    // filtering the old list over a new walk; *ovf records a list that
+    // could not be kept (over capacity or the neighbour cap).
+    float skin;
+    float4 *sref;
+    const uint32_t *reuse;
+    uint32_t *ovf;
 };
+
+// Device words of the skin-list schedule: [0] reuse, [1] overflow, [2 + k]
+// largest displacement / h since the list build, seen in iteration k (k <
+// kSkinWords - 3), [kSkinWords - 1] iterations of the step that reused.
+constexpr uint32_t kSkinWords = 64;
 
 struct ConstraintBuffers {
     uint32_t count;        // constrained particles
@@ -67,10 +81,21 @@ cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, u
                               uint32_t *slot, uint32_t *counts, cudaStream_t s);
 // counts[0..cells] -> exclusive offsets; counts[cells] must be zero on entry.
 cudaError_t launch_exclusive_scan(uint32_t *data, uint32_t elements, uint32_t *partials,
-                                  cudaStream_t s);
+                                  cudaStream_t s, const uint32_t *skip = nullptr);
+// skip: device word; when nonzero the kernels return at once (a reused
+// skin list keeps the previous grid).  nullptr = always run.
 cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers &g,
                                const float4 *x, const int *phase, const float *rho0,
-                               cudaStream_t s);
+                               cudaStream_t s, const uint32_t *skip = nullptr);
+// The grid build of a later iteration under the skin-list schedule: clear
+// the counts, hash and count -- each skipped when *skip is set.
+cudaError_t launch_grid_begin(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash, uint32_t *slot,
+                              uint32_t *counts, const uint32_t *skip, cudaStream_t s);
+// Skin-list check of iteration `iter`: refreshes the sorted positions from
+// x and records the largest displacement / h since the list build in
+// words[2 + iter]; then decides words[0] (reuse) from it and words[1].
+cudaError_t launch_skin_check(const DevParams &P, uint32_t n, uint32_t iter, float skin, const GridBuffers &g,
+                              const float4 *x, const float4 *sref, uint32_t *words, cudaStream_t s);
 // The whole grid build into caller buffers: cell hashes, counting sort in
 // (hash, index) order, and the reference's cellStart / cellEnd layout.
 // hash, slot, tmp: [n]; cell_first: [cells + 1]; partials:

@@ -161,6 +161,14 @@ void free_list(pbd_system *s) {
     s->list_valid = false;
 }
 
+// Buffers of the skin-list schedule, once fluid and a skin are both there.
+int alloc_skin(pbd_system *s) {
+    if (!(s->skin > 0.f) || !s->n_fluid) return PBD_OK;
+    if (!s->sref) CUDA_TRY(s, dalloc(&s->sref, s->cap));
+    if (!s->skin_words) CUDA_TRY(s, dalloc(&s->skin_words, pbd::kSkinWords));
+    return PBD_OK;
+}
+
 void drop_graph(pbd_system *s) {
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->graph_exec = nullptr;
@@ -475,17 +483,45 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     const uint32_t dist_kernels =
         s->cons.count ? (s->cons.any_distance ? 2u : (s->cons.any_pin ? 1u : 0u)) : 0u;
     const uint32_t iters = P.iterations;
+    // skin lists: built at the first iteration, reused by later ones while
+    // the device check allows (the grid kernels then return at once)
+    bool skin = s->skin > 0.f && s->tpp == 1 && s->nbl.slot && s->sref && s->skin_words && s->n_fluid &&
+                iters > 1;
+    if (skin && !P.table) {
+        // the skin's stencil must not alias on the grid (a batch checks per
+        // scene on the device)
+        const int r = (int)std::ceil(P.h * (1.f + s->skin) / P.cell * 1.000001f);
+        skin = (uint32_t)(2 * r + 1) <= std::min(P.gx, std::min(P.gy, P.gz));
+    }
+    pbd::NbList L = s->nbl;
+    if (skin) {
+        L.skin = s->skin;
+        L.sref = s->sref;
+        L.ovf = s->skin_words + 1;
+        CUDA_TRY(s, cudaMemsetAsync(s->skin_words, 0, pbd::kSkinWords * sizeof(uint32_t), st));
+    }
     for (uint32_t it = 0; it < iters; ++it) {
         const uint32_t left = iters - 1u - it;
-        if (int rc = build_grid(s, st, it == 0)) return rc;
+        if (skin && it > 0 && it + 3u < pbd::kSkinWords) {
+            Stage t(s, st, PBD_STAGE_GRID, 2u + 1u + (n ? 6u : 3u));
+            CUDA_TRY(s, pbd::launch_skin_check(P, n, it, s->skin, s->grid, s->x, s->sref, s->skin_words, st));
+            CUDA_TRY(s, pbd::launch_grid_begin(P, n, s->x, s->grid.hash, s->grid.slot, s->grid.cell_first,
+                                               s->skin_words, st));
+            CUDA_TRY(s, pbd::launch_grid_finish(P, n, s->grid, s->x, s->phase, s->rho0, st, s->skin_words));
+            s->grid_valid = true;
+            L.reuse = s->skin_words;
+        } else {
+            if (int rc = build_grid(s, st, it == 0)) return rc;
+            L.reuse = nullptr;
+        }
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
-            CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, s->nbl, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, L, s->tpp, st));
             s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
         }
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
-            CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, s->nbl,
+            CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, L,
                                           s->list_valid, s->tpp, st));
         }
         if (dist_kernels) {
@@ -503,7 +539,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
     }
     if (any_xsph(s)) {
         Stage t(s, st, PBD_STAGE_XSPH, 2);
-        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, s->nbl, s->list_valid, s->tpp, st));
+        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, L, s->list_valid, s->tpp, st));
     }
     ++s->steps;
     return PBD_OK;
@@ -645,6 +681,8 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->rho0);
     dfree(s->sxl);
     free_list(s);
+    dfree(s->sref);
+    dfree(s->skin_words);
     dfree(s->vs);
     dfree(s->flag);
     dfree(s->grid.hash);
@@ -818,6 +856,7 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
         s->nbl.capacity = s->list_capacity;
         s->nbl.stride = s->cap;
     }
+    if (int rc = alloc_skin(s)) return rc;
     s->grid_valid = false;
     ++s->version;
     if (first_index) *first_index = off;
@@ -1018,7 +1057,11 @@ int pbd_set_tuning(pbd_system *s, const pbd_tuning *t) {
     const uint32_t cap = t->neighbor_list_capacity;
     if (cap % 4u || cap > 1024u)
         return fail(s, PBD_ERR_INVALID_ARGUMENT, "neighbor_list_capacity must be a multiple of 4, at most 1024");
+    if (!(t->neighbor_skin >= 0.f && t->neighbor_skin <= 1.f))
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "neighbor_skin must be in [0, 1]");
     s->tpp = k;
+    s->skin = t->neighbor_skin;
+    if (int rc = alloc_skin(s)) return rc;
     if (cap != s->list_capacity) {
         free_list(s);
         s->list_capacity = cap;
@@ -1039,6 +1082,7 @@ int pbd_get_tuning(const pbd_system *s, pbd_tuning *out) {
     std::memset(out, 0, sizeof *out);
     out->threads_per_particle = s->tpp;
     out->neighbor_list_capacity = s->list_capacity;
+    out->neighbor_skin = s->skin;
     return PBD_OK;
 }
 
@@ -1075,19 +1119,37 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
                                 nb * sizeof(float4), cudaMemcpyDeviceToDevice, st);
         return e;
     };
+    // candidates: one lane per particle with neighbour lists rebuilt every
+    // iteration or kept with a skin of 0.1, 0.2, 0.3 h (list capacity grown
+    // with the list volume), and the lane groups
+    pbd_tuning base{};
+    pbd_get_tuning(s, &base);
+    const uint32_t cap0 = base.neighbor_list_capacity ? base.neighbor_list_capacity : 64u;
+    std::vector<pbd_tuning> cands;
+    auto cand = [&](uint32_t tpp, float skin) {
+        pbd_tuning t{};
+        t.threads_per_particle = tpp;
+        t.neighbor_skin = skin;
+        const double grow = std::pow(1.0 + (double)skin, 3.0);
+        t.neighbor_list_capacity = std::min<uint32_t>(1024u, 4u * (uint32_t)std::ceil(cap0 * grow / 4.0));
+        cands.push_back(t);
+    };
+    cand(1, 0.f);
+    if (s->n_fluid && s->dev.iterations > 1 && base.neighbor_list_capacity)
+        for (float f : {0.1f, 0.2f, 0.3f}) cand(1, f);
+    for (uint32_t k : {2u, 4u, 8u, 16u, 32u}) cand(k, 0.f);
     cudaEvent_t a = nullptr, b = nullptr;
     int rc = PBD_OK;
-    const uint32_t saved_tpp = s->tpp;
     const bool saved_prof = s->profiling;
     s->profiling = false;
-    uint32_t best = saved_tpp;
+    pbd_tuning best = base;
     float best_ms = 0.f;
+    bool have = false;
     if (copy(true) != cudaSuccess || cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
         rc = fail(s, PBD_ERR_CUDA, "autotune: setup failed");
     }
-    const uint32_t choices[] = {1, 2, 4, 8, 16, 32};
-    for (uint32_t k = 0; rc == PBD_OK && k < 6; ++k) {
-        s->tpp = choices[k];
+    for (size_t k = 0; rc == PBD_OK && k < cands.size(); ++k) {
+        if ((rc = pbd_set_tuning(s, &cands[k])) != PBD_OK) break;
         if (copy(false) != cudaSuccess || (rc = enqueue_update(s, dt, st)) != PBD_OK) break;  // untimed warm-up
         if (copy(false) != cudaSuccess) break;
         cudaEventRecord(a, st);
@@ -1098,9 +1160,10 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
             if (!rc) rc = fail(s, PBD_ERR_CUDA, "autotune: timing failed");
             break;
         }
-        if (k == 0 || ms < best_ms) {
+        if (!have || ms < best_ms) {
             best_ms = ms;
-            best = choices[k];
+            best = cands[k];
+            have = true;
         }
     }
     if (copy(false) != cudaSuccess && !rc) rc = fail(s, PBD_ERR_CUDA, "autotune: restore failed");
@@ -1109,11 +1172,22 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     if (b) cudaEventDestroy(b);
     release();
     s->profiling = saved_prof;
-    s->tpp = rc ? saved_tpp : best;
+    const int rc2 = pbd_set_tuning(s, rc ? &base : &best);
+    if (!rc) rc = rc2;
     s->grid_valid = false;
     ++s->version;
     if (chosen) pbd_get_tuning(s, chosen);
     return rc;
+}
+
+int pbd_list_reuses(pbd_system *s, uint32_t *count) {
+    SYS_GUARD(s);
+    if (!count) return fail(s, PBD_ERR_INVALID_ARGUMENT, "count is NULL");
+    *count = 0;
+    if (!s->skin_words) return PBD_OK;
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    CUDA_TRY(s, cudaMemcpy(count, s->skin_words + pbd::kSkinWords - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return PBD_OK;
 }
 
 int pbd_set_profiling(pbd_system *s, int enable) {

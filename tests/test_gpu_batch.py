@@ -141,3 +141,22 @@ def test_batch_scene_params_can_change():
     alone = load_alone(sc)
     alone.update(1.0 / 60.0)
     assert_same_state(batch.positions()[firsts[1]:], alone.positions(), "pbf block with 2 iterations")
+
+
+def test_batch_with_skin_lists_matches_oracle():
+    scenes = mixed_batch()
+    batch, firsts = load_batch(scenes)
+    batch.set_tuning(neighbor_skin=0.2, neighbor_list_capacity=128)
+    for _ in range(5):
+        batch.update(1.0 / 60.0)
+    pos = batch.positions()
+    for k, sc in enumerate(scenes):
+        o = Oracle(default_params(**sc.params), sc.n)
+        W.apply_to(sc, o)
+        for _ in range(5):
+            o.update(1.0 / 60.0)
+        mine = pos[firsts[k]:firsts[k] + sc.n]
+        if sc.name == "granular_column":
+            check_granular(mine, o.positions(), 1e-3)
+        else:
+            check_trajectory(mine, o.positions(), sc.pos_w)
