@@ -180,17 +180,80 @@ __device__ __forceinline__ void for_each_contact(const DevParams &P, uint32_t i,
     });
 }
 
-// Forward of the fused pass for sorted particle i: u = x_i + sum of its
-// contact terms (phases >= CLOTH), then walls.  The adjoint of u from the
-// adjoint gy of the written position, and the walls' part of the adjoint
-// of x_old; stores u's adjoint and i's contact count for the gather.
+// Walks the fluid neighbours of sorted particle i (|r| < h, any phase) in
+// the reference's visiting order, capped at max_nb as the forward pass:
+// f(j) for each.  Returns the count.
+template <class F>
+__device__ __forceinline__ uint32_t for_each_fluid_nb(const DevParams &P, uint32_t i, float3 pi,
+                                                      const float4 *__restrict__ sx,
+                                                      const uint32_t *__restrict__ cell_first, F &&f) {
+    uint32_t nb = 0;
+    for_each_candidate(P, grid_pos(P, pi), P.fluid_rad, cell_first, [&](uint32_t j) {
+        const float d2 = dist2_exact(pi, f3(sx[j]));
+        if (!(d2 < P.h2) || j == i) return true;
+        if (nb >= P.max_nb) return false;
+        ++nb;
+        f(j);
+        return true;
+    });
+    return nb;
+}
+
+__device__ __forceinline__ float mass_factor(const DevParams &P, float inv_wi, float wj) {
+    return (P.flags & kFlagDensityNeighborMass) ? ((wj > 0.f) ? 1.f / wj : 0.f) : inv_wi;
+}
+
+// The lambda pass recomputed for sorted fluid particle i, keeping its sums
+// for the adjoint: fl1 = (sum of neighbour density terms, sum |sg|^2,
+// lambda, neighbour count), fl2 = (grad = -sum sg, divisor of the delta
+// pass).  Other particles: lambda 0.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_fluid_lambda(DevParams P0, uint32_t n, const float4 *__restrict__ sx,
+                                                             const SortedAttr *__restrict__ sattr,
+                                                             const uint32_t *__restrict__ cell_first,
+                                                             float4 *__restrict__ fl1, float4 *__restrict__ fl2) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    const SortedAttr a = sattr[i];
+    if (a.phase != kFluid) {
+        fl1[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        fl2[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+        return;
+    }
+    const float4 pi4 = sx[i];
+    const float3 pi = f3(pi4);
+    const float inv_w = 1.f / pi4.w, inv_rho0 = 1.f / a.rho0;
+    const float spiky_r = -P.spiky * inv_rho0;
+    float ro = 0.f, denom = 0.f;
+    V3<float> grad{0.f, 0.f, 0.f};
+    const uint32_t nb = for_each_fluid_nb(P, i, pi, sx, cell_first, [&](uint32_t j) {
+        const float4 pj4 = sx[j];
+        const LambdaTerm<float> t = lambda_term<float>(P, lift<float>(pi), lift<float>(f3(pj4)),
+                                                       mass_factor(P, inv_w, pj4.w), spiky_r);
+        ro += t.ro;
+        denom += gdot(t.sg, t.sg);
+        grad = grad - t.sg;
+    });
+    const float lam = lambda_of<float>(P, ro, denom, grad, inv_w, inv_rho0);
+    const float div = (P.flags & kFlagDeltaOverRho0) ? a.rho0 : a.rho0 + (float)nb;
+    fl1[i] = make_float4(ro, denom, lam, (float)nb);
+    fl2[i] = make_float4(grad.x, grad.y, grad.z, div);
+}
+
+// Forward of the fused pass for sorted particle i: u = x_i + its fluid
+// delta (fluid) or its contact terms (phases >= CLOTH), then walls.  The
+// adjoint of u from the adjoint gy of the written position, and the walls'
+// part of the adjoint of x_old; stores u's adjoint and i's contact count.
 template <bool B>
 __global__ void __launch_bounds__(kBlock) k_adj_solve_prep(DevParams P0, uint32_t n, uint32_t iter_left,
-                                                           bool contacts, const float4 *__restrict__ sx,
+                                                           bool contacts, bool fluids, const float4 *__restrict__ sx,
                                                            const SortedAttr *__restrict__ sattr,
                                                            const uint32_t *__restrict__ sidx,
                                                            const uint32_t *__restrict__ cell_first,
                                                            const float4 *__restrict__ x_old,
+                                                           const float4 *__restrict__ fl1,
+                                                           const float4 *__restrict__ fl2,
                                                            const float4 *__restrict__ gy,
                                                            float4 *__restrict__ gu, uint32_t *__restrict__ cnt,
                                                            float4 *__restrict__ gxo) {
@@ -210,7 +273,15 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_prep(DevParams P0, uint32_
     const float3 prev = f3(x_old[orig]);
     float3 u = pi;
     uint32_t nb = 0;
-    if (contacts && phi >= kCloth) {
+    if (fluids && phi == kFluid) {
+        const float lam_i = fl1[i].z, div = fl2[i].w;
+        const float poly6_ref = P.poly6 * P.scorr_inv_ref;
+        V3<float> acc{0.f, 0.f, 0.f};
+        for_each_fluid_nb(P, i, pi, sx, cell_first, [&](uint32_t j) {
+            acc = acc + delta_term<float>(P, lift<float>(pi), lift<float>(f3(sx[j])), lam_i + fl1[j].z, poly6_ref);
+        });
+        u = make_float3(pi.x + acc.x / div, pi.y + acc.y / div, pi.z + acc.z / div);
+    } else if (contacts && phi >= kCloth) {
         for_each_contact(P, i, pi, phi, sx, sattr, cell_first, [&](uint32_t) { ++nb; });
         if (nb) {
             V3<float> acc = lift<float>(make_float3(0.f, 0.f, 0.f));
@@ -233,17 +304,67 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_prep(DevParams P0, uint32_
     gxo[orig] = make_float4(o.x + go3.x, o.y + go3.y, o.z + go3.z, 0.f);
 }
 
+// d delta_term / d lambda_sum: the direction a unit of lambda moves i.
+__device__ __forceinline__ float3 delta_dlam(const DevParams &P, float3 pi, float3 pj, float lam_sum, float poly6_ref) {
+    Dual<1> l = dconst<1>(lam_sum);
+    l.d[0] = 1.f;
+    const V3<Dual<1>> t = delta_term<Dual<1>>(P, lift<Dual<1>>(pi), lift<Dual<1>>(pj), l, poly6_ref);
+    return make_float3(t.x.d[0], t.y.d[0], t.z.d[0]);
+}
+
+// Adjoint of lambda_i: lambda_i enters i's own delta and the delta of
+// every fluid neighbour j (lambda_i + lambda_j).
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_fluid_lbar(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                           const float4 *__restrict__ sx,
+                                                           const SortedAttr *__restrict__ sattr,
+                                                           const uint32_t *__restrict__ cell_first,
+                                                           const float4 *__restrict__ fl1,
+                                                           const float4 *__restrict__ fl2,
+                                                           const float4 *__restrict__ gu, float *__restrict__ lbar) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    if (!scene_active<B>(P, iter_left) || sattr[i].phase != kFluid) {
+        lbar[i] = 0.f;
+        return;
+    }
+    const float3 pi = f3(sx[i]);
+    const float lam_i = fl1[i].z, div_i = fl2[i].w;
+    const float4 gi4 = gu[i];
+    const float poly6_ref = P.poly6 * P.scorr_inv_ref;
+    float acc = 0.f;
+    for_each_fluid_nb(P, i, pi, sx, cell_first, [&](uint32_t j) {
+        const float3 pj = f3(sx[j]);
+        const float lam_j = fl1[j].z;
+        const float3 a = delta_dlam(P, pi, pj, lam_i + lam_j, poly6_ref);
+        acc += (gi4.x * a.x + gi4.y * a.y + gi4.z * a.z) / div_i;
+        if (sattr[j].phase == kFluid) {
+            const float3 b = delta_dlam(P, pj, pi, lam_j + lam_i, poly6_ref);
+            const float4 gj4 = gu[j];
+            acc += (gj4.x * b.x + gj4.y * b.y + gj4.z * b.z) / fl2[j].w;
+        }
+    });
+    lbar[i] = acc;
+}
+
 // Gather for sorted particle j: the adjoint of its start-of-iteration
-// position (identity plus its own contact terms, plus every partner i's
-// terms through x_j) and the contact terms' part of the adjoint of
-// x_old_j.
+// position -- identity, plus its own contact / fluid delta terms and its
+// own lambda, plus every partner's contact term, fluid delta term and
+// lambda through x_j -- and the contact terms' part of the adjoint of
+// x_old_j.  A partner's lambda in x_j comes from perturbing only the pair
+// (i, j) term of its kept sums.
 template <bool B>
 __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint32_t n, uint32_t iter_left,
-                                                             bool contacts, const float4 *__restrict__ sx,
+                                                             bool contacts, bool fluids,
+                                                             const float4 *__restrict__ sx,
                                                              const SortedAttr *__restrict__ sattr,
                                                              const uint32_t *__restrict__ sidx,
                                                              const uint32_t *__restrict__ cell_first,
                                                              const float4 *__restrict__ x_old,
+                                                             const float4 *__restrict__ fl1,
+                                                             const float4 *__restrict__ fl2,
+                                                             const float *__restrict__ lbar,
                                                              const float4 *__restrict__ gu,
                                                              const uint32_t *__restrict__ cnt,
                                                              float4 *__restrict__ gstart, float4 *__restrict__ gxo) {
@@ -253,7 +374,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
     const uint32_t orig = sidx[j];
     const float4 guj4 = gu[j];
     const float3 guj = make_float3(guj4.x, guj4.y, guj4.z);
-    if (!scene_active<B>(P, iter_left) || !contacts) {
+    if (!scene_active<B>(P, iter_left) || !(contacts || fluids)) {
         gstart[orig] = make_float4(guj.x, guj.y, guj.z, 0.f);
         return;
     }
@@ -261,32 +382,179 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
     const float3 pj = f3(pj4);
     const int phj = sattr[j].phase;
     const float3 prevj = f3(x_old[orig]);
-    const uint32_t nj = cnt[j];
     float3 gx = guj, go = make_float3(0.f, 0.f, 0.f);
-    for_each_contact(P, j, pj, phj, sx, sattr, cell_first, [&](uint32_t i) {
-        const float4 pi4 = sx[i];
-        const int phi = sattr[i].phase;
-        const float3 previ = f3(x_old[sidx[i]]);
-        if (phj >= kCloth && nj) {  // j's own term c_ji, in x_j and x_old_j
-            const V3<Dual<6>> c = contact_pair<Dual<6>>(P, seed<6>(pj, 0), pj4.w, phj, seed<6>(prevj, 3),
-                                                        lift<Dual<6>>(f3(pi4)), pi4.w, phi, lift<Dual<6>>(previ),
-                                                        (float)nj);
-            gx = add3(gx, contract(c, guj, 0));
-            go = add3(go, contract(c, guj, 3));
+    if (contacts) {
+        const uint32_t nj = cnt[j];
+        for_each_contact(P, j, pj, phj, sx, sattr, cell_first, [&](uint32_t i) {
+            const float4 pi4 = sx[i];
+            const int phi = sattr[i].phase;
+            const float3 previ = f3(x_old[sidx[i]]);
+            if (phj >= kCloth && phj != kFluid && nj) {  // j's own term c_ji, in x_j and x_old_j
+                const V3<Dual<6>> c = contact_pair<Dual<6>>(P, seed<6>(pj, 0), pj4.w, phj, seed<6>(prevj, 3),
+                                                            lift<Dual<6>>(f3(pi4)), pi4.w, phi, lift<Dual<6>>(previ),
+                                                            (float)nj);
+                gx = add3(gx, contract(c, guj, 0));
+                go = add3(go, contract(c, guj, 3));
+            }
+            const uint32_t ni = cnt[i];
+            if (phi >= kCloth && ni) {  // partner's term c_ij, in x_j and x_old_j
+                const float4 gui4 = gu[i];
+                const float3 gui = make_float3(gui4.x, gui4.y, gui4.z);
+                const V3<Dual<6>> c = contact_pair<Dual<6>>(P, lift<Dual<6>>(f3(pi4)), pi4.w, phi,
+                                                            lift<Dual<6>>(previ), seed<6>(pj, 0), pj4.w, phj,
+                                                            seed<6>(prevj, 3), (float)ni);
+                gx = add3(gx, contract(c, gui, 0));
+                go = add3(go, contract(c, gui, 3));
+            }
+        });
+    }
+    if (fluids) {
+        const float poly6_ref = P.poly6 * P.scorr_inv_ref;
+        const bool jf = phj == kFluid;
+        const float lam_j = fl1[j].z, div_j = fl2[j].w, lbar_j = lbar[j];
+        const float inv_wj = 1.f / pj4.w;
+        const float inv_rho0_j = 1.f / sattr[j].rho0;
+        // own lambda_j in x_j: the whole sum on dual numbers
+        Dual<3> ro = dconst<3>(0.f), denom = dconst<3>(0.f);
+        V3<Dual<3>> grad = lift<Dual<3>>(make_float3(0.f, 0.f, 0.f));
+        const V3<Dual<3>> pjd = seed<3>(pj, 0);
+        for_each_fluid_nb(P, j, pj, sx, cell_first, [&](uint32_t i) {
+            const float4 pi4 = sx[i];
+            const float3 pi = f3(pi4);
+            const float lam_i = fl1[i].z;
+            if (jf) {
+                // own delta term, in x_j
+                const V3<Dual<3>> t = delta_term<Dual<3>>(P, pjd, lift<Dual<3>>(pi), cst<Dual<3>>(lam_j + lam_i),
+                                                          poly6_ref);
+                gx = add3(gx, contract(t, make_float3(guj.x / div_j, guj.y / div_j, guj.z / div_j), 0));
+                const LambdaTerm<Dual<3>> lt =
+                    lambda_term<Dual<3>>(P, pjd, lift<Dual<3>>(pi), mass_factor(P, inv_wj, pi4.w), -P.spiky * inv_rho0_j);
+                ro = ro + lt.ro;
+                denom = denom + gdot(lt.sg, lt.sg);
+                grad = grad - lt.sg;
+            }
+            if (sattr[i].phase == kFluid) {
+                // partner's delta term, in x_j
+                const float div_i = fl2[i].w;
+                const float4 gui4 = gu[i];
+                const V3<Dual<3>> t = delta_term<Dual<3>>(P, lift<Dual<3>>(pi), pjd, cst<Dual<3>>(lam_i + lam_j),
+                                                          poly6_ref);
+                gx = add3(gx, contract(t, make_float3(gui4.x / div_i, gui4.y / div_i, gui4.z / div_i), 0));
+                // partner's lambda, in x_j: only the (i, j) term of its sums moves
+                const float inv_wi = 1.f / pi4.w, inv_rho0_i = 1.f / sattr[i].rho0;
+                const float mf = mass_factor(P, inv_wi, pj4.w), sr = -P.spiky * inv_rho0_i;
+                const LambdaTerm<float> tv = lambda_term<float>(P, lift<float>(pi), lift<float>(pj), mf, sr);
+                const LambdaTerm<Dual<3>> td = lambda_term<Dual<3>>(P, lift<Dual<3>>(pi), pjd, mf, sr);
+                const float4 s1 = fl1[i], s2 = fl2[i];
+                const Dual<3> ro_i = cst<Dual<3>>(s1.x - tv.ro) + td.ro;
+                const Dual<3> de_i = cst<Dual<3>>(s1.y - gdot(tv.sg, tv.sg)) + gdot(td.sg, td.sg);
+                const V3<Dual<3>> gr_i = lift<Dual<3>>(make_float3(s2.x + tv.sg.x, s2.y + tv.sg.y, s2.z + tv.sg.z)) - td.sg;
+                const Dual<3> li = lambda_of<Dual<3>>(P, ro_i, de_i, gr_i, inv_wi, inv_rho0_i);
+                const float lb = lbar[i];
+                gx = make_float3(gx.x + lb * li.d[0], gx.y + lb * li.d[1], gx.z + lb * li.d[2]);
+            }
+        });
+        if (jf) {
+            const Dual<3> lj = lambda_of<Dual<3>>(P, ro, denom, grad, inv_wj, inv_rho0_j);
+            gx = make_float3(gx.x + lbar_j * lj.d[0], gx.y + lbar_j * lj.d[1], gx.z + lbar_j * lj.d[2]);
         }
-        const uint32_t ni = cnt[i];
-        if (phi >= kCloth && ni) {  // partner's term c_ij, in x_j and x_old_j
-            const float4 gui4 = gu[i];
-            const float3 gui = make_float3(gui4.x, gui4.y, gui4.z);
-            const V3<Dual<6>> c = contact_pair<Dual<6>>(P, lift<Dual<6>>(f3(pi4)), pi4.w, phi, lift<Dual<6>>(previ),
-                                                        seed<6>(pj, 0), pj4.w, phj, seed<6>(prevj, 3), (float)ni);
-            gx = add3(gx, contract(c, gui, 0));
-            go = add3(go, contract(c, gui, 3));
-        }
-    });
+    }
     gstart[orig] = make_float4(gx.x, gx.y, gx.z, 0.f);
-    const float4 o = gxo[orig];
-    gxo[orig] = make_float4(o.x + go.x, o.y + go.y, o.z + go.z, 0.f);
+    if (contacts) {
+        const float4 o = gxo[orig];
+        gxo[orig] = make_float4(o.x + go.x, o.y + go.y, o.z + go.z, 0.f);
+    }
+}
+
+// ------------------------------------------------------------------ XSPH
+
+// XSPH (k_xsph) over the last iteration's grid: for fluid i,
+// v'_i = v_i + (c / rho0_i) sum_j m_j (v_j - v_i) W(x_i - x_j) over fluid
+// neighbours.  Given the adjoint g of v' (sorted, gvs), the adjoint of v
+// (written to gv_out, original order) and of the positions (added to gx_out,
+// original order).  vs: velocities before XSPH, sorted.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_xsph(DevParams P0, uint32_t n, const float4 *__restrict__ sx,
+                                                     const SortedAttr *__restrict__ sattr,
+                                                     const uint32_t *__restrict__ sidx,
+                                                     const uint32_t *__restrict__ cell_first,
+                                                     const float4 *__restrict__ vs, const float4 *__restrict__ gvs,
+                                                     float4 *__restrict__ gv_out, float4 *__restrict__ gx_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    const uint32_t orig = sidx[i];
+    const float4 gi4 = gvs[i];
+    const bool fi = sattr[i].phase == kFluid && P.xsph_c != 0.f && P.iterations > 0u;
+    if (!fi) {
+        gv_out[orig] = gi4;
+        gx_out[orig] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float4 xi4 = sx[i];
+    const float3 xi = f3(xi4);
+    const float3 vi = f3(vs[i]);
+    const float3 gi = f3(gi4);
+    const float ci = P.xsph_c / sattr[i].rho0;
+    const float mi = (xi4.w > 0.f) ? 1.f / xi4.w : 0.f;
+    float3 gv = gi, gx = make_float3(0.f, 0.f, 0.f);
+    const V3<Dual<3>> xid = seed<3>(xi, 0);
+    uint32_t nb = 0;
+    for_each_candidate(P, grid_pos(P, xi), P.fluid_rad, cell_first, [&](uint32_t j) {
+        const float4 xj4 = sx[j];
+        const float d2 = dist2_exact(xi, f3(xj4));
+        if (!(d2 < P.h2) || j == i || sattr[j].phase != kFluid) return true;
+        if (nb >= P.max_nb) return false;
+        ++nb;
+        const float3 vj = f3(vs[j]);
+        const float3 gj = f3(gvs[j]);
+        const float cj = P.xsph_c / sattr[j].rho0;
+        const float mj = (xj4.w > 0.f) ? 1.f / xj4.w : 0.f;
+        const V3<Dual<3>> dr = xid - lift<Dual<3>>(f3(xj4));
+        const Dual<3> hm2 = P.h2 - gdot(dr, dr);
+        const Dual<3> W = hm2 * hm2 * hm2 * P.poly6;
+        // own: v'_i += ci mj (vj - vi) W
+        gv = make_float3(gv.x - gi.x * ci * mj * W.v, gv.y - gi.y * ci * mj * W.v, gv.z - gi.z * ci * mj * W.v);
+        const float own = ci * mj * (gi.x * (vj.x - vi.x) + gi.y * (vj.y - vi.y) + gi.z * (vj.z - vi.z));
+        // partner: v'_j += cj mi (vi - vj) W (the same W, symmetric in x)
+        gv = make_float3(gv.x + gj.x * cj * mi * W.v, gv.y + gj.y * cj * mi * W.v, gv.z + gj.z * cj * mi * W.v);
+        const float par = cj * mi * (gj.x * (vi.x - vj.x) + gj.y * (vi.y - vj.y) + gj.z * (vi.z - vj.z));
+        const float k = own + par;
+        gx = make_float3(gx.x + k * W.d[0], gx.y + k * W.d[1], gx.z + k * W.d[2]);
+        return true;
+    });
+    gv_out[orig] = make_float4(gv.x, gv.y, gv.z, 0.f);
+    gx_out[orig] = make_float4(gx.x, gx.y, gx.z, 0.f);
+}
+
+// Sorted copies for the XSPH adjoint: vs = v_before[sidx], gvs = g[sidx].
+__global__ void __launch_bounds__(kBlock) k_adj_gather_sorted(uint32_t n, const uint32_t *__restrict__ sidx,
+                                                              const float4 *__restrict__ a, const float4 *__restrict__ b,
+                                                              float4 *__restrict__ as, float4 *__restrict__ bs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = sidx[i];
+    as[i] = a[o];
+    bs[i] = b[o];
+}
+
+// v before XSPH: (x_fin - x_old) / min(dt, max_dt), as k_velocity.
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_vel_of(DevParams P0, uint32_t n, float dt,
+                                                       const float4 *__restrict__ xfin,
+                                                       const float4 *__restrict__ xold, float4 *__restrict__ v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = xfin[i], o = xold[i];
+    const float nd = -fminf(dt, scene_params<B>(P0, i).max_dt);
+    v[i] = make_float4((o.x - p.x) / nd, (o.y - p.y) / nd, (o.z - p.z) / nd, 0.f);
+}
+
+__global__ void __launch_bounds__(kBlock) k_add4(uint32_t n, float4 *__restrict__ a, const float4 *__restrict__ b) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 x = a[i], y = b[i];
+    a[i] = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, 0.f);
 }
 
 // ------------------------------------------------------------ host side
@@ -310,40 +578,10 @@ cudaError_t grow(T **p, size_t &have, size_t want) {
 }
 
 int differentiable(pbd_system *s) {
-    if (s->n_fluid)
-        return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED,
-                                 "differentiation covers contacts, walls, distance constraints, pins and the "
-                                 "integrator; this system has fluid particles");
     if (s->bodies.count)
         return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED,
-                                 "differentiation covers contacts, walls, distance constraints, pins and the "
-                                 "integrator; this system has rigid bodies");
-    return PBD_OK;
-}
-
-// The forward step with the positions the projectors read recorded:
-// rec[0] = x at the start (x_old), then per iteration the position at the
-// iteration start and after the contact / wall pass.  The same launches in
-// the same order as enqueue_update for a system without fluid or bodies.
-int record_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec) {
-    const DevParams &P = s->dev;
-    const uint32_t n = s->n;
-    const size_t bytes = (size_t)n * sizeof(float4);
-    ADJ_TRY(s, cudaMemcpyAsync(rec, s->x, bytes, cudaMemcpyDeviceToDevice, st));
-    ADJ_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
-    ADJ_TRY(s, launch_predict(P, n, dt, s->x, s->v, s->x_old, s->grid.hash, s->grid.slot, s->grid.cell_first, st));
-    uint32_t mask = kDoWorld;
-    if (s->n_contact) mask |= kDoContact;
-    const uint32_t iters = P.iterations;
-    for (uint32_t it = 0; it < iters; ++it) {
-        const uint32_t left = iters - 1u - it;
-        if (int rc = pbd_internal_build_grid(s, st, it == 0)) return rc;
-        ADJ_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 2 * it) * n, s->x, bytes, cudaMemcpyDeviceToDevice, st));
-        ADJ_TRY(s, launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, s->nbl, false, s->tpp, st));
-        ADJ_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 2 * it) * n, s->x, bytes, cudaMemcpyDeviceToDevice, st));
-        if (s->cons.count) ADJ_TRY(s, launch_distance(P, left, s->cons, s->x, true, true, st));
-    }
-    ADJ_TRY(s, launch_velocity(P, n, dt, s->x, s->x_old, s->v, st));
+                                 "differentiation covers PBF fluid, XSPH, contacts, walls, distance constraints, "
+                                 "pins and the integrator; this system has rigid bodies");
     return PBD_OK;
 }
 
@@ -355,14 +593,16 @@ using namespace pbd;
 void pbd_internal_free_adjoint(pbd_system *s) {
     auto &a = s->adj;
     for (float4 **p : {&a.ckpt_x, &a.ckpt_v, &a.rec, &a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu, &a.save_x, &a.save_v,
-                       &a.save_xo}) {
+                       &a.save_xo, &a.fl1, &a.fl2, &a.w1, &a.w2, &a.w3}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
     if (a.cnt) cudaFree(a.cnt);
     if (a.gstiff) cudaFree(a.gstiff);
+    if (a.lbar) cudaFree(a.lbar);
     a.cnt = nullptr;
     a.gstiff = nullptr;
+    a.lbar = nullptr;
     a.ckpt_cap = a.rec_cap = 0;
     a.work_cap = a.stiff_cap = 0;
     a.recorded = false;
@@ -454,20 +694,25 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
     const bool batched = P.table != nullptr;
     const uint32_t iters = P.iterations;
     const size_t bytes = (size_t)n * sizeof(float4);
-    const size_t per_step = 1u + 2u * iters;
+    const size_t per_step = 2u + 2u * iters;
+    const uint64_t launches0 = s->launches, steps0 = s->steps;
     // work arrays
     size_t rec_have = a.rec_cap;
     ADJ_TRY(s, grow(&a.rec, rec_have, per_step * a.every * (size_t)n));
     a.rec_cap = rec_have;
     if (a.work_cap < s->cap) {
-        for (float4 **p : {&a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu, &a.save_x, &a.save_v, &a.save_xo}) {
+        for (float4 **p : {&a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu, &a.save_x, &a.save_v, &a.save_xo, &a.fl1, &a.fl2,
+                           &a.w1, &a.w2, &a.w3}) {
             if (*p) cudaFree(*p);
             *p = nullptr;
             ADJ_TRY(s, cudaMalloc((void **)p, (size_t)s->cap * sizeof(float4)));
         }
         if (a.cnt) cudaFree(a.cnt);
+        if (a.lbar) cudaFree(a.lbar);
         a.cnt = nullptr;
+        a.lbar = nullptr;
         ADJ_TRY(s, cudaMalloc((void **)&a.cnt, (size_t)s->cap * sizeof(uint32_t)));
+        ADJ_TRY(s, cudaMalloc((void **)&a.lbar, (size_t)s->cap * sizeof(float)));
         a.work_cap = s->cap;
     }
     const uint32_t m = s->cons.m;
@@ -488,9 +733,12 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
     if (dL_dv) ADJ_TRY(s, cudaMemcpyAsync(a.gv, dL_dv, bytes, cudaMemcpyDeviceToDevice, st));
     else ADJ_TRY(s, cudaMemsetAsync(a.gv, 0, bytes, st));
     const bool contacts = s->n_contact != 0;
+    const bool fluids = s->n_fluid != 0;
+    const bool xsph = pbd_internal_any_xsph(s);
     const ConstraintBuffers &c = s->cons;
     const unsigned nb = blocks_for(n);
     const float dt = a.dt;
+    const GridBuffers &g = s->grid;
 #define ADJ_LAUNCH(KERNEL, GRID, ...)                                                     \
     do {                                                                                  \
         if (batched) KERNEL<true><<<(GRID), kBlock, 0, st>>>(__VA_ARGS__);                \
@@ -504,12 +752,25 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
         ADJ_TRY(s, cudaMemcpyAsync(s->x, a.ckpt_x + (size_t)seg * n, bytes, cudaMemcpyDeviceToDevice, st));
         ADJ_TRY(s, cudaMemcpyAsync(s->v, a.ckpt_v + (size_t)seg * n, bytes, cudaMemcpyDeviceToDevice, st));
         for (uint32_t t = t0; t < t1; ++t)
-            if (int rc = record_update(s, dt, st, a.rec + (t - t0) * per_step * n)) return rc;
+            if (int rc = pbd_internal_enqueue_update(s, dt, st, a.rec + (t - t0) * per_step * n)) return rc;
         // reverse over its steps
         for (int t = (int)t1 - 1; t >= (int)t0; --t) {
             float4 *rec = a.rec + (size_t)(t - (int)t0) * per_step * n;
+            const float4 *xfin = rec + (size_t)(1 + 2 * iters) * n;
             // x_old of this step for the friction and wall terms
             ADJ_TRY(s, cudaMemcpyAsync(s->x_old, rec, bytes, cudaMemcpyDeviceToDevice, st));
+            if (xsph) {
+                // XSPH over the last iteration's grid: gv (after XSPH) -> gv
+                // (after the velocity update), w3 = its position part
+                ADJ_TRY(s, cudaMemcpyAsync(s->x, rec + (size_t)(1 + 2 * (iters - 1)) * n, bytes,
+                                           cudaMemcpyDeviceToDevice, st));
+                if (int rc = pbd_internal_build_grid(s, st, false)) return rc;
+                ADJ_LAUNCH(k_adj_vel_of, nb, P, n, dt, xfin, rec, a.w1);
+                k_adj_gather_sorted<<<nb, kBlock, 0, st>>>(n, g.sorted_idx, a.w1, a.gv, a.w2, a.gu);
+                ADJ_TRY(s, cudaGetLastError());
+                ADJ_LAUNCH(k_adj_xsph, nb, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, a.w2, a.gu,
+                           a.gv, a.w3);
+            }
             // gy <- adjoint of the final positions, gxo <- -gv / dt
             ADJ_LAUNCH(k_adj_velocity, nb, P, n, dt, a.gx, a.gv, a.gy, a.gxo);
             for (int it = (int)iters - 1; it >= 0; --it) {
@@ -529,20 +790,31 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
                                    c.con_stiff, c.occ_of, ysolve, a.gt, a.gstiff);
                     }
                 }
-                // contacts and walls: rebuild this iteration's grid, then
-                // prep (walls, u's adjoint, counts) and gather
+                // contacts, fluid and walls: rebuild this iteration's grid,
+                // recompute lambda, then prep (walls, u's adjoint, counts),
+                // lambda's adjoint and the gather
                 ADJ_TRY(s, cudaMemcpyAsync(s->x, xstart, bytes, cudaMemcpyDeviceToDevice, st));
                 if (int rc = pbd_internal_build_grid(s, st, false)) return rc;
-                ADJ_LAUNCH(k_adj_solve_prep, nb, P, n, left, contacts, s->grid.sorted_x, s->grid.sorted_attr,
-                           s->grid.sorted_idx, s->grid.cell_first, s->x_old, a.gy, a.gu, a.cnt, a.gxo);
-                ADJ_LAUNCH(k_adj_solve_gather, nb, P, n, left, contacts, s->grid.sorted_x, s->grid.sorted_attr,
-                           s->grid.sorted_idx, s->grid.cell_first, s->x_old, a.gu, a.cnt, a.gy, a.gxo);
+                if (fluids) ADJ_LAUNCH(k_adj_fluid_lambda, nb, P, n, g.sorted_x, g.sorted_attr, g.cell_first, a.fl1, a.fl2);
+                ADJ_LAUNCH(k_adj_solve_prep, nb, P, n, left, contacts, fluids, g.sorted_x, g.sorted_attr, g.sorted_idx,
+                           g.cell_first, s->x_old, a.fl1, a.fl2, a.gy, a.gu, a.cnt, a.gxo);
+                if (fluids)
+                    ADJ_LAUNCH(k_adj_fluid_lbar, nb, P, n, left, g.sorted_x, g.sorted_attr, g.cell_first, a.fl1, a.fl2,
+                               a.gu, a.lbar);
+                ADJ_LAUNCH(k_adj_solve_gather, nb, P, n, left, contacts, fluids, g.sorted_x, g.sorted_attr,
+                           g.sorted_idx, g.cell_first, s->x_old, a.fl1, a.fl2, a.lbar, a.gu, a.cnt, a.gy, a.gxo);
+                if (xsph && it == (int)iters - 1) {  // XSPH read this iteration's start positions
+                    k_add4<<<nb, kBlock, 0, st>>>(n, a.gy, a.w3);
+                    ADJ_TRY(s, cudaGetLastError());
+                }
             }
             // predict: gy is now the adjoint of the predicted positions
             ADJ_LAUNCH(k_adj_predict, nb, P, n, dt, a.gy, a.gxo, a.gx, a.gv);
         }
     }
 #undef ADJ_LAUNCH
+    s->launches = launches0;  // the recomputation is not a user step
+    s->steps = steps0;
     if (dL_dx0) ADJ_TRY(s, cudaMemcpyAsync(dL_dx0, a.gx, bytes, cudaMemcpyDeviceToDevice, st));
     if (dL_dv0) ADJ_TRY(s, cudaMemcpyAsync(dL_dv0, a.gv, bytes, cudaMemcpyDeviceToDevice, st));
     if (dL_dstiffness && m)

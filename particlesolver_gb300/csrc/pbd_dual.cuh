@@ -133,11 +133,27 @@ __device__ __forceinline__ Dual<N> grsqrt(const Dual<N> &a) {
     for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * h;
     return r;
 }
-// min(a, b) with b a constant: the derivative of the chosen branch
+// min / max with a constant: the derivative of the chosen branch
 __device__ __forceinline__ float gmin(float a, float b) { return fminf(a, b); }
 template <int N>
 __device__ __forceinline__ Dual<N> gmin(const Dual<N> &a, float b) {
     return (a.v <= b) ? a : dconst<N>(b);
+}
+__device__ __forceinline__ float gmax(float a, float b) { return fmaxf(a, b); }
+template <int N>
+__device__ __forceinline__ Dual<N> gmax(const Dual<N> &a, float b) {
+    return (a.v >= b) ? a : dconst<N>(b);
+}
+// a^n for a constant real n
+__device__ __forceinline__ float gpow(float a, float n) { return powf(a, n); }
+template <int N>
+__device__ __forceinline__ Dual<N> gpow(const Dual<N> &a, float n) {
+    Dual<N> r;
+    r.v = powf(a.v, n);
+    const float g = (a.v != 0.f) ? n * powf(a.v, n - 1.f) : 0.f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * g;
+    return r;
 }
 
 template <class T>
@@ -289,6 +305,76 @@ __device__ __forceinline__ V3<T> distance_term(const DevParams &P, V3<T> xk, flo
         mag = (rest - dist) * .5f;
     }
     return (rel / dist) * (mag * stiff);
+}
+
+// ----------------------------------------------------------------- PBF
+
+// One neighbour's terms of the lambda pass (LambdaAcc::add): its poly6
+// density term and its spiky gradient over rho0 (zero below the 1e-4
+// length cut-off).  mass_factor: 1 / w_i, or 1 / w_j with
+// PBD_FLAG_DENSITY_NEIGHBOR_MASS.
+template <class T>
+struct LambdaTerm {
+    T ro;
+    V3<T> sg;
+};
+
+template <class T>
+__device__ __forceinline__ LambdaTerm<T> lambda_term(const DevParams &P, V3<T> pi, V3<T> pj, float mass_factor,
+                                                     float spiky_r) {
+    const V3<T> dr = pi - pj;
+    const T d2 = gdot(dr, dr);
+    const T hm2 = P.h2 - d2;
+    LambdaTerm<T> t;
+    t.ro = hm2 * hm2 * hm2 * (P.poly6 * mass_factor);
+    const T rs = grsqrt(gmax(d2, kMinSpiky2));
+    const T hm = P.h - d2 * rs;
+    if (val(d2) >= kMinSpiky2) t.sg = dr * (hm * hm * rs * spiky_r);
+    else t.sg = lift<T>(make_float3(0.f, 0.f, 0.f));
+    return t;
+}
+
+// lambda from the pass's sums: ro (neighbour terms, own term added here),
+// denom = sum |sg|^2 and grad = -sum sg.
+template <class T>
+__device__ __forceinline__ T lambda_of(const DevParams &P, T ro, T denom, V3<T> grad, float inv_w, float inv_rho0) {
+    const T r = ro + P.poly6_self * inv_w;
+    return -(r * inv_rho0 - 1.f) / (denom + gdot(grad, grad) + P.relax);
+}
+
+// s_corr ratio^n (scorr_pow).
+template <class T>
+__device__ __forceinline__ T scorr_pow_g(const DevParams &P, T ratio) {
+    if (P.scorr_n_int == 4) {
+        const T r2 = ratio * ratio;
+        return r2 * r2;
+    }
+    if (P.scorr_n_int > 0) {
+        T r = ratio;
+        for (int k = 1; k < P.scorr_n_int; ++k) r = r * ratio;
+        return r;
+    }
+    return gpow(ratio, P.scorr_n);
+}
+
+// One neighbour's term of the delta pass (delta_add) before the division
+// by rho0 + n: (lambda_i + lambda_j + s_corr) times the spiky gradient,
+// with the reference's (0, EPS, 0) direction below the cut-off.
+template <class T>
+__device__ __forceinline__ V3<T> delta_term(const DevParams &P, V3<T> pi, V3<T> pj, T lam_sum, float poly6_ref) {
+    const V3<T> dr = pi - pj;
+    const T d2 = gdot(dr, dr);
+    const T hm2 = P.h2 - d2;
+    const T coef = lam_sum - P.scorr_k * scorr_pow_g<T>(P, hm2 * hm2 * hm2 * poly6_ref);
+    if (val(d2) >= kMinSpiky2) {
+        const T rs = grsqrt(d2);
+        const T hm = P.h - d2 * rs;
+        return dr * (coef * (-P.spiky) * hm * hm * rs);
+    }
+    const T hz = P.h - gsqrt(d2);
+    V3<T> out = lift<T>(make_float3(0.f, 0.f, 0.f));
+    out.y = coef * (-P.spiky * kEps) * hz * hz;
+    return out;
 }
 
 }  // namespace pbd

@@ -469,9 +469,14 @@ uint32_t solve_mask(const pbd_system *s) {
 // several scenes every launch covers all of them; a scene with fewer
 // iterations than the batch's most sits out the first ones (its particles
 // keep their predicted positions, so the grids it skips change nothing).
-int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
+// rec (the adjoint's recording, or nullptr): x before the step, then per
+// iteration x at its start and after the contact / fluid / wall pass, then
+// x after the last iteration (2 + 2 iterations states of n float4).
+int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullptr) {
     const pbd::DevParams &P = s->dev;
     const uint32_t n = s->n;
+    const size_t nbytes = (size_t)n * sizeof(float4);
+    if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
     {
         // predict, with the first grid build's hash and cell counts fused in
         Stage t(s, st, PBD_STAGE_PREDICT, 1);
@@ -514,6 +519,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
             if (int rc = build_grid(s, st, it == 0)) return rc;
             L.reuse = nullptr;
         }
+        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 2 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
             CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, L, s->tpp, st));
@@ -524,6 +530,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
             CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, L,
                                           s->list_valid, s->tpp, st));
         }
+        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 2 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (dist_kernels) {
             Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
             CUDA_TRY(s, pbd::launch_distance(P, left, s->cons, s->x, true, true, st));
@@ -533,6 +540,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st) {
             CUDA_TRY(s, pbd::launch_shapes(P, left, s->bodies, s->x, st));
         }
     }
+    if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 2 * iters) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
     {
         Stage t(s, st, PBD_STAGE_VELOCITY, 1);
         CUDA_TRY(s, pbd::launch_velocity(P, n, dt, s->x, s->x_old, s->v, st));
@@ -561,7 +569,10 @@ int pbd_internal_guard(pbd_system *s) {
 int pbd_internal_build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict) {
     return build_grid(s, st, hashed_in_predict);
 }
-int pbd_internal_enqueue_update(pbd_system *s, float dt, cudaStream_t st) { return enqueue_update(s, dt, st); }
+int pbd_internal_enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec) {
+    return enqueue_update(s, dt, st, rec);
+}
+bool pbd_internal_any_xsph(const pbd_system *s) { return any_xsph(s); }
 float pbd_internal_clamp_dt(const pbd_system *s, float dt) { return clamp_dt(s, dt); }
 
 int pbd_internal_device_params(const pbd_params *params, pbd::DevParams *out, std::string *why) {

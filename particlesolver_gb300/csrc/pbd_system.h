@@ -105,6 +105,8 @@ struct pbd_system {
         size_t rec_cap = 0;                           // states allocated
         float4 *gx = nullptr, *gv = nullptr, *gxo = nullptr, *gt = nullptr, *gy = nullptr, *gu = nullptr;
         float4 *save_x = nullptr, *save_v = nullptr, *save_xo = nullptr;
+        float4 *fl1 = nullptr, *fl2 = nullptr, *w1 = nullptr, *w2 = nullptr, *w3 = nullptr;
+        float *lbar = nullptr;
         uint32_t *cnt = nullptr;
         float *gstiff = nullptr;
         uint32_t work_cap = 0, stiff_cap = 0;
@@ -124,6 +126,8 @@ void pbd_internal_set_thread_error(const std::string &msg);
 int pbd_internal_fail(pbd_system *s, int code, const std::string &msg);
 int pbd_internal_guard(pbd_system *s);  // handle check + its device current
 int pbd_internal_build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict);
-int pbd_internal_enqueue_update(pbd_system *s, float dt, cudaStream_t st);
+// rec: the adjoint's recording of the step's positions, or nullptr.
+int pbd_internal_enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullptr);
+bool pbd_internal_any_xsph(const pbd_system *s);
 float pbd_internal_clamp_dt(const pbd_system *s, float dt);
 void pbd_internal_free_adjoint(pbd_system *s);

@@ -194,8 +194,50 @@ def test_backward_is_deterministic_and_restores_state():
         np.testing.assert_array_equal(a, b)
 
 
+def fluid_scene(xsph):
+    """A PBF block with the smooth delta divisor (PBD_FLAG_DELTA_OVER_RHO0:
+    the reference's rho0 + n jumps whenever a neighbour count changes, so
+    central differences of a fluid step only converge without it)."""
+    from particlesolver_gb300 import FLAG_DELTA_OVER_RHO0
+
+    sc = W.dam_break(8, 8, 6, xsph=xsph)
+    sc.params["flags"] = sc.params["flags"] | FLAG_DELTA_OVER_RHO0
+    return sc
+
+
+@pytest.mark.parametrize("xsph,steps,every", [(0.0, 1, 1), (0.0, 3, 2), (0.01, 3, 2)])
+def test_fluid_gradient_matches_fd(xsph, steps, every):
+    """PBF density / lambda, the fluid delta with s_corr, walls, XSPH and
+    the integrator (eps 1e-6: the oracle's central differences agree to 6
+    digits from 1e-6 down)."""
+    check_directional(fluid_scene(xsph), steps, every, seed=7 + steps, eps=1e-6)
+
+
+def test_fluid_on_solid_gradient_matches_fd():
+    """Fluid falling onto solid grains: lambda and delta over neighbours of
+    both phases, contacts of the grains with the fluid."""
+    from particlesolver_gb300 import FLAG_DELTA_OVER_RHO0
+
+    sc = W.dam_break(8, 8, 4, xsph=0.01)
+    sc.params["flags"] = sc.params["flags"] | FLAG_DELTA_OVER_RHO0
+    n = sc.n
+    pos = sc.pos_w.copy()
+    pos[:, 1] += 0.06
+    grains = np.stack(np.meshgrid(np.arange(8), np.arange(4), indexing="ij"), -1).reshape(-1, 2)
+    gpos = np.zeros((len(grains), 4), np.float32)
+    gpos[:, 0] = 0.03 + grains[:, 0] * 0.055  # apart (contact at 2.001 r = 0.050025)
+    gpos[:, 1] = 0.026                         # just above the floor clamp (r = 0.025)
+    gpos[:, 2] = 0.03 + grains[:, 1] * 0.055
+    gpos[:, 3] = 1.0
+    sc = W.Scene("fluid_on_grains", sc.params, np.concatenate([pos, gpos]),
+                 np.concatenate([sc.phase, np.full(len(gpos), W.PHASE_SOLID, np.int32)]),
+                 rest_density=np.concatenate([sc.rest_density, np.ones(len(gpos), np.float32)]), dt=sc.dt)
+    assert sc.n == n + len(gpos)
+    check_directional(sc, 3, 2, seed=21, eps=1e-6)
+
+
 def test_unsupported_scenes_are_rejected():
-    sc = W.dam_break(8, 8, 4)
+    sc = W.rigid_boxes(count=2)
     sys = ParticleSystem(default_params(**sc.params), sc.n)
     W.apply_to(sc, sys)
     with pytest.raises(PbdError) as e:
