@@ -373,14 +373,17 @@ int pbd_load_state(pbd_system *sys, const void *src, uint64_t size);
 
 /* ------------------------------------------------------- differentiation
  *
- * Reverse-mode gradients of a rollout (no counterpart in the reference).
- * Covered: prediction and the velocity update, contacts with friction, the
- * world walls (with their friction), distance constraints (including the
- * gradient of each constraint's stiffness) and pins; a system with fluid
- * particles or rigid bodies returns PBD_ERR_UNSUPPORTED.  Contact pairs,
+ * Reverse-mode gradients of a rollout (no counterpart in the reference),
+ * through every stage of the step: prediction and the velocity update, the
+ * PBF density / lambda solve and its delta (s_corr included), contacts with
+ * friction, the world walls (with their friction), distance constraints
+ * (including the gradient of each constraint's stiffness), pins, shape
+ * matching and XSPH.  Neighbour and contact sets, neighbour counts,
  * friction modes, wall clamps and cut-offs are those of the forward pass,
- * held fixed (the gradient of the piecewise-smooth step where it is
- * smooth).  Works on batched systems (every scene at once). */
+ * held fixed: the gradient of the piecewise-smooth step where it is smooth
+ * (the reference's PBF divisor rho0 + n jumps when a neighbour count
+ * changes; PBD_FLAG_DELTA_OVER_RHO0 makes the fluid step smooth).  Rigid
+ * bodies' rest shapes are constants.  Works on batched systems. */
 
 /* Replaces the stiffness of every distance constraint, in add order
  * (count = number of constraints; values in [0, 1]; host or device array). */

@@ -1,7 +1,9 @@
 // Differentiation of the PBD step: rollouts with checkpoints, and a
-// backward pass of hand-written adjoint kernels for the integrator (predict
-// and velocity), contacts with friction, the world walls, distance
-// constraints (with the gradient of every constraint's stiffness) and pins.
+// backward pass of hand-written adjoint kernels for every projector of the
+// step -- the integrator (predict and velocity), the PBF density / lambda
+// solve and its delta with s_corr, contacts with friction, the world walls,
+// distance constraints (with the gradient of every constraint's
+// stiffness), pins, shape matching (through the polar rotation) and XSPH.
 //
 // pbd_rollout runs `steps` updates and keeps (x, v) every `every` steps in
 // device memory.  pbd_backward walks the checkpoint segments from last to
@@ -466,6 +468,179 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
     }
 }
 
+// ---------------------------------------------------------- shape matching
+
+__device__ __forceinline__ float wsum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Polar rotation of A (the forward kernel's extraction, Mueller, Bender,
+// Chentanez, Macklin 2016), run from the identity to convergence.
+__device__ void polar_rotation(const float A[3][3], float R[3][3]) {
+    float q[4] = {0.f, 0.f, 0.f, 1.f};
+    for (int it = 0; it < 64; ++it) {
+        float M[3][3];
+        const float xx = q[0] * q[0], yy = q[1] * q[1], zz = q[2] * q[2];
+        const float xy = q[0] * q[1], xz = q[0] * q[2], yz = q[1] * q[2];
+        const float wx = q[3] * q[0], wy = q[3] * q[1], wz = q[3] * q[2];
+        M[0][0] = 1.f - 2.f * (yy + zz); M[0][1] = 2.f * (xy - wz);       M[0][2] = 2.f * (xz + wy);
+        M[1][0] = 2.f * (xy + wz);       M[1][1] = 1.f - 2.f * (xx + zz); M[1][2] = 2.f * (yz - wx);
+        M[2][0] = 2.f * (xz - wy);       M[2][1] = 2.f * (yz + wx);       M[2][2] = 1.f - 2.f * (xx + yy);
+        float ox = 0.f, oy = 0.f, oz = 0.f, dsum = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float rx = M[0][c], ry = M[1][c], rz = M[2][c];
+            const float ax = A[0][c], ay = A[1][c], az = A[2][c];
+            ox += ry * az - rz * ay;
+            oy += rz * ax - rx * az;
+            oz += rx * ay - ry * ax;
+            dsum += rx * ax + ry * ay + rz * az;
+        }
+        const float inv = 1.f / (fabsf(dsum) + 1.0e-9f);
+        ox *= inv;
+        oy *= inv;
+        oz *= inv;
+        const float wl = sqrtf(ox * ox + oy * oy + oz * oz);
+        if (wl < 1.0e-9f) break;
+        const float sh = sinf(0.5f * wl) / wl, ch = cosf(0.5f * wl);
+        const float d[4] = {ox * sh, oy * sh, oz * sh, ch};
+        float r[4];
+        r[3] = d[3] * q[3] - d[0] * q[0] - d[1] * q[1] - d[2] * q[2];
+        r[0] = d[3] * q[0] + d[0] * q[3] + d[1] * q[2] - d[2] * q[1];
+        r[1] = d[3] * q[1] - d[0] * q[2] + d[1] * q[3] + d[2] * q[0];
+        r[2] = d[3] * q[2] + d[0] * q[1] - d[1] * q[0] + d[2] * q[3];
+        const float qn = rsqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+        for (int k = 0; k < 4; ++k) q[k] = r[k] * qn;
+    }
+    const float xx = q[0] * q[0], yy = q[1] * q[1], zz = q[2] * q[2];
+    const float xy = q[0] * q[1], xz = q[0] * q[2], yz = q[1] * q[2];
+    const float wx = q[3] * q[0], wy = q[3] * q[1], wz = q[3] * q[2];
+    R[0][0] = 1.f - 2.f * (yy + zz); R[0][1] = 2.f * (xy - wz);       R[0][2] = 2.f * (xz + wy);
+    R[1][0] = 2.f * (xy + wz);       R[1][1] = 1.f - 2.f * (xx + zz); R[1][2] = 2.f * (yz - wx);
+    R[2][0] = 2.f * (xz - wy);       R[2][1] = 2.f * (yz + wx);       R[2][2] = 1.f - 2.f * (xx + yy);
+}
+
+// Shape matching (k_shapes): x'_k = x_k + s (c + R q_k - x_k), c the
+// mass-weighted centre, R the polar rotation of A = sum m_k (x_k - c) q_k^T.
+// Adjoint, one warp per body, g the adjoint of x' (in place):
+//   cbar = s sum g_k,  Rbar = s sum g_k q_k^T,
+//   Abar = R [y]x with (tr S I - S) y = vee(R^T Rbar - Rbar^T R), S = R^T A
+//   (the derivative of the polar rotation),
+//   xbar_k = (1 - s) g_k + m_k / M cbar + m_k Abar q_k
+// (the centre's part of A vanishes: sum m_k q_k = 0 by construction).
+template <bool B>
+__global__ void __launch_bounds__(kBlock) k_adj_shapes(DevParams P0, uint32_t iter_left, uint32_t bodies,
+                                                       const uint4 *__restrict__ range, const float *__restrict__ stiff,
+                                                       const float4 *__restrict__ rest, const float4 *__restrict__ x,
+                                                       float4 *__restrict__ g) {
+    const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= bodies) return;
+    const uint4 rg = range[b];
+    const uint32_t first = rg.x, count = rg.y, roff = rg.z;
+    if (!scene_active<B>(scene_params<B>(P0, first), iter_left)) return;
+    const float3 o = f3(x[first]);
+    float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f;
+    for (uint32_t k = lane; k < count; k += 32) {
+        const float4 p = x[first + k];
+        const float m = rest[roff + k].w;
+        sx += m * (p.x - o.x);
+        sy += m * (p.y - o.y);
+        sz += m * (p.z - o.z);
+        sm += m;
+    }
+    sx = wsum(sx);
+    sy = wsum(sy);
+    sz = wsum(sz);
+    sm = wsum(sm);
+    const float3 c = make_float3(o.x + sx / sm, o.y + sy / sm, o.z + sz / sm);
+    float A[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float Rb[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float cb[3] = {0.f, 0.f, 0.f};
+    for (uint32_t k = lane; k < count; k += 32) {
+        const float4 p = x[first + k];
+        const float4 q = rest[roff + k];
+        const float4 gk = g[first + k];
+        const float d[3] = {q.w * (p.x - c.x), q.w * (p.y - c.y), q.w * (p.z - c.z)};
+        const float gg[3] = {gk.x, gk.y, gk.z};
+        const float qq[3] = {q.x, q.y, q.z};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            cb[r] += gg[r];
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                A[r][cc] += d[r] * qq[cc];
+                Rb[r][cc] += gg[r] * qq[cc];
+            }
+        }
+    }
+    const float st = stiff[b];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        cb[r] = wsum(cb[r]) * st;
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) {
+            A[r][cc] = wsum(A[r][cc]);
+            Rb[r][cc] = wsum(Rb[r][cc]) * st;
+        }
+    }
+    float R[3][3];
+    polar_rotation(A, R);
+    // S = sym(R^T A), M = R^T Rbar
+    float S[3][3], M[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) {
+            float sa = 0.f, mm = 0.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                sa += R[k][r] * A[k][cc];
+                mm += R[k][r] * Rb[k][cc];
+            }
+            S[r][cc] = sa;
+            M[r][cc] = mm;
+        }
+    const float u[3] = {M[2][1] - M[1][2], M[0][2] - M[2][0], M[1][0] - M[0][1]};
+    const float tr = S[0][0] + S[1][1] + S[2][2];
+    float K[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) K[r][cc] = ((r == cc) ? tr : 0.f) - 0.5f * (S[r][cc] + S[cc][r]);
+    // y = K^-1 u by the adjugate (K symmetric positive definite for a
+    // non-degenerate body)
+    const float c00 = K[1][1] * K[2][2] - K[1][2] * K[2][1], c01 = K[1][2] * K[2][0] - K[1][0] * K[2][2],
+                c02 = K[1][0] * K[2][1] - K[1][1] * K[2][0];
+    const float det = K[0][0] * c00 + K[0][1] * c01 + K[0][2] * c02;
+    const float id = (fabsf(det) > 1e-20f) ? 1.f / det : 0.f;
+    const float Ki[3][3] = {
+        {c00 * id, (K[0][2] * K[2][1] - K[0][1] * K[2][2]) * id, (K[0][1] * K[1][2] - K[0][2] * K[1][1]) * id},
+        {c01 * id, (K[0][0] * K[2][2] - K[0][2] * K[2][0]) * id, (K[0][2] * K[1][0] - K[0][0] * K[1][2]) * id},
+        {c02 * id, (K[0][1] * K[2][0] - K[0][0] * K[2][1]) * id, (K[0][0] * K[1][1] - K[0][1] * K[1][0]) * id}};
+    const float y[3] = {Ki[0][0] * u[0] + Ki[0][1] * u[1] + Ki[0][2] * u[2],
+                        Ki[1][0] * u[0] + Ki[1][1] * u[1] + Ki[1][2] * u[2],
+                        Ki[2][0] * u[0] + Ki[2][1] * u[1] + Ki[2][2] * u[2]};
+    const float Y[3][3] = {{0.f, -y[2], y[1]}, {y[2], 0.f, -y[0]}, {-y[1], y[0], 0.f}};
+    float Ab[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) Ab[r][cc] = R[r][0] * Y[0][cc] + R[r][1] * Y[1][cc] + R[r][2] * Y[2][cc];
+    for (uint32_t k = lane; k < count; k += 32) {
+        const float4 q = rest[roff + k];
+        const float4 gk = g[first + k];
+        const float m = q.w, mf = q.w / sm;
+        const float ax = Ab[0][0] * q.x + Ab[0][1] * q.y + Ab[0][2] * q.z;
+        const float ay = Ab[1][0] * q.x + Ab[1][1] * q.y + Ab[1][2] * q.z;
+        const float az = Ab[2][0] * q.x + Ab[2][1] * q.y + Ab[2][2] * q.z;
+        g[first + k] = make_float4((1.f - st) * gk.x + mf * cb[0] + m * ax, (1.f - st) * gk.y + mf * cb[1] + m * ay,
+                                   (1.f - st) * gk.z + mf * cb[2] + m * az, 0.f);
+    }
+}
+
 // ------------------------------------------------------------------ XSPH
 
 // XSPH (k_xsph) over the last iteration's grid: for fluid i,
@@ -577,13 +752,7 @@ cudaError_t grow(T **p, size_t &have, size_t want) {
     return e;
 }
 
-int differentiable(pbd_system *s) {
-    if (s->bodies.count)
-        return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED,
-                                 "differentiation covers PBF fluid, XSPH, contacts, walls, distance constraints, "
-                                 "pins and the integrator; this system has rigid bodies");
-    return PBD_OK;
-}
+int differentiable(pbd_system *) { return PBD_OK; }
 
 }  // namespace
 }  // namespace pbd
@@ -592,8 +761,8 @@ using namespace pbd;
 
 void pbd_internal_free_adjoint(pbd_system *s) {
     auto &a = s->adj;
-    for (float4 **p : {&a.ckpt_x, &a.ckpt_v, &a.rec, &a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu, &a.save_x, &a.save_v,
-                       &a.save_xo, &a.fl1, &a.fl2, &a.w1, &a.w2, &a.w3}) {
+    for (float4 **p : {&a.ckpt_x, &a.ckpt_v, &a.ckpt_q, &a.rec, &a.gx, &a.gv, &a.gxo, &a.gt, &a.gy, &a.gu,
+                       &a.save_x, &a.save_v, &a.save_xo, &a.fl1, &a.fl2, &a.w1, &a.w2, &a.w3}) {
         if (*p) cudaFree(*p);
         *p = nullptr;
     }
@@ -603,7 +772,7 @@ void pbd_internal_free_adjoint(pbd_system *s) {
     a.cnt = nullptr;
     a.gstiff = nullptr;
     a.lbar = nullptr;
-    a.ckpt_cap = a.rec_cap = 0;
+    a.ckpt_cap = a.rec_cap = a.ckpt_q_cap = 0;
     a.work_cap = a.stiff_cap = 0;
     a.recorded = false;
 }
@@ -661,6 +830,15 @@ int pbd_rollout(pbd_system *s, float dt, uint32_t steps, uint32_t every, void *s
         ADJ_TRY(s, cudaMalloc((void **)&a.ckpt_v, want * sizeof(float4)));
         a.ckpt_cap = want;
     }
+    const uint32_t nb = s->bodies.count;
+    const size_t want_q = (size_t)nck * nb + nb;  // checkpoints + the final rotations
+    if (nb && (a.ckpt_q_cap < want_q || !a.ckpt_q)) {
+        if (a.ckpt_q) cudaFree(a.ckpt_q);
+        a.ckpt_q = nullptr;
+        a.ckpt_q_cap = 0;
+        ADJ_TRY(s, cudaMalloc((void **)&a.ckpt_q, want_q * sizeof(float4)));
+        a.ckpt_q_cap = want_q;
+    }
     cudaStream_t st = (cudaStream_t)stream;
     dt = pbd_internal_clamp_dt(s, dt);
     const size_t bytes = (size_t)n * sizeof(float4);
@@ -669,6 +847,9 @@ int pbd_rollout(pbd_system *s, float dt, uint32_t steps, uint32_t every, void *s
             const size_t off = (size_t)(t / every) * n;
             ADJ_TRY(s, cudaMemcpyAsync(a.ckpt_x + off, s->x, bytes, cudaMemcpyDeviceToDevice, st));
             ADJ_TRY(s, cudaMemcpyAsync(a.ckpt_v + off, s->v, bytes, cudaMemcpyDeviceToDevice, st));
+            if (nb)
+                ADJ_TRY(s, cudaMemcpyAsync(a.ckpt_q + (size_t)(t / every) * nb, s->bodies.quat, nb * sizeof(float4),
+                                           cudaMemcpyDeviceToDevice, st));
         }
         if (int rc = pbd_internal_enqueue_update(s, dt, st)) return rc;
     }
@@ -694,7 +875,7 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
     const bool batched = P.table != nullptr;
     const uint32_t iters = P.iterations;
     const size_t bytes = (size_t)n * sizeof(float4);
-    const size_t per_step = 2u + 2u * iters;
+    const size_t per_step = 2u + 3u * iters;
     const uint64_t launches0 = s->launches, steps0 = s->steps;
     // work arrays
     size_t rec_have = a.rec_cap;
@@ -724,6 +905,11 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
     }
     if (m) ADJ_TRY(s, cudaMemsetAsync(a.gstiff, 0, (size_t)m * sizeof(float), st));
     // the state after the rollout, restored at the end
+    const uint32_t nbod = s->bodies.count;
+    const size_t qbytes = (size_t)nbod * sizeof(float4);
+    if (nbod)
+        ADJ_TRY(s, cudaMemcpyAsync(a.ckpt_q + (size_t)a.nckpt * nbod, s->bodies.quat, qbytes, cudaMemcpyDeviceToDevice,
+                                   st));
     ADJ_TRY(s, cudaMemcpyAsync(a.save_x, s->x, bytes, cudaMemcpyDeviceToDevice, st));
     ADJ_TRY(s, cudaMemcpyAsync(a.save_v, s->v, bytes, cudaMemcpyDeviceToDevice, st));
     ADJ_TRY(s, cudaMemcpyAsync(a.save_xo, s->x_old, bytes, cudaMemcpyDeviceToDevice, st));
@@ -751,18 +937,21 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
         // recompute the segment from its checkpoint, recording
         ADJ_TRY(s, cudaMemcpyAsync(s->x, a.ckpt_x + (size_t)seg * n, bytes, cudaMemcpyDeviceToDevice, st));
         ADJ_TRY(s, cudaMemcpyAsync(s->v, a.ckpt_v + (size_t)seg * n, bytes, cudaMemcpyDeviceToDevice, st));
+        if (nbod)
+            ADJ_TRY(s, cudaMemcpyAsync(s->bodies.quat, a.ckpt_q + (size_t)seg * nbod, qbytes, cudaMemcpyDeviceToDevice,
+                                       st));
         for (uint32_t t = t0; t < t1; ++t)
             if (int rc = pbd_internal_enqueue_update(s, dt, st, a.rec + (t - t0) * per_step * n)) return rc;
         // reverse over its steps
         for (int t = (int)t1 - 1; t >= (int)t0; --t) {
             float4 *rec = a.rec + (size_t)(t - (int)t0) * per_step * n;
-            const float4 *xfin = rec + (size_t)(1 + 2 * iters) * n;
+            const float4 *xfin = rec + (size_t)(1 + 3 * iters) * n;
             // x_old of this step for the friction and wall terms
             ADJ_TRY(s, cudaMemcpyAsync(s->x_old, rec, bytes, cudaMemcpyDeviceToDevice, st));
             if (xsph) {
                 // XSPH over the last iteration's grid: gv (after XSPH) -> gv
                 // (after the velocity update), w3 = its position part
-                ADJ_TRY(s, cudaMemcpyAsync(s->x, rec + (size_t)(1 + 2 * (iters - 1)) * n, bytes,
+                ADJ_TRY(s, cudaMemcpyAsync(s->x, rec + (size_t)(1 + 3 * (iters - 1)) * n, bytes,
                                            cudaMemcpyDeviceToDevice, st));
                 if (int rc = pbd_internal_build_grid(s, st, false)) return rc;
                 ADJ_LAUNCH(k_adj_vel_of, nb, P, n, dt, xfin, rec, a.w1);
@@ -775,8 +964,15 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
             ADJ_LAUNCH(k_adj_velocity, nb, P, n, dt, a.gx, a.gv, a.gy, a.gxo);
             for (int it = (int)iters - 1; it >= 0; --it) {
                 const uint32_t left = iters - 1u - (uint32_t)it;
-                const float4 *xstart = rec + (size_t)(1 + 2 * it) * n;
-                const float4 *ysolve = rec + (size_t)(2 + 2 * it) * n;
+                const float4 *xstart = rec + (size_t)(1 + 3 * it) * n;
+                const float4 *ysolve = rec + (size_t)(2 + 3 * it) * n;
+                const float4 *zdist = rec + (size_t)(3 + 3 * it) * n;
+                // shape matching: gy (after shapes) -> gy (after pins)
+                if (s->bodies.count) {
+                    const BodyBuffers &bb = s->bodies;
+                    ADJ_LAUNCH(k_adj_shapes, blocks_for(bb.count * 32u), P, left, bb.count, bb.range, bb.stiff, bb.rest,
+                               zdist, a.gy);
+                }
                 // pins and distance constraints: gy (after pins) -> gt -> gy
                 if (c.count) {
                     ADJ_TRY(s, cudaMemcpyAsync(a.gt, a.gy, bytes, cudaMemcpyDeviceToDevice, st));
@@ -822,6 +1018,9 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
     ADJ_TRY(s, cudaMemcpyAsync(s->x, a.save_x, bytes, cudaMemcpyDeviceToDevice, st));
     ADJ_TRY(s, cudaMemcpyAsync(s->v, a.save_v, bytes, cudaMemcpyDeviceToDevice, st));
     ADJ_TRY(s, cudaMemcpyAsync(s->x_old, a.save_xo, bytes, cudaMemcpyDeviceToDevice, st));
+    if (nbod)
+        ADJ_TRY(s, cudaMemcpyAsync(s->bodies.quat, a.ckpt_q + (size_t)a.nckpt * nbod, qbytes, cudaMemcpyDeviceToDevice,
+                                   st));
     s->grid_valid = false;
     return PBD_OK;
 }

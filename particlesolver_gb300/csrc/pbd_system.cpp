@@ -470,8 +470,9 @@ uint32_t solve_mask(const pbd_system *s) {
 // iterations than the batch's most sits out the first ones (its particles
 // keep their predicted positions, so the grids it skips change nothing).
 // rec (the adjoint's recording, or nullptr): x before the step, then per
-// iteration x at its start and after the contact / fluid / wall pass, then
-// x after the last iteration (2 + 2 iterations states of n float4).
+// iteration x at its start, after the contact / fluid / wall pass and
+// after the distance constraints and pins, then x after the last iteration
+// (2 + 3 iterations states of n float4).
 int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullptr) {
     const pbd::DevParams &P = s->dev;
     const uint32_t n = s->n;
@@ -519,7 +520,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
             if (int rc = build_grid(s, st, it == 0)) return rc;
             L.reuse = nullptr;
         }
-        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 2 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
+        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 3 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (s->n_fluid) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
             CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, L, s->tpp, st));
@@ -530,17 +531,18 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
             CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, L,
                                           s->list_valid, s->tpp, st));
         }
-        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 2 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
+        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 3 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (dist_kernels) {
             Stage t(s, st, PBD_STAGE_DISTANCE, dist_kernels);
             CUDA_TRY(s, pbd::launch_distance(P, left, s->cons, s->x, true, true, st));
         }
+        if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(3 + 3 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (s->bodies.count) {
             Stage t(s, st, PBD_STAGE_SHAPES, 1);
             CUDA_TRY(s, pbd::launch_shapes(P, left, s->bodies, s->x, st));
         }
     }
-    if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 2 * iters) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
+    if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 3 * iters) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
     {
         Stage t(s, st, PBD_STAGE_VELOCITY, 1);
         CUDA_TRY(s, pbd::launch_velocity(P, n, dt, s->x, s->x_old, s->v, st));

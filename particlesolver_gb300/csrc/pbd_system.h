@@ -100,6 +100,8 @@ struct pbd_system {
         float dt = 0.f;
         uint32_t steps = 0, every = 0, nckpt = 0;
         float4 *ckpt_x = nullptr, *ckpt_v = nullptr;  // [nckpt][cap]
+        float4 *ckpt_q = nullptr;  // body rotations: [nckpt + 1][bodies] (the last: after the rollout)
+        size_t ckpt_q_cap = 0;
         size_t ckpt_cap = 0;                          // states allocated
         float4 *rec = nullptr;                        // segment recording
         size_t rec_cap = 0;                           // states allocated

@@ -13,7 +13,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from oracle import Oracle  # noqa: E402
-from particlesolver_gb300 import PBD_ERR_UNSUPPORTED, ParticleSystem, PbdError, default_params  # noqa: E402
+from particlesolver_gb300 import ParticleSystem, PbdError, default_params  # noqa: E402
 from particlesolver_gb300 import workloads as W  # noqa: E402
 from particlesolver_gb300.autograd import rollout  # noqa: E402
 
@@ -65,16 +65,19 @@ def gpu_gradients(sc, stiffness, steps, every, c):
 
 
 def oracle_loss(sc, stiffness, x0, v0, steps, c):
+    """L of the FP64 oracle from (x0, v0): the scene is loaded as given
+    (rigid bodies take their rest shapes from the scene's positions, as in
+    the differentiated rollout), then the state is set."""
     o = Oracle(default_params(**sc.params), sc.n)
+    W.apply_to(W.Scene(sc.name, sc.params, sc.pos_w, sc.phase, rest_density=sc.rest_density, pairs=sc.pairs,
+                       rest=sc.rest, stiffness=None if stiffness is None else np.asarray(stiffness),
+                       pins=sc.pins, pin_points=sc.pin_points, bodies=sc.bodies), o)
     pos = np.asarray(sc.pos_w, np.float64).copy()
     pos[:, :3] = x0
     vel = np.zeros((sc.n, 4))
     vel[:, :3] = v0
-    o.add_particles(pos, vel, sc.phase, sc.rest_density)
-    if sc.pairs is not None and len(sc.pairs):
-        o.add_distance_constraints(sc.pairs, sc.rest, stiffness)
-    if sc.pins is not None and len(sc.pins):
-        o.add_point_constraints(sc.pins, sc.pin_points)
+    o.set_positions(pos)
+    o.set_velocities(vel)
     for _ in range(steps):
         o.update(sc.dt)
     return float(np.sum(o.positions()[:, :3] * c))
@@ -236,13 +239,26 @@ def test_fluid_on_solid_gradient_matches_fd():
     check_directional(sc, 3, 2, seed=21, eps=1e-6)
 
 
-def test_unsupported_scenes_are_rejected():
-    sc = W.rigid_boxes(count=2)
-    sys = ParticleSystem(default_params(**sc.params), sc.n)
-    W.apply_to(sc, sys)
-    with pytest.raises(PbdError) as e:
-        sys.rollout(sc.dt, 2, 1)
-    assert e.value.code == PBD_ERR_UNSUPPORTED
+def spinning_boxes(stiffness, seed=5):
+    sc = W.rigid_boxes(count=3, stiffness=stiffness)
+    rng = np.random.default_rng(seed)
+    vel = np.zeros((sc.n, 4), np.float32)
+    for f, cnt, _ in sc.bodies:
+        w = rng.standard_normal(3) * 2.0
+        r = sc.pos_w[f:f + cnt, :3] - sc.pos_w[f:f + cnt, :3].mean(0)
+        vel[f:f + cnt, :3] = rng.standard_normal(3) + np.cross(w, r)
+    sc.vel = vel
+    return sc
+
+
+@pytest.mark.parametrize("stiffness,steps", [(1.0, 1), (1.0, 4), (0.6, 4)])
+def test_shape_matching_gradient_matches_fd(stiffness, steps):
+    """Shape matching of spinning boxes: the adjoint of the centre of mass
+    and of the polar rotation (tr S I - S) y = vee(R^T Rbar - Rbar^T R)."""
+    check_directional(spinning_boxes(stiffness), steps, 2, seed=30 + steps)
+
+
+def test_unsupported_and_state_errors():
     sys2 = ParticleSystem(default_params(**small_scene().params), 10)
     with pytest.raises(PbdError):
         sys2.backward_device(None, None, None, None, None)  # no rollout yet
