@@ -275,6 +275,78 @@ def run_batched(args, dev, stream, flush):
                                   f"granular column by coin flip (seeded)"}
 
 
+def time_scene(sc, stream, flush, steps, warmup=3):
+    """Steps/s of one scene replayed from its CUDA graph (per-step events,
+    L2 flushed before each step), with its per-stage times and launches."""
+    import torch
+
+    from particlesolver_gb300 import ParticleSystem, default_params
+    from particlesolver_gb300 import workloads as W
+
+    sh = stream.cuda_stream
+    sysm = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, sysm)
+    for _ in range(warmup):
+        sysm.update(sc.dt, sh)
+    sysm.autotune(sc.dt, 2, sh)
+    sysm.update_graph(sc.dt, 1, sh)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    sysm.reset_profile()
+    with torch.cuda.stream(stream):
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            sysm.update_graph(sc.dt, 1, sh)
+            b.record(stream)
+    torch.cuda.synchronize()
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    launches = sysm.profile()["kernel_launches"]
+    sysm.set_profiling(True)
+    sysm.reset_profile()
+    for _ in range(3):
+        sysm.update(sc.dt, sh)
+    prof = sysm.profile()
+    sysm.check_finite(sh)
+    sysm.close()
+    return {"value": steps / t, "unit": "steps/s", "ms_per_step": 1e3 * t / steps, "steps": steps,
+            "particles": sc.n, "gpu_launches": launches,
+            "stage_ms_per_step": {k: v / 3 for k, v in prof["stage_ms"].items() if v}}
+
+
+def run_other_configs(args, stream, flush):
+    """The mixed cloth / rope / rigid scene (833,536 particles) and the 2-D
+    granular column (1,600 particles, 600-step runs in the reference), each
+    on the GPU, the column also with the oracle on one host thread."""
+    from particlesolver_gb300 import workloads as W
+
+    out = {}
+    mixed = W.mixed_scene()
+    r = time_scene(mixed, stream, flush, args.other_steps)
+    r.update(workload=f"mixed: 256x256 cloth (stretch/shear/bend, pinned edges), 2000 ropes x 64, 10000 random-pose "
+                      f"4x4x4 shape-matched bodies; {mixed.info['constraints']} distance constraints, 4 iterations, "
+                      f"dt 1/60")
+    out["mixed_scene"] = r
+    col = W.granular_column()
+    r = time_scene(col, stream, flush, args.other_steps)
+    from oracle import Oracle
+    from particlesolver_gb300 import default_params
+
+    o = Oracle(default_params(**col.params), col.n, threads=1)
+    W.apply_to(col, o)
+    t0 = time.perf_counter()
+    k = 0
+    while k < 600 and time.perf_counter() - t0 < 10.0:
+        o.update(col.dt)
+        k += 1
+    cpu = k / (time.perf_counter() - t0)
+    r.update(workload="2-D granular column: 40x40 lattice spacing 2r, jitter U(+-0.01r), mu_s 0.5, mu_k 0.3, "
+                      "3 iterations, dt 1/60",
+             cpu_oracle_1_thread={"value": cpu, "unit": "steps/s", "steps": k, "kind": "port"})
+    out["granular_2d"] = r
+    return out
+
+
 def run_adjoint(args, dev, stream):
     """Differentiation: 64 batched cloth / rope / grain scenes (4,552
     particles each), 120 steps of 1/60 with checkpoints every 10.  Times one
@@ -297,35 +369,47 @@ def run_adjoint(args, dev, stream):
     x0 = torch.tensor(cat("pos_w"), device=dev)
     v_hidden = torch.tensor(cat("vel"), device=dev)
     s_hidden = torch.tensor(cat("stiffness"), device=dev)
-    with torch.cuda.stream(stream):
-        with torch.no_grad():
-            target, _ = rollout(sysm, s_hidden, x0, v_hidden, dt, T, every)
-        # one timed forward + backward at a parameter guess
-        s0 = torch.full((m,), 0.6, device=dev)
-        v_init = torch.zeros_like(v_hidden)
+    # on torch's current stream: the autograd engine runs the backward on
+    # the stream of the forward, and timing is wall clock between device
+    # synchronisations (the backward is a host-driven sequence of segments)
+    with torch.no_grad():
+        target, _ = rollout(sysm, s_hidden, x0, v_hidden, dt, T, every)
+    s0 = torch.full((m,), 0.6, device=dev)
+    v_init = torch.zeros_like(v_hidden)
+    # warm-up forward + backward (first launches, work-array allocation)
+    for _ in range(2):
         st = s0.clone().requires_grad_(True)
         v0 = v_init.clone().requires_grad_(True)
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        torch.cuda.synchronize()
-        e[0].record(stream)
         xT, _ = rollout(sysm, st, x0, v0, dt, T, every)
-        e[1].record(stream)
+        xT[:, :3].sum().backward()
+    fwd, bwd = [], []
+    for _ in range(3):
+        st = s0.clone().requires_grad_(True)
+        v0 = v_init.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xT, _ = rollout(sysm, st, x0, v0, dt, T, every)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
         loss = ((xT[:, :3] - target[:, :3]) ** 2).sum(1).mean()
         loss.backward()
-        e[2].record(stream)
         torch.cuda.synchronize()
-        fwd_ms, bwd_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
-        grains = torch.tensor(np.concatenate([sc.phase == 3 for sc in scenes]), device=dev)
-        t0 = time.perf_counter()
-        st_fit, v_fit, losses = fit(sysm, x0, target, s0, v_init, dt, T, every, args.adjoint_iters)
-        torch.cuda.synchronize()
-        fit_s = time.perf_counter() - t0
+        t2 = time.perf_counter()
+        fwd.append(1e3 * (t1 - t0))
+        bwd.append(1e3 * (t2 - t1))
+    fwd_ms, bwd_ms = statistics.median(fwd), statistics.median(bwd)
+    grains = torch.tensor(np.concatenate([sc.phase == 3 for sc in scenes]), device=dev)
+    t0 = time.perf_counter()
+    st_fit, v_fit, losses = fit(sysm, x0, target, s0, v_init, dt, T, every, args.adjoint_iters)
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
     s_err0 = float((s0 - s_hidden).abs().mean())
     s_err1 = float((st_fit - s_hidden).abs().mean())
     v_err0 = float((v_init - v_hidden)[grains, :3].norm(dim=1).mean())
     v_err1 = float((v_fit - v_hidden)[grains, :3].norm(dim=1).mean())
     return {"scenes": len(scenes), "particles": n, "constraints": m, "steps": T, "checkpoint_every": every,
             "dt": dt, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "timing": "wall clock between device synchronisations, median of 3 after 2 warm-up passes",
             "backward_over_forward": bwd_ms / fwd_ms, "particle_steps_per_s_fwd_bwd": n * T / ((fwd_ms + bwd_ms) * 1e-3),
             "fit_iterations": len(losses), "fit_s": fit_s, "loss_first": losses[0] if losses else None,
             "loss_last": losses[-1] if losses else None, "loss_min": min(losses) if losses else None,
@@ -452,6 +536,7 @@ def run_ours(args, world, rank, local_rank):
         sysm.close()
         batched = run_batched(args, dev, stream, flush)
     adjoint = run_adjoint(args, dev, stream) if args.adjoint_scenes else None
+    others = run_other_configs(args, stream, flush) if args.other_steps else None
 
     if rank != 0:
         return
@@ -509,6 +594,7 @@ def run_ours(args, world, rank, local_rank):
         "cpu_baseline": cpu,
         "batched": batched,
         "adjoint": adjoint,
+        "other_configs": others,
     }
     print(json.dumps(line), flush=True)
 
@@ -532,6 +618,7 @@ def main():
     ap.add_argument("--adjoint-scenes", type=int, default=64, help="differentiation measurement (0 = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=120)
     ap.add_argument("--adjoint-iters", type=int, default=20)
+    ap.add_argument("--other-steps", type=int, default=20, help="mixed scene / 2-D column measurement (0 = skip)")
     args = ap.parse_args()
     world, rank, local_rank = dist_env()
     if args.impl == "reference":

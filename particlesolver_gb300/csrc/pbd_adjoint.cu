@@ -355,10 +355,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_fluid_lbar(DevParams P0, uint32_
 // own lambda, plus every partner's contact term, fluid delta term and
 // lambda through x_j -- and the contact terms' part of the adjoint of
 // x_old_j.  A partner's lambda in x_j comes from perturbing only the pair
-// (i, j) term of its kept sums.
-template <bool B>
+// (i, j) term of its kept sums.  CONTACTS / FLUIDS: the scene has contact
+// particles / fluid (compile-time, so each variant carries only the dual
+// code it needs).
+template <bool B, bool CONTACTS, bool FLUIDS>
 __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint32_t n, uint32_t iter_left,
-                                                             bool contacts, bool fluids,
                                                              const float4 *__restrict__ sx,
                                                              const SortedAttr *__restrict__ sattr,
                                                              const uint32_t *__restrict__ sidx,
@@ -376,7 +377,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
     const uint32_t orig = sidx[j];
     const float4 guj4 = gu[j];
     const float3 guj = make_float3(guj4.x, guj4.y, guj4.z);
-    if (!scene_active<B>(P, iter_left) || !(contacts || fluids)) {
+    if (!scene_active<B>(P, iter_left) || !(CONTACTS || FLUIDS)) {
         gstart[orig] = make_float4(guj.x, guj.y, guj.z, 0.f);
         return;
     }
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
     const int phj = sattr[j].phase;
     const float3 prevj = f3(x_old[orig]);
     float3 gx = guj, go = make_float3(0.f, 0.f, 0.f);
-    if (contacts) {
+    if (CONTACTS) {
         const uint32_t nj = cnt[j];
         for_each_contact(P, j, pj, phj, sx, sattr, cell_first, [&](uint32_t i) {
             const float4 pi4 = sx[i];
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
             }
         });
     }
-    if (fluids) {
+    if (FLUIDS) {
         const float poly6_ref = P.poly6 * P.scorr_inv_ref;
         const bool jf = phj == kFluid;
         const float lam_j = fl1[j].z, div_j = fl2[j].w, lbar_j = lbar[j];
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
         }
     }
     gstart[orig] = make_float4(gx.x, gx.y, gx.z, 0.f);
-    if (contacts) {
+    if (CONTACTS) {
         const float4 o = gxo[orig];
         gxo[orig] = make_float4(o.x + go.x, o.y + go.y, o.z + go.z, 0.f);
     }
@@ -997,8 +998,23 @@ int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *d
                 if (fluids)
                     ADJ_LAUNCH(k_adj_fluid_lbar, nb, P, n, left, g.sorted_x, g.sorted_attr, g.cell_first, a.fl1, a.fl2,
                                a.gu, a.lbar);
-                ADJ_LAUNCH(k_adj_solve_gather, nb, P, n, left, contacts, fluids, g.sorted_x, g.sorted_attr,
-                           g.sorted_idx, g.cell_first, s->x_old, a.fl1, a.fl2, a.lbar, a.gu, a.cnt, a.gy, a.gxo);
+#define ADJ_GATHER(BB, CC, FF)                                                                            \
+    k_adj_solve_gather<BB, CC, FF><<<nb, kBlock, 0, st>>>(P, n, left, g.sorted_x, g.sorted_attr, g.sorted_idx,    \
+                                                          g.cell_first, s->x_old, a.fl1, a.fl2, a.lbar, a.gu,    \
+                                                          a.cnt, a.gy, a.gxo)
+                if (batched) {
+                    if (contacts && fluids) ADJ_GATHER(true, true, true);
+                    else if (contacts) ADJ_GATHER(true, true, false);
+                    else if (fluids) ADJ_GATHER(true, false, true);
+                    else ADJ_GATHER(true, false, false);
+                } else {
+                    if (contacts && fluids) ADJ_GATHER(false, true, true);
+                    else if (contacts) ADJ_GATHER(false, true, false);
+                    else if (fluids) ADJ_GATHER(false, false, true);
+                    else ADJ_GATHER(false, false, false);
+                }
+#undef ADJ_GATHER
+                ADJ_TRY(s, cudaGetLastError());
                 if (xsph && it == (int)iters - 1) {  // XSPH read this iteration's start positions
                     k_add4<<<nb, kBlock, 0, st>>>(n, a.gy, a.w3);
                     ADJ_TRY(s, cudaGetLastError());

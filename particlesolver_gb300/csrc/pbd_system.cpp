@@ -1197,7 +1197,7 @@ int pbd_list_reuses(pbd_system *s, uint32_t *count) {
     SYS_GUARD(s);
     if (!count) return fail(s, PBD_ERR_INVALID_ARGUMENT, "count is NULL");
     *count = 0;
-    if (!s->skin_words) return PBD_OK;
+    if (!s->skin_words || !(s->skin > 0.f)) return PBD_OK;
     CUDA_TRY(s, cudaDeviceSynchronize());
     CUDA_TRY(s, cudaMemcpy(count, s->skin_words + pbd::kSkinWords - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return PBD_OK;
