@@ -51,6 +51,25 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(seconds: float, world: int, device=None) -> float:
+    """The slowest rank's time: the job ends when it does (replicas run
+    independently, so this is the only cross-rank exchange)."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job units per second: every rank's units over the slowest
+    rank's time (weak scaling: per-rank work is fixed)."""
+    return world * units_per_rank / seconds
+
+
 def read_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -485,13 +504,8 @@ def run_ours(args, world, rank, local_rank):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_s = sum(step_ms) / 1e3
     launches = sysm.profile()["kernel_launches"]
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * args.steps / total_s
+    total_s = max_over_ranks(total_s, world, dev)
+    value = job_throughput(args.steps, world, total_s)
 
     # ---- per-stage device times (eager, events between stage groups)
     sysm.set_profiling(True)
@@ -521,14 +535,8 @@ def run_ours(args, world, rank, local_rank):
         sysm.update_graph(sc.dt, 1, sh)
         sysm._check(lib.pbd_get_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
         sysm._check(lib.pbd_get_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * e2e_steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = job_throughput(e2e_steps, world, e2e_s)
     sysm.check_finite(sh)
     reuses = sysm.list_reuses()
     batched = None
