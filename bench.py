@@ -565,6 +565,19 @@ def run_ours(args, world, rank, local_rank):
         traffic = traffic_tab["per_launch_bytes"][dom]
     step_bytes = (B_STEP_FIXED + 4 * B_ITER) * n
     ms_per_step = 1e3 * total_s / args.steps
+    # FP32 beside HBM: the dominant kernel's FP32 flops (instruction mix
+    # measured by ncu, profiles/) over its launch time, against the FP32
+    # FMA throughput measured here
+    from particlesolver_gb300 import measure_fp32_peak
+
+    fp32 = None
+    flops_pp = (traffic_tab or {}).get("fp32_flops_per_particle", {}).get(dom)
+    if flops_pp:
+        peak32 = measure_fp32_peak(sh)
+        ach32 = flops_pp * n / (dom_ms * 1e-3) / 1e9
+        fp32 = {"kernel": dom, "flops_per_particle": flops_pp, "achieved_gflops": ach32,
+                "peak_gflops": peak32, "frac": ach32 / peak32, "peak_source": "measured (pbd_measure_fp32_peak)",
+                "flops_source": "ncu instruction mix (profiles/dam_break_131k_fp32_mix.md)"}
 
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
@@ -594,6 +607,7 @@ def run_ours(args, world, rank, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "fp32": fp32,
         "stage_ms_per_step": {k: v / prof_steps for k, v in prof["stage_ms"].items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * n, "d2h_bytes_per_step": 2 * 16 * n,
                 "steps": e2e_steps},

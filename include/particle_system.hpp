@@ -58,7 +58,39 @@ class ParticleSystem {
     ParticleSystem(const ParticleSystem &) = delete;
     ParticleSystem &operator=(const ParticleSystem &) = delete;
 
-    void update(float deltaTime, cudaStream_t stream = nullptr) { check(pbd_update(sys_, deltaTime, stream)); }
+    // ParticleSystem::update (particlesystem.cpp:144-246): queued particles
+    // join first (addNewStuff), then one step.
+    void update(float deltaTime, cudaStream_t stream = nullptr) {
+        addNewStuff();
+        check(pbd_update(sys_, deltaTime, stream));
+    }
+
+    // Runtime insertion (particlesystem.cpp:249-350): queued here, added at
+    // the start of the next update().  A "shot" particle is solid (phase
+    // PBD_PHASE_SOLID, rest density 1.5) with jitter U(-0.01 r, 0.01 r) on
+    // x and y (seeded here; the reference used rand()); a fluid particle
+    // starts with velocity (0, -1, 0).  The reference silently dropped
+    // particles past capacity; here update() throws pbd::Error.
+    void setParticleToAdd(float3 pos, float3 vel, float mass) {
+        const float j = radius_ * 0.01f;
+        pos.x += (uniform() * 2.f - 1.f) * j;
+        pos.y += (uniform() * 2.f - 1.f) * j;
+        queue(pos, vel, mass, 1.5f, PBD_PHASE_SOLID);
+    }
+    void setFluidToAdd(float3 pos, float3 /*color*/, float mass, float density) {
+        queue(pos, make_float3(0.f, -1.f, 0.f), mass, density, PBD_PHASE_FLUID);
+    }
+    void addNewStuff() {
+        if (add_phase_.empty()) return;
+        const uint32_t n = (uint32_t)add_phase_.size();
+        const int rc = pbd_add_particles(sys_, n, add_pos_.data(), add_vel_.data(), add_phase_.data(),
+                                         add_rho_.data(), nullptr);
+        add_pos_.clear();
+        add_vel_.clear();
+        add_phase_.clear();
+        add_rho_.clear();
+        check(rc);
+    }
 
     void addFluid(int3 ll, int3 ur, float mass, float density, float3 /*color*/) {
         const int32_t a[3] = {ll.x, ll.y, ll.z}, b[3] = {ur.x, ur.y, ur.z};
@@ -108,6 +140,21 @@ class ParticleSystem {
     pbd_system *handle() { return sys_; }
 
   private:
+    void queue(float3 pos, float3 vel, float mass, float rho0, int32_t phase) {
+        const float w = 1.f / mass;
+        add_pos_.insert(add_pos_.end(), {pos.x, pos.y, pos.z, w});
+        add_vel_.insert(add_vel_.end(), {vel.x, vel.y, vel.z, 0.f});
+        add_phase_.push_back(phase);
+        add_rho_.push_back(rho0);
+    }
+    // splitmix64 in [0, 1)
+    float uniform() {
+        uint64_t z = (jitter_ += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (float)((z >> 40) * (1.0 / 16777216.0));
+    }
     void check(int rc, const pbd_system *s) const {
         if (rc) throw Error(rc, pbd_last_error(s));
     }
@@ -117,6 +164,9 @@ class ParticleSystem {
     float radius_ = 0.f;
     int3 minB_{}, maxB_{};
     uint64_t seed_ = 1;
+    uint64_t jitter_ = 0x5eedull;
+    std::vector<float> add_pos_, add_vel_, add_rho_;
+    std::vector<int32_t> add_phase_;
 };
 
 }  // namespace pbd

@@ -335,6 +335,12 @@ int pbd_autotune(pbd_system *sys, float dt, uint32_t steps, void *stream, pbd_tu
 
 /* --------------------------------------------------------------- timing */
 
+/* Measured FP32 FMA throughput of the current device in GFLOP/s (a
+ * kernel of independent fused multiply-adds on every SM, best of three
+ * timed launches): the denominator of an instruction-bound kernel's FP32
+ * fraction.  Synchronous; errors via pbd_last_error(NULL). */
+int pbd_measure_fp32_peak(double *gflops, void *stream);
+
 /* Kernel groups of one step, for the per-stage device timing (no
  * counterpart in the reference, whose only readout was an FPS counter,
  * cpu/src/view.cpp:66,189). */

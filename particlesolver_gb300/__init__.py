@@ -189,6 +189,7 @@ _SIGNATURES = {
     "pbd_set_distance_stiffness": ([_P, _U32, _P, _I, _P], _I),
     "pbd_rollout": ([_P, _F, _U32, _U32, _P], _I),
     "pbd_list_reuses": ([_P, _PU], _I),
+    "pbd_measure_fp32_peak": ([ctypes.POINTER(ctypes.c_double), _P], _I),
     "pbd_num_distance_constraints": ([_P], _U32),
     "pbd_backward": ([_P, _P, _P, _P, _P, _P, _P], _I),
     "pbd_load_state": ([_P, _P, ctypes.c_uint64], _I),
@@ -548,3 +549,13 @@ class ParticleSystem:
     def load_state(self, blob: bytes):
         buf = ctypes.create_string_buffer(blob, len(blob))
         self._check(self.lib.pbd_load_state(self.h, ctypes.cast(buf, ctypes.c_void_p), len(blob)))
+
+
+def measure_fp32_peak(stream=None) -> float:
+    """Measured FP32 FMA throughput of the current device, GFLOP/s."""
+    lib = load_library()
+    g = ctypes.c_double()
+    rc = lib.pbd_measure_fp32_peak(ctypes.byref(g), stream)
+    if rc:
+        raise PbdError(rc, lib.pbd_last_error(None).decode())
+    return g.value

@@ -18,7 +18,7 @@ CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_DIR = PKG_DIR / "_lib"
 LIB_NAME = "libpbd_gb300.so"
-SOURCES = ["pbd_kernels.cu", "pbd_system.cpp", "pbd_scenes.cpp", "pbd_noalloc.cu", "pbd_adjoint.cu"]
+SOURCES = ["pbd_kernels.cu", "pbd_system.cpp", "pbd_scenes.cpp", "pbd_noalloc.cu", "pbd_adjoint.cu", "pbd_peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
