@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define PBD_ABI_VERSION 1
+#define PBD_ABI_VERSION 2
 
 typedef enum pbd_status {
     PBD_OK = 0,
@@ -106,6 +106,13 @@ typedef struct pbd_params {
     uint32_t max_neighbors;  /* per-particle neighbour cap (500)            */
     float twod_z;            /* z of every particle in PBD_FLAG_TWOD mode   */
     uint32_t flags;          /* PBD_FLAG_*                                  */
+    float solid_density_weight; /* weight of a neighbour of phase >= CLOTH in
+                                a fluid particle's density and in its own
+                                constraint gradient: 1 = the GPU reference
+                                (every neighbour counts), 0 = the CPU
+                                reference's S_SOLID (totalfluidconstraint.h:
+                                30, .cpp:66-68,154); fluid-solid coupling
+                                in between (>= 0)                           */
 } pbd_params;
 
 typedef struct pbd_system pbd_system;

@@ -385,15 +385,19 @@ static void compute_lambdas(orc_system *s) {
                 double rlen = sqrt(r2);
                 double hm2 = h2 - r2, hm = h - rlen;
                 double wpoly = s->poly6 * hm2 * hm2 * hm2;
-                if (nb_mass) ro += pj[3] > 0 ? wpoly / pj[3] : 0.0;
-                else ro += wpoly / w;
+                /* a solid-like neighbour's weight in the density and in the
+                 * particle's own gradient (totalfluidconstraint.cpp:66-68,
+                 * 154); the pair gradient itself is not weighted */
+                const double sw = s->sphase[list[k]] >= PBD_PHASE_CLOTH ? (double)s->p.solid_density_weight : 1.0;
+                if (nb_mass) ro += pj[3] > 0 ? sw * wpoly / pj[3] : 0.0;
+                else ro += sw * wpoly / w;
                 double sg[3] = {0, 0, 0};
                 /* the cut-off is decided on the FP32 length, as the kernel does */
                 if (dist2f(s->sx32 + 4 * i, s->sx32 + 4 * list[k]) >= K_MIN_SPIKY2)
                     for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * (-s->spiky * hm * hm);
                 for (int d = 0; d < 3; ++d) {
                     sg[d] /= rho0;
-                    grad[d] -= sg[d];
+                    grad[d] -= sw * sg[d];
                     denom += sg[d] * sg[d];
                 }
             }

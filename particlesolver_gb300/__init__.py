@@ -35,6 +35,9 @@ FLAG_KERNEL_UNITS = 1 << 4
 HEADER = _build.ROOT / "include" / "pbd.h"
 
 
+ABI_VERSION = 2  # PBD_ABI_VERSION of include/pbd.h that these mirrors follow
+
+
 class PbdParams(ctypes.Structure):
     """Mirror of ``pbd_params`` (include/pbd.h)."""
 
@@ -61,7 +64,13 @@ class PbdParams(ctypes.Structure):
         ("max_neighbors", ctypes.c_uint32),
         ("twod_z", ctypes.c_float),
         ("flags", ctypes.c_uint32),
+        ("solid_density_weight", ctypes.c_float),
     ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.solid_density_weight = 1.0  # pbd_default_params' value
+        self.update(**kw)
 
     def as_dict(self) -> dict:
         out = {}
@@ -216,6 +225,8 @@ def load_library(build: bool = True) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = res
+    if lib.pbd_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{path} has ABI {lib.pbd_abi_version()}, this binding expects {ABI_VERSION}: rebuild it")
     _LIB = lib
     return lib
 

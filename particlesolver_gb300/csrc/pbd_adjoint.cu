@@ -233,9 +233,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_fluid_lambda(DevParams P0, uint3
         const float4 pj4 = sx[j];
         const LambdaTerm<float> t = lambda_term<float>(P, lift<float>(pi), lift<float>(f3(pj4)),
                                                        mass_factor(P, inv_w, pj4.w), spiky_r);
-        ro += t.ro;
+        const float sw = density_weight(P, sattr, j);
+        ro += t.ro * sw;
         denom += gdot(t.sg, t.sg);
-        grad = grad - t.sg;
+        grad = grad - t.sg * sw;
     });
     const float lam = lambda_of<float>(P, ro, denom, grad, inv_w, inv_rho0);
     const float div = (P.flags & kFlagDeltaOverRho0) ? a.rho0 : a.rho0 + (float)nb;
@@ -432,9 +433,10 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
                 gx = add3(gx, contract(t, make_float3(guj.x / div_j, guj.y / div_j, guj.z / div_j), 0));
                 const LambdaTerm<Dual<3>> lt =
                     lambda_term<Dual<3>>(P, pjd, lift<Dual<3>>(pi), mass_factor(P, inv_wj, pi4.w), -P.spiky * inv_rho0_j);
-                ro = ro + lt.ro;
+                const float sw = density_weight(P, sattr, i);
+                ro = ro + lt.ro * sw;
                 denom = denom + gdot(lt.sg, lt.sg);
-                grad = grad - lt.sg;
+                grad = grad - lt.sg * sw;
             }
             if (sattr[i].phase == kFluid) {
                 // partner's delta term, in x_j
@@ -448,10 +450,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_solve_gather(DevParams P0, uint3
                 const float mf = mass_factor(P, inv_wi, pj4.w), sr = -P.spiky * inv_rho0_i;
                 const LambdaTerm<float> tv = lambda_term<float>(P, lift<float>(pi), lift<float>(pj), mf, sr);
                 const LambdaTerm<Dual<3>> td = lambda_term<Dual<3>>(P, lift<Dual<3>>(pi), pjd, mf, sr);
+                const float sw = density_weight(P, sattr, j);  // j's weight in i's sums
                 const float4 s1 = fl1[i], s2 = fl2[i];
-                const Dual<3> ro_i = cst<Dual<3>>(s1.x - tv.ro) + td.ro;
+                const Dual<3> ro_i = cst<Dual<3>>(s1.x - tv.ro * sw) + td.ro * sw;
                 const Dual<3> de_i = cst<Dual<3>>(s1.y - gdot(tv.sg, tv.sg)) + gdot(td.sg, td.sg);
-                const V3<Dual<3>> gr_i = lift<Dual<3>>(make_float3(s2.x + tv.sg.x, s2.y + tv.sg.y, s2.z + tv.sg.z)) - td.sg;
+                const V3<Dual<3>> gr_i =
+                    lift<Dual<3>>(make_float3(s2.x + sw * tv.sg.x, s2.y + sw * tv.sg.y, s2.z + sw * tv.sg.z)) - td.sg * sw;
                 const Dual<3> li = lambda_of<Dual<3>>(P, ro_i, de_i, gr_i, inv_wi, inv_rho0_i);
                 const float lb = lbar[i];
                 gx = make_float3(gx.x + lb * li.d[0], gx.y + lb * li.d[1], gx.z + lb * li.d[2]);

@@ -59,6 +59,7 @@ struct DevParams {
     uint32_t max_nb;
     float twod_z;
     uint32_t flags;
+    float solid_w;       // density weight of neighbours of phase >= CLOTH
     float rands[6];      // wall jitter uniforms
     uint32_t iterations; // solver iterations per step
     float max_dt;        // step length clamp
@@ -165,6 +166,18 @@ __device__ __forceinline__ bool scene_active(const DevParams &P, uint32_t iter_l
 }
 
 #endif  // __CUDACC__
+
+#if defined(__CUDACC__)
+// Weight of neighbour j in a fluid particle's density sum and own gradient
+// (pbd_params.solid_density_weight for phases >= CLOTH, else 1); the phase
+// is only read when the weight is not 1.
+template <class AttrPtr>
+__device__ __forceinline__ float density_weight(const DevParams &P, AttrPtr sattr, uint32_t j) {
+    float w = 1.f;
+    if (P.solid_w != 1.f && sattr[j].phase >= kCloth) w = P.solid_w;
+    return w;
+}
+#endif
 
 // Per-particle attributes gathered into sorted order with the positions.
 struct __align__(8) SortedAttr {

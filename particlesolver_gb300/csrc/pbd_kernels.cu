@@ -423,19 +423,22 @@ __device__ __forceinline__ uint32_t group_walk(const DevParams &P, const Group<T
 // Per-neighbour terms of findLambdasD (integration_kernel.cuh:561-589),
 // evaluated under the neighbour mask `ok` so the candidate loop has no
 // data-dependent branch: poly6 weight, and the spiky gradient over rho0
-// (zero below the reference's 1e-4 length cut-off).
+// (zero below the reference's 1e-4 length cut-off).  sw: the neighbour's
+// density weight (density_weight), applied to its density term and to the
+// particle's own gradient; the pair gradient in the denominator is not
+// weighted (the CPU reference's grad(), totalfluidconstraint.cpp:145-158).
 struct LambdaAcc {
     float ro, denom;
     float3 grad;
     __device__ __forceinline__ void add(const DevParams &P, bool ok, float d2, float3 dr, float mass_factor,
-                                        float spiky_r) {
+                                        float spiky_r, float sw = 1.f) {
         const float hm2 = P.h2 - d2;
-        ro += ok ? P.poly6 * hm2 * hm2 * hm2 * mass_factor : 0.f;
+        ro += ok ? P.poly6 * hm2 * hm2 * hm2 * mass_factor * sw : 0.f;
         const float rs = rsqrtf(fmaxf(d2, kMinSpiky2));
         const float hm = P.h - d2 * rs;
         const float sc = (ok && d2 >= kMinSpiky2) ? spiky_r * hm * hm * rs : 0.f;
         const float3 sg = dr * sc;
-        grad -= sg;
+        grad -= sg * sw;
         denom += dot3(sg, sg);
     }
 };
@@ -483,7 +486,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
                 const bool ok = d2 < P.h2 && j != i;
                 nb += ok ? 1u : 0u;
                 const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-                acc.add(P, ok, d2, pi - f3(pj), mf, spiky_r);
+                acc.add(P, ok, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
             }
             return true;
         });
@@ -496,9 +499,9 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
         group_walk<TPP>(
             P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
             [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
-            [&](uint32_t, const float4 &pj, float d2) {
+            [&](uint32_t j, const float4 &pj, float d2) {
                 const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-                acc.add(P, true, d2, pi - f3(pj), mf, spiky_r);
+                acc.add(P, true, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
             });
         acc.ro = G.sum(acc.ro);
         acc.denom = G.sum(acc.denom);
@@ -821,15 +824,15 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
     const float inv_rho0 = 1.f / a.rho0;
     const float spiky_r = -P.spiky * inv_rho0;
     LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-    auto add = [&](const float4 &pj, float d2) {
+    auto add = [&](uint32_t j, const float4 &pj, float d2) {
         const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-        acc.add(P, true, d2, pi - f3(pj), mf, spiky_r);
+        acc.add(P, true, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
     };
     if (reuse) {
         for_each_listed(L, i, L.count[i], [&](uint32_t j) {
             const float4 pj = __ldg(sx + j);
             const float d2 = dist2_exact(pi, f3(pj));
-            if (d2 < h2) add(pj, d2);
+            if (d2 < h2) add(j, pj, d2);
         });
     } else {
         const int3 g = grid_pos(P, pi);
@@ -874,7 +877,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
             for_each_listed(L, i, cnt, [&](uint32_t j) {
                 const float4 pj = __ldg(sx + j);
                 const float d2 = dist2_exact(pi, f3(pj));
-                if (!SKIN || d2 < h2) add(pj, d2);
+                if (!SKIN || d2 < h2) add(j, pj, d2);
             });
         } else {
             if (SKIN) atomicOr(L.ovf, 1u);  // this list cannot be reused
@@ -882,7 +885,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
             group_walk<1>(
                 P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
                 [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
-                [&](uint32_t, const float4 &pj, float d2) { add(pj, d2); });
+                [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2); });
         }
     }
     const float ro = acc.ro + P.poly6_self * inv_w;

@@ -49,6 +49,10 @@ int validate_params(const pbd_params *p, std::string &why) {
     if (p->max_neighbors == 0) { why = "max_neighbors must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
     if (!(p->scorr_dq >= 0.f && p->scorr_dq < 1.f)) { why = "scorr_dq must be in [0, 1)"; return PBD_ERR_INVALID_ARGUMENT; }
     if (p->flags & ~PBD_FLAGS_ALL) { why = "unknown bits in flags"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->solid_density_weight >= 0.f) || !std::isfinite(p->solid_density_weight)) {
+        why = "solid_density_weight must be finite and >= 0";
+        return PBD_ERR_INVALID_ARGUMENT;
+    }
     return PBD_OK;
 }
 
@@ -98,6 +102,7 @@ pbd::DevParams make_dev(const pbd_params &p, const float rands[6]) {
     d.max_nb = p.max_neighbors;
     d.twod_z = p.twod_z;
     d.flags = p.flags;
+    d.solid_w = p.solid_density_weight;
     for (int k = 0; k < 6; ++k) d.rands[k] = rands[k];
     d.iterations = p.iterations;
     d.max_dt = p.max_dt;
@@ -621,6 +626,7 @@ void pbd_default_params(pbd_params *p) {
     p->max_neighbors = 500;
     p->twod_z = 0.f;
     p->flags = 0;
+    p->solid_density_weight = 1.f;
 }
 
 const char *pbd_last_error(const pbd_system *s) {

@@ -16,7 +16,9 @@ def test_library_builds_and_loads():
     path = _build.build()
     assert path.exists()
     lib = pbd.load_library()
-    assert lib.pbd_abi_version() == 1
+    from particlesolver_gb300 import ABI_VERSION
+
+    assert lib.pbd_abi_version() == ABI_VERSION
 
 
 def test_every_header_symbol_is_exported():
@@ -60,6 +62,7 @@ def test_default_params_are_reference_values():
     assert list(p.grid_size) == [64, 64, 64] and p.iterations == 5
     assert abs(p.relaxation - 0.01) < 1e-9 and p.max_neighbors == 500
     assert list(p.box_min) == [-50, 0, -50] and list(p.box_max) == [50, 200, 50]
+    assert p.solid_density_weight == 1.0  # the GPU reference: every neighbour counts
 
 
 def test_create_without_gpu_fails_cleanly():

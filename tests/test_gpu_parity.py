@@ -98,6 +98,43 @@ def test_pbf_lambda_and_delta_reference_constants(flags):
     assert_projection(g.positions(), o.positions(), sc.pos_w, TOL_STAGE)
 
 
+def fluid_around_solid():
+    """A fluid block with a solid column through it and solid grains
+    below: fluid particles with solid neighbours."""
+    a = W.reference_fluid(ll=(-4, 0, -3), ur=(4, 4, 3), density=2.0, mass=1.0, seed=3)
+    inside = (np.abs(a.pos_w[:, 0]) < 1.0) & (np.abs(a.pos_w[:, 2]) < 1.0)
+    phase = a.phase.copy()
+    phase[inside] = W.PHASE_SOLID
+    return W.Scene("fluid_solid", a.params, a.pos_w, phase, rest_density=a.rest_density)
+
+
+@pytest.mark.parametrize("weight", [0.0, 0.5, 1.0])
+def test_fluid_solid_coupling_weight(weight):
+    """pbd_params.solid_density_weight: solid-like neighbours in a fluid
+    particle's density and own gradient (0 = the CPU reference's S_SOLID,
+    1 = the GPU reference)."""
+    sc = fluid_around_solid()
+    g, o = make_pair(sc, solid_density_weight=weight)
+    g.build_grid()
+    o.build_grid()
+    g.solve_fluids()
+    o.solve_fluids()
+    assert norm_err(g.lambdas(), o.lambdas()) < TOL_STAGE
+    assert_projection(g.positions(), o.positions(), sc.pos_w, TOL_STAGE)
+
+
+def test_fluid_solid_weight_changes_lambda():
+    sc = fluid_around_solid()
+    out = []
+    for weight in (0.0, 1.0):
+        g, _ = make_pair(sc, solid_density_weight=weight)
+        g.build_grid()
+        g.solve_fluids()
+        out.append(g.lambdas())
+    fluid = sc.phase == W.PHASE_FLUID
+    assert np.max(np.abs(out[0][fluid] - out[1][fluid])) > 1e-3
+
+
 @pytest.mark.parametrize("dims,cell_div", [((16, 16, 8), 1), ((40, 24, 20), 1), ((24, 20, 12), 2),
                                            ((20, 16, 12), 3)])
 def test_pbf_dam_break_block_one_iteration(dims, cell_div):
