@@ -22,10 +22,18 @@ def _pbd_params_type():
     return PbdParams
 
 
-def load():
-    global _LIB
-    if _LIB is None:
-        path = _buildmod.build_oracle()
+_LIB_DUAL = None
+
+
+def load(dual: bool = False):
+    """The FP64 oracle, or (dual=True) the same source on dual numbers."""
+    global _LIB, _LIB_DUAL
+    if dual and _LIB_DUAL is not None:
+        return _LIB_DUAL
+    if not dual and _LIB is not None:
+        return _LIB
+    if True:
+        path = _buildmod.build_oracle_dual() if dual else _buildmod.build_oracle()
         lib = ctypes.CDLL(str(path))
         P = ctypes.c_void_p
         PD = ctypes.POINTER(ctypes.c_double)
@@ -61,12 +69,18 @@ def load():
             "orc_get_lambdas": ([P, PD], None),
             "orc_get_neighbor_counts": ([P, PU, PU], None),
         }
+        if dual:
+            sig["orc_seed_tangents"] = ([P, PD, PD, PD], None)
+            sig["orc_get_tangents"] = ([P, PD, PD], None)
         for name, (a, r) in sig.items():
             f = getattr(lib, name)
             f.argtypes = a
             f.restype = r
-        _LIB = lib
-    return _LIB
+        if dual:
+            _LIB_DUAL = lib
+        else:
+            _LIB = lib
+    return lib
 
 
 def _d(a):
@@ -77,8 +91,10 @@ def _d(a):
 class Oracle:
     """FP64 replay of the reference step with the same stage API as the CUDA system."""
 
+    _dual = False
+
     def __init__(self, params, capacity: int, threads: int = 0):
-        self.lib = load()
+        self.lib = load(self._dual)
         self.lib.orc_set_threads(int(threads))
         self.params = params
         self.s = self.lib.orc_create(ctypes.byref(params), int(capacity))
@@ -205,3 +221,33 @@ class Oracle:
         pu = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))  # noqa: E731
         self.lib.orc_get_neighbor_counts(self.s, pu(f), pu(c))
         return f, c
+
+
+class OracleDual(Oracle):
+    """The oracle on forward-mode dual numbers: seed a direction in
+    (positions, velocities, stiffness), run the same stages, read the exact
+    directional derivative of the FP64 replay (branches as in the values)."""
+
+    _dual = True
+
+    def seed_tangents(self, dx=None, dv=None, dstiffness=None):
+        n = self.num_particles
+        args = []
+        for a, shape in ((dx, (n, 4)), (dv, (n, 4))):
+            if a is None:
+                args.append(None)
+                continue
+            a = np.asarray(a, np.float64)
+            if a.shape[-1] == 3:
+                a = np.concatenate([a, np.zeros((n, 1))], 1)
+            args.append(_d(a.reshape(shape))[0])
+        st = None if dstiffness is None else _d(dstiffness)[0]
+        ptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        self.lib.orc_seed_tangents(self.s, ptr(args[0]), ptr(args[1]), ptr(st))
+
+    def tangents(self):
+        n = self.num_particles
+        dx = np.empty((n, 4))
+        dv = np.empty((n, 4))
+        self.lib.orc_get_tangents(self.s, _d(dx)[1], _d(dv)[1])
+        return dx, dv

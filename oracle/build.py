@@ -21,6 +21,7 @@ BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 REFERENCE = Path(os.environ.get("PBD_REFERENCE_DIR", "/root/reference"))
 ORACLE_LIB = BUILD / "libpbd_oracle.so"
+ORACLE_DUAL_LIB = BUILD / "libpbd_oracle_dual.so"
 
 
 def _cc() -> str:
@@ -55,6 +56,19 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
+def build_oracle_dual(force: bool = False) -> Path:
+    """The same restatement compiled as C++ on dual numbers (oracle/dual.hpp):
+    forward-mode directional derivatives of the FP64 replay."""
+    srcs = [HERE / "pbd_oracle.c", HERE / "pbd_oracle.h", HERE / "dual.hpp", ROOT / "include" / "pbd.h"]
+    if force or _stale(ORACLE_DUAL_LIB, srcs):
+        BUILD.mkdir(exist_ok=True)
+        tmp = ORACLE_DUAL_LIB.with_suffix(".tmp.so")
+        _run([_cxx(), "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-DORC_DUAL",
+              "-I", str(ROOT / "include"), "-I", str(HERE), "-x", "c++", str(HERE / "pbd_oracle.c"), "-o", str(tmp)])
+        os.replace(tmp, ORACLE_DUAL_LIB)
+    return ORACLE_DUAL_LIB
+
+
 def reference_available() -> bool:
     return (REFERENCE / "gpu" / "src" / "cuda" / "integration_kernel.cuh").exists()
 
@@ -69,7 +83,7 @@ def build_reference(force: bool = False) -> dict[str, Path]:
 
 
 def build_all(force: bool = False) -> dict[str, Path]:
-    out = {"oracle": build_oracle(force)}
+    out = {"oracle": build_oracle(force), "oracle_dual": build_oracle_dual(force)}
     out.update(build_reference(force))
     return out
 

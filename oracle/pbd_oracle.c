@@ -26,6 +26,15 @@
 #include <omp.h>
 #endif
 
+/* The arithmetic type: double, or (compiled as C++ with ORC_DUAL, see
+ * oracle/dual.hpp) a dual number carrying one directional derivative. */
+#ifdef ORC_DUAL
+#include "dual.hpp"
+#else
+typedef double real;
+#define R_VAL(x) (x)
+#endif
+
 #define K_EPS 0.001            /* EPS, integration_kernel.cuh:20        */
 #define K_MIN_SPIKY2 1e-8f     /* |r| < 1e-4, integration_kernel.cuh:580,625, decided on |r|^2 */
 #define K_MIN_DIST 0.0001      /* solver_kernel.cuh:57                  */
@@ -39,24 +48,28 @@ struct orc_system {
     double poly6, spiky, poly6_self, scorr_inv_ref, scorr_k, relax, ws, wk;
     double rands[6];
     /* particle state, original order */
-    double *x, *v, *x_old, *rho0;
+    real *x, *v, *x_old;
+    double *rho0;
     int32_t *phase;
     /* grid */
     uint32_t *hash, *sorted_idx, *cell_first;
     int grid_valid;
-    double *sx, *srho0;       /* sorted FP64 positions (4n), rest densities */
+    real *sx;                 /* sorted FP64 positions (4n)               */
+    double *srho0;            /* sorted rest densities                    */
     float *sx32;              /* sorted FP32 positions (4n) for the tests  */
     int32_t *sphase;
-    double *lambda;           /* sorted order */
+    real *lambda;             /* sorted order */
     uint32_t *nb_fluid, *nb_contact;  /* original order */
     /* distance constraints (add order) and pins */
     uint32_t m, m_cap, *da, *db;
-    double *drest, *dstiff;
+    double *drest;
+    real *dstiff;
     uint32_t npin, pin_cap, *pin_idx;
     double *pin_pts;
     /* rigid bodies */
     uint32_t nb, nb_cap, *bfirst, *bcount;
-    double *bstiff, *bquat;   /* 4 per body: x y z w */
+    double *bstiff;
+    real *bquat;              /* 4 per body: x y z w */
     double *brest;            /* 4 per particle of the body: q xyz, mass; indexed by particle */
 };
 
@@ -154,19 +167,19 @@ orc_system *orc_create(const pbd_params *params, uint32_t cap) {
     s->relax = ku ? (double)params->relaxation / (h * h) : (double)params->relaxation;
     s->ws = sqrt((double)params->wall_static_friction);
     s->wk = sqrt((double)params->wall_kinetic_friction);
-    s->x = (double *)calloc(4ull * cap, sizeof(double));
-    s->v = (double *)calloc(4ull * cap, sizeof(double));
-    s->x_old = (double *)calloc(4ull * cap, sizeof(double));
+    s->x = (real *)calloc(4ull * cap, sizeof(real));
+    s->v = (real *)calloc(4ull * cap, sizeof(real));
+    s->x_old = (real *)calloc(4ull * cap, sizeof(real));
     s->rho0 = (double *)calloc(cap, sizeof(double));
     s->phase = (int32_t *)calloc(cap, sizeof(int32_t));
     s->hash = (uint32_t *)calloc(cap, sizeof(uint32_t));
     s->sorted_idx = (uint32_t *)calloc(cap, sizeof(uint32_t));
     s->cell_first = (uint32_t *)calloc((size_t)s->cells + 1, sizeof(uint32_t));
-    s->sx = (double *)calloc(4ull * cap, sizeof(double));
+    s->sx = (real *)calloc(4ull * cap, sizeof(real));
     s->srho0 = (double *)calloc(cap, sizeof(double));
     s->sx32 = (float *)calloc(4ull * cap, sizeof(float));
     s->sphase = (int32_t *)calloc(cap, sizeof(int32_t));
-    s->lambda = (double *)calloc(cap, sizeof(double));
+    s->lambda = (real *)calloc(cap, sizeof(real));
     s->nb_fluid = (uint32_t *)calloc(cap, sizeof(uint32_t));
     s->nb_contact = (uint32_t *)calloc(cap, sizeof(uint32_t));
     s->brest = (double *)calloc(4ull * cap, sizeof(double));
@@ -210,7 +223,7 @@ int orc_add_distance_constraints(orc_system *s, uint32_t m, const uint32_t *pair
         s->da = (uint32_t *)xrealloc(s->da, s->m_cap * sizeof(uint32_t));
         s->db = (uint32_t *)xrealloc(s->db, s->m_cap * sizeof(uint32_t));
         s->drest = (double *)xrealloc(s->drest, s->m_cap * sizeof(double));
-        s->dstiff = (double *)xrealloc(s->dstiff, s->m_cap * sizeof(double));
+        s->dstiff = (real *)xrealloc(s->dstiff, s->m_cap * sizeof(real));
     }
     for (uint32_t c = 0; c < m; ++c) {
         s->da[s->m] = pairs[2 * c];
@@ -245,19 +258,19 @@ int orc_add_rigid_body(orc_system *s, uint32_t first, uint32_t count, double sti
         s->bfirst = (uint32_t *)xrealloc(s->bfirst, s->nb_cap * sizeof(uint32_t));
         s->bcount = (uint32_t *)xrealloc(s->bcount, s->nb_cap * sizeof(uint32_t));
         s->bstiff = (double *)xrealloc(s->bstiff, s->nb_cap * sizeof(double));
-        s->bquat = (double *)xrealloc(s->bquat, 4ull * s->nb_cap * sizeof(double));
+        s->bquat = (real *)xrealloc(s->bquat, 4ull * s->nb_cap * sizeof(real));
     }
     double c[3] = {0, 0, 0}, msum = 0;
     for (uint32_t k = first; k < first + count; ++k) {
-        double m = 1.0 / (double)(float)s->x[4 * k + 3];
-        for (int d = 0; d < 3; ++d) c[d] += m * s->x[4 * k + d];
+        double m = 1.0 / (double)(float)R_VAL(s->x[4 * k + 3]);
+        for (int d = 0; d < 3; ++d) c[d] += m * R_VAL(s->x[4 * k + d]);
         msum += m;
     }
     for (int d = 0; d < 3; ++d) c[d] /= msum;
     for (uint32_t k = first; k < first + count; ++k) {
         /* rounded to FP32 like the CUDA path's stored rest offsets */
-        for (int d = 0; d < 3; ++d) s->brest[4 * k + d] = (double)(float)(s->x[4 * k + d] - c[d]);
-        s->brest[4 * k + 3] = (double)(float)(1.0 / s->x[4 * k + 3]);
+        for (int d = 0; d < 3; ++d) s->brest[4 * k + d] = (double)(float)(R_VAL(s->x[4 * k + d]) - c[d]);
+        s->brest[4 * k + 3] = (double)(float)(1.0 / R_VAL(s->x[4 * k + 3]));
     }
     s->bfirst[s->nb] = first;
     s->bcount[s->nb] = count;
@@ -283,7 +296,7 @@ void orc_integrate(orc_system *s, double dt) {
     for (uint32_t i = 0; i < s->n; ++i) {
         for (int d = 0; d < 4; ++d) s->x_old[4 * i + d] = s->x[4 * i + d];
         for (int d = 0; d < 3; ++d) {
-            double vv = s->v[4 * i + d] + (double)s->p.gravity[d] * dt;
+            real vv = s->v[4 * i + d] + (double)s->p.gravity[d] * dt;
             s->x[4 * i + d] += vv * dt;
         }
     }
@@ -298,7 +311,7 @@ void orc_build_grid(orc_system *s) {
     const uint32_t n = s->n;
     memset(s->cell_first, 0, ((size_t)s->cells + 1) * sizeof(uint32_t));
     for (uint32_t i = 0; i < n; ++i) {
-        float p[3] = {(float)s->x[4 * i], (float)s->x[4 * i + 1], (float)s->x[4 * i + 2]};
+        float p[3] = {(float)R_VAL(s->x[4 * i]), (float)R_VAL(s->x[4 * i + 1]), (float)R_VAL(s->x[4 * i + 2])};
         int g[3];
         grid_cell(s, p, g);
         s->hash[i] = grid_hash(s, g);
@@ -321,7 +334,7 @@ void orc_build_grid(orc_system *s) {
         uint32_t i = s->sorted_idx[p];
         for (int d = 0; d < 4; ++d) {
             s->sx[4 * p + d] = s->x[4 * i + d];
-            s->sx32[4 * p + d] = (float)s->x[4 * i + d];
+            s->sx32[4 * p + d] = (float)R_VAL(s->x[4 * i + d]);
         }
         s->sphase[p] = s->phase[i];
         s->srho0[p] = s->rho0[i];
@@ -374,24 +387,25 @@ static void compute_lambdas(orc_system *s) {
             }
             uint32_t nb = fluid_neighbors(s, i, list);
             s->nb_fluid[s->sorted_idx[i]] = nb;
-            const double *pi = s->sx + 4 * i;
-            const double w = pi[3], rho0 = s->srho0[i];
+            const real *pi = s->sx + 4 * i;
+            const real w = pi[3];
+            const double rho0 = s->srho0[i];
             const double h = s->p.kernel_radius, h2 = h * h;
-            double ro = 0, denom = 0, grad[3] = {0, 0, 0};
+            real ro = 0, denom = 0, grad[3] = {0, 0, 0};
             for (uint32_t k = 0; k < nb; ++k) {
-                const double *pj = s->sx + 4 * list[k];
-                double r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
-                double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-                double rlen = sqrt(r2);
-                double hm2 = h2 - r2, hm = h - rlen;
-                double wpoly = s->poly6 * hm2 * hm2 * hm2;
+                const real *pj = s->sx + 4 * list[k];
+                real r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+                real r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+                real rlen = sqrt(r2);
+                real hm2 = h2 - r2, hm = h - rlen;
+                real wpoly = s->poly6 * hm2 * hm2 * hm2;
                 /* a solid-like neighbour's weight in the density and in the
                  * particle's own gradient (totalfluidconstraint.cpp:66-68,
                  * 154); the pair gradient itself is not weighted */
                 const double sw = s->sphase[list[k]] >= PBD_PHASE_CLOTH ? (double)s->p.solid_density_weight : 1.0;
                 if (nb_mass) ro += pj[3] > 0 ? sw * wpoly / pj[3] : 0.0;
                 else ro += sw * wpoly / w;
-                double sg[3] = {0, 0, 0};
+                real sg[3] = {0, 0, 0};
                 /* the cut-off is decided on the FP32 length, as the kernel does */
                 if (dist2f(s->sx32 + 4 * i, s->sx32 + 4 * list[k]) >= K_MIN_SPIKY2)
                     for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * (-s->spiky * hm * hm);
@@ -409,31 +423,31 @@ static void compute_lambdas(orc_system *s) {
     }
 }
 
-static double scorr_pow(const orc_system *s, double ratio) { return pow(ratio, (double)s->p.scorr_n); }
+static real scorr_pow(const orc_system *s, real ratio) { return pow(ratio, (double)s->p.scorr_n); }
 
 /* solveFluidsD (integration_kernel.cuh:596-642). */
-static void fluid_delta(const orc_system *s, uint32_t i, uint32_t *list, double out[3]) {
+static void fluid_delta(const orc_system *s, uint32_t i, uint32_t *list, real out[3]) {
     uint32_t nb = fluid_neighbors(s, i, list);
-    const double *pi = s->sx + 4 * i;
+    const real *pi = s->sx + 4 * i;
     const double h = s->p.kernel_radius, h2 = h * h;
-    double delta[3] = {0, 0, 0};
+    real delta[3] = {0, 0, 0};
     for (uint32_t k = 0; k < nb; ++k) {
         uint32_t j = list[k];
-        const double *pj = s->sx + 4 * j;
-        double r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
-        double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-        double rlen = sqrt(r2);
-        double hm2 = h2 - r2, hm = h - rlen;
-        double sc = -s->spiky * hm * hm;
-        double sg[3];
+        const real *pj = s->sx + 4 * j;
+        real r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+        real r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        real rlen = sqrt(r2);
+        real hm2 = h2 - r2, hm = h - rlen;
+        real sc = -s->spiky * hm * hm;
+        real sg[3];
         if (dist2f(s->sx32 + 4 * i, s->sx32 + 4 * j) < K_MIN_SPIKY2) {
             sg[0] = 0; sg[1] = K_EPS * sc; sg[2] = 0;
         } else {
             for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * sc;
         }
-        double ratio = s->poly6 * hm2 * hm2 * hm2 * s->scorr_inv_ref;
-        double corr = -s->scorr_k * scorr_pow(s, ratio);
-        double coef = s->lambda[i] + s->lambda[j] + corr;
+        real ratio = s->poly6 * hm2 * hm2 * hm2 * s->scorr_inv_ref;
+        real corr = -s->scorr_k * scorr_pow(s, ratio);
+        real coef = s->lambda[i] + s->lambda[j] + corr;
         for (int d = 0; d < 3; ++d) delta[d] += coef * sg[d];
     }
     double div = (s->p.flags & PBD_FLAG_DELTA_OVER_RHO0) ? s->srho0[i] : s->srho0[i] + (double)nb;
@@ -461,11 +475,11 @@ static int contact_visit(void *vctx, uint32_t j) {
     return 0;
 }
 
-static double scaled_w(double w, double y) { return w != 0.0 ? 1.0 / ((1.0 / w) * exp(-y)) : w; }
+static real scaled_w(real w, real y) { return w != 0.0 ? 1.0 / ((1.0 / w) * exp(-y)) : w; }
 
 /* collideD + collideCell (integration_kernel.cuh:303-462).  Pairs with zero
  * total inverse mass or zero separation are skipped (NaN in the reference). */
-static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, double out[3]) {
+static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real out[3]) {
     ct_ctx c = {s, i, 0, s->sphase[i], list};
     int g[3];
     grid_cell(s, s->sx32 + 4 * i, g);
@@ -473,26 +487,27 @@ static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, doubl
     s->nb_contact[s->sorted_idx[i]] = c.nb;
     out[0] = out[1] = out[2] = 0;
     if (!c.nb) return;
-    const double *pi = s->sx + 4 * i;
-    const double w = pi[3], sw = scaled_w(w, pi[1]), fnb = (double)c.nb;
-    const double *prev = s->x_old + 4 * s->sorted_idx[i];
+    const real *pi = s->sx + 4 * i;
+    const real w = pi[3], sw = scaled_w(w, pi[1]);
+    const double fnb = (double)c.nb;
+    const real *prev = s->x_old + 4 * s->sorted_idx[i];
     const int ph = s->sphase[i];
     const double cdist = (double)s->collidef;
     for (uint32_t k = 0; k < c.nb; ++k) {
         uint32_t j = list[k];
-        const double *pj = s->sx + 4 * j;
+        const real *pj = s->sx + 4 * j;
         int phj = s->sphase[j];
-        double diff[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
-        double dist = sqrt(diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]);
-        double mag = dist - cdist;
-        double colw = w, colw2 = pj[3];
+        real diff[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+        real dist = sqrt(diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]);
+        real mag = dist - cdist;
+        real colw = w, colw2 = pj[3];
         if (ph >= PBD_PHASE_SOLID && phj >= PBD_PHASE_SOLID) {
             colw = sw;
             colw2 = scaled_w(pj[3], pi[1]);
         }
-        double wsum = colw + colw2;
+        real wsum = colw + colw2;
         if (wsum == 0.0 || dist == 0.0) continue;
-        double scale = mag / wsum, dp[3], dp1[3], dp2[3];
+        real scale = mag / wsum, dp[3], dp1[3], dp2[3];
         for (int d = 0; d < 3; ++d) {
             dp[d] = diff[d] * (scale / dist);
             dp1[d] = -colw * dp[d] / fnb;
@@ -500,25 +515,25 @@ static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, doubl
             out[d] += dp1[d];
         }
         if (ph < PBD_PHASE_SOLID || phj < PBD_PHASE_SOLID) continue;
-        const double *prev2 = s->x_old + 4 * s->sorted_idx[j];
-        double nf[3] = {diff[0] / dist, diff[1] / dist, diff[2] / dist};
-        double dprel[3], dpt[3];
+        const real *prev2 = s->x_old + 4 * s->sorted_idx[j];
+        real nf[3] = {diff[0] / dist, diff[1] / dist, diff[2] / dist};
+        real dprel[3], dpt[3];
         for (int d = 0; d < 3; ++d) dprel[d] = (pi[d] + dp1[d] - prev[d]) - (prev[d] + dp2[d] - prev2[d]);
-        double dn = dprel[0] * nf[0] + dprel[1] * nf[1] + dprel[2] * nf[2];
+        real dn = dprel[0] * nf[0] + dprel[1] * nf[1] + dprel[2] * nf[2];
         for (int d = 0; d < 3; ++d) dpt[d] = dprel[d] - dn * nf[d];
-        double ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
+        real ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
         if (ldpt < K_EPS) continue;
         if (ldpt < (double)s->p.contact_static_friction * dist) {
             for (int d = 0; d < 3; ++d) out[d] -= dpt[d] * colw / wsum;
         } else {
-            double f = fmin((double)s->p.contact_kinetic_friction * dist / ldpt, 1.0);
+            real f = fmin((double)s->p.contact_kinetic_friction * dist / ldpt, 1.0);
             for (int d = 0; d < 3; ++d) out[d] -= dpt[d] * f;
         }
     }
 }
 
 /* collide_world_functor (integration_kernel.cuh:57-157). */
-static void world_collide(const orc_system *s, double e[3], int phase, const double *xold) {
+static void world_collide(const orc_system *s, real e[3], int phase, const real *xold) {
     const double r = s->p.particle_radius, d = r;
     const double *bmin = NULL;
     double lo[3] = {s->p.box_min[0], s->p.box_min[1], s->p.box_min[2]};
@@ -539,16 +554,16 @@ static void world_collide(const orc_system *s, double e[3], int phase, const dou
         e[2] = s->p.twod_z;
     }
     if (sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) < K_EPS || phase < PBD_PHASE_CLOTH) return;
-    double pos[3] = {xold[0], xold[1], twod ? (double)s->p.twod_z : xold[2]};
-    double dp[3] = {e[0] - pos[0], e[1] - pos[1], e[2] - pos[2]};
-    double dn = dp[0] * n[0] + dp[1] * n[1] + dp[2] * n[2];
-    double dpt[3] = {dp[0] - dn * n[0], dp[1] - dn * n[1], dp[2] - dn * n[2]};
-    double ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
+    real pos[3] = {xold[0], xold[1], twod ? (real)s->p.twod_z : xold[2]};
+    real dp[3] = {e[0] - pos[0], e[1] - pos[1], e[2] - pos[2]};
+    real dn = dp[0] * n[0] + dp[1] * n[1] + dp[2] * n[2];
+    real dpt[3] = {dp[0] - dn * n[0], dp[1] - dn * n[1], dp[2] - dn * n[2]};
+    real ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
     if (ldpt < K_EPS) return;
     if (ldpt < s->ws * d) {
         for (int k = 0; k < 3; ++k) e[k] -= dpt[k];
     } else {
-        double f = fmin(s->wk * d / ldpt, 1.0);
+        real f = fmin(s->wk * d / ldpt, 1.0);
         for (int k = 0; k < 3; ++k) e[k] -= dpt[k] * f;
     }
 }
@@ -561,7 +576,7 @@ enum { DO_CONTACT = 1, DO_FLUID = 2, DO_WORLD = 4 };
 static void solve_pass(orc_system *s, int mask) {
     const uint32_t n = s->n;
     if (mask & DO_FLUID) compute_lambdas(s);
-    double *out = (double *)malloc(4ull * (n ? n : 1) * sizeof(double));
+    real *out = (real *)malloc(4ull * (n ? n : 1) * sizeof(real));
     unsigned char *touched = (unsigned char *)calloc(n ? n : 1, 1);
     set_threads();
 #pragma omp parallel
@@ -571,7 +586,7 @@ static void solve_pass(orc_system *s, int mask) {
         for (long long ii = 0; ii < (long long)n; ++ii) {
             uint32_t i = (uint32_t)ii, o = s->sorted_idx[i];
             int ph = s->sphase[i];
-            double np[3] = {s->sx[4 * i], s->sx[4 * i + 1], s->sx[4 * i + 2]}, dd[3];
+            real np[3] = {s->sx[4 * i], s->sx[4 * i + 1], s->sx[4 * i + 2]}, dd[3];
             int t = 0;
             if ((mask & DO_FLUID) && ph == PBD_PHASE_FLUID) {
                 fluid_delta(s, i, list, dd);
@@ -620,7 +635,7 @@ void orc_collide_world(orc_system *s) { solve_pass(s, DO_WORLD); }
 void orc_solve_distance_constraints(orc_system *s) {
     const uint32_t n = s->n;
     if (!s->m) return;
-    double *acc = (double *)calloc(3ull * n, sizeof(double));
+    real *acc = (real *)calloc(3ull * n, sizeof(real));
     uint32_t *occ = (uint32_t *)calloc(n, sizeof(uint32_t));
     for (uint32_t c = 0; c < s->m; ++c) {
         ++occ[s->da[c]];
@@ -629,13 +644,13 @@ void orc_solve_distance_constraints(orc_system *s) {
     for (uint32_t k = 0; k < s->npin; ++k) ++occ[s->pin_idx[k]];
     const int mw = (s->p.flags & PBD_FLAG_DISTANCE_MASS_WEIGHTED) != 0;
     for (uint32_t c = 0; c < s->m; ++c) {
-        const double *a = s->x + 4 * s->da[c], *b = s->x + 4 * s->db[c];
-        double rel[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
-        double dist = sqrt(rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2]);
+        const real *a = s->x + 4 * s->da[c], *b = s->x + 4 * s->db[c];
+        real rel[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+        real dist = sqrt(rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2]);
         if (!(dist > K_MIN_DIST)) continue;
-        double ma, mb;
+        real ma, mb;
         if (mw) {
-            double ws = a[3] + b[3];
+            real ws = a[3] + b[3];
             ma = ws > 0 ? (s->drest[c] - dist) * (a[3] / ws) : 0.0;
             mb = ws > 0 ? (s->drest[c] - dist) * (b[3] / ws) : 0.0;
         } else {
@@ -664,8 +679,8 @@ void orc_solve_point_constraints(orc_system *s) {
 
 /* ---- shape matching */
 
-static void quat_to_mat(const double q[4], double R[3][3]) {
-    double x = q[0], y = q[1], z = q[2], w = q[3];
+static void quat_to_mat(const real q[4], real R[3][3]) {
+    real x = q[0], y = q[1], z = q[2], w = q[3];
     R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z);     R[0][2] = 2 * (x * z + w * y);
     R[1][0] = 2 * (x * y + w * z);     R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
     R[2][0] = 2 * (x * z - w * y);     R[2][1] = 2 * (y * z + w * x);     R[2][2] = 1 - 2 * (x * x + y * y);
@@ -673,31 +688,31 @@ static void quat_to_mat(const double q[4], double R[3][3]) {
 
 /* Rotation extraction of Mueller, Bender, Chentanez, Macklin, "A Robust
  * Method to Extract the Rotational Part of Deformations" (MIG 2016). */
-static void extract_rotation(const double A[3][3], double q[4], int iters) {
+static void extract_rotation(const real A[3][3], real q[4], int iters) {
     for (int it = 0; it < iters; ++it) {
-        double R[3][3];
+        real R[3][3];
         quat_to_mat(q, R);
-        double o[3] = {0, 0, 0}, dsum = 0;
+        real o[3] = {0, 0, 0}, dsum = 0;
         for (int c = 0; c < 3; ++c) {
-            double rx = R[0][c], ry = R[1][c], rz = R[2][c];
-            double ax = A[0][c], ay = A[1][c], az = A[2][c];
+            real rx = R[0][c], ry = R[1][c], rz = R[2][c];
+            real ax = A[0][c], ay = A[1][c], az = A[2][c];
             o[0] += ry * az - rz * ay;
             o[1] += rz * ax - rx * az;
             o[2] += rx * ay - ry * ax;
             dsum += rx * ax + ry * ay + rz * az;
         }
-        double inv = 1.0 / (fabs(dsum) + 1.0e-9);
+        real inv = 1.0 / (fabs(dsum) + 1.0e-9);
         for (int k = 0; k < 3; ++k) o[k] *= inv;
-        double wl = sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+        real wl = sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
         if (wl < 1.0e-9) break;
-        double sh = sin(0.5 * wl) / wl, ch = cos(0.5 * wl);
-        double d[4] = {o[0] * sh, o[1] * sh, o[2] * sh, ch};
-        double r[4];
+        real sh = sin(0.5 * wl) / wl, ch = cos(0.5 * wl);
+        real d[4] = {o[0] * sh, o[1] * sh, o[2] * sh, ch};
+        real r[4];
         r[3] = d[3] * q[3] - d[0] * q[0] - d[1] * q[1] - d[2] * q[2];
         r[0] = d[3] * q[0] + d[0] * q[3] + d[1] * q[2] - d[2] * q[1];
         r[1] = d[3] * q[1] - d[0] * q[2] + d[1] * q[3] + d[2] * q[0];
         r[2] = d[3] * q[2] + d[0] * q[1] - d[1] * q[0] + d[2] * q[3];
-        double qn = 1.0 / sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+        real qn = 1.0 / sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
         for (int k = 0; k < 4; ++k) q[k] = r[k] * qn;
     }
 }
@@ -708,27 +723,28 @@ static void extract_rotation(const double A[3][3], double q[4], int iters) {
 void orc_solve_shapes(orc_system *s) {
     for (uint32_t b = 0; b < s->nb; ++b) {
         uint32_t f = s->bfirst[b], cnt = s->bcount[b];
-        double c[3] = {0, 0, 0}, msum = 0;
+        real c[3] = {0, 0, 0};
+        double msum = 0;
         for (uint32_t k = f; k < f + cnt; ++k) {
             double m = s->brest[4 * k + 3];
             for (int d = 0; d < 3; ++d) c[d] += m * s->x[4 * k + d];
             msum += m;
         }
         for (int d = 0; d < 3; ++d) c[d] /= msum;
-        double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        real A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (uint32_t k = f; k < f + cnt; ++k) {
             const double *q = s->brest + 4 * k;
             for (int r = 0; r < 3; ++r)
                 for (int cc = 0; cc < 3; ++cc) A[r][cc] += q[3] * (s->x[4 * k + r] - c[r]) * q[cc];
         }
-        double *q = s->bquat + 4 * b;
+        real *q = s->bquat + 4 * b;
         extract_rotation(A, q, K_SHAPE_ITERS);
-        double R[3][3];
+        real R[3][3];
         quat_to_mat(q, R);
         for (uint32_t k = f; k < f + cnt; ++k) {
             const double *r = s->brest + 4 * k;
             for (int d = 0; d < 3; ++d) {
-                double g = c[d] + R[d][0] * r[0] + R[d][1] * r[1] + R[d][2] * r[2];
+                real g = c[d] + R[d][0] * r[0] + R[d][1] * r[1] + R[d][2] * r[2];
                 s->x[4 * k + d] += (g - s->x[4 * k + d]) * s->bstiff[b];
             }
         }
@@ -768,7 +784,7 @@ static int xsph_visit(void *vctx, uint32_t j) {
 
 void orc_apply_xsph(orc_system *s) {
     const uint32_t n = s->n;
-    double *vnew = (double *)malloc(3ull * (n ? n : 1) * sizeof(double));
+    real *vnew = (real *)malloc(3ull * (n ? n : 1) * sizeof(real));
     const double h2 = (double)s->p.kernel_radius * (double)s->p.kernel_radius;
     set_threads();
 #pragma omp parallel
@@ -783,15 +799,15 @@ void orc_apply_xsph(orc_system *s) {
             int g[3];
             grid_cell(s, s->sx32 + 4 * i, g);
             for_each_candidate(s, g, s->fluid_rad, xsph_visit, &c);
-            const double *xi = s->sx + 4 * i, *vi = s->v + 4 * o;
-            double acc[3] = {0, 0, 0};
+            const real *xi = s->sx + 4 * i, *vi = s->v + 4 * o;
+            real acc[3] = {0, 0, 0};
             for (uint32_t k = 0; k < c.nb; ++k) {
                 const uint32_t j = list[k];
-                const double *xj = s->sx + 4 * j, *vj = s->v + 4 * s->sorted_idx[j];
-                double r2 = 0;
+                const real *xj = s->sx + 4 * j, *vj = s->v + 4 * s->sorted_idx[j];
+                real r2 = 0;
                 for (int d = 0; d < 3; ++d) r2 += (xi[d] - xj[d]) * (xi[d] - xj[d]);
-                double hm2 = h2 - r2;
-                double wgt = s->poly6 * hm2 * hm2 * hm2 * (xj[3] > 0 ? 1.0 / xj[3] : 0.0);
+                real hm2 = h2 - r2;
+                real wgt = s->poly6 * hm2 * hm2 * hm2 * (xj[3] > 0 ? 1.0 / xj[3] : (real)0.0);
                 for (int d = 0; d < 3; ++d) acc[d] += (vj[d] - vi[d]) * wgt;
             }
             for (int d = 0; d < 3; ++d) vnew[3 * i + d] = vi[d] + acc[d] * ((double)s->p.xsph_c / s->srho0[i]);
@@ -832,13 +848,20 @@ void orc_update(orc_system *s, double dt) {
 
 uint32_t orc_num_particles(const orc_system *s) { return s->n; }
 
-void orc_get_positions(const orc_system *s, double *out) { memcpy(out, s->x, 4ull * s->n * sizeof(double)); }
-void orc_get_velocities(const orc_system *s, double *out) { memcpy(out, s->v, 4ull * s->n * sizeof(double)); }
+void orc_get_positions(const orc_system *s, double *out) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) out[k] = R_VAL(s->x[k]);
+}
+void orc_get_velocities(const orc_system *s, double *out) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) out[k] = R_VAL(s->v[k]);
+}
+/* (with ORC_DUAL these set the values and clear the tangents) */
 void orc_set_positions(orc_system *s, const double *p) {
-    memcpy(s->x, p, 4ull * s->n * sizeof(double));
+    for (size_t k = 0; k < 4ull * s->n; ++k) s->x[k] = p[k];
     s->grid_valid = 0;
 }
-void orc_set_velocities(orc_system *s, const double *v) { memcpy(s->v, v, 4ull * s->n * sizeof(double)); }
+void orc_set_velocities(orc_system *s, const double *v) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) s->v[k] = v[k];
+}
 
 void orc_get_grid(const orc_system *s, uint32_t *sorted_hash, uint32_t *sorted_index, uint32_t *cell_start,
                   uint32_t *cell_end) {
@@ -854,8 +877,30 @@ void orc_get_grid(const orc_system *s, uint32_t *sorted_hash, uint32_t *sorted_i
 }
 
 void orc_get_lambdas(const orc_system *s, double *out) {
-    for (uint32_t p = 0; p < s->n; ++p) out[s->sorted_idx[p]] = s->lambda[p];
+    for (uint32_t p = 0; p < s->n; ++p) out[s->sorted_idx[p]] = R_VAL(s->lambda[p]);
 }
+
+#ifdef ORC_DUAL
+/* Seeds the direction of differentiation: tangents of the positions and
+ * velocities (4n each) and of the distance-constraint stiffness (m); NULL
+ * = zero. */
+void orc_seed_tangents(orc_system *s, const double *dx, const double *dv, const double *dstiff) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) {
+        s->x[k].d = dx ? dx[k] : 0.0;
+        s->v[k].d = dv ? dv[k] : 0.0;
+    }
+    for (uint32_t c = 0; c < s->m; ++c) s->dstiff[c].d = dstiff ? dstiff[c] : 0.0;
+    s->grid_valid = 0;
+}
+
+/* The directional derivatives of the positions and velocities. */
+void orc_get_tangents(const orc_system *s, double *dx, double *dv) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) {
+        if (dx) dx[k] = s->x[k].d;
+        if (dv) dv[k] = s->v[k].d;
+    }
+}
+#endif
 
 void orc_get_neighbor_counts(const orc_system *s, uint32_t *fluid, uint32_t *contact) {
     if (fluid) memcpy(fluid, s->nb_fluid, s->n * sizeof(uint32_t));

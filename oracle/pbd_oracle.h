@@ -57,6 +57,9 @@ void orc_get_grid(const orc_system *s, uint32_t *sorted_hash, uint32_t *sorted_i
 void orc_get_lambdas(const orc_system *s, double *out);
 /* Neighbour count of every particle in the last fluid / contact pass. */
 void orc_get_neighbor_counts(const orc_system *s, uint32_t *fluid, uint32_t *contact);
+/* Only in the dual-number build (liboracle_dual.so). */
+void orc_seed_tangents(orc_system *s, const double *dx, const double *dv, const double *dstiff);
+void orc_get_tangents(const orc_system *s, double *dx, double *dv);
 
 #ifdef __cplusplus
 }

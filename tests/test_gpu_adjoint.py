@@ -1,18 +1,21 @@
 """Adjoint (reverse-mode) gradients of rollouts, through the C ABI and the
 torch.autograd bridge, against central finite differences of the FP64
-oracle.
+oracle and against the forward-mode dual-number derivative of the same
+FP64 replay.
 
 Loss L = sum_i c_i . x_T,i with fixed random c.  The FP32 adjoint's
-directional derivative along a random direction in (stiffness, x0, v0)
-must match the oracle's (L(p + eps d) - L(p - eps d)) / (2 eps) to 1e-3
-relative; eps = 1e-5 is far inside the range where the oracle's central
-difference has converged and no contact switches on or off."""
+directional derivative along a random direction d in (stiffness, x0, v0)
+must match, to 1e-3 relative, both the oracle's
+(L(p + eps d) - L(p - eps d)) / (2 eps) (eps = 1e-5 is far inside the range
+where the oracle's central difference has converged and no contact switches
+on or off) and sum_i c_i . dx_T,i of the dual-number oracle seeded with d
+(exact for the branches the FP64 replay takes, no step size)."""
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
-from oracle import Oracle  # noqa: E402
+from oracle import Oracle, OracleDual  # noqa: E402
 from particlesolver_gb300 import ParticleSystem, PbdError, default_params  # noqa: E402
 from particlesolver_gb300 import workloads as W  # noqa: E402
 from particlesolver_gb300.autograd import rollout  # noqa: E402
@@ -64,11 +67,13 @@ def gpu_gradients(sc, stiffness, steps, every, c):
     return gs, x0.grad.cpu().numpy()[:, :3], v0.grad.cpu().numpy()[:, :3], xT.detach().cpu().numpy()
 
 
-def oracle_loss(sc, stiffness, x0, v0, steps, c):
+def oracle_loss(sc, stiffness, x0, v0, steps, c, tangent=None):
     """L of the FP64 oracle from (x0, v0): the scene is loaded as given
     (rigid bodies take their rest shapes from the scene's positions, as in
-    the differentiated rollout), then the state is set."""
-    o = Oracle(default_params(**sc.params), sc.n)
+    the differentiated rollout), then the state is set.  With
+    tangent = (ds, dx, dv) the dual-number oracle runs instead and the
+    directional derivative of L along that direction is returned."""
+    o = (Oracle if tangent is None else OracleDual)(default_params(**sc.params), sc.n)
     W.apply_to(W.Scene(sc.name, sc.params, sc.pos_w, sc.phase, rest_density=sc.rest_density, pairs=sc.pairs,
                        rest=sc.rest, stiffness=None if stiffness is None else np.asarray(stiffness),
                        pins=sc.pins, pin_points=sc.pin_points, bodies=sc.bodies), o)
@@ -78,9 +83,17 @@ def oracle_loss(sc, stiffness, x0, v0, steps, c):
     vel[:, :3] = v0
     o.set_positions(pos)
     o.set_velocities(vel)
+    if tangent is not None:
+        o.seed_tangents(tangent[1], tangent[2], tangent[0])
     for _ in range(steps):
         o.update(sc.dt)
+    if tangent is not None:
+        return float(np.sum(o.tangents()[0][:, :3] * c))
     return float(np.sum(o.positions()[:, :3] * c))
+
+
+def dual_directional(sc, stiffness, x0, v0, steps, c, ds, dx, dv):
+    return oracle_loss(sc, stiffness, x0, v0, steps, c, tangent=(ds, dx, dv))
 
 
 def check_directional(sc, steps, every, seed, eps=1e-5):
@@ -99,7 +112,9 @@ def check_directional(sc, steps, every, seed, eps=1e-5):
     lp = oracle_loss(sc, None if s0 is None else s0 + eps * ds, x0 + eps * dx, v0 + eps * dv, steps, c)
     lm = oracle_loss(sc, None if s0 is None else s0 - eps * ds, x0 - eps * dx, v0 - eps * dv, steps, c)
     fd = (lp - lm) / (2 * eps)
+    dual = dual_directional(sc, s0, x0, v0, steps, c, ds if m else None, dx, dv)
     assert abs(ad - fd) <= TOL * abs(fd), (ad, fd)
+    assert abs(ad - dual) <= TOL * abs(dual), (ad, dual)
     return ad, fd
 
 
@@ -128,7 +143,9 @@ def test_each_parameter_block_matches_fd():
         ad = float(np.dot(gs, ds) + np.sum(gx * dx) + np.sum(gv * dv))
         fd = (oracle_loss(sc, s0 + eps * ds, x0 + eps * dx, v0 + eps * dv, steps, c)
               - oracle_loss(sc, s0 - eps * ds, x0 - eps * dx, v0 - eps * dv, steps, c)) / (2 * eps)
+        dual = dual_directional(sc, s0, x0, v0, steps, c, ds, dx, dv)
         assert abs(ad - fd) <= TOL * abs(fd), (which, ad, fd)
+        assert abs(ad - dual) <= TOL * abs(dual), (which, ad, dual)
 
 
 def test_wall_clamps_and_friction_gradient():
