@@ -326,7 +326,13 @@ typedef struct pbd_tuning {
                                       the summation order differs.  0 = off
                                       (grid and list rebuilt every
                                       iteration, the reference's schedule)  */
-    uint32_t reserved[5];          /* zero                                  */
+    uint32_t list_assembly;        /* with a list: where the lambda pass
+                                      collects a particle's neighbours before
+                                      storing them: 0 = shared memory, one
+                                      column per thread (default; capacities
+                                      up to 88, larger ones use registers),
+                                      1 = registers                         */
+    uint32_t reserved[4];          /* zero                                  */
 } pbd_tuning;
 
 int pbd_set_tuning(pbd_system *sys, const pbd_tuning *tuning);

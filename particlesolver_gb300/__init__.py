@@ -107,7 +107,8 @@ STAGES = ["predict", "grid", "lambda", "solve", "distance", "shapes", "velocity"
 
 class PbdTuning(ctypes.Structure):
     _fields_ = [("threads_per_particle", ctypes.c_uint32), ("neighbor_list_capacity", ctypes.c_uint32),
-                ("neighbor_skin", ctypes.c_float), ("reserved", ctypes.c_uint32 * 5)]
+                ("neighbor_skin", ctypes.c_float), ("list_assembly", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 4)]
 
 
 class PbdProfile(ctypes.Structure):
@@ -480,8 +481,10 @@ class ParticleSystem:
         return t
 
     def set_tuning(self, threads_per_particle: int | None = None, neighbor_list_capacity: int | None = None,
-                   neighbor_skin: float | None = None):
+                   neighbor_skin: float | None = None, list_assembly: int | None = None):
         t = self.tuning()
+        if list_assembly is not None:
+            t.list_assembly = int(list_assembly)
         if threads_per_particle is not None:
             t.threads_per_particle = int(threads_per_particle)
         if neighbor_list_capacity is not None:

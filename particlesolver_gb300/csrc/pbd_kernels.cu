@@ -14,6 +14,17 @@ namespace pbd {
 namespace {
 
 constexpr int kBlock = 256;
+// Block of the shared-memory list build, and the largest list capacity it
+// assembles: (capacity + 1) x kListBlock words stay under the 48 KB of
+// dynamic shared memory a launch gets without opting in.
+constexpr int kListBlock = 128;
+constexpr uint32_t kSharedListMax = 88;
+static_assert((kSharedListMax + 1) * kListBlock * 4 <= 48 * 1024,
+              "shared-memory list build exceeds the default dynamic shared memory");
+// NbList::assemble: kListShared selects the shared-memory build (any other
+// value, the register quads); both store four entries to a uint4,
+// [capacity / 4][stride].
+constexpr uint32_t kListShared = 0u;
 
 inline unsigned blocks_for(uint32_t n, int per_block = kBlock) {
     return (unsigned)((n + (uint32_t)per_block - 1u) / (uint32_t)per_block);
@@ -893,6 +904,116 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
     sxl[i] = make_float4(pi.x, pi.y, pi.z, -(ro * inv_rho0 - 1.f) / (denom + P.relax));
 }
 
+// k_lambda_list with the list assembled in shared memory.  Each lane owns
+// one column of a [capacity + 1][kListBlock] word array (the word index is
+// row * kListBlock + lane, so every store of a warp lands in its own bank
+// whatever the lanes' counts), and the candidate loop costs one predicated
+// 4-byte store and a clamped column-offset bump per candidate instead of
+// k_lambda_list's register quad and 16-byte store.  Row `capacity` absorbs
+// stores past capacity; a particle that reaches it counts as over capacity
+// and takes the exact stencil walk.  The finished list goes to global
+// memory four entries to a uint4 (the layout k_lambda_list writes) and lambda
+// is summed from the shared copy.  Same neighbour sets, visiting order and
+// results as k_lambda_list.
+template <int RAD, bool B, bool SKIN>
+__global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                                const float4 *__restrict__ sx,
+                                                                const SortedAttr *__restrict__ sattr,
+                                                                const uint32_t *__restrict__ cell_first,
+                                                                float4 *__restrict__ sxl, NbList L) {
+    extern __shared__ uint32_t s_nb[];
+    const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
+    if (i >= n) return;
+    const DevParams P = scene_params<B>(P0, i);
+    const bool reuse = SKIN && L.reuse && *L.reuse;
+    // A scene sitting out this iteration needs nothing -- except when a skin
+    // list is built: every scene's list must exist for the later
+    // iterations that reuse it.
+    if (!scene_active<B>(P, iter_left) && (reuse || !SKIN)) return;
+    const SortedAttr a = sattr[i];
+    const float4 pi4 = sx[i];
+    const float3 pi = f3(pi4);
+    if (SKIN && !reuse) L.sref[i] = pi4;
+    if (a.phase != kFluid) {
+        sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
+        if (!reuse) L.count[i] = 0u;
+        return;
+    }
+    const float h2 = P.h2;
+    const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
+    const float inv_w = 1.f / pi4.w;
+    const float inv_rho0 = 1.f / a.rho0;
+    const float spiky_r = -P.spiky * inv_rho0;
+    LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
+    auto add = [&](uint32_t j, const float4 &pj, float d2) {
+        const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
+        acc.add(P, true, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
+    };
+    if (reuse) {
+        for_each_listed(L, i, L.count[i], [&](uint32_t j) {
+            const float4 pj = __ldg(sx + j);
+            const float d2 = dist2_exact(pi, f3(pj));
+            if (d2 < h2) add(j, pj, d2);
+        });
+    } else {
+        const int3 g = grid_pos(P, pi);
+        const uint32_t cap = L.capacity;
+        int rad = P.fluid_rad;
+        float reach2 = h2;
+        bool trim = P.trim_fluid;
+        if (SKIN) {
+            const int r = list_rad(P, L.skin);
+            if ((uint32_t)(2 * r + 1) <= min(P.gx, min(P.gy, P.gz))) {
+                const float lr = P.h * (1.f + L.skin);
+                rad = r;
+                reach2 = lr * lr;
+                trim = true;
+            } else {
+                atomicOr(L.ovf, 1u);
+            }
+        }
+        uint32_t *const col = s_nb + threadIdx.x;
+        const uint32_t wend = cap * (uint32_t)kListBlock;
+        uint32_t w = 0;  // word offset of this lane's next entry
+        stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
+#pragma unroll 4
+            for (uint32_t j = b; j < e; ++j) {
+                const float4 q = __ldg(sx + j);
+                const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
+                if (ok) col[w] = j;
+                w = ok ? min(w + (uint32_t)kListBlock, wend) : w;
+            }
+            return true;
+        });
+        const uint32_t cnt = (w == wend) ? cap + 1u : w / (uint32_t)kListBlock;
+        L.count[i] = cnt;
+        if (list_usable(P, L, cnt)) {
+            uint4 *const dst = L.slot + i;
+            for (uint32_t q = 0; 4u * q < cnt; ++q) {
+                const uint32_t k = 4u * q * (uint32_t)kListBlock;
+                dst[q * L.stride] = make_uint4(col[k], col[k + kListBlock], col[k + 2 * kListBlock],
+                                               col[k + 3 * kListBlock]);
+            }
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const uint32_t j = col[k * (uint32_t)kListBlock];
+                const float4 pj = __ldg(sx + j);
+                const float d2 = dist2_exact(pi, f3(pj));
+                if (!SKIN || d2 < h2) add(j, pj, d2);
+            }
+        } else {
+            if (SKIN) atomicOr(L.ovf, 1u);
+            const Group<1> G;
+            group_walk<1>(
+                P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+                [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+                [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2); });
+        }
+    }
+    const float ro = acc.ro + P.poly6_self * inv_w;
+    const float denom = acc.denom + dot3(acc.grad, acc.grad);
+    sxl[i] = make_float4(pi.x, pi.y, pi.z, -(ro * inv_rho0 - 1.f) / (denom + P.relax));
+}
+
 // solveFluidsD (integration_kernel.cuh:596-642) over the lambda pass's list.
 __device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t i, float3 pi, float rho0,
                                                    const float4 *__restrict__ sxl,
@@ -1419,16 +1540,32 @@ void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, co
         // the host enables a skin only where its stencil does not alias)
         rad = P.table ? 0 : (int)std::ceil(P.h * (1.f + L.skin) / P.cell * 1.000001f);
     }
-#define PBD_LIST(R, S) \
-    k_lambda_list<R, B, S><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, L)
+    const bool shared = L.assemble == kListShared && L.capacity <= kSharedListMax;
+    const unsigned nbs = blocks_for(n, kListBlock);
+    const size_t smem = (size_t)(L.capacity + 1u) * kListBlock * sizeof(uint32_t);
+#define PBD_LIST(R, S)                                                                                      \
+    if (shared)                                                                                             \
+        k_lambda_slist<R, B, S><<<nbs, kListBlock, smem, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr,   \
+                                                              g.cell_first, sxl, L);                        \
+    else                                                                                                    \
+        k_lambda_list<R, B, S><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, \
+                                                     sxl, L)
     if (L.sref) {
-        if (rad == 1) PBD_LIST(1, true);
-        else if (rad == 2) PBD_LIST(2, true);
-        else PBD_LIST(0, true);
+        if (rad == 1) {
+            PBD_LIST(1, true);
+        } else if (rad == 2) {
+            PBD_LIST(2, true);
+        } else {
+            PBD_LIST(0, true);
+        }
     } else {
-        if (rad == 1) PBD_LIST(1, false);
-        else if (rad == 2) PBD_LIST(2, false);
-        else PBD_LIST(0, false);
+        if (rad == 1) {
+            PBD_LIST(1, false);
+        } else if (rad == 2) {
+            PBD_LIST(2, false);
+        } else {
+            PBD_LIST(0, false);
+        }
     }
 #undef PBD_LIST
 }

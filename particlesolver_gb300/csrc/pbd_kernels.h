@@ -38,6 +38,9 @@ struct NbList {
     float4 *sref;
     const uint32_t *reuse;
     uint32_t *ovf;
+    // Where the lambda pass assembles a list before storing it: 0 = shared
+    // memory (capacities up to 88), 1 = registers.
+    uint32_t assemble;
 };
 
 // Device words of the skin-list schedule: [0] reuse, [1] overflow, [2 + k]

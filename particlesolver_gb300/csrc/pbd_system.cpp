@@ -1078,8 +1078,10 @@ int pbd_set_tuning(pbd_system *s, const pbd_tuning *t) {
         return fail(s, PBD_ERR_INVALID_ARGUMENT, "neighbor_list_capacity must be a multiple of 4, at most 1024");
     if (!(t->neighbor_skin >= 0.f && t->neighbor_skin <= 1.f))
         return fail(s, PBD_ERR_INVALID_ARGUMENT, "neighbor_skin must be in [0, 1]");
+    if (t->list_assembly > 1u) return fail(s, PBD_ERR_INVALID_ARGUMENT, "list_assembly must be 0 or 1");
     s->tpp = k;
     s->skin = t->neighbor_skin;
+    s->nbl.assemble = t->list_assembly;
     if (int rc = alloc_skin(s)) return rc;
     if (cap != s->list_capacity) {
         free_list(s);
@@ -1102,6 +1104,7 @@ int pbd_get_tuning(const pbd_system *s, pbd_tuning *out) {
     out->threads_per_particle = s->tpp;
     out->neighbor_list_capacity = s->list_capacity;
     out->neighbor_skin = s->skin;
+    out->list_assembly = s->nbl.assemble;
     return PBD_OK;
 }
 
@@ -1154,6 +1157,11 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
         cands.push_back(t);
     };
     cand(1, 0.f);
+    if (s->n_fluid && base.neighbor_list_capacity)
+    {
+        cand(1, 0.f);
+        cands.back().list_assembly = 1u;
+    }
     if (s->n_fluid && s->dev.iterations > 1 && base.neighbor_list_capacity)
         for (float f : {0.1f, 0.2f, 0.3f}) cand(1, f);
     for (uint32_t k : {2u, 4u, 8u, 16u, 32u}) cand(k, 0.f);

@@ -532,6 +532,31 @@ def test_neighbor_list_capacity_and_fallback(capacity):
     assert norm_err(g.velocities()[:, :3], o.velocities()[:, :3]) < TOL_STAGE
 
 
+@pytest.mark.parametrize("capacity,skin", [(64, 0.0), (24, 0.0), (88, 0.0), (92, 0.0), (80, 0.2)])
+def test_list_assembly_shared_equals_registers(capacity, skin):
+    """The lambda pass assembles a particle's neighbour list in shared
+    memory (list_assembly 0) or in registers (1): the same neighbours in
+    the same order with the same arithmetic, so updates agree bit for bit,
+    also when particles overflow the list (24), at the largest shared
+    capacity (88), above it (92: both use registers) and with a skin
+    list."""
+    mode = 0
+    sc = W.dam_break(24, 20, 12)
+    sc.params["grid_size"] = [64, 16, 16]
+    a = ParticleSystem(default_params(**sc.params), sc.n)
+    b = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, a)
+    W.apply_to(sc, b)
+    a.set_tuning(threads_per_particle=1, neighbor_list_capacity=capacity, neighbor_skin=skin, list_assembly=mode)
+    b.set_tuning(threads_per_particle=1, neighbor_list_capacity=capacity, neighbor_skin=skin, list_assembly=1)
+    assert a.tuning().list_assembly == mode and b.tuning().list_assembly == 1
+    for _ in range(4):
+        a.update(sc.dt)
+        b.update(sc.dt)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+
+
 # ------------------------------------------------------------ skin lists
 
 def test_skin_list_forced_rebuild_is_bitwise_the_plain_schedule():
