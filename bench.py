@@ -210,7 +210,8 @@ def load_scenes(scenes, max_particles=None):
         W.apply_to(W.Scene(sc.name, sc.params, sc.pos_w, sc.phase, vel=sc.vel, rest_density=sc.rest_density,
                            pairs=None if sc.pairs is None else sc.pairs + first, rest=sc.rest,
                            stiffness=sc.stiffness, pins=None if sc.pins is None else sc.pins + first,
-                           pin_points=sc.pin_points, bodies=[(f + first, c, st) for f, c, st in sc.bodies]), sysm)
+                           pin_points=sc.pin_points, bodies=[(f + first, c, st) for f, c, st in sc.bodies],
+                           open_gas=[(f + first, c) for f, c in sc.open_gas]), sysm)
     return sysm
 
 

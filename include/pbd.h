@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define PBD_ABI_VERSION 2
+#define PBD_ABI_VERSION 3
 
 typedef enum pbd_status {
     PBD_OK = 0,
@@ -113,6 +113,24 @@ typedef struct pbd_params {
                                 reference's S_SOLID (totalfluidconstraint.h:
                                 30, .cpp:66-68,154); fluid-solid coupling
                                 in between (>= 0)                           */
+    /* Gas phase (PBD_PHASE_GAS; the CPU reference's GasConstraint,
+     * cpu/src/constraint/gasconstraint.cpp:34-134, with its constants from
+     * gasconstraint.h:11-21 and simulation.h:21).  Gas particles are PBF
+     * particles with their own rest density whose neighbours are the
+     * particles with w > 0; a gas particle's correction uses only gas
+     * neighbours' lambdas and is divided by (neighbours + 1) rest
+     * densities; every iteration it adds the reference's vorticity term
+     * (and, in an open gas, the density drag) to a force that the next
+     * prediction applies. */
+    float gas_gravity_scale; /* gravity on gas particles times this (ALPHA
+                                -0.2: gas rises)                            */
+    float gas_scorr_k;       /* gas artificial pressure k (K_P 0.2)         */
+    float gas_scorr_dq;      /* gas artificial pressure dq / h (DQ_P 0.25)  */
+    float gas_solid_density_weight; /* weight of a neighbour of phase >=
+                                CLOTH in a gas particle's density (S_SOLID
+                                0.5)                                        */
+    float gas_drag;          /* open gas: force += v (1 - rho / rho0) *
+                                (-gas_drag) per iteration (50)              */
 } pbd_params;
 
 typedef struct pbd_system pbd_system;
@@ -208,6 +226,15 @@ int pbd_get_positions(pbd_system *sys, uint32_t first, uint32_t count, float *ds
 int pbd_get_velocities(pbd_system *sys, uint32_t first, uint32_t count, float *dst,
                        int dst_on_device, void *stream);
 int pbd_get_phases(pbd_system *sys, int32_t *dst);
+/* Marks the gas particles of [first, first+count) as an open gas (open != 0)
+ * or a closed one: createGas(..., open) of the CPU reference
+ * (simulation.cpp:408-429, gasconstraint.cpp:80).  Non-gas particles in the
+ * range are left alone; gas starts closed. */
+int pbd_set_gas_open(pbd_system *sys, uint32_t first, uint32_t count, int open);
+/* The force every particle carries into the next prediction (4n floats,
+ * xyz and 0; the reference's Particle::f, particle.h): vorticity and open
+ * drag of gas particles, zero elsewhere.  Synchronous. */
+int pbd_get_forces(pbd_system *sys, float *dst);
 int pbd_get_device_buffers(pbd_system *sys, pbd_device_buffers *out);
 
 /* Scene builders of the reference class, with its lattice spacings and

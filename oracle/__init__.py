@@ -68,6 +68,9 @@ def load(dual: bool = False):
             "orc_get_grid": ([P, PU, PU, PU, PU], None),
             "orc_get_lambdas": ([P, PD], None),
             "orc_get_neighbor_counts": ([P, PU, PU], None),
+            "orc_set_gas_open": ([P, U, U, ctypes.c_int], None),
+            "orc_get_forces": ([P, PD], None),
+            "orc_set_forces": ([P, PD], None),
         }
         if dual:
             sig["orc_seed_tangents"] = ([P, PD, PD, PD], None)
@@ -214,6 +217,18 @@ class Oracle:
         out = np.empty(self.num_particles, np.float64)
         self.lib.orc_get_lambdas(self.s, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         return out
+
+    def set_gas_open(self, first: int, count: int, open_: bool = True):
+        self.lib.orc_set_gas_open(self.s, int(first), int(count), int(bool(open_)))
+
+    def forces(self) -> np.ndarray:
+        out = np.empty((self.num_particles, 4), np.float64)
+        self.lib.orc_get_forces(self.s, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return out
+
+    def set_forces(self, f):
+        f, fp = _d(np.asarray(f, np.float64).reshape(-1, 4))
+        self.lib.orc_set_forces(self.s, fp)
 
     def neighbor_counts(self):
         n = self.num_particles

@@ -32,6 +32,7 @@
 
 #define private public
 #include "simulation.h"
+#include "gasconstraint.h"
 #undef private
 
 #include <cstdint>
@@ -93,5 +94,40 @@ void refcpu_get(void *h, double *xy, double *v) {
 }
 
 void refcpu_destroy(void *h) { delete static_cast<Simulation *>(h); }
+
+// The reference's own gas projection, GasConstraint::project
+// (gasconstraint.cpp:34-134), on n 2-D particles: those with solid[i] == 0
+// form one gas of rest density `density` (open or closed), the others are
+// SOLID neighbours; positions are taken as the estimates, contact counts are
+// zero, and project() runs `iterations` times (once per solver iteration,
+// as the reference's ITERATIVE loop calls it).  xy, v: 2n doubles; imass: n
+// inverse masses (0 = fixed, which the gas ignores).  Out: the estimates
+// and each particle's force, 2n doubles each.  Used to pin the oracle's
+// gas formulas.
+void refcpu_gas_project(int n, const double *xy, const double *v, const double *imass, const int *solid,
+                        double density, int open, int iterations, double *xy_out, double *f_out) {
+    QList<Particle *> ps;
+    QList<int> members;
+    for (int i = 0; i < n; ++i) {
+        Particle *p = new Particle(glm::dvec2(xy[2 * i], xy[2 * i + 1]), 1.0, solid[i] ? SOLID : GAS);
+        p->imass = imass[i];
+        p->ep = p->p;
+        p->v = glm::dvec2(v[2 * i], v[2 * i + 1]);
+        ps.append(p);
+        if (!solid[i]) members.append(i);
+    }
+    {
+        GasConstraint c(density, &members, open != 0);
+        std::vector<int> counts(n, 0);
+        for (int it = 0; it < iterations; ++it) c.project(&ps, counts.data());
+    }
+    for (int i = 0; i < n; ++i) {
+        xy_out[2 * i] = ps.at(i)->ep.x;
+        xy_out[2 * i + 1] = ps.at(i)->ep.y;
+        f_out[2 * i] = ps.at(i)->f.x;
+        f_out[2 * i + 1] = ps.at(i)->f.y;
+        delete ps.at(i);
+    }
+}
 
 }  // extern "C"

@@ -71,6 +71,12 @@ struct orc_system {
     double *bstiff;
     real *bquat;              /* 4 per body: x y z w */
     double *brest;            /* 4 per particle of the body: q xyz, mass; indexed by particle */
+    /* gas phase (gasconstraint.cpp) */
+    int has_gas;
+    double gas_scorr_k, gas_scorr_inv_ref;
+    real *force;              /* 4n, original order: Particle::f            */
+    unsigned char *gas_open;  /* original order                             */
+    real *glambda;            /* sorted order                               */
 };
 
 static int g_threads = 0;
@@ -165,6 +171,11 @@ orc_system *orc_create(const pbd_params *params, uint32_t cap) {
     const int ku = (params->flags & PBD_FLAG_KERNEL_UNITS) != 0;
     s->scorr_k = ku ? (double)params->scorr_k * h * h : (double)params->scorr_k;
     s->relax = ku ? (double)params->relaxation / (h * h) : (double)params->relaxation;
+    s->gas_scorr_k = ku ? (double)params->gas_scorr_k * h * h : (double)params->gas_scorr_k;
+    {
+        const double gdq = (double)params->gas_scorr_dq * h, gt2 = h * h - gdq * gdq;
+        s->gas_scorr_inv_ref = 1.0 / (s->poly6 * gt2 * gt2 * gt2);
+    }
     s->ws = sqrt((double)params->wall_static_friction);
     s->wk = sqrt((double)params->wall_kinetic_friction);
     s->x = (real *)calloc(4ull * cap, sizeof(real));
@@ -183,6 +194,9 @@ orc_system *orc_create(const pbd_params *params, uint32_t cap) {
     s->nb_fluid = (uint32_t *)calloc(cap, sizeof(uint32_t));
     s->nb_contact = (uint32_t *)calloc(cap, sizeof(uint32_t));
     s->brest = (double *)calloc(4ull * cap, sizeof(double));
+    s->force = (real *)calloc(4ull * cap, sizeof(real));
+    s->gas_open = (unsigned char *)calloc(cap ? cap : 1, 1);
+    s->glambda = (real *)calloc(cap, sizeof(real));
     return s;
 }
 
@@ -195,6 +209,7 @@ void orc_destroy(orc_system *s) {
     free(s->da); free(s->db); free(s->drest); free(s->dstiff);
     free(s->pin_idx); free(s->pin_pts);
     free(s->bfirst); free(s->bcount); free(s->bstiff); free(s->bquat); free(s->brest);
+    free(s->force); free(s->gas_open); free(s->glambda);
     free(s);
 }
 
@@ -210,6 +225,7 @@ int orc_add_particles(orc_system *s, uint32_t n, const double *pos_w, const doub
         }
         s->phase[k] = phase[i];
         s->rho0[k] = rest_density ? rest_density[i] : 1.0;
+        if (phase[i] == PBD_PHASE_GAS) s->has_gas = 1;
     }
     s->n += n;
     s->grid_valid = 0;
@@ -290,15 +306,25 @@ void orc_set_wall_jitter(orc_system *s, const double r[6]) {
 /* ------------------------------------------------------------- stages */
 
 /* integrate_functor + copyToXstar (integration_kernel.cuh:159-184,
- * shared_variables.cu:91-96). */
+ * shared_variables.cu:91-96).  With gas particles in the system, the CPU
+ * reference's step velocity (simulation.cpp:142-153): v' = v + dt g' + dt f
+ * with g' = g * gas_gravity_scale on gas (ALPHA, simulation.h:21), f the
+ * force of the last step, which is cleared; v' is kept for the gas terms. */
 void orc_integrate(orc_system *s, double dt) {
     dt = fmin(dt, (double)s->p.max_dt);
     for (uint32_t i = 0; i < s->n; ++i) {
         for (int d = 0; d < 4; ++d) s->x_old[4 * i + d] = s->x[4 * i + d];
+        const double gs = (s->has_gas && s->phase[i] == PBD_PHASE_GAS) ? (double)s->p.gas_gravity_scale : 1.0;
         for (int d = 0; d < 3; ++d) {
-            real vv = s->v[4 * i + d] + (double)s->p.gravity[d] * dt;
+            real vv = s->v[4 * i + d] + ((double)s->p.gravity[d] * gs) * dt;
+            if (s->has_gas) {
+                vv = vv + s->force[4 * i + d] * dt;
+                s->v[4 * i + d] = vv;
+            }
             s->x[4 * i + d] += vv * dt;
         }
+        if (s->has_gas)
+            for (int d = 0; d < 4; ++d) s->force[4 * i + d] = 0.0;
     }
     s->grid_valid = 0;
 }
@@ -370,6 +396,65 @@ static uint32_t fluid_neighbors(const orc_system *s, uint32_t i, uint32_t *list)
     return c.nb;
 }
 
+/* Neighbours of gas particle i: particles with w > 0 (gasconstraint.cpp:46)
+ * closer than h, in visiting order, at most max_neighbors. */
+static int gas_visit(void *vctx, uint32_t j) {
+    nb_ctx *c = (nb_ctx *)vctx;
+    if (j == c->i) return 0;
+    float d2 = dist2f(c->pi32, c->s->sx32 + 4 * j);
+    if (d2 < c->s->h2f && c->s->sx32[4 * j + 3] > 0.f) {
+        if (c->nb >= c->s->p.max_neighbors) return 1;
+        c->list[c->nb++] = j;
+    }
+    return 0;
+}
+
+static uint32_t gas_neighbors(const orc_system *s, uint32_t i, uint32_t *list) {
+    nb_ctx c = {s, i, 0, s->p.max_neighbors, s->sx32 + 4 * i, list};
+    int g[3];
+    grid_cell(s, s->sx32 + 4 * i, g);
+    for_each_candidate(s, g, s->fluid_rad, gas_visit, &c);
+    return c.nb;
+}
+
+/* The lambda half of GasConstraint::project (gasconstraint.cpp:34-83):
+ * rho = sum poly6 m_j s_j + poly6(0) m_i (s_j = S_SOLID for solid-like
+ * neighbours), gradients unweighted, lambda = -(rho / rho0 - 1) / (denom +
+ * relaxation); an open gas adds v' (1 - rho / rho0) (-drag) to the force
+ * (gasconstraint.cpp:80). */
+static void gas_lambda(orc_system *s, uint32_t i, uint32_t *list) {
+    uint32_t nb = gas_neighbors(s, i, list);
+    s->nb_fluid[s->sorted_idx[i]] = nb;
+    const real *pi = s->sx + 4 * i;
+    const double rho0 = s->srho0[i];
+    const double h = s->p.kernel_radius, h2 = h * h;
+    real ro = 0, denom = 0, grad[3] = {0, 0, 0};
+    for (uint32_t k = 0; k < nb; ++k) {
+        const real *pj = s->sx + 4 * list[k];
+        real r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+        real r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        real rlen = sqrt(r2);
+        real hm2 = h2 - r2, hm = h - rlen;
+        const double sw = s->sphase[list[k]] >= PBD_PHASE_CLOTH ? (double)s->p.gas_solid_density_weight : 1.0;
+        ro += sw * s->poly6 * hm2 * hm2 * hm2 / pj[3];
+        real sg[3] = {0, 0, 0};
+        if (dist2f(s->sx32 + 4 * i, s->sx32 + 4 * list[k]) >= K_MIN_SPIKY2)
+            for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * (-s->spiky * hm * hm) / rho0;
+        for (int d = 0; d < 3; ++d) {
+            grad[d] -= sg[d];
+            denom += sg[d] * sg[d];
+        }
+    }
+    ro += s->poly6_self / pi[3];
+    denom += grad[0] * grad[0] + grad[1] * grad[1] + grad[2] * grad[2];
+    const real ratio = ro / rho0;
+    s->glambda[i] = -(ratio - 1.0) / (denom + s->relax);
+    s->lambda[i] = 0.0;
+    const uint32_t o = s->sorted_idx[i];
+    if (s->gas_open[o])
+        for (int d = 0; d < 3; ++d) s->force[4 * o + d] += s->v[4 * o + d] * ((1.0 - ratio) * -(double)s->p.gas_drag);
+}
+
 /* findLambdasD (integration_kernel.cuh:521-593). */
 static void compute_lambdas(orc_system *s) {
     const uint32_t n = s->n;
@@ -381,6 +466,10 @@ static void compute_lambdas(orc_system *s) {
 #pragma omp for schedule(dynamic, 1024)
         for (long long ii = 0; ii < (long long)n; ++ii) {
             uint32_t i = (uint32_t)ii;
+            if (s->sphase[i] == PBD_PHASE_GAS) {
+                gas_lambda(s, i, list);
+                continue;
+            }
             if (s->sphase[i] != PBD_PHASE_FLUID) {
                 s->lambda[i] = 0.0;
                 continue;
@@ -451,6 +540,51 @@ static void fluid_delta(const orc_system *s, uint32_t i, uint32_t *list, real ou
         for (int d = 0; d < 3; ++d) delta[d] += coef * sg[d];
     }
     double div = (s->p.flags & PBD_FLAG_DELTA_OVER_RHO0) ? s->srho0[i] : s->srho0[i] + (double)nb;
+    for (int d = 0; d < 3; ++d) out[d] = delta[d] / div;
+}
+
+/* The delta half of GasConstraint::project (gasconstraint.cpp:86-121):
+ * sum (lambda_i + lambda_j + s_corr) spikyGrad / rho0 / (neighbours + 1),
+ * lambda_j of gas neighbours only (the reference's per-constraint lambdas),
+ * s_corr = -K_P (poly6(r) / poly6(DQ_P h))^n, spikyGrad zero below the FP32
+ * length cut-off.  The vorticity term goes to the force: f += sum (-|w| r_y,
+ * |w| r_x, 0) poly6(r), w = spikyGrad evaluated at |r|^2 (the reference
+ * passes glm::dot(r, r)) times v'_j componentwise; zero for |r|^2 >= h. */
+static void gas_delta(orc_system *s, uint32_t i, uint32_t *list, real out[3]) {
+    uint32_t nb = gas_neighbors(s, i, list);
+    const real *pi = s->sx + 4 * i;
+    const double h = s->p.kernel_radius, h2 = h * h;
+    real delta[3] = {0, 0, 0}, fv[2] = {0, 0};
+    for (uint32_t k = 0; k < nb; ++k) {
+        uint32_t j = list[k];
+        const real *pj = s->sx + 4 * j;
+        real r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+        real r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        real rlen = sqrt(r2);
+        real hm2 = h2 - r2, hm = h - rlen;
+        real wp = s->poly6 * hm2 * hm2 * hm2;
+        const int far = dist2f(s->sx32 + 4 * i, s->sx32 + 4 * j) >= K_MIN_SPIKY2;
+        real sg[3] = {0, 0, 0};
+        if (far)
+            for (int d = 0; d < 3; ++d) sg[d] = r[d] / rlen * (-s->spiky * hm * hm);
+        real corr = -s->gas_scorr_k * scorr_pow(s, wp * s->gas_scorr_inv_ref);
+        real lj = s->sphase[j] == PBD_PHASE_GAS ? s->glambda[j] : (real)0.0;
+        real coef = s->glambda[i] + lj + corr;
+        for (int d = 0; d < 3; ++d) delta[d] += coef * sg[d];
+        if (far && r2 < h) {
+            const real *vj = s->v + 4 * s->sorted_idx[j];
+            real hq = h - r2;
+            real w[3];
+            for (int d = 0; d < 3; ++d) w[d] = r[d] / rlen * (-s->spiky * hq * hq) * vj[d];
+            real wl = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            fv[0] -= wl * r[1] * wp;
+            fv[1] += wl * r[0] * wp;
+        }
+    }
+    const uint32_t o = s->sorted_idx[i];
+    s->force[4 * o] += fv[0];
+    s->force[4 * o + 1] += fv[1];
+    const double div = s->srho0[i] * (double)(nb + 1);
     for (int d = 0; d < 3; ++d) out[d] = delta[d] / div;
 }
 
@@ -590,6 +724,10 @@ static void solve_pass(orc_system *s, int mask) {
             int t = 0;
             if ((mask & DO_FLUID) && ph == PBD_PHASE_FLUID) {
                 fluid_delta(s, i, list, dd);
+                for (int d = 0; d < 3; ++d) np[d] += dd[d];
+                t = 1;
+            } else if ((mask & DO_FLUID) && ph == PBD_PHASE_GAS) {
+                gas_delta(s, i, list, dd);
                 for (int d = 0; d < 3; ++d) np[d] += dd[d];
                 t = 1;
             } else if ((mask & DO_CONTACT) && ph >= PBD_PHASE_CLOTH) {
@@ -831,7 +969,7 @@ void orc_update(orc_system *s, double dt) {
         any_fluid |= s->phase[i] == PBD_PHASE_FLUID;
         any_contact |= s->phase[i] >= PBD_PHASE_CLOTH;
     }
-    int mask = DO_WORLD | (any_fluid ? DO_FLUID : 0) | (any_contact ? DO_CONTACT : 0);
+    int mask = DO_WORLD | ((any_fluid || s->has_gas) ? DO_FLUID : 0) | (any_contact ? DO_CONTACT : 0);
     orc_integrate(s, dt);
     for (uint32_t it = 0; it < s->p.iterations; ++it) {
         orc_build_grid(s);
@@ -877,7 +1015,21 @@ void orc_get_grid(const orc_system *s, uint32_t *sorted_hash, uint32_t *sorted_i
 }
 
 void orc_get_lambdas(const orc_system *s, double *out) {
-    for (uint32_t p = 0; p < s->n; ++p) out[s->sorted_idx[p]] = R_VAL(s->lambda[p]);
+    for (uint32_t p = 0; p < s->n; ++p)
+        out[s->sorted_idx[p]] = R_VAL(s->sphase[p] == PBD_PHASE_GAS ? s->glambda[p] : s->lambda[p]);
+}
+
+void orc_set_gas_open(orc_system *s, uint32_t first, uint32_t count, int open) {
+    for (uint32_t k = first; k < first + count && k < s->n; ++k)
+        if (s->phase[k] == PBD_PHASE_GAS) s->gas_open[k] = open ? 1 : 0;
+}
+
+void orc_get_forces(const orc_system *s, double *out) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) out[k] = R_VAL(s->force[k]);
+}
+
+void orc_set_forces(orc_system *s, const double *f) {
+    for (size_t k = 0; k < 4ull * s->n; ++k) s->force[k] = f[k];
 }
 
 #ifdef ORC_DUAL

@@ -55,6 +55,11 @@ void orc_set_velocities(orc_system *s, const double *vel);
 void orc_get_grid(const orc_system *s, uint32_t *sorted_hash, uint32_t *sorted_index,
                   uint32_t *cell_start, uint32_t *cell_end);
 void orc_get_lambdas(const orc_system *s, double *out);
+/* Gas phase: open / close the gas of [first, first+count); the force every
+ * particle carries into the next step (4n doubles). */
+void orc_set_gas_open(orc_system *s, uint32_t first, uint32_t count, int open);
+void orc_get_forces(const orc_system *s, double *out);
+void orc_set_forces(orc_system *s, const double *f);
 /* Neighbour count of every particle in the last fluid / contact pass. */
 void orc_get_neighbor_counts(const orc_system *s, uint32_t *fluid, uint32_t *contact);
 /* Only in the dual-number build (liboracle_dual.so). */

@@ -40,6 +40,7 @@ def load():
         lib.refcpu_num.restype = I
         lib.refcpu_get.argtypes = [P, PD, PD]
         lib.refcpu_destroy.argtypes = [P]
+        lib.refcpu_gas_project.argtypes = [I, PD, PD, PD, ctypes.POINTER(ctypes.c_int), D, I, I, PD, PD]
         _lib = lib
     return _lib
 
@@ -80,3 +81,22 @@ class RefCPU:
             self.close()
         except Exception:
             pass
+
+
+def gas_project(xy, v, imass, solid, density: float, open_: bool, iterations: int):
+    """The reference's GasConstraint::project run `iterations` times on 2-D
+    particles (solid[i] != 0: SOLID neighbour, else gas); returns the
+    estimates and forces, (n, 2) each."""
+    lib = load()
+    xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+    n = xy.shape[0]
+    v = np.ascontiguousarray(v, np.float64).reshape(n, 2)
+    imass = np.ascontiguousarray(imass, np.float64).reshape(n)
+    solid = np.ascontiguousarray(solid, np.int32).reshape(n)
+    out_x = np.empty((n, 2))
+    out_f = np.empty((n, 2))
+    pd = ctypes.POINTER(ctypes.c_double)
+    lib.refcpu_gas_project(n, xy.ctypes.data_as(pd), v.ctypes.data_as(pd), imass.ctypes.data_as(pd),
+                           solid.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), float(density), int(bool(open_)),
+                           int(iterations), out_x.ctypes.data_as(pd), out_f.ctypes.data_as(pd))
+    return out_x, out_f

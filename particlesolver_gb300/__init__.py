@@ -35,7 +35,7 @@ FLAG_KERNEL_UNITS = 1 << 4
 HEADER = _build.ROOT / "include" / "pbd.h"
 
 
-ABI_VERSION = 2  # PBD_ABI_VERSION of include/pbd.h that these mirrors follow
+ABI_VERSION = 3  # PBD_ABI_VERSION of include/pbd.h that these mirrors follow
 
 
 class PbdParams(ctypes.Structure):
@@ -65,11 +65,22 @@ class PbdParams(ctypes.Structure):
         ("twod_z", ctypes.c_float),
         ("flags", ctypes.c_uint32),
         ("solid_density_weight", ctypes.c_float),
+        ("gas_gravity_scale", ctypes.c_float),
+        ("gas_scorr_k", ctypes.c_float),
+        ("gas_scorr_dq", ctypes.c_float),
+        ("gas_solid_density_weight", ctypes.c_float),
+        ("gas_drag", ctypes.c_float),
     ]
 
     def __init__(self, **kw):
         super().__init__()
-        self.solid_density_weight = 1.0  # pbd_default_params' value
+        # pbd_default_params' values of the fields whose zero means something
+        self.solid_density_weight = 1.0
+        self.gas_gravity_scale = -0.2
+        self.gas_scorr_k = 0.2
+        self.gas_scorr_dq = 0.25
+        self.gas_solid_density_weight = 0.5
+        self.gas_drag = 50.0
         self.update(**kw)
 
     def as_dict(self) -> dict:
@@ -165,6 +176,8 @@ _SIGNATURES = {
     "pbd_get_positions": ([_P, _U32, _U32, _P, _I, _P], _I),
     "pbd_get_velocities": ([_P, _U32, _U32, _P, _I, _P], _I),
     "pbd_get_phases": ([_P, _PI], _I),
+    "pbd_set_gas_open": ([_P, _U32, _U32, _I], _I),
+    "pbd_get_forces": ([_P, _PF], _I),
     "pbd_get_device_buffers": ([_P, ctypes.POINTER(PbdDeviceBuffers)], _I),
     "pbd_add_fluid": ([_P, _PI, _PI, _F, _F, ctypes.c_uint64], _I),
     "pbd_add_particle_grid": ([_P, _PI, _PI, _F, _I, ctypes.c_uint64], _I),
@@ -452,6 +465,16 @@ class ParticleSystem:
     def phases(self) -> np.ndarray:
         out = np.empty(self.num_particles, np.int32)
         self._check(self.lib.pbd_get_phases(self.h, out.ctypes.data_as(_PI)))
+        return out
+
+    def set_gas_open(self, first: int, count: int, open_: bool = True):
+        """Open (or close) the gas particles of [first, first + count)."""
+        self._check(self.lib.pbd_set_gas_open(self.h, int(first), int(count), int(bool(open_))))
+
+    def forces(self) -> np.ndarray:
+        """(n, 4) force each particle carries into the next prediction."""
+        out = np.empty((self.num_particles, 4), np.float32)
+        self._check(self.lib.pbd_get_forces(self.h, out.ctypes.data_as(_PF)))
         return out
 
     def device_buffers(self) -> PbdDeviceBuffers:

@@ -757,7 +757,12 @@ cudaError_t grow(T **p, size_t &have, size_t want) {
     return e;
 }
 
-int differentiable(pbd_system *) { return PBD_OK; }
+// The adjoint covers every stage of the step except the gas phase.
+int differentiable(pbd_system *s) {
+    if (s->n_gas)
+        return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED, "the adjoint does not cover the gas phase (the system holds gas particles)");
+    return PBD_OK;
+}
 
 }  // namespace
 }  // namespace pbd

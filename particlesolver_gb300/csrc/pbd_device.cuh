@@ -20,6 +20,10 @@ enum : uint32_t {
     kFlagDeltaOverRho0 = 1u << 2,
     kFlagDistanceMassWeighted = 1u << 3,
     kFlagKernelUnits = 1u << 4,
+    // Set by the host, never by the caller: the system holds gas particles,
+    // so the prediction applies the per-particle force and the gas gravity
+    // and keeps the step's velocity v' for the gas terms.
+    kFlagHasGas = 1u << 16,
 };
 
 // Stage mask of the fused per-particle solve kernel.
@@ -61,6 +65,12 @@ struct DevParams {
     uint32_t flags;
     float solid_w;       // density weight of neighbours of phase >= CLOTH
     float rands[6];      // wall jitter uniforms
+    // gas phase (gasconstraint.cpp / .h, simulation.h:21)
+    float3 gas_gravity;     // gravity times gas_gravity_scale
+    float gas_scorr_k;      // K_P (times h^2 in kernel units)
+    float gas_scorr_inv_ref;// 1 / (poly6 * (h^2 - (DQ_P h)^2)^3)
+    float gas_solid_w;      // S_SOLID: density weight of phases >= CLOTH
+    float gas_drag;         // open gas: force += v (1 - rho / rho0) (-gas_drag)
     uint32_t iterations; // solver iterations per step
     float max_dt;        // step length clamp
     // First cell of this scene in the cell space shared by every scene of a

@@ -38,15 +38,21 @@ inline unsigned blocks_for(uint32_t n, int per_block = kBlock) {
 // from positions at the end of the step).  When counts is given, the cell
 // hash of the predicted position is computed and counted here too, which is
 // the first grid build's calcHashD (integration_kernel.cuh:206-225).  The
-// step is min(dt, max_dt) of the particle's scene.
+// step is min(dt, max_dt) of the particle's scene.  In a system with gas
+// (kFlagHasGas) the step's velocity is the CPU reference's (simulation.cpp:
+// 142-153): v' = v + dt g' + dt f, with g' = gravity * gas_gravity_scale for
+// gas particles and f the force the gas terms accumulated in the last step,
+// which is cleared; v' is stored for the gas terms of this step (the final
+// velocity update overwrites it).
 template <bool B>
 __global__ void __launch_bounds__(kBlock) k_predict(DevParams P0, uint32_t n, float dt_in,
                                                     float4 *__restrict__ x,
-                                                    const float4 *__restrict__ v,
+                                                    float4 *__restrict__ v,
                                                     float4 *__restrict__ x_old,
                                                     uint32_t *__restrict__ hash,
                                                     uint32_t *__restrict__ slot,
-                                                    uint32_t *__restrict__ counts) {
+                                                    uint32_t *__restrict__ counts,
+                                                    GasBuffers gas) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DevParams P = scene_params<B>(P0, i);
@@ -54,7 +60,19 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevParams P0, uint32_t n, fl
     float4 p = x[i];
     const float4 vel = v[i];
     x_old[i] = p;
-    float3 vv = make_float3(vel.x, vel.y, vel.z) + P.gravity * dt;
+    float3 vv;
+    if (P.flags & kFlagHasGas) {
+        const float3 g = gas.phase[i] == kGas ? P.gas_gravity : P.gravity;
+        const float3 f = f3(gas.force[i]);
+        gas.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        // v + dt g' + dt f with the rounding fixed (the same in every
+        // instantiation of this kernel)
+        vv = make_float3(__fmaf_rn(f.x, dt, __fmaf_rn(g.x, dt, vel.x)), __fmaf_rn(f.y, dt, __fmaf_rn(g.y, dt, vel.y)),
+                         __fmaf_rn(f.z, dt, __fmaf_rn(g.z, dt, vel.z)));
+        v[i] = make_float4(vv.x, vv.y, vv.z, vel.w);
+    } else {
+        vv = make_float3(vel.x, vel.y, vel.z) + P.gravity * dt;
+    }
     p.x += vv.x * dt;
     p.y += vv.y * dt;
     p.z += vv.z * dt;
@@ -454,6 +472,64 @@ struct LambdaAcc {
     }
 };
 
+// The lambda half of GasConstraint::project (cpu/src/constraint/
+// gasconstraint.cpp:34-83) for gas particle i (sorted slot), every lane of
+// its group taking part: neighbours are the particles with w > 0 (any phase)
+// closer than h, first max_nb in visiting order; rho = sum poly6(r) m_j s_j +
+// poly6(0) m_i with s_j = gas_solid_w for phases >= CLOTH (S_SOLID, gas
+// weights no gradient); grad_j = -spiky(r) / rho0; lambda = -(rho / rho0 -
+// 1) / (sum |grad_j|^2 + |sum grad_j|^2 + relaxation).  The gas lambda goes
+// to gas.lam (sxl keeps 0, so fluid corrections see no gas lambda, as the
+// reference's per-constraint lambdas, gasconstraint.cpp:99), and an open
+// gas adds v' (1 - rho / rho0) (-gas_drag) to the particle's force
+// (gasconstraint.cpp:80).
+template <int TPP>
+__device__ void gas_lambda(const DevParams &P, const Group<TPP> &G, uint32_t i, float4 pi4, float rho0,
+                           const float4 *__restrict__ sx, const SortedAttr *__restrict__ sattr,
+                           const uint32_t *__restrict__ cell_first, const GasBuffers &gas,
+                           float4 *__restrict__ sxl) {
+    const float3 pi = f3(pi4);
+    const float inv_rho0 = 1.f / rho0;
+    const float spiky_r = -P.spiky * inv_rho0;
+    float ro = 0.f, denom = 0.f;
+    float3 grad = make_float3(0.f, 0.f, 0.f);
+    group_walk<TPP>(
+        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+        [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && pj.w > 0.f; },
+        [&](uint32_t j, const float4 &pj, float d2) {
+            const float hm2 = P.h2 - d2;
+            const float sw = (sattr[j].phase >= kCloth) ? P.gas_solid_w : 1.f;
+            ro += P.poly6 * hm2 * hm2 * hm2 / pj.w * sw;
+            const float rs = rsqrtf(fmaxf(d2, kMinSpiky2));
+            const float hm = P.h - d2 * rs;
+            const float sc = (d2 >= kMinSpiky2) ? spiky_r * hm * hm * rs : 0.f;
+            const float3 sg = (pi - f3(pj)) * sc;
+            grad -= sg;
+            denom += dot3(sg, sg);
+        });
+    ro = G.sum(ro);
+    denom = G.sum(denom);
+    grad.x = G.sum(grad.x);
+    grad.y = G.sum(grad.y);
+    grad.z = G.sum(grad.z);
+    if (G.lane != 0) return;
+    ro += P.poly6_self / pi4.w;
+    denom += dot3(grad, grad);
+    const float ratio = ro * inv_rho0;
+    gas.lam[i] = -(ratio - 1.f) / (denom + P.relax);
+    sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
+    const uint32_t o = gas.sidx[i];
+    if (gas.open[o]) {
+        const float4 vv = gas.v[o];
+        float4 f = gas.force[o];
+        const float k = (1.f - ratio) * -P.gas_drag;
+        f.x += vv.x * k;
+        f.y += vv.y * k;
+        f.z += vv.z * k;
+        gas.force[o] = f;
+    }
+}
+
 // findLambdasD + collideCellRadius (integration_kernel.cuh:481-593): for a
 // fluid particle, neighbours are all particles with |r|^2 < h^2 in the
 // (2 ceil(h/cell) + 1)^3 stencil (no phase filter), capped at max_nb in
@@ -468,7 +544,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
                                                    const float4 *__restrict__ sx,
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
-                                                   float4 *__restrict__ sxl) {
+                                                   float4 *__restrict__ sxl, GasBuffers gas) {
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -477,6 +553,10 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
     const SortedAttr a = sattr[i];
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
+    if (a.phase == kGas) {
+        gas_lambda<TPP>(P, G, i, pi4, a.rho0, sx, sattr, cell_first, gas, sxl);
+        return;
+    }
     if (a.phase != kFluid) {
         if (G.lane == 0) sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
         return;
@@ -558,6 +638,63 @@ __device__ __forceinline__ void delta_add(const DevParams &P, float3 &delta, boo
         const float hz = P.h - sqrtf(d2);
         delta.y += coef * (-P.spiky * hz * hz * kEps);
     }
+}
+
+// The delta half of GasConstraint::project (gasconstraint.cpp:86-121) for
+// gas particle i, every lane of its group taking part and each returning
+// the total: the lambda pass's neighbours (w > 0, closer than h), delta =
+// sum (lambda_i + lambda_j + s_corr) spiky(r) / rho0 / (neighbours + 1),
+// lambda_j from gas neighbours only, s_corr = -gas_scorr_k (W(r) / W(DQ_P
+// h))^n; the spiky gradient is zero below the 1e-4 length cut-off (the
+// reference returned zero at r = 0).  The reference's vorticity term goes
+// to the force: f += sum (-|w| r_y, |w| r_x, 0) poly6(r) with w = g(r) * v'_j
+// componentwise and g the spiky gradient evaluated at |r|^2 in place of
+// |r| (gasconstraint.cpp:109-113 passes glm::dot(r, r)), zero for |r|^2 >= h.
+// The particle's contact count (gasconstraint.cpp:119) is zero here: gas
+// takes no part in contacts.
+template <int TPP>
+__device__ float3 gas_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float3 pi, float rho0,
+                            const float4 *__restrict__ sx, const SortedAttr *__restrict__ sattr,
+                            const uint32_t *__restrict__ cell_first, const GasBuffers &gas) {
+    const float lam_i = gas.lam[i];
+    float3 delta = make_float3(0.f, 0.f, 0.f), fv = make_float3(0.f, 0.f, 0.f);
+    const uint32_t nb = group_walk<TPP>(
+        P, G, pi, grid_pos(P, pi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+        [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && pj.w > 0.f; },
+        [&](uint32_t j, const float4 &pj, float d2) {
+            const float3 r = pi - f3(pj);
+            const float hm2 = P.h2 - d2;
+            const float wp = P.poly6 * hm2 * hm2 * hm2;
+            const float lam_j = (sattr[j].phase == kGas) ? gas.lam[j] : 0.f;
+            const float corr = -P.gas_scorr_k * scorr_pow(P, wp * P.gas_scorr_inv_ref);
+            const float rs = rsqrtf(fmaxf(d2, kMinSpiky2));
+            const float hm = P.h - d2 * rs;
+            const bool far = d2 >= kMinSpiky2;
+            const float sc = far ? -P.spiky * hm * hm * rs : 0.f;
+            delta += r * ((lam_i + lam_j + corr) * sc);
+            if (far && d2 < P.h) {
+                const float hq = P.h - d2;
+                const float gsc = -P.spiky * hq * hq * rs;
+                const float4 vj = gas.v[gas.sidx[j]];
+                const float3 w = make_float3(r.x * gsc * vj.x, r.y * gsc * vj.y, r.z * gsc * vj.z);
+                const float wl = len3(w) * wp;
+                fv.x -= wl * r.y;
+                fv.y += wl * r.x;
+            }
+        });
+    delta.x = G.sum(delta.x);
+    delta.y = G.sum(delta.y);
+    delta.z = G.sum(delta.z);
+    fv.x = G.sum(fv.x);
+    fv.y = G.sum(fv.y);
+    if (G.lane == 0) {
+        const uint32_t o = gas.sidx[i];
+        float4 f = gas.force[o];
+        f.x += fv.x;
+        f.y += fv.y;
+        gas.force[o] = f;
+    }
+    return delta / (rho0 * (float)(nb + 1u));
 }
 
 // solveFluidsD (integration_kernel.cuh:596-642): same neighbour set as the
@@ -811,7 +948,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
                                                         const float4 *__restrict__ sx,
                                                         const SortedAttr *__restrict__ sattr,
                                                         const uint32_t *__restrict__ cell_first,
-                                                        float4 *__restrict__ sxl, NbList L) {
+                                                        float4 *__restrict__ sxl, NbList L, GasBuffers gas) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DevParams P = scene_params<B>(P0, i);
@@ -824,6 +961,11 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
     if (SKIN && !reuse) L.sref[i] = pi4;
+    if (a.phase == kGas) {  // no list: the gas passes walk the grid (skin lists are off with gas)
+        L.count[i] = 0u;
+        gas_lambda<1>(P, Group<1>(), i, pi4, a.rho0, sx, sattr, cell_first, gas, sxl);
+        return;
+    }
     if (a.phase != kFluid) {
         sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
         if (!reuse) L.count[i] = 0u;
@@ -920,7 +1062,8 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
                                                                 const float4 *__restrict__ sx,
                                                                 const SortedAttr *__restrict__ sattr,
                                                                 const uint32_t *__restrict__ cell_first,
-                                                                float4 *__restrict__ sxl, NbList L) {
+                                                                float4 *__restrict__ sxl, NbList L,
+                                                                GasBuffers gas) {
     extern __shared__ uint32_t s_nb[];
     const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
     if (i >= n) return;
@@ -934,6 +1077,11 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
     const float4 pi4 = sx[i];
     const float3 pi = f3(pi4);
     if (SKIN && !reuse) L.sref[i] = pi4;
+    if (a.phase == kGas) {  // no list: the gas passes walk the grid (skin lists are off with gas)
+        L.count[i] = 0u;
+        gas_lambda<1>(P, Group<1>(), i, pi4, a.rho0, sx, sattr, cell_first, gas, sxl);
+        return;
+    }
     if (a.phase != kFluid) {
         sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
         if (!reuse) L.count[i] = 0u;
@@ -1103,7 +1251,8 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint
                                                   const uint32_t *__restrict__ cell_first,
                                                   const float4 *__restrict__ sxl,
                                                   const float4 *__restrict__ x_old,
-                                                  float4 *__restrict__ x, NbList L, bool use_list) {
+                                                  float4 *__restrict__ x, NbList L, bool use_list,
+                                                  GasBuffers gas) {
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -1117,6 +1266,9 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint
     if ((mask & kDoFluid) && a.phase == kFluid) {
         if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, cell_first, L);
         else np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
+        touched = true;
+    } else if ((mask & kDoFluid) && a.phase == kGas) {
+        np = np + gas_delta<TPP>(P, G, i, np, a.rho0, sx, sattr, cell_first, gas);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
         np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
@@ -1435,12 +1587,12 @@ size_t scan_partial_count(uint32_t elements) {
     return (elements + kScanTile - 1) / kScanTile;
 }
 
-cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, const float4 *v,
+cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, float4 *v,
                            float4 *x_old, uint32_t *hash, uint32_t *slot, uint32_t *counts,
-                           cudaStream_t s) {
+                           cudaStream_t s, const GasBuffers &gas) {
     if (n == 0) return cudaSuccess;
-    if (P.table) k_predict<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts);
-    else k_predict<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts);
+    if (P.table) k_predict<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts, gas);
+    else k_predict<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts, gas);
     return cudaGetLastError();
 }
 
@@ -1530,7 +1682,7 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
 
 template <bool B>
 void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
-                          const NbList &L, cudaStream_t s) {
+                          const NbList &L, cudaStream_t s, const GasBuffers &gas) {
     const unsigned nb = blocks_for(n);
     // the list radius's stencil; a batch whose fluid scenes differ, and any
     // batch with a skin, runs the runtime-radius walk (rad 0)
@@ -1546,10 +1698,10 @@ void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, co
 #define PBD_LIST(R, S)                                                                                      \
     if (shared)                                                                                             \
         k_lambda_slist<R, B, S><<<nbs, kListBlock, smem, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr,   \
-                                                              g.cell_first, sxl, L);                        \
+                                                              g.cell_first, sxl, L, gas);                   \
     else                                                                                                    \
         k_lambda_list<R, B, S><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, \
-                                                     sxl, L)
+                                                     sxl, L, gas)
     if (L.sref) {
         if (rad == 1) {
             PBD_LIST(1, true);
@@ -1571,32 +1723,32 @@ void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, co
 }
 
 cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
-                          const NbList &L, uint32_t tpp, cudaStream_t s) {
+                          const NbList &L, uint32_t tpp, cudaStream_t s, const GasBuffers &gas) {
     if (n == 0) return cudaSuccess;
     if (tpp == 1 && L.slot) {
-        if (P.table) lambda_list_dispatch<true>(P, n, iter_left, g, sxl, L, s);
-        else lambda_list_dispatch<false>(P, n, iter_left, g, sxl, L, s);
+        if (P.table) lambda_list_dispatch<true>(P, n, iter_left, g, sxl, L, s, gas);
+        else lambda_list_dispatch<false>(P, n, iter_left, g, sxl, L, s, gas);
         return cudaGetLastError();
     }
     if (P.table) {
-        PBD_TPP_DISPATCH(tpp, true, k_lambda, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
+        PBD_TPP_DISPATCH(tpp, true, k_lambda, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, gas);
     } else {
-        PBD_TPP_DISPATCH(tpp, false, k_lambda, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl);
+        PBD_TPP_DISPATCH(tpp, false, k_lambda, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, sxl, gas);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t iter_left, const GridBuffers &g,
                          const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
-                         uint32_t tpp, cudaStream_t s) {
+                         uint32_t tpp, cudaStream_t s, const GasBuffers &gas) {
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
     if (P.table) {
         PBD_TPP_DISPATCH(tpp, true, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
-                         g.cell_first, sxl, x_old, x, L, use_list);
+                         g.cell_first, sxl, x_old, x, L, use_list, gas);
     } else {
         PBD_TPP_DISPATCH(tpp, false, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
-                         g.cell_first, sxl, x_old, x, L, use_list);
+                         g.cell_first, sxl, x_old, x, L, use_list, gas);
     }
     return cudaGetLastError();
 }

@@ -43,6 +43,17 @@ struct NbList {
     uint32_t assemble;
 };
 
+// Per-particle arrays of the gas phase (all null in a system without gas
+// particles).
+struct GasBuffers {
+    const int *phase;      // [cap] original order
+    float4 *force;         // [cap] original order: force the next prediction applies
+    const uint8_t *open;   // [cap] original order: 1 = open gas
+    float *lam;            // [cap] sorted order: gas lambda
+    float4 *v;             // [cap] original order: the step's velocity v' (set by the prediction)
+    const uint32_t *sidx;  // [cap] sorted slot -> original index
+};
+
 // Device words of the skin-list schedule: [0] reuse, [1] overflow, [2 + k]
 // largest displacement / h since the list build, seen in iteration k (k <
 // kSkinWords - 3), [kSkinWords - 1] iterations of the step that reused.
@@ -77,9 +88,9 @@ struct BodyBuffers {
 
 size_t scan_partial_count(uint32_t elements);
 
-cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, const float4 *v,
+cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, float4 *v,
                            float4 *x_old, uint32_t *hash, uint32_t *slot, uint32_t *counts,
-                           cudaStream_t s);
+                           cudaStream_t s, const GasBuffers &gas = GasBuffers{});
 cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash,
                               uint32_t *slot, uint32_t *counts, cudaStream_t s);
 // counts[0..cells] -> exclusive offsets; counts[cells] must be zero on entry.
@@ -119,10 +130,10 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
 // in the step after this one (a scene with K iterations is active while
 // iter_left < K); the single-stage entry points pass 0.
 cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, const GridBuffers &g, float4 *sxl,
-                          const NbList &L, uint32_t tpp, cudaStream_t s);
+                          const NbList &L, uint32_t tpp, cudaStream_t s, const GasBuffers &gas = GasBuffers{});
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t iter_left, const GridBuffers &g,
                          const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
-                         uint32_t tpp, cudaStream_t s);
+                         uint32_t tpp, cudaStream_t s, const GasBuffers &gas = GasBuffers{});
 cudaError_t launch_distance(const DevParams &P, uint32_t iter_left, const ConstraintBuffers &c, float4 *x,
                             bool apply_distance, bool apply_pins, cudaStream_t s);
 cudaError_t launch_shapes(const DevParams &P, uint32_t iter_left, const BodyBuffers &b, float4 *x, cudaStream_t s);

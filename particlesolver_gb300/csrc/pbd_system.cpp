@@ -53,6 +53,15 @@ int validate_params(const pbd_params *p, std::string &why) {
         why = "solid_density_weight must be finite and >= 0";
         return PBD_ERR_INVALID_ARGUMENT;
     }
+    if (!(p->gas_scorr_dq >= 0.f && p->gas_scorr_dq < 1.f)) { why = "gas_scorr_dq must be in [0, 1)"; return PBD_ERR_INVALID_ARGUMENT; }
+    if (!(p->gas_solid_density_weight >= 0.f) || !std::isfinite(p->gas_solid_density_weight)) {
+        why = "gas_solid_density_weight must be finite and >= 0";
+        return PBD_ERR_INVALID_ARGUMENT;
+    }
+    if (!std::isfinite(p->gas_gravity_scale) || !std::isfinite(p->gas_scorr_k) || !std::isfinite(p->gas_drag)) {
+        why = "gas_gravity_scale, gas_scorr_k and gas_drag must be finite";
+        return PBD_ERR_INVALID_ARGUMENT;
+    }
     return PBD_OK;
 }
 
@@ -104,6 +113,14 @@ pbd::DevParams make_dev(const pbd_params &p, const float rands[6]) {
     d.flags = p.flags;
     d.solid_w = p.solid_density_weight;
     for (int k = 0; k < 6; ++k) d.rands[k] = rands[k];
+    d.gas_gravity = make_float3(p.gravity[0] * p.gas_gravity_scale, p.gravity[1] * p.gas_gravity_scale,
+                                p.gravity[2] * p.gas_gravity_scale);
+    d.gas_scorr_k = ku ? (float)((double)p.gas_scorr_k * h * h) : p.gas_scorr_k;
+    const double gdq = p.gas_scorr_dq * h;
+    const double gt2 = h * h - gdq * gdq;
+    d.gas_scorr_inv_ref = (float)(1.0 / (poly6 * gt2 * gt2 * gt2));
+    d.gas_solid_w = p.gas_solid_density_weight;
+    d.gas_drag = p.gas_drag;
     d.iterations = p.iterations;
     d.max_dt = p.max_dt;
     d.cell_base = 0;
@@ -201,6 +218,7 @@ int refresh_scenes(pbd_system *s) {
     int rad = -1;
     for (pbd_scene &sc : s->scenes) {
         sc.dev = make_dev(sc.params, s->rands);
+        if (s->n_gas) sc.dev.flags |= pbd::kFlagHasGas;
         sc.dev.cell_base = (uint32_t)base;
         base += sc.dev.num_cells;
         if (base >= (1ull << 31))
@@ -462,7 +480,7 @@ int build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict) {
 
 uint32_t solve_mask(const pbd_system *s) {
     uint32_t m = pbd::kDoWorld;
-    if (s->n_fluid) m |= pbd::kDoFluid;
+    if (s->any_pbf()) m |= pbd::kDoFluid;
     if (s->n_contact) m |= pbd::kDoContact;
     return m;
 }
@@ -488,7 +506,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
         Stage t(s, st, PBD_STAGE_PREDICT, 1);
         CUDA_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
         CUDA_TRY(s, pbd::launch_predict(P, n, dt, s->x, s->v, s->x_old, s->grid.hash, s->grid.slot,
-                                        s->grid.cell_first, st));
+                                        s->grid.cell_first, st, s->gas_buffers()));
     }
     const uint32_t mask = solve_mask(s);
     const uint32_t dist_kernels =
@@ -496,7 +514,9 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
     const uint32_t iters = P.iterations;
     // skin lists: built at the first iteration, reused by later ones while
     // the device check allows (the grid kernels then return at once)
-    bool skin = s->skin > 0.f && s->tpp == 1 && s->nbl.slot && s->sref && s->skin_words && s->n_fluid &&
+    // (not with gas: the gas passes walk the grid, which a reused list's
+    // iterations do not rebuild)
+    bool skin = s->skin > 0.f && s->tpp == 1 && s->nbl.slot && s->sref && s->skin_words && s->n_fluid && !s->n_gas &&
                 iters > 1;
     if (skin && !P.table) {
         // the skin's stencil must not alias on the grid (a batch checks per
@@ -526,15 +546,15 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
             L.reuse = nullptr;
         }
         if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 3 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
-        if (s->n_fluid) {
+        if (s->any_pbf()) {
             Stage t(s, st, PBD_STAGE_LAMBDA, 1);
-            CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, L, s->tpp, st));
+            CUDA_TRY(s, pbd::launch_lambda(P, n, left, s->grid, s->sxl, L, s->tpp, st, s->gas_buffers()));
             s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
         }
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
             CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, L,
-                                          s->list_valid, s->tpp, st));
+                                          s->list_valid, s->tpp, st, s->gas_buffers()));
         }
         if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 3 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (dist_kernels) {
@@ -627,6 +647,11 @@ void pbd_default_params(pbd_params *p) {
     p->twod_z = 0.f;
     p->flags = 0;
     p->solid_density_weight = 1.f;
+    p->gas_gravity_scale = -0.2f;
+    p->gas_scorr_k = 0.2f;
+    p->gas_scorr_dq = 0.25f;
+    p->gas_solid_density_weight = 0.5f;
+    p->gas_drag = 50.f;
 }
 
 const char *pbd_last_error(const pbd_system *s) {
@@ -703,6 +728,9 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->sref);
     dfree(s->skin_words);
     dfree(s->vs);
+    dfree(s->force);
+    dfree(s->gas_open);
+    dfree(s->glam);
     dfree(s->flag);
     dfree(s->grid.hash);
     dfree(s->grid.slot);
@@ -825,7 +853,7 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
     if (!pos_w || !phase) return fail(s, PBD_ERR_INVALID_ARGUMENT, "pos_w and phase are required");
     if ((uint64_t)s->n + n > s->cap)
         return fail(s, PBD_ERR_CAPACITY, "adding %u particles to %u exceeds capacity %u", n, s->n, s->cap);
-    uint32_t nf = 0, nc = 0;
+    uint32_t nf = 0, nc = 0, ng = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const float *p = pos_w + 4ull * i;
         for (int k = 0; k < 4; ++k)
@@ -837,6 +865,13 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
             if (rest_density && !(rest_density[i] > 0.f))
                 return fail(s, PBD_ERR_INVALID_ARGUMENT, "fluid particle %u needs rest density > 0", i);
             ++nf;
+        }
+        if (phase[i] == PBD_PHASE_GAS) {
+            // createGas refuses fixed particles (simulation.cpp:418-421)
+            if (!(p[3] > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "gas particle %u needs inverse mass > 0", i);
+            if (rest_density && !(rest_density[i] > 0.f))
+                return fail(s, PBD_ERR_INVALID_ARGUMENT, "gas particle %u needs rest density > 0", i);
+            ++ng;
         }
         if (phase[i] >= PBD_PHASE_CLOTH) ++nc;
         if (vel)
@@ -859,15 +894,26 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
         const std::vector<uint16_t> tag(n, (uint16_t)(s->scenes.size() - 1u));
         CUDA_TRY(s, cudaMemcpy(s->d_scene_of + off, tag.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
     }
+    if (ng && !s->force) {
+        CUDA_TRY(s, dalloc(&s->force, s->cap));
+        CUDA_TRY(s, dalloc(&s->gas_open, s->cap));
+        CUDA_TRY(s, dalloc(&s->glam, s->cap));
+        CUDA_TRY(s, cudaMemset(s->force, 0, s->cap * sizeof(float4)));
+        CUDA_TRY(s, cudaMemset(s->gas_open, 0, s->cap));
+        CUDA_TRY(s, cudaMemset(s->glam, 0, s->cap * sizeof(float)));
+    }
     s->n += n;
     s->n_fluid += nf;
     s->n_contact += nc;
+    s->n_gas += ng;
     pbd_scene &cur = s->scenes.back();
     cur.count += n;
     cur.n_fluid += nf;
     cur.n_contact += nc;
-    if (nf && cur.n_fluid == nf)
-        if (int rc = refresh_scenes(s)) return rc;  // the shared stencil radius may change
+    cur.n_gas += ng;
+    // the shared stencil radius may change; the first gas sets the has-gas flag
+    if ((nf && cur.n_fluid == nf) || (ng && s->n_gas == ng))
+        if (int rc = refresh_scenes(s)) return rc;
     if (s->n_fluid && !s->vs) CUDA_TRY(s, dalloc(&s->vs, s->cap));
     if (s->n_fluid && !s->nbl.slot && s->list_capacity) {
         CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
@@ -1002,6 +1048,33 @@ int pbd_get_phases(pbd_system *s, int32_t *dst) {
     if (!dst) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dst is NULL");
     CUDA_TRY(s, cudaDeviceSynchronize());
     if (s->n) CUDA_TRY(s, cudaMemcpy(dst, s->phase, s->n * 4ull, cudaMemcpyDeviceToHost));
+    return PBD_OK;
+}
+
+int pbd_set_gas_open(pbd_system *s, uint32_t first, uint32_t count, int open) {
+    SYS_GUARD(s);
+    if ((uint64_t)first + count > s->n)
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "range [%u, %u) exceeds the %u particles", first, first + count, s->n);
+    if (count == 0 || !s->n_gas) return PBD_OK;
+    std::vector<int32_t> ph(count);
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    CUDA_TRY(s, cudaMemcpy(ph.data(), s->phase + first, count * 4ull, cudaMemcpyDeviceToHost));
+    std::vector<uint8_t> flag(count);
+    CUDA_TRY(s, cudaMemcpy(flag.data(), s->gas_open + first, count, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < count; ++k)
+        if (ph[k] == PBD_PHASE_GAS) flag[k] = open ? 1u : 0u;
+    CUDA_TRY(s, cudaMemcpy(s->gas_open + first, flag.data(), count, cudaMemcpyHostToDevice));
+    ++s->version;
+    return PBD_OK;
+}
+
+int pbd_get_forces(pbd_system *s, float *dst) {
+    SYS_GUARD(s);
+    if (!dst) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dst is NULL");
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    if (!s->n) return PBD_OK;
+    if (s->force) CUDA_TRY(s, cudaMemcpy(dst, s->force, s->n * sizeof(float4), cudaMemcpyDeviceToHost));
+    else std::memset(dst, 0, s->n * sizeof(float4));
     return PBD_OK;
 }
 
@@ -1252,7 +1325,7 @@ int pbd_integrate(pbd_system *s, float dt, void *stream) {
     SYS_GUARD(s);
     if (!(dt > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be > 0");
     CUDA_TRY(s, pbd::launch_predict(s->dev, s->n, clamp_dt(s, dt), s->x, s->v, s->x_old, nullptr,
-                                    nullptr, nullptr, (cudaStream_t)stream));
+                                    nullptr, nullptr, (cudaStream_t)stream, s->gas_buffers()));
     s->launches += 1;
     s->grid_valid = false;
     return PBD_OK;
@@ -1276,10 +1349,10 @@ int pbd_solve_fluids(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, 0u, s->grid, s->sxl, s->nbl, s->tpp, st));
+    CUDA_TRY(s, pbd::launch_lambda(s->dev, s->n, 0u, s->grid, s->sxl, s->nbl, s->tpp, st, s->gas_buffers()));
     s->list_valid = s->tpp == 1 && s->nbl.slot != nullptr;
     CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoFluid, 0u, s->grid, s->sxl, s->x_old, s->x, s->nbl,
-                                  s->list_valid, s->tpp, st));
+                                  s->list_valid, s->tpp, st, s->gas_buffers()));
     s->launches += 2;
     return PBD_OK;
 }
@@ -1365,6 +1438,14 @@ int pbd_get_lambdas(pbd_system *s, float *dst) {
     CUDA_TRY(s, cudaMemcpy(idx.data(), s->grid.sorted_idx, n * 4ull, cudaMemcpyDeviceToHost));
     CUDA_TRY(s, cudaMemcpy(sl.data(), s->sxl, n * sizeof(float4), cudaMemcpyDeviceToHost));
     for (uint32_t p = 0; p < n; ++p) dst[idx[p]] = sl[p].w;
+    if (s->n_gas) {  // gas lambdas live in their own sorted array
+        std::vector<float> gl(n);
+        std::vector<int32_t> ph(n);
+        CUDA_TRY(s, cudaMemcpy(gl.data(), s->glam, n * 4ull, cudaMemcpyDeviceToHost));
+        CUDA_TRY(s, cudaMemcpy(ph.data(), s->phase, n * 4ull, cudaMemcpyDeviceToHost));
+        for (uint32_t p = 0; p < n; ++p)
+            if (ph[idx[p]] == PBD_PHASE_GAS) dst[idx[p]] = gl[p];
+    }
     return PBD_OK;
 }
 
@@ -1390,16 +1471,18 @@ int pbd_synchronize(pbd_system *s, void *stream) {
 // body rotations.
 static const uint32_t kStateMagic = 0x50424431u;  // "PBD1"
 
+// State blob: header {magic, version, n, bodies}, x, v, body rotations and,
+// in a system with gas (version 2), the force carried into the next step.
 uint64_t pbd_state_size(const pbd_system *s) {
     if (!s) return 0;
-    return 16ull + 2ull * s->n * sizeof(float4) + (uint64_t)s->bodies.count * sizeof(float4);
+    return 16ull + (s->n_gas ? 3ull : 2ull) * s->n * sizeof(float4) + (uint64_t)s->bodies.count * sizeof(float4);
 }
 
 int pbd_save_state(pbd_system *s, void *dst, uint64_t size) {
     SYS_GUARD(s);
     if (!dst || size < pbd_state_size(s)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "state buffer too small");
     CUDA_TRY(s, cudaDeviceSynchronize());
-    uint32_t hdr[4] = {kStateMagic, 1u, s->n, s->bodies.count};
+    uint32_t hdr[4] = {kStateMagic, s->n_gas ? 2u : 1u, s->n, s->bodies.count};
     char *p = (char *)dst;
     std::memcpy(p, hdr, 16);
     p += 16;
@@ -1411,6 +1494,8 @@ int pbd_save_state(pbd_system *s, void *dst, uint64_t size) {
     p += 2 * pb;
     if (s->bodies.count)
         CUDA_TRY(s, cudaMemcpy(p, s->bodies.quat, s->bodies.count * sizeof(float4), cudaMemcpyDeviceToHost));
+    p += (size_t)s->bodies.count * sizeof(float4);
+    if (s->n_gas && pb) CUDA_TRY(s, cudaMemcpy(p, s->force, pb, cudaMemcpyDeviceToHost));
     return PBD_OK;
 }
 
@@ -1419,7 +1504,8 @@ int pbd_load_state(pbd_system *s, const void *src, uint64_t size) {
     if (!src || size < 16) return fail(s, PBD_ERR_INVALID_ARGUMENT, "state buffer too small");
     uint32_t hdr[4];
     std::memcpy(hdr, src, 16);
-    if (hdr[0] != kStateMagic || hdr[1] != 1u) return fail(s, PBD_ERR_INVALID_ARGUMENT, "not a state blob");
+    if (hdr[0] != kStateMagic || hdr[1] != (s->n_gas ? 2u : 1u))
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "not a state blob of this system");
     if (hdr[2] != s->n || hdr[3] != s->bodies.count)
         return fail(s, PBD_ERR_INVALID_ARGUMENT, "state blob holds %u particles / %u bodies, system has %u / %u",
                     hdr[2], hdr[3], s->n, s->bodies.count);
@@ -1434,6 +1520,8 @@ int pbd_load_state(pbd_system *s, const void *src, uint64_t size) {
     p += 2 * pb;
     if (s->bodies.count)
         CUDA_TRY(s, cudaMemcpy(s->bodies.quat, p, s->bodies.count * sizeof(float4), cudaMemcpyHostToDevice));
+    p += (size_t)s->bodies.count * sizeof(float4);
+    if (s->n_gas && pb) CUDA_TRY(s, cudaMemcpy(s->force, p, pb, cudaMemcpyHostToDevice));
     s->grid_valid = false;
     return PBD_OK;
 }

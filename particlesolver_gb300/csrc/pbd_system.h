@@ -15,7 +15,7 @@ struct pbd_scene {
     pbd_params params{};
     pbd::DevParams dev{};  // parameter block (cell_base set, no table)
     uint32_t first = 0, count = 0;
-    uint32_t n_fluid = 0, n_contact = 0;
+    uint32_t n_fluid = 0, n_contact = 0, n_gas = 0;
 };
 
 struct pbd_system {
@@ -38,6 +38,10 @@ struct pbd_system {
     float4 *sxl = nullptr;  // sorted order: position xyz, PBF lambda w
     float4 *vs = nullptr;   // XSPH scratch: velocities in sorted order
     uint32_t *flag = nullptr;  // finite check
+    // gas phase (allocated with the first gas particle)
+    float4 *force = nullptr;     // force the next prediction applies, original order
+    uint8_t *gas_open = nullptr; // 1 = open gas, original order
+    float *glam = nullptr;       // gas lambda, sorted order
 
     pbd::GridBuffers grid{};
     uint32_t grid_cells = 0;  // cells the grid arrays were sized for
@@ -57,7 +61,7 @@ struct pbd_system {
     pbd::BodyBuffers bodies{};
 
     // phase census for stage selection (all scenes)
-    uint32_t n_fluid = 0, n_contact = 0;
+    uint32_t n_fluid = 0, n_contact = 0, n_gas = 0;
     bool any_xsph = false;  // some scene with fluid, xsph_c != 0 and iterations > 0
 
     uint32_t tpp = 1;     // lanes per particle in the neighbour passes
@@ -117,6 +121,11 @@ struct pbd_system {
     std::string err;
 
     bool batched() const { return scenes.size() > 1; }
+    bool any_pbf() const { return n_fluid || n_gas; }
+    pbd::GasBuffers gas_buffers() const {
+        if (!n_gas) return pbd::GasBuffers{};
+        return pbd::GasBuffers{phase, force, gas_open, glam, v, grid.sorted_idx};
+    }
     const pbd_params &cur_params() const { return scenes.back().params; }
 };
 

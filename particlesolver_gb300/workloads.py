@@ -51,6 +51,7 @@ class Scene:
     pins: np.ndarray | None = None         # (P,) uint32
     pin_points: np.ndarray | None = None   # (P, 3) float32
     bodies: list = field(default_factory=list)  # (first, count, stiffness)
+    open_gas: list = field(default_factory=list)  # (first, count) ranges of open gas
     dt: float = 1.0 / 60.0
     info: dict = field(default_factory=dict)
 
@@ -255,6 +256,8 @@ def apply_to(scene: Scene, system, params=None):
         system.add_point_constraints(scene.pins, scene.pin_points)
     for first, count, st in scene.bodies:
         system.add_rigid_body(first, count, st)
+    for first, count in scene.open_gas:
+        system.set_gas_open(first, count, True)
     return system
 
 
@@ -418,6 +421,71 @@ def granular_column(count: int = 1600, width: int | None = None, radius: float =
                   wall_kinetic_friction=kinetic_friction, twod_z=0.0, flags=FLAG_TWOD)
     return Scene("granular_column", params, pos_w, np.full(count, PHASE_SOLID, np.int32), dt=1.0 / 60.0,
                  info=dict(width=width, rows=rows, seed=seed))
+
+
+def smoke_box(spacing: float = 0.63, half: float = 4.0, twod: bool = False, density: float | None = None,
+              open_gas: bool = True, seed: int = 1096, iterations: int = 3, solid_floor: bool = False) -> Scene:
+    """The CPU reference's smoke scene (initSmokeOpen / initSmokeClosed,
+    cpu/src/simulation.cpp:1096-1134) in 3-D, or in 2-D with twod: gas
+    particles of unit mass on a lattice of spacing 0.63 over [-4, 4)^d,
+    jitter 0.2 U(-0.5, 0.5) per axis (the reference's .2 (frand() - .5),
+    seeded), one gas, open or closed, of rest density 1.5 in 2-D (the
+    reference's value, about the 2-D lattice's poly6 sum) and the lattice's
+    poly6 sum in 3-D unless `density` is given; h = 2, cell h,
+    relaxation 0.01 and the gas constants of gasconstraint.h (the
+    pbd_params defaults), gravity -9.8 (x ALPHA = -0.2 on gas: it rises),
+    3 iterations, dt 1/60, box x (and z) in [-6, 6], y in [-4, 200].  With
+    solid_floor, a fixed solid plate (w = 0) of the same spacing lies below
+    the gas, and a layer of movable solid grains on it, so gas particles
+    have solid neighbours (weighted S_SOLID) and fixed ones (ignored)."""
+    axis = np.arange(-half, half - 1e-9, spacing)
+    dims = 2 if twod else 3
+    if density is None:
+        density = 1.5 if twod else poly6_rest_density(spacing, 2.0)
+    grids = np.meshgrid(*([axis] * dims), indexing="ij")
+    lat = np.stack([g.ravel() for g in grids], 1)
+    n = lat.shape[0]
+    pos = np.zeros((n, 3))
+    pos[:, 0] = lat[:, 0]
+    pos[:, 1] = lat[:, 1]
+    if not twod:
+        pos[:, 2] = lat[:, 2]
+    pos[:, :dims] += 0.2 * uniform(seed, (n, dims), -0.5, 0.5)
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0
+    phase = np.full(n, PHASE_GAS, np.int32)
+    rho0 = np.full(n, density, np.float32)
+    if solid_floor:
+        plane = np.meshgrid(*([axis] * (dims - 1)), indexing="ij")
+        flat = np.stack([g.ravel() for g in plane], 1)
+        m = flat.shape[0]
+        extra = []
+        for y, w in ((-half - 1.2, 0.0), (-half - 0.6, 1.0)):  # fixed plate, then grains
+            q = np.zeros((m, 4), np.float32)
+            q[:, 0] = flat[:, 0]
+            q[:, 1] = y
+            if not twod:
+                q[:, 2] = flat[:, 1]
+            q[:, 3] = w
+            extra.append(q)
+        pos_w = np.concatenate([pos_w] + extra)
+        phase = np.concatenate([phase, np.full(2 * m, PHASE_SOLID, np.int32)])
+        rho0 = np.concatenate([rho0, np.ones(2 * m, np.float32)])
+    h = 2.0
+    cell = h
+    box_lo, box_hi = [-6.0, -4.0 - (2.0 if solid_floor else 0.0), -6.0], [6.0, 200.0, 6.0]
+    grid = [next_pow2((box_hi[0] - box_lo[0]) / cell), next_pow2((box_hi[1] - box_lo[1]) / cell),
+            4 if twod else next_pow2((box_hi[2] - box_lo[2]) / cell)]
+    origin = [box_lo[0], box_lo[1], -2.0 * cell if twod else box_lo[2]]
+    params = dict(particle_radius=0.25, kernel_radius=h, cell_size=cell, grid_size=grid, world_origin=origin,
+                  gravity=[0.0, -9.8, 0.0], box_min=[box_lo[0], box_lo[1], -1.0 if twod else box_lo[2]],
+                  box_max=[box_hi[0], box_hi[1], 1.0 if twod else box_hi[2]], iterations=iterations,
+                  relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0, max_dt=1.0 / 60.0,
+                  max_neighbors=500, twod_z=0.0, flags=FLAG_TWOD if twod else 0)
+    return Scene("smoke_box", params, pos_w, phase, rest_density=rho0,
+                 open_gas=[(0, n)] if open_gas else [], dt=1.0 / 60.0,
+                 info=dict(gas=n, solids=int(pos_w.shape[0] - n), seed=seed, open=open_gas))
 
 
 def batched_scenes(count: int = 512, seed: int = 512, lo: int = 1024, hi: int = 65536) -> list:

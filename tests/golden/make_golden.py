@@ -1,12 +1,17 @@
 """Generates the golden fixtures of tests/golden/ from the reference's own
 code: the reference GPU kernels and thrust functors compiled for the CPU
 (oracle/_ref/librefgpu.so, built from gpu/src/cuda/*.cuh in the reference
-tree).  Run where the reference sources exist:
+tree), and the reference's 2-D CPU solver (oracle/_ref/librefcpu.so, built
+from cpu/src).  Run where the reference sources exist:
 
     python tests/golden/make_golden.py
 
-Each fixture holds the seeded inputs of one small scene and the reference's
-outputs after the grid build, each solver stage and full updates.
+Each ref_*.npz fixture holds the seeded inputs of one small scene and the
+reference's outputs after the grid build, each solver stage and full
+updates.  gas_project.npz holds a 2-D smoke box with solid and fixed
+neighbours and the outputs of the reference's GasConstraint::project
+(gasconstraint.cpp:34-134) after 1 and 3 calls, open and closed: the
+estimates and each particle's force.
 """
 from __future__ import annotations
 
@@ -91,9 +96,36 @@ def scenes():
     }
 
 
+def gas_fixture() -> dict:
+    """Inputs and the reference's gas projection outputs (see the module
+    docstring); velocities are seeded U(-1, 1) per axis."""
+    from oracle import refcpu
+
+    sc = W.smoke_box(twod=True, solid_floor=True, seed=1097)
+    n = sc.n
+    xy = sc.pos_w[:, :2].astype(np.float64)
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :2] = W.uniform(1098, (n, 2), -1.0, 1.0)
+    imass = sc.pos_w[:, 3].astype(np.float64)
+    solid = (sc.phase != W.PHASE_GAS).astype(np.int32)
+    out = dict(pos_w=sc.pos_w, phase=sc.phase, rest_density=sc.rest_density, vel=vel)
+    for open_ in (0, 1):
+        for k in (1, 3):
+            ex, f = refcpu.gas_project(xy, vel[:, :2].astype(np.float64), imass, solid, 1.5, bool(open_), k)
+            out[f"open{open_}_k{k}_pos"] = ex
+            out[f"open{open_}_k{k}_force"] = f
+    return out
+
+
 def main():
     if not refgpu.available():
         raise SystemExit("reference sources not found")
+    from oracle import refcpu
+
+    if refcpu.available():
+        path = HERE / "gas_project.npz"
+        np.savez_compressed(path, **gas_fixture())
+        print(path, path.stat().st_size, "bytes")
     for name, sc in scenes().items():
         data = scene_inputs(sc)
         data.update(stage_outputs(sc))

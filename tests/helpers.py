@@ -131,3 +131,31 @@ def check_granular(pos, gold_pos, rel: float):
     assert abs(mean_y - gmean_y) <= rel * abs(gmean_y), (mean_y, gmean_y)
     sx, gsx = p[:, 0].std(), g[:, 0].std()
     assert abs(sx - gsx) <= rel * gsx, (sx, gsx)
+
+
+def oracle_gas_projection(pos_w, phase, rest_density, vel, params: dict, open_: bool, calls: int):
+    """The oracle's gas passes run `calls` times from the given positions
+    and step velocities (grid build + lambda / delta, no prediction and no
+    walls): the counterpart of one GasConstraint::project per call.  Returns
+    the positions and forces, (n, 2) each."""
+    from oracle import Oracle
+
+    p = params_nolib(params)
+    n = len(pos_w)
+    o = Oracle(p, n)
+    o.add_particles(pos_w, vel, phase, rest_density)
+    if open_:
+        o.set_gas_open(0, n, True)
+    for _ in range(calls):
+        o.build_grid()
+        o.solve_fluids()
+    return o.positions()[:, :2], o.forces()[:, :2]
+
+
+def assert_gas_projection(pos, force, ref_pos, ref_force, start, gas, tol):
+    """Gas displacements and forces within tol of the reference, relative to
+    the largest of each; particles that are not gas stay where they were."""
+    d_ref = ref_pos[gas] - start[gas]
+    assert norm_err(pos[gas] - start[gas], d_ref) < tol
+    assert norm_err(force[gas], ref_force[gas]) < tol
+    assert np.max(np.abs(pos[~gas] - start[~gas])) == 0.0

@@ -45,3 +45,26 @@ def test_updates_match_reference_golden(path):
 
 def test_fixtures_present():
     assert len(FIXTURES) >= 3
+
+
+GAS = GOLDEN / "gas_project.npz"
+
+
+@pytest.mark.parametrize("open_", [0, 1])
+@pytest.mark.parametrize("calls", [1, 3])
+def test_gas_projection_matches_reference_golden(open_, calls):
+    """The oracle's gas passes against the reference's own
+    GasConstraint::project (gasconstraint.cpp:34-134) on a 2-D smoke box
+    with solid (S_SOLID-weighted) and fixed (ignored) neighbours: estimates
+    and forces (vorticity, open drag) after 1 and 3 calls, to 1e-7 of the
+    largest displacement / force (FP64 on both sides; the two differ in
+    summation order only)."""
+    from helpers import assert_gas_projection, oracle_gas_projection
+
+    data = np.load(GAS)
+    params = W.smoke_box(twod=True, solid_floor=True).params
+    pos, force = oracle_gas_projection(data["pos_w"], data["phase"], data["rest_density"], data["vel"], params,
+                                       bool(open_), calls)
+    gas = data["phase"] == W.PHASE_GAS
+    assert_gas_projection(pos, force, data[f"open{open_}_k{calls}_pos"], data[f"open{open_}_k{calls}_force"],
+                          data["pos_w"][:, :2].astype(np.float64), gas, 1e-7)

@@ -41,7 +41,8 @@ def load_batch(scenes):
         shifted = W.Scene(sc.name, sc.params, sc.pos_w, sc.phase, vel=sc.vel, rest_density=sc.rest_density,
                           pairs=None if sc.pairs is None else sc.pairs + first, rest=sc.rest,
                           stiffness=sc.stiffness, pins=None if sc.pins is None else sc.pins + first,
-                          pin_points=sc.pin_points, bodies=[(f + first, c, s) for f, c, s in sc.bodies])
+                          pin_points=sc.pin_points, bodies=[(f + first, c, s) for f, c, s in sc.bodies],
+                          open_gas=[(f + first, c) for f, c in sc.open_gas])
         W.apply_to(shifted, sys)
     return sys, firsts
 

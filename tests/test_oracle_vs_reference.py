@@ -158,3 +158,27 @@ def test_full_update_trajectory(builder, steps):
     assert np.max(np.abs(d_r.mean(0) - d_o.mean(0))) / scale < 1e-3
     v_o, v_r = o.velocities()[:, :3], r.velocities()[:, :3]
     assert np.max(np.abs(v_r.mean(0) - v_o.mean(0))) / np.max(np.abs(v_o)) < 1e-3
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_gas_projection_matches_reference_cpu(seed):
+    """The oracle's gas phase against the reference's GasConstraint::project
+    compiled from the reference tree (oracle/_ref/librefcpu.so), on fresh
+    seeded 2-D smoke boxes with solid and fixed neighbours and random step
+    velocities, open and closed, 1 and 3 calls, to 1e-7."""
+    from helpers import assert_gas_projection, oracle_gas_projection
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    sc = W.smoke_box(twod=True, solid_floor=True, seed=100 + seed)
+    vel = np.zeros((sc.n, 4))
+    vel[:, :2] = W.uniform(200 + seed, (sc.n, 2), -2.0, 2.0)
+    gas = sc.phase == W.PHASE_GAS
+    start = sc.pos_w[:, :2].astype(np.float64)
+    for open_ in (False, True):
+        for calls in (1, 3):
+            ref_pos, ref_f = refcpu.gas_project(start, vel[:, :2], sc.pos_w[:, 3].astype(np.float64),
+                                                (~gas).astype(np.int32), 1.5, open_, calls)
+            pos, f = oracle_gas_projection(sc.pos_w, sc.phase, sc.rest_density, vel, sc.params, open_, calls)
+            assert_gas_projection(pos, f, ref_pos, ref_f, start, gas, 1e-7)
