@@ -598,6 +598,7 @@ def run_ours(args, world, rank, local_rank):
                    "threads_per_particle": tpp, "tpp_source": "fixed" if args.tpp else "autotuned",
                    "neighbor_skin": float(tuning.neighbor_skin),
                    "neighbor_list_capacity": int(tuning.neighbor_list_capacity),
+                   "list_assembly": "shared memory" if int(tuning.list_assembly) == 0 else "registers",
                    "list_reuses_last_step": reuses,
                    "dt": sc.dt, "l2": "flushed before each timed step (256 MiB write)",
                    "timing": "per-step CUDA events on the launching stream, CUDA graph replay",
