@@ -211,7 +211,7 @@ def load_scenes(scenes, max_particles=None):
                            pairs=None if sc.pairs is None else sc.pairs + first, rest=sc.rest,
                            stiffness=sc.stiffness, pins=None if sc.pins is None else sc.pins + first,
                            pin_points=sc.pin_points, bodies=[(f + first, c, st) for f, c, st in sc.bodies],
-                           open_gas=[(f + first, c) for f, c in sc.open_gas]), sysm)
+                           open_gas=[(f + first, c) for f, c in sc.open_gas], sdf=sc.sdf), sysm)
     return sysm
 
 

@@ -212,6 +212,20 @@ int pbd_add_point_constraints(pbd_system *sys, uint32_t p, const uint32_t *index
  * cpu/src/simulation.cpp:371-406).  Every particle needs w > 0. */
 int pbd_add_rigid_body(pbd_system *sys, uint32_t first, uint32_t count, float stiffness,
                        uint32_t *body_index);
+/* Signed-distance data of a rigid body's particles for the CPU reference's
+ * rigid contact (RigidContactConstraint, cpu/src/constraint/
+ * rigidcontactconstraint.cpp:13-96; SDFData, particle.h:82-93): sdf holds 4
+ * floats per particle of the body, in the body's rest frame (the frame of
+ * its rest offsets): the outward surface direction xyz and the particle's
+ * depth below the body's surface (>= 0; < 0 = no data for that particle).
+ * In a contact of two particles that both have data, the one nearer its
+ * surface supplies the contact normal (rotated by its body's current
+ * rotation) and depth, a particle closer than one diameter to the surface
+ * takes the normal reflected against the pair direction (initBoundary),
+ * and the correction and friction use the CPU solver's height-scaled
+ * masses; other contacts keep the particle-particle model.  The gradients
+ * are normalised here. */
+int pbd_set_rigid_sdf(pbd_system *sys, uint32_t body, const float *sdf);
 /* The six uniforms the reference drew from cuRAND for the wall jitter every
  * iteration (integration.cu:326); here an explicit input, default zeros. */
 int pbd_set_wall_jitter(pbd_system *sys, const float rands[6]);

@@ -71,6 +71,7 @@ def load(dual: bool = False):
             "orc_set_gas_open": ([P, U, U, ctypes.c_int], None),
             "orc_get_forces": ([P, PD], None),
             "orc_set_forces": ([P, PD], None),
+            "orc_set_rigid_sdf": ([P, U, PD], None),
         }
         if dual:
             sig["orc_seed_tangents"] = ([P, PD, PD, PD], None)
@@ -149,6 +150,12 @@ class Oracle:
 
     def add_rigid_body(self, first, count, stiffness=1.0):
         self.lib.orc_add_rigid_body(self.s, first, count, stiffness)
+        self._bodies = getattr(self, "_bodies", 0) + 1
+        return self._bodies - 1
+
+    def set_rigid_sdf(self, body, sdf):
+        sdf, sp = _d(np.asarray(sdf, np.float64).reshape(-1, 4))
+        self.lib.orc_set_rigid_sdf(self.s, int(body), sp)
 
     def set_wall_jitter(self, r):
         r, rp = _d(np.asarray(r).reshape(6))

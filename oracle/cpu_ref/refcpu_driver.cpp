@@ -33,6 +33,7 @@
 #define private public
 #include "simulation.h"
 #include "gasconstraint.h"
+#include "rigidcontactconstraint.h"
 #undef private
 
 #include <cstdint>
@@ -128,6 +129,57 @@ void refcpu_gas_project(int n, const double *xy, const double *v, const double *
         f_out[2 * i + 1] = ps.at(i)->f.y;
         delete ps.at(i);
     }
+}
+
+// The reference's rigid contact, RigidContactConstraint::project
+// (rigidcontactconstraint.cpp:30-96), on n 2-D SOLID particles: p are the
+// start-of-step positions, ep the estimates; body[i] >= 0 puts particle i in
+// that body with signed-distance data sdf[3i..3i+2] (rest-frame normal x, y,
+// depth); the bodies' angles rotate the normals (Particle::getSDFData,
+// particle.cpp:3-13).  Masses are height-scaled (scaleMass, particle.h:67-
+// 73); each particle's count is its number of listed pairs; the pairs
+// (i1 < i2) are projected once each, in order.  Out: the estimates.
+void refcpu_rigid_contacts(int n, const double *p, const double *ep, const double *imass, const int *body,
+                           const double *sdf, int nbodies, const double *angles, int npairs, const int *pairs,
+                           double s_friction, double k_friction, double *ep_out) {
+    QList<Particle *> ps;
+    for (int i = 0; i < n; ++i) {
+        Particle *q = new Particle(glm::dvec2(p[2 * i], p[2 * i + 1]), 1.0, SOLID);
+        q->imass = imass[i];
+        q->ep = glm::dvec2(ep[2 * i], ep[2 * i + 1]);
+        q->bod = body[i];
+        q->sFriction = s_friction;
+        q->kFriction = k_friction;
+        q->scaleMass();
+        ps.append(q);
+    }
+    QList<Body *> bodies;
+    for (int b = 0; b < nbodies; ++b) {
+        Body *bd = new Body();
+        bd->shape = nullptr;
+        bd->angle = angles[b];
+        bodies.append(bd);
+    }
+    for (int i = 0; i < n; ++i)
+        if (body[i] >= 0) {
+            bodies.at(body[i])->particles.append(i);
+            bodies.at(body[i])->sdf[i] = SDFData(glm::dvec2(sdf[3 * i], sdf[3 * i + 1]), sdf[3 * i + 2]);
+        }
+    std::vector<int> counts(n, 0);
+    for (int k = 0; k < npairs; ++k) {
+        ++counts[pairs[2 * k]];
+        ++counts[pairs[2 * k + 1]];
+    }
+    for (int k = 0; k < npairs; ++k) {
+        RigidContactConstraint c(pairs[2 * k], pairs[2 * k + 1], &bodies, false);
+        c.project(&ps, counts.data());
+    }
+    for (int i = 0; i < n; ++i) {
+        ep_out[2 * i] = ps.at(i)->ep.x;
+        ep_out[2 * i + 1] = ps.at(i)->ep.y;
+        delete ps.at(i);
+    }
+    for (int b = 0; b < nbodies; ++b) delete bodies.at(b);
 }
 
 }  // extern "C"

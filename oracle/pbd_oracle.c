@@ -77,6 +77,10 @@ struct orc_system {
     real *force;              /* 4n, original order: Particle::f            */
     unsigned char *gas_open;  /* original order                             */
     real *glambda;            /* sorted order                               */
+    /* rigid-body signed-distance data (rigidcontactconstraint.cpp) */
+    double *sdf;              /* 4 per particle: rest-frame normal, depth (< 0: none) */
+    int32_t *body_of;         /* body of each particle, -1 for none          */
+    int any_sdf;
 };
 
 static int g_threads = 0;
@@ -197,6 +201,12 @@ orc_system *orc_create(const pbd_params *params, uint32_t cap) {
     s->force = (real *)calloc(4ull * cap, sizeof(real));
     s->gas_open = (unsigned char *)calloc(cap ? cap : 1, 1);
     s->glambda = (real *)calloc(cap, sizeof(real));
+    s->sdf = (double *)calloc(4ull * (cap ? cap : 1), sizeof(double));
+    s->body_of = (int32_t *)malloc((cap ? cap : 1) * sizeof(int32_t));
+    for (uint32_t k = 0; k < cap; ++k) {
+        s->sdf[4 * k + 3] = -1.0;
+        s->body_of[k] = -1;
+    }
     return s;
 }
 
@@ -209,7 +219,7 @@ void orc_destroy(orc_system *s) {
     free(s->da); free(s->db); free(s->drest); free(s->dstiff);
     free(s->pin_idx); free(s->pin_pts);
     free(s->bfirst); free(s->bcount); free(s->bstiff); free(s->bquat); free(s->brest);
-    free(s->force); free(s->gas_open); free(s->glambda);
+    free(s->force); free(s->gas_open); free(s->glambda); free(s->sdf); free(s->body_of);
     free(s);
 }
 
@@ -288,6 +298,7 @@ int orc_add_rigid_body(orc_system *s, uint32_t first, uint32_t count, double sti
         for (int d = 0; d < 3; ++d) s->brest[4 * k + d] = (double)(float)(R_VAL(s->x[4 * k + d]) - c[d]);
         s->brest[4 * k + 3] = (double)(float)(1.0 / R_VAL(s->x[4 * k + 3]));
     }
+    for (uint32_t k = first; k < first + count; ++k) s->body_of[k] = (int32_t)s->nb;
     s->bfirst[s->nb] = first;
     s->bcount[s->nb] = count;
     s->bstiff[s->nb] = stiffness;
@@ -611,6 +622,79 @@ static int contact_visit(void *vctx, uint32_t j) {
 
 static real scaled_w(real w, real y) { return w != 0.0 ? 1.0 / ((1.0 / w) * exp(-y)) : w; }
 
+#define CPU_EPS 0.0001 /* EPSILON, cpu/src/includes.h:34 */
+
+static void quat_rotate(const real q[4], const double v[3], real out[3]) {
+    real t[3] = {2.0 * (q[1] * v[2] - q[2] * v[1]), 2.0 * (q[2] * v[0] - q[0] * v[2]), 2.0 * (q[0] * v[1] - q[1] * v[0])};
+    out[0] = v[0] + q[3] * t[0] + (q[1] * t[2] - q[2] * t[1]);
+    out[1] = v[1] + q[3] * t[1] + (q[2] * t[0] - q[0] * t[2]);
+    out[2] = v[2] + q[3] * t[2] + (q[0] * t[1] - q[1] * t[0]);
+}
+
+/* RigidContactConstraint::project (rigidcontactconstraint.cpp:30-96) for a
+ * pair of particles with signed-distance data, as seen by particle `self`
+ * (original index) against `other`: the pair is ordered by original index;
+ * depth and normal from the particle nearer its surface, replaced below
+ * one diameter + EPSILON by initBoundary (:13-27); correction and friction
+ * shared by the height-scaled inverse masses tmass = w e^y at the
+ * start-of-step heights (Particle::scaleMass); averaged over `cnt` (this
+ * particle's contact count, for both ends).  Adds to out. */
+static void sdf_contact(const orc_system *s, uint32_t self, uint32_t other, const real *xs, const real *xo,
+                        const real *ps, const real *po, double cnt, real out[3]) {
+    const int first = self < other;
+    const uint32_t o1 = first ? self : other, o2 = first ? other : self;
+    const real *x1 = first ? xs : xo, *x2 = first ? xo : xs, *p1 = first ? ps : po, *p2 = first ? po : ps;
+    const double *s1 = s->sdf + 4 * o1, *s2 = s->sdf + 4 * o2;
+    real n1[3], n2[3], n[3];
+    quat_rotate(s->bquat + 4 * s->body_of[o1], s1, n1);
+    quat_rotate(s->bquat + 4 * s->body_of[o2], s2, n2);
+    real d;
+    if (s1[3] < s2[3]) {
+        d = s1[3];
+        for (int k = 0; k < 3; ++k) n[k] = n1[k];
+    } else {
+        d = s2[3];
+        for (int k = 0; k < 3; ++k) n[k] = -n2[k];
+    }
+    const double diam = 2.0 * (double)s->p.particle_radius;
+    if (d < diam + CPU_EPS) {
+        real x12[3] = {x1[0] - x2[0], x1[1] - x2[1], x1[2] - x2[2]};
+        real len = sqrt(x12[0] * x12[0] + x12[1] * x12[1] + x12[2] * x12[2]);
+        d = diam - len;
+        if (d < CPU_EPS) return;
+        if (len > CPU_EPS) {
+            for (int k = 0; k < 3; ++k) x12[k] = x12[k] / len;
+        } else {
+            x12[0] = 0.0; x12[1] = 1.0; x12[2] = 0.0;
+        }
+        real dp = x12[0] * n[0] + x12[1] * n[1] + x12[2] * n[2];
+        for (int k = 0; k < 3; ++k) n[k] = dp < 0.0 ? x12[k] - 2.0 * dp * n[k] : x12[k];
+    }
+    const double w1 = R_VAL(x1[3]), w2 = R_VAL(x2[3]);
+    real t1 = w1 * exp(p1[1]), t2 = w2 * exp(p2[1]);
+    real tsum = t1 + t2;
+    if (!(R_VAL(tsum) > 0.0)) return;
+    real a1 = t1 / tsum, a2 = t2 / tsum, dp1[3], dp2[3];
+    for (int k = 0; k < 3; ++k) {
+        dp1[k] = -a1 * d * n[k] / cnt;
+        dp2[k] = a2 * d * n[k] / cnt;
+        out[k] += first ? dp1[k] : dp2[k];
+    }
+    real nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    real nf[3] = {n[0] / nl, n[1] / nl, n[2] / nl}, dpf[3], dpt[3];
+    for (int k = 0; k < 3; ++k) dpf[k] = (x1[k] + dp1[k] - p1[k]) - (x2[k] + dp2[k] - p2[k]);
+    real dn = dpf[0] * nf[0] + dpf[1] * nf[1] + dpf[2] * nf[2];
+    for (int k = 0; k < 3; ++k) dpt[k] = dpf[k] - dn * nf[k];
+    real ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
+    if (ldpt < CPU_EPS) return;
+    real f = 1.0;
+    if (!(ldpt < (double)s->p.contact_static_friction * d)) {
+        f = (double)s->p.contact_kinetic_friction * d / ldpt;
+        if (f > 1.0) f = 1.0;
+    }
+    for (int k = 0; k < 3; ++k) out[k] += (first ? -a1 : a2) * dpt[k] * f;
+}
+
 /* collideD + collideCell (integration_kernel.cuh:303-462).  Pairs with zero
  * total inverse mass or zero separation are skipped (NaN in the reference). */
 static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real out[3]) {
@@ -627,10 +711,17 @@ static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real 
     const real *prev = s->x_old + 4 * s->sorted_idx[i];
     const int ph = s->sphase[i];
     const double cdist = (double)s->collidef;
+    const uint32_t oi = s->sorted_idx[i];
+    const int sdf_i = s->any_sdf && ph >= PBD_PHASE_SOLID && s->sdf[4 * oi + 3] >= 0.0;
     for (uint32_t k = 0; k < c.nb; ++k) {
         uint32_t j = list[k];
         const real *pj = s->sx + 4 * j;
         int phj = s->sphase[j];
+        if (sdf_i && phj >= PBD_PHASE_SOLID && s->sdf[4 * s->sorted_idx[j] + 3] >= 0.0) {
+            const uint32_t oj = s->sorted_idx[j];
+            sdf_contact(s, oi, oj, pi, pj, prev, s->x_old + 4 * oj, fnb, out);
+            continue;
+        }
         real diff[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
         real dist = sqrt(diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]);
         real mag = dist - cdist;
@@ -1022,6 +1113,24 @@ void orc_get_lambdas(const orc_system *s, double *out) {
 void orc_set_gas_open(orc_system *s, uint32_t first, uint32_t count, int open) {
     for (uint32_t k = first; k < first + count && k < s->n; ++k)
         if (s->phase[k] == PBD_PHASE_GAS) s->gas_open[k] = open ? 1 : 0;
+}
+
+void orc_set_rigid_sdf(orc_system *s, uint32_t body, const double *sdf) {
+    if (body >= s->nb) return;
+    for (uint32_t k = 0; k < s->bcount[body]; ++k) {
+        const double *e = sdf + 4 * k;
+        double *o = s->sdf + 4 * (s->bfirst[body] + k);
+        if (e[3] < 0.0) {
+            o[0] = o[1] = o[2] = 0.0;
+            o[3] = -1.0;
+            continue;
+        }
+        /* the CUDA path stores the FP32-normalised normal */
+        const double len = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        for (int d = 0; d < 3; ++d) o[d] = (double)(float)(e[d] / len);
+        o[3] = (double)(float)e[3];
+    }
+    s->any_sdf = 1;
 }
 
 void orc_get_forces(const orc_system *s, double *out) {

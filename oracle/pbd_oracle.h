@@ -60,6 +60,8 @@ void orc_get_lambdas(const orc_system *s, double *out);
 void orc_set_gas_open(orc_system *s, uint32_t first, uint32_t count, int open);
 void orc_get_forces(const orc_system *s, double *out);
 void orc_set_forces(orc_system *s, const double *f);
+/* Signed-distance data of rigid body `body` (4 doubles per particle). */
+void orc_set_rigid_sdf(orc_system *s, uint32_t body, const double *sdf);
 /* Neighbour count of every particle in the last fluid / contact pass. */
 void orc_get_neighbor_counts(const orc_system *s, uint32_t *fluid, uint32_t *contact);
 /* Only in the dual-number build (liboracle_dual.so). */

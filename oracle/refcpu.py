@@ -41,6 +41,8 @@ def load():
         lib.refcpu_get.argtypes = [P, PD, PD]
         lib.refcpu_destroy.argtypes = [P]
         lib.refcpu_gas_project.argtypes = [I, PD, PD, PD, ctypes.POINTER(ctypes.c_int), D, I, I, PD, PD]
+        PI = ctypes.POINTER(ctypes.c_int)
+        lib.refcpu_rigid_contacts.argtypes = [I, PD, PD, PD, PI, PD, I, PD, I, PI, D, D, PD]
         _lib = lib
     return _lib
 
@@ -100,3 +102,27 @@ def gas_project(xy, v, imass, solid, density: float, open_: bool, iterations: in
                            solid.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), float(density), int(bool(open_)),
                            int(iterations), out_x.ctypes.data_as(pd), out_f.ctypes.data_as(pd))
     return out_x, out_f
+
+
+def rigid_contacts(p, ep, imass, body, sdf, angles, pairs, s_friction: float, k_friction: float):
+    """The reference's RigidContactConstraint::project, once per listed pair
+    (i1 < i2), on 2-D SOLID particles with start positions p and estimates
+    ep, (n, 2) each; body[i] (-1 = none) with signed-distance data sdf (n, 3:
+    rest-frame normal x, y, depth) and body angles.  Returns the estimates."""
+    lib = load()
+    p = np.ascontiguousarray(p, np.float64).reshape(-1, 2)
+    n = p.shape[0]
+    ep = np.ascontiguousarray(ep, np.float64).reshape(n, 2)
+    imass = np.ascontiguousarray(imass, np.float64).reshape(n)
+    body = np.ascontiguousarray(body, np.int32).reshape(n)
+    sdf = np.ascontiguousarray(sdf, np.float64).reshape(n, 3)
+    angles = np.ascontiguousarray(angles, np.float64).reshape(-1)
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    out = np.empty((n, 2))
+    pd = ctypes.POINTER(ctypes.c_double)
+    pi = ctypes.POINTER(ctypes.c_int)
+    lib.refcpu_rigid_contacts(n, p.ctypes.data_as(pd), ep.ctypes.data_as(pd), imass.ctypes.data_as(pd),
+                              body.ctypes.data_as(pi), sdf.ctypes.data_as(pd), angles.shape[0],
+                              angles.ctypes.data_as(pd), pairs.shape[0], pairs.ctypes.data_as(pi),
+                              float(s_friction), float(k_friction), out.ctypes.data_as(pd))
+    return out

@@ -177,6 +177,7 @@ _SIGNATURES = {
     "pbd_get_velocities": ([_P, _U32, _U32, _P, _I, _P], _I),
     "pbd_get_phases": ([_P, _PI], _I),
     "pbd_set_gas_open": ([_P, _U32, _U32, _I], _I),
+    "pbd_set_rigid_sdf": ([_P, _U32, _PF], _I),
     "pbd_get_forces": ([_P, _PF], _I),
     "pbd_get_device_buffers": ([_P, ctypes.POINTER(PbdDeviceBuffers)], _I),
     "pbd_add_fluid": ([_P, _PI, _PI, _F, _F, ctypes.c_uint64], _I),
@@ -343,6 +344,12 @@ class ParticleSystem:
         b = ctypes.c_uint32()
         self._check(self.lib.pbd_add_rigid_body(self.h, first, count, stiffness, ctypes.byref(b)))
         return b.value
+
+    def set_rigid_sdf(self, body: int, sdf):
+        """Signed-distance data of a rigid body's particles: (count, 4)
+        rest-frame normal xyz and depth (< 0 = none)."""
+        a = _f32(sdf, 4).reshape(-1, 4)
+        self._check(self.lib.pbd_set_rigid_sdf(self.h, int(body), _fptr(a)))
 
     def set_wall_jitter(self, rands):
         r = _f32(rands).reshape(6)

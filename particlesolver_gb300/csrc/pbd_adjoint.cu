@@ -761,6 +761,8 @@ cudaError_t grow(T **p, size_t &have, size_t want) {
 int differentiable(pbd_system *s) {
     if (s->n_gas)
         return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED, "the adjoint does not cover the gas phase (the system holds gas particles)");
+    if (s->any_sdf)
+        return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED, "the adjoint does not cover the signed-distance rigid contact (a body has sdf data)");
     return PBD_OK;
 }
 

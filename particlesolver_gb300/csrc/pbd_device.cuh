@@ -24,6 +24,9 @@ enum : uint32_t {
     // so the prediction applies the per-particle force and the gas gravity
     // and keeps the step's velocity v' for the gas terms.
     kFlagHasGas = 1u << 16,
+    // Set by the host: some rigid body carries signed-distance data, so the
+    // contact pass looks it up for solid pairs.
+    kFlagHasSdf = 1u << 17,
 };
 
 // Stage mask of the fused per-particle solve kernel.

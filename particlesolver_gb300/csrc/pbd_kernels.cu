@@ -742,6 +742,79 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
     return delta / div;
 }
 
+// v rotated by the unit quaternion q (xyzw).
+__device__ __forceinline__ float3 quat_rotate(float4 q, float3 v) {
+    const float3 u = make_float3(q.x, q.y, q.z);
+    const float3 t = make_float3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x) * 2.f;
+    return v + t * q.w + make_float3(u.y * t.z - u.z * t.y, u.z * t.x - u.x * t.z, u.x * t.y - u.y * t.x);
+}
+
+// EPSILON of the CPU reference (cpu/src/includes.h:34).
+constexpr float kEpsCpu = 0.0001f;
+
+// RigidContactConstraint::project (cpu/src/constraint/
+// rigidcontactconstraint.cpp:30-96) for a pair of particles that both carry
+// signed-distance data, evaluated for particle `self` (original index) with
+// partner `other`; the pair is ordered by original index (the reference's
+// i1 < i2, simulation.cpp:171-193), so both particles evaluate the same
+// constraint.  Depth and normal come from the particle nearer its surface
+// (normal of the first, or minus that of the second); a depth below one
+// diameter + EPSILON is replaced by initBoundary (:13-27): the overlap of
+// the pair, with the normal reflected against the pair direction when they
+// point apart.  The correction d n is shared by the height-scaled inverse
+// masses tmass = w e^y (Particle::scaleMass, particle.h:67-73, at the
+// start-of-step heights; formed here as the overflow-free shares
+// tmass_k / (tmass_1 + tmass_2)) and averaged over the contact count; this
+// particle's count stands in for its partner's, as the GPU reference's
+// contact friction does.  Friction: the tangential relative displacement
+// since the step's start, removed if below sqrt(mu_s mu_s) d (static), else
+// cut by min(sqrt(mu_k mu_k) d / |dpt|, 1).
+__device__ __forceinline__ float3 sdf_contact(const DevParams &P, uint32_t self, uint32_t other, float3 xs,
+                                              float3 xo, float3 ps, float3 po, float ws, float wo, float ds,
+                                              float dso, float3 ns, float3 no, float cnt) {
+    const bool first = self < other;
+    const float3 x1 = first ? xs : xo, x2 = first ? xo : xs;
+    const float3 p1 = first ? ps : po, p2 = first ? po : ps;
+    const float w1 = first ? ws : wo, w2 = first ? wo : ws;
+    const float dd1 = first ? ds : dso, dd2 = first ? dso : ds;
+    float d;
+    float3 n;
+    if (dd1 < dd2) {
+        d = dd1;
+        n = first ? ns : no;
+    } else {
+        d = dd2;
+        n = -(first ? no : ns);
+    }
+    const float diam = 2.f * P.r;
+    if (d < diam + kEpsCpu) {
+        float3 x12 = x1 - x2;
+        const float len = len3(x12);
+        d = diam - len;
+        if (d < kEpsCpu) return make_float3(0.f, 0.f, 0.f);
+        x12 = len > kEpsCpu ? x12 / len : make_float3(0.f, 1.f, 0.f);
+        const float dp = dot3(x12, n);
+        n = dp < 0.f ? x12 - n * (2.f * dp) : x12;
+    }
+    const float m = fmaxf(p1.y, p2.y);
+    const float t1 = w1 * expf(p1.y - m), t2 = w2 * expf(p2.y - m);
+    const float tsum = t1 + t2;
+    if (!(tsum > 0.f)) return make_float3(0.f, 0.f, 0.f);
+    const float a1 = t1 / tsum, a2 = t2 / tsum;
+    const float3 dp1 = n * (-a1 * d / cnt), dp2 = n * (a2 * d / cnt);
+    float3 out = first ? dp1 : dp2;
+    const float3 nf = n * rsqrtf(dot3(n, n));
+    // (x1 + dp1 - p1) - (x2 + dp2 - p2), grouped so that the large
+    // coordinates cancel before the small corrections are added
+    const float3 dpf = ((x1 - p1) - (x2 - p2)) + (dp1 - dp2);
+    const float3 dpt = dpf - nf * dot3(dpf, nf);
+    const float ldpt = len3(dpt);
+    if (ldpt < kEpsCpu) return out;
+    const float3 slip = (ldpt < P.cs * d) ? dpt : dpt * fminf(P.ck * d / ldpt, 1.f);
+    out += first ? slip * -a1 : slip * a2;
+    return out;
+}
+
 // collideD + collideCell (integration_kernel.cuh:303-462): contacts of a
 // non-fluid particle with every particle closer than 2.001 r in the 27-cell
 // stencil (same-object pairs skipped, capped at max_nb), each averaged over
@@ -754,14 +827,15 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
 // reference's w e^y became inf and the correction inf * 0 = NaN.  Pairs
 // with zero total inverse mass or zero separation are skipped (the
 // reference produced NaN there).  Two walks: the count, then the
-// corrections.
+// corrections.  A pair of solid particles that both carry signed-distance
+// data takes the CPU reference's rigid contact instead (sdf_contact).
 template <int TPP>
 __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float4 pi4,
                                                 int ph, uint32_t orig, const float4 *__restrict__ sx,
                                                 const SortedAttr *__restrict__ sattr,
                                                 const uint32_t *__restrict__ sidx,
                                                 const uint32_t *__restrict__ cell_first,
-                                                const float4 *__restrict__ x_old) {
+                                                const float4 *__restrict__ x_old, const RigidSdf &rs) {
     const float3 pi = f3(pi4);
     const int3 g = grid_pos(P, pi);
     auto test = [&](uint32_t j, const float4 &, float d2) {
@@ -776,9 +850,25 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
     const float w = pi4.w;
     const float3 prev = f3(x_old[orig]);
     const float fnb = (float)nb;
+    // this particle's signed-distance data, its normal in the world frame
+    float4 si = make_float4(0.f, 0.f, 0.f, -1.f);
+    float3 ni = make_float3(0.f, 0.f, 0.f);
+    if ((P.flags & kFlagHasSdf) && ph >= kSolid) {
+        si = rs.sdf[orig];
+        if (si.w >= 0.f) ni = quat_rotate(rs.quat[rs.body[orig]], f3(si));
+    }
     group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, nb, test,
                     [&](uint32_t j, const float4 &pj4, float) {
         const int phj = sattr[j].phase;
+        if (si.w >= 0.f && phj >= kSolid) {
+            const uint32_t oj = sidx[j];
+            const float4 sj = rs.sdf[oj];
+            if (sj.w >= 0.f) {
+                delta += sdf_contact(P, orig, oj, pi, f3(pj4), prev, f3(x_old[oj]), w, pj4.w, si.w, sj.w, ni,
+                                     quat_rotate(rs.quat[rs.body[oj]], f3(sj)), fnb);
+                return;
+            }
+        }
         const float3 pj = f3(pj4);
         const float3 diff = pi - pj;
         const float dist = len3(diff);
@@ -1252,7 +1342,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint
                                                   const float4 *__restrict__ sxl,
                                                   const float4 *__restrict__ x_old,
                                                   float4 *__restrict__ x, NbList L, bool use_list,
-                                                  GasBuffers gas) {
+                                                  GasBuffers gas, RigidSdf rs) {
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -1271,7 +1361,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint
         np = np + gas_delta<TPP>(P, G, i, np, a.rho0, sx, sattr, cell_first, gas);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
-        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old);
+        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old, rs);
         touched = true;
     }
     if (G.lane != 0) return;
@@ -1740,15 +1830,15 @@ cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, co
 
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t iter_left, const GridBuffers &g,
                          const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
-                         uint32_t tpp, cudaStream_t s, const GasBuffers &gas) {
+                         uint32_t tpp, cudaStream_t s, const GasBuffers &gas, const RigidSdf &sdf) {
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
     if (P.table) {
         PBD_TPP_DISPATCH(tpp, true, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
-                         g.cell_first, sxl, x_old, x, L, use_list, gas);
+                         g.cell_first, sxl, x_old, x, L, use_list, gas, sdf);
     } else {
         PBD_TPP_DISPATCH(tpp, false, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
-                         g.cell_first, sxl, x_old, x, L, use_list, gas);
+                         g.cell_first, sxl, x_old, x, L, use_list, gas, sdf);
     }
     return cudaGetLastError();
 }

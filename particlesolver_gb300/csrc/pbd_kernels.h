@@ -54,6 +54,13 @@ struct GasBuffers {
     const uint32_t *sidx;  // [cap] sorted slot -> original index
 };
 
+// Signed-distance data of rigid-body particles (all null without any).
+struct RigidSdf {
+    const float4 *sdf;   // [cap] original order: rest-frame unit normal xyz, depth (< 0: none)
+    const int *body;     // [cap] original order: body of the particle, -1 for none
+    const float4 *quat;  // [bodies] current rotation of each body (xyzw)
+};
+
 // Device words of the skin-list schedule: [0] reuse, [1] overflow, [2 + k]
 // largest displacement / h since the list build, seen in iteration k (k <
 // kSkinWords - 3), [kSkinWords - 1] iterations of the step that reused.
@@ -133,7 +140,8 @@ cudaError_t launch_lambda(const DevParams &P, uint32_t n, uint32_t iter_left, co
                           const NbList &L, uint32_t tpp, cudaStream_t s, const GasBuffers &gas = GasBuffers{});
 cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t iter_left, const GridBuffers &g,
                          const float4 *sxl, const float4 *x_old, float4 *x, const NbList &L, bool use_list,
-                         uint32_t tpp, cudaStream_t s, const GasBuffers &gas = GasBuffers{});
+                         uint32_t tpp, cudaStream_t s, const GasBuffers &gas = GasBuffers{},
+                         const RigidSdf &sdf = RigidSdf{});
 cudaError_t launch_distance(const DevParams &P, uint32_t iter_left, const ConstraintBuffers &c, float4 *x,
                             bool apply_distance, bool apply_pins, cudaStream_t s);
 cudaError_t launch_shapes(const DevParams &P, uint32_t iter_left, const BodyBuffers &b, float4 *x, cudaStream_t s);

@@ -219,6 +219,7 @@ int refresh_scenes(pbd_system *s) {
     for (pbd_scene &sc : s->scenes) {
         sc.dev = make_dev(sc.params, s->rands);
         if (s->n_gas) sc.dev.flags |= pbd::kFlagHasGas;
+        if (s->any_sdf) sc.dev.flags |= pbd::kFlagHasSdf;
         sc.dev.cell_base = (uint32_t)base;
         base += sc.dev.num_cells;
         if (base >= (1ull << 31))
@@ -554,7 +555,7 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
         {
             Stage t(s, st, PBD_STAGE_SOLVE, 1);
             CUDA_TRY(s, pbd::launch_solve(P, n, mask, left, s->grid, s->sxl, s->x_old, s->x, L,
-                                          s->list_valid, s->tpp, st, s->gas_buffers()));
+                                          s->list_valid, s->tpp, st, s->gas_buffers(), s->sdf_buffers()));
         }
         if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(2 + 3 * it) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
         if (dist_kernels) {
@@ -731,6 +732,8 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->force);
     dfree(s->gas_open);
     dfree(s->glam);
+    dfree(s->sdf);
+    dfree(s->body_of);
     dfree(s->flag);
     dfree(s->grid.hash);
     dfree(s->grid.slot);
@@ -973,6 +976,54 @@ int pbd_add_point_constraints(pbd_system *s, uint32_t p, const uint32_t *index, 
     return upload_constraints(s);
 }
 
+// Uploads the signed-distance data and the particle -> body map (the map is
+// rebuilt from the body ranges; particles without data keep depth -1).
+static int upload_sdf(pbd_system *s) {
+    if (!s->sdf) {
+        CUDA_TRY(s, dalloc(&s->sdf, s->cap));
+        CUDA_TRY(s, dalloc(&s->body_of, s->cap));
+        const std::vector<float4> none(s->cap, make_float4(0.f, 0.f, 0.f, -1.f));
+        CUDA_TRY(s, cudaMemcpy(s->sdf, none.data(), s->cap * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    std::vector<int> body(s->cap, -1);
+    for (size_t b = 0; b < s->body_range.size(); ++b)
+        for (uint32_t k = 0; k < s->body_range[b].y; ++k) body[s->body_range[b].x + k] = (int)b;
+    CUDA_TRY(s, cudaMemcpy(s->body_of, body.data(), s->cap * sizeof(int), cudaMemcpyHostToDevice));
+    if (!s->sdf_host.empty())
+        CUDA_TRY(s, cudaMemcpy(s->sdf, s->sdf_host.data(), s->sdf_host.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    return PBD_OK;
+}
+
+int pbd_set_rigid_sdf(pbd_system *s, uint32_t body, const float *sdf) {
+    SYS_GUARD(s);
+    if (body >= s->body_range.size()) return fail(s, PBD_ERR_INVALID_ARGUMENT, "no rigid body %u", body);
+    if (!sdf) return fail(s, PBD_ERR_INVALID_ARGUMENT, "sdf is NULL");
+    const uint4 r = s->body_range[body];
+    std::vector<float4> val(r.y);
+    for (uint32_t k = 0; k < r.y; ++k) {
+        const float *e = sdf + 4ull * k;
+        if (!std::isfinite(e[0]) || !std::isfinite(e[1]) || !std::isfinite(e[2]) || !std::isfinite(e[3]))
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "sdf entry %u is not finite", k);
+        if (e[3] < 0.f) {
+            val[k] = make_float4(0.f, 0.f, 0.f, -1.f);
+            continue;
+        }
+        const double len = std::sqrt((double)e[0] * e[0] + (double)e[1] * e[1] + (double)e[2] * e[2]);
+        if (!(len > 0.0)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "sdf entry %u has a zero normal", k);
+        val[k] = make_float4((float)(e[0] / len), (float)(e[1] / len), (float)(e[2] / len), e[3]);
+    }
+    if (s->sdf_host.size() < s->n) s->sdf_host.resize(s->n, make_float4(0.f, 0.f, 0.f, -1.f));
+    std::copy(val.begin(), val.end(), s->sdf_host.begin() + r.x);
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    if (int rc = upload_sdf(s)) return rc;
+    const bool first = !s->any_sdf;
+    s->any_sdf = true;
+    if (first)
+        if (int rc = refresh_scenes(s)) return rc;
+    ++s->version;
+    return PBD_OK;
+}
+
 int pbd_add_rigid_body(pbd_system *s, uint32_t first, uint32_t count, float stiffness,
                        uint32_t *body_index) {
     SYS_GUARD(s);
@@ -1011,7 +1062,8 @@ int pbd_add_rigid_body(pbd_system *s, uint32_t first, uint32_t count, float stif
     s->body_stiff.push_back(stiffness);
     if (body_index) *body_index = (uint32_t)s->body_range.size() - 1u;
     ++s->version;
-    return upload_bodies(s, quats);
+    if (int rc = upload_bodies(s, quats)) return rc;
+    return s->sdf ? upload_sdf(s) : PBD_OK;
 }
 
 static int copy_state(pbd_system *s, float4 *buf, uint32_t first, uint32_t count, float *host_or_dev,
@@ -1340,7 +1392,7 @@ int pbd_collide(pbd_system *s, void *stream) {
     SYS_GUARD(s);
     if (int rc = need_grid(s)) return rc;
     CUDA_TRY(s, pbd::launch_solve(s->dev, s->n, pbd::kDoContact, 0u, s->grid, s->sxl, s->x_old, s->x, s->nbl,
-                                  false, s->tpp, (cudaStream_t)stream));
+                                  false, s->tpp, (cudaStream_t)stream, pbd::GasBuffers{}, s->sdf_buffers()));
     s->launches += 1;
     return PBD_OK;
 }

@@ -42,6 +42,11 @@ struct pbd_system {
     float4 *force = nullptr;     // force the next prediction applies, original order
     uint8_t *gas_open = nullptr; // 1 = open gas, original order
     float *glam = nullptr;       // gas lambda, sorted order
+    // rigid-body signed-distance data (allocated with the first pbd_set_rigid_sdf)
+    float4 *sdf = nullptr;       // [cap] rest-frame normal xyz, depth (< 0: none)
+    int *body_of = nullptr;      // [cap] body of each particle, -1 for none
+    std::vector<float4> sdf_host;  // host copy of sdf for the live particles
+    bool any_sdf = false;
 
     pbd::GridBuffers grid{};
     uint32_t grid_cells = 0;  // cells the grid arrays were sized for
@@ -125,6 +130,10 @@ struct pbd_system {
     pbd::GasBuffers gas_buffers() const {
         if (!n_gas) return pbd::GasBuffers{};
         return pbd::GasBuffers{phase, force, gas_open, glam, v, grid.sorted_idx};
+    }
+    pbd::RigidSdf sdf_buffers() const {
+        if (!any_sdf) return pbd::RigidSdf{};
+        return pbd::RigidSdf{sdf, body_of, bodies.quat};
     }
     const pbd_params &cur_params() const { return scenes.back().params; }
 };

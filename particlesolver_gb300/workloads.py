@@ -52,6 +52,7 @@ class Scene:
     pin_points: np.ndarray | None = None   # (P, 3) float32
     bodies: list = field(default_factory=list)  # (first, count, stiffness)
     open_gas: list = field(default_factory=list)  # (first, count) ranges of open gas
+    sdf: list = field(default_factory=list)  # per body (same order): (count, 4) sdf data or None
     dt: float = 1.0 / 60.0
     info: dict = field(default_factory=dict)
 
@@ -225,9 +226,39 @@ def quat_rotate(q: np.ndarray, v: np.ndarray) -> np.ndarray:
     return v + w * t + np.cross(u, t)
 
 
-def rigid_boxes(count=8, side=4, radius=0.25, seed=5, iterations=4, drop_height=6.0, stiffness=1.0) -> Scene:
+def box_sdf(dims, radius: float) -> np.ndarray:
+    """Signed-distance data of a box of particles on a lattice of spacing
+    2 r, in the lattice order of np.meshgrid(..., indexing="ij") over dims
+    (2 or 3 axes): (N, 4) outward normal xyz and depth.  The reference's
+    SDF boxes (simulation.cpp:666-672) generalised: the normal is the
+    normalised sum of the outward axes whose faces are nearest, the depth
+    that face distance times sqrt(number of such axes) -- r on a face, r
+    sqrt(2) on an edge, r sqrt(3) at a corner; a particle whose nearest
+    faces cancel (the centre of an odd axis) points up."""
+    dims = list(dims)
+    idx = np.stack(np.meshgrid(*[np.arange(k) for k in dims], indexing="ij"), -1).reshape(-1, len(dims))
+    n = np.asarray(dims)
+    face = (np.minimum(idx, n - 1 - idx) * 2 + 1) * radius  # distance to the nearer face, per axis
+    dmin = face.min(1, keepdims=True)
+    near = np.isclose(face, dmin)
+    side = np.where(idx < n - 1 - idx, -1.0, np.where(idx > n - 1 - idx, 1.0, 0.0))
+    g = np.zeros((idx.shape[0], 3))
+    g[:, :len(dims)] = np.where(near, side, 0.0)
+    t = near.sum(1)
+    ln = np.linalg.norm(g, axis=1)
+    g[ln == 0.0] = [0.0, 1.0, 0.0]
+    g /= np.linalg.norm(g, axis=1, keepdims=True)
+    out = np.empty((idx.shape[0], 4))
+    out[:, :3] = g
+    out[:, 3] = dmin[:, 0] * np.sqrt(t)
+    return out
+
+
+def rigid_boxes(count=8, side=4, radius=0.25, seed=5, iterations=4, drop_height=6.0, stiffness=1.0,
+                sdf: bool = False) -> Scene:
     """count shape-matched side^3 boxes at seeded random orientations above
-    the floor, as separate objects (phase RIGID + id)."""
+    the floor, as separate objects (phase RIGID + id); with sdf, each body
+    carries box_sdf data in its rest frame (the frame it was added in)."""
     params = reference_scene_params(radius, iterations=iterations)
     d = 2.0 * radius
     g = (np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3) - (side - 1) / 2.0) * d
@@ -235,15 +266,74 @@ def rigid_boxes(count=8, side=4, radius=0.25, seed=5, iterations=4, drop_height=
     centers = np.stack([(np.arange(count) % 4) * (side * d * 2.0) - 4.0,
                         drop_height + (np.arange(count) // 4) * side * d * 2.0,
                         uniform(seed + 1, (count,), -1.0, 1.0)], 1)
-    pos, ph, bodies = [], [], []
+    pos, ph, bodies, sdfs = [], [], [], []
+    lattice_sdf = box_sdf([side] * 3, radius) if sdf else None
     for b in range(count):
-        pts = quat_rotate(np.broadcast_to(qs[b], (g.shape[0], 4)), g) + centers[b]
+        qb = np.broadcast_to(qs[b], (g.shape[0], 4))
+        pts = quat_rotate(qb, g) + centers[b]
         bodies.append((len(pos), g.shape[0], stiffness))
+        if sdf:
+            e = lattice_sdf.copy()
+            e[:, :3] = quat_rotate(qb, lattice_sdf[:, :3])
+            sdfs.append(e.astype(np.float32))
         for p in pts:
             pos.append([*p, 1.0])
             ph.append(PHASE_RIGID + b)
     return Scene("rigid_boxes", params, np.asarray(pos, np.float32), np.asarray(ph, np.int32), bodies=bodies,
-                 dt=1.0 / 60.0)
+                 sdf=sdfs, dt=1.0 / 60.0)
+
+
+def sdf_contact_pairs(pairs: int = 24, radius: float = 0.25, seed: int = 9) -> dict:
+    """2-D pinning case of the signed-distance rigid contact: `pairs` pairs
+    of 2 x 2 boxes (spacing 2 r, the reference's SDF corners: normal
+    (+-1, +-1) / sqrt(2), depth r sqrt(2)), each body rotated by a seeded
+    angle, the second box of a pair placed so that exactly one corner of
+    each touches (centre distance U(1.5 r, 1.95 r)) while every other pair
+    of particles of different bodies stays beyond 2.05 r; estimates =
+    start + U(-0.05 r, 0.05 r).  Pairs are 10 apart along x.  Returns the
+    lattice-frame positions (rest shape), start and estimate positions
+    (n, 2), inverse masses U(0.5, 2), body of each particle, lattice-frame
+    sdf (n, 4), body angles and the touching particle pairs (i1 < i2)."""
+    d = 2.0 * radius
+    lat = (np.array([[0, 0], [0, 1], [1, 0], [1, 1]], float) - 0.5) * d
+    corner_sdf = np.zeros((4, 4))
+    corner_sdf[:, :2] = np.sign(lat) / np.sqrt(2.0)
+    corner_sdf[:, 3] = radius * np.sqrt(2.0)
+    rot = lambda a, v: np.stack([np.cos(a) * v[:, 0] - np.sin(a) * v[:, 1],  # noqa: E731
+                                 np.sin(a) * v[:, 0] + np.cos(a) * v[:, 1]], 1)
+    rng_seed = seed
+    start, angles, body, touching = [], [], [], []
+    k = 0
+    while len(touching) < pairs:
+        u = uniform(rng_seed, (6,), 0.0, 1.0)
+        rng_seed += 1
+        a_ang, b_ang = u[0] * 2 * np.pi, u[1] * 2 * np.pi
+        base = np.array([10.0 * len(touching), 5.0])
+        pa = rot(a_ang, lat) + base
+        ca = int(u[2] * 4) % 4
+        cb = int(u[3] * 4) % 4
+        dirn = pa[ca] - pa.mean(0)
+        dirn = rot((u[4] - 0.5) * 0.8, (dirn / np.linalg.norm(dirn))[None])[0]
+        gap = (1.5 + 0.45 * u[5]) * radius
+        lb = rot(b_ang, lat)
+        pb = lb - lb[cb] + pa[ca] + gap * dirn
+        dist = np.linalg.norm(pa[:, None, :] - pb[None, :, :], axis=2)
+        close = dist < 2.05 * radius
+        if close.sum() != 1 or not close[ca, cb]:
+            continue
+        first = 8 * len(touching)
+        start += [pa, pb]
+        angles += [a_ang, b_ang]
+        body += [2 * len(touching)] * 4 + [2 * len(touching) + 1] * 4
+        touching.append((first + ca, first + 4 + cb))
+        k += 1
+    start = np.concatenate(start)
+    n = start.shape[0]
+    est = start + uniform(seed + 1000, (n, 2), -0.05 * radius, 0.05 * radius)
+    return dict(lattice=np.tile(lat, (2 * pairs, 1)), start=start, estimate=est,
+                imass=uniform(seed + 2000, (n,), 0.5, 2.0), body=np.asarray(body, np.int32),
+                sdf=np.tile(corner_sdf, (2 * pairs, 1)), angles=np.asarray(angles),
+                pairs=np.asarray(touching, np.int32))
 
 
 def apply_to(scene: Scene, system, params=None):
@@ -254,8 +344,10 @@ def apply_to(scene: Scene, system, params=None):
         system.add_distance_constraints(scene.pairs, scene.rest, scene.stiffness)
     if scene.pins is not None and len(scene.pins):
         system.add_point_constraints(scene.pins, scene.pin_points)
-    for first, count, st in scene.bodies:
-        system.add_rigid_body(first, count, st)
+    for k, (first, count, st) in enumerate(scene.bodies):
+        b = system.add_rigid_body(first, count, st)
+        if k < len(scene.sdf) and scene.sdf[k] is not None:
+            system.set_rigid_sdf(b, scene.sdf[k])
     for first, count in scene.open_gas:
         system.set_gas_open(first, count, True)
     return system

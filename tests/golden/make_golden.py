@@ -11,7 +11,9 @@ reference's outputs after the grid build, each solver stage and full
 updates.  gas_project.npz holds a 2-D smoke box with solid and fixed
 neighbours and the outputs of the reference's GasConstraint::project
 (gasconstraint.cpp:34-134) after 1 and 3 calls, open and closed: the
-estimates and each particle's force.
+estimates and each particle's force.  sdf_contacts.npz holds 2-D body
+pairs touching at one corner each and the reference's
+RigidContactConstraint::project (rigidcontactconstraint.cpp:30-96) result.
 """
 from __future__ import annotations
 
@@ -117,15 +119,28 @@ def gas_fixture() -> dict:
     return out
 
 
+def sdf_fixture() -> dict:
+    """The 2-D signed-distance pinning case (workloads.sdf_contact_pairs)
+    and the reference's RigidContactConstraint::project estimates (static
+    friction 0.4, kinetic 0.3)."""
+    from oracle import refcpu
+
+    case = W.sdf_contact_pairs(24)
+    out = refcpu.rigid_contacts(case["start"], case["estimate"], case["imass"], case["body"],
+                                case["sdf"][:, [0, 1, 3]], case["angles"], case["pairs"], 0.4, 0.3)
+    return dict(case, reference=out)
+
+
 def main():
     if not refgpu.available():
         raise SystemExit("reference sources not found")
     from oracle import refcpu
 
     if refcpu.available():
-        path = HERE / "gas_project.npz"
-        np.savez_compressed(path, **gas_fixture())
-        print(path, path.stat().st_size, "bytes")
+        for name, fix in (("gas_project", gas_fixture), ("sdf_contacts", sdf_fixture)):
+            path = HERE / f"{name}.npz"
+            np.savez_compressed(path, **fix())
+            print(path, path.stat().st_size, "bytes")
     for name, sc in scenes().items():
         data = scene_inputs(sc)
         data.update(stage_outputs(sc))

@@ -159,3 +159,61 @@ def assert_gas_projection(pos, force, ref_pos, ref_force, start, gas, tol):
     assert norm_err(pos[gas] - start[gas], d_ref) < tol
     assert norm_err(force[gas], ref_force[gas]) < tol
     assert np.max(np.abs(pos[~gas] - start[~gas])) == 0.0
+
+
+SDF_PIN_PARAMS = dict(particle_radius=0.25, kernel_radius=1.0, cell_size=0.5, grid_size=[1024, 32, 4],
+                      world_origin=[-5.0, 0.0, -1.0], gravity=[0.0, 0.0, 0.0], box_min=[-100.0, -100.0, -1.0],
+                      box_max=[1000.0, 100.0, 1.0], iterations=1, max_dt=1.0, contact_static_friction=0.4,
+                      contact_kinetic_friction=0.3, twod_z=0.0, max_neighbors=500, flags=1)
+
+
+def load_sdf_pin(system, case, fp32_inputs: bool = False):
+    """One contact pass of the 2-D signed-distance pinning case
+    (workloads.sdf_contact_pairs) on `system` (the CUDA system or the
+    oracle: same methods).  Each body is added in a rest frame within 0.7
+    rad of its target angle (its sdf normals rotated with it) and posed at
+    its target angle, every body centred at the origin -- one
+    shape-matching pass there stores the remaining rotation, the pose
+    being rigid and the coordinates small (FP32 shape matching far from
+    the origin loses digits in the centred offsets); then the start
+    positions are set and become x_old by a prediction at rest, the
+    estimates are set and the grid and the contact pass run.  fp32_inputs
+    rounds start and estimates to FP32 first, so that the CUDA path and the
+    oracle see the same inputs.  Returns the positions (n, 2)."""
+    from particlesolver_gb300 import workloads as W
+
+    n = len(case["start"])
+    nb = n // 4
+    rot = lambda a, v: np.stack([np.cos(a) * v[:, 0] - np.sin(a) * v[:, 1],  # noqa: E731
+                                 np.sin(a) * v[:, 0] + np.cos(a) * v[:, 1]], 1)
+    phi = case["angles"] - W.uniform(77, (nb,), -0.7, 0.7)
+    pos = np.zeros((n, 4))
+    pos[:, 3] = case["imass"]
+    sdf = np.zeros((n, 4))
+    posed = pos.copy()
+    for b in range(nb):
+        k = slice(4 * b, 4 * b + 4)
+        pos[k, :2] = rot(phi[b], case["lattice"][k])
+        posed[k, :2] = rot(case["angles"][b], case["lattice"][k])
+        sdf[k, :2] = rot(phi[b], case["sdf"][k, :2])
+        sdf[k, 3] = case["sdf"][k, 3]
+    system.add_particles(pos, None, (W.PHASE_RIGID + case["body"]).astype(np.int32), None)
+    for b in range(nb):
+        system.add_rigid_body(4 * b, 4, 1.0)
+        system.set_rigid_sdf(b, sdf[4 * b:4 * b + 4])
+    system.set_positions(posed)
+    system.solve_shapes()
+    rnd = (lambda a: a.astype(np.float32).astype(np.float64)) if fp32_inputs else (lambda a: a)  # noqa: E731
+    st = pos.copy()
+    st[:, :2] = case["start"]
+    st = rnd(st)
+    system.set_positions(st)
+    system.set_velocities(np.zeros((n, 4)))
+    system.integrate(1.0 / 60.0)
+    est = st.copy()
+    est[:, :2] = case["estimate"]
+    est = rnd(est)
+    system.set_positions(est)
+    system.build_grid()
+    system.collide()
+    return np.asarray(system.positions(), np.float64)[:, :2]

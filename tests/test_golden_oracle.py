@@ -68,3 +68,21 @@ def test_gas_projection_matches_reference_golden(open_, calls):
     gas = data["phase"] == W.PHASE_GAS
     assert_gas_projection(pos, force, data[f"open{open_}_k{calls}_pos"], data[f"open{open_}_k{calls}_force"],
                           data["pos_w"][:, :2].astype(np.float64), gas, 1e-7)
+
+
+def test_sdf_rigid_contact_matches_reference_golden():
+    """The oracle's signed-distance rigid contact against the reference's own
+    RigidContactConstraint::project (rigidcontactconstraint.cpp:30-96): 24
+    pairs of rotated 2-D boxes touching at one corner each (so the
+    reference's sequential projections and the Jacobi pass coincide), with
+    height-scaled masses and friction, to 1e-6 of the largest correction
+    (the body rotations come from one shape-matching pass)."""
+    from helpers import SDF_PIN_PARAMS, load_sdf_pin, norm_err
+
+    data = dict(np.load(GOLDEN / "sdf_contacts.npz"))
+    n = len(data["start"])
+    o = Oracle(params_nolib(SDF_PIN_PARAMS), n)
+    pos = load_sdf_pin(o, data)
+    d_ref = data["reference"] - data["estimate"]
+    assert np.max(np.abs(d_ref)) > 1e-3
+    assert norm_err(pos - data["estimate"], d_ref) < 1e-6

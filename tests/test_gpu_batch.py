@@ -42,7 +42,7 @@ def load_batch(scenes):
                           pairs=None if sc.pairs is None else sc.pairs + first, rest=sc.rest,
                           stiffness=sc.stiffness, pins=None if sc.pins is None else sc.pins + first,
                           pin_points=sc.pin_points, bodies=[(f + first, c, s) for f, c, s in sc.bodies],
-                          open_gas=[(f + first, c) for f, c in sc.open_gas])
+                          open_gas=[(f + first, c) for f, c in sc.open_gas], sdf=sc.sdf)
         W.apply_to(shifted, sys)
     return sys, firsts
 

@@ -182,3 +182,21 @@ def test_gas_projection_matches_reference_cpu(seed):
                                                 (~gas).astype(np.int32), 1.5, open_, calls)
             pos, f = oracle_gas_projection(sc.pos_w, sc.phase, sc.rest_density, vel, sc.params, open_, calls)
             assert_gas_projection(pos, f, ref_pos, ref_f, start, gas, 1e-7)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_sdf_rigid_contact_matches_reference_cpu(seed):
+    """The oracle's signed-distance rigid contact against the reference's
+    RigidContactConstraint::project compiled from the reference tree, on
+    fresh seeded 2-D body pairs touching at one corner, to 1e-6."""
+    from helpers import SDF_PIN_PARAMS, load_sdf_pin
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    case = W.sdf_contact_pairs(16, seed=seed)
+    ref = refcpu.rigid_contacts(case["start"], case["estimate"], case["imass"], case["body"],
+                                case["sdf"][:, [0, 1, 3]], case["angles"], case["pairs"], 0.4, 0.3)
+    o = Oracle(params_nolib(SDF_PIN_PARAMS), len(case["start"]))
+    pos = load_sdf_pin(o, case)
+    assert norm_err(pos - case["estimate"], ref - case["estimate"]) < 1e-6
