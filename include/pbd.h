@@ -270,6 +270,60 @@ int pbd_add_rope(pbd_system *sys, const float start[3], const float spacing[3], 
 int pbd_add_static_sphere(pbd_system *sys, const int32_t ll[3], const int32_t ur[3],
                           float spacing);
 
+/* The entry points under the names of the hot-path contract: each forwards
+ * to (or is a special case of) one above.  pbd_add_fluid_group makes
+ * [first, first+count) fluid with rest density rest_density (the
+ * reference's per-particle ros, integration.cu:23-34; every particle needs
+ * w > 0); pbd_add_rigid_group is pbd_add_rigid_body without the index;
+ * pbd_set_box replaces the world box of the scene being filled (the
+ * reference's minBounds / maxBounds, particlesystem.cpp:36-69). */
+int pbd_add_fluid_group(pbd_system *sys, uint32_t first, uint32_t count, float rest_density);
+int pbd_add_rigid_group(pbd_system *sys, uint32_t first, uint32_t count, float stiffness);
+int pbd_set_box(pbd_system *sys, const float box_min[3], const float box_max[3]);
+
+/* Emitters (the CPU reference's FluidEmitter, cpu/src/fluidemitter.cpp:
+ * 13-76, and OpenSmokeEmitter, opensmokeemitter.cpp:17-43; the reference
+ * GPU path has none).  An emitter appends a particle at `position` every
+ * 1 / rate seconds of emitter time while its elapsed time is below
+ * `duration` (<= 0: no limit), with velocity `velocity` plus U(0, 1) *
+ * velocity_jitter per axis from a seeded splitmix64 stream (the reference
+ * fluid emitter: velocity (frand(), 1)), phase FLUID or GAS, the given
+ * inverse mass and rest density, gas joining an open gas if open_gas.
+ * With solidify, the emitted particles and [group_first, group_first +
+ * group_count) take part in the fluid emitter's solidification: a fluid
+ * particle slower than solidify_speed at a height <= solidify_height counts
+ * its timer (initially 4) down by 1 per emitter tick while its lambda of the
+ * last update is <= 0, and up by dt (to 3 at most) while it is > 0; at 0 it
+ * becomes a fixed solid (phase SOLID, inverse mass 0, at rest), held where
+ * it stopped by a point constraint (as the reference GPU holds its static
+ * particles, particlesystem.cpp:672-681).  The
+ * reference's smoke emitter also advected drawing-only tracer particles;
+ * they take no part in the simulation and are not built. */
+typedef struct pbd_emitter {
+    float position[3];
+    float rate;              /* particles per second                        */
+    float duration;          /* seconds of emission (FluidEmitter: 5)       */
+    int32_t phase;           /* PBD_PHASE_FLUID or PBD_PHASE_GAS            */
+    float inverse_mass;      /* of an emitted particle (reference: 1)       */
+    float rest_density;
+    int32_t open_gas;
+    float velocity[3];
+    float velocity_jitter[3];
+    uint64_t seed;
+    int32_t solidify;
+    float solidify_speed;    /* reference 0.06                              */
+    float solidify_height;   /* reference 5                                 */
+    uint32_t group_first, group_count;
+} pbd_emitter;
+
+int pbd_add_emitter(pbd_system *sys, const pbd_emitter *emitter, uint32_t *id);
+/* Advances every emitter by dt -- the reference ticks its emitters after
+ * each simulation step (simulation.cpp:357-365): appends the particles due
+ * (as many as the capacity leaves room for; *emitted receives the number,
+ * may be NULL) and runs the solidification on the lambdas of the last
+ * update.  Synchronous. */
+int pbd_emit(pbd_system *sys, float dt, uint32_t *emitted, void *stream);
+
 /* ------------------------------------------------------------------ step */
 
 /* One simulation step (replaces ParticleSystem::update, particlesystem.cpp:
@@ -280,6 +334,11 @@ int pbd_update(pbd_system *sys, float dt, void *stream);
 /* nsteps updates captured once into a CUDA graph and replayed (same
  * results as nsteps pbd_update calls). */
 int pbd_update_graph(pbd_system *sys, float dt, uint32_t nsteps, void *stream);
+/* pbd_update under the contract's name (ParticleSystem::update = tick). */
+int pbd_tick(pbd_system *sys, float dt, void *stream);
+/* Every scene of a batched system (pbd_begin_scene) advanced nsteps from a
+ * captured CUDA graph: pbd_update_graph under the contract's name. */
+int pbd_batch_tick(pbd_system *sys, float dt, uint32_t nsteps, void *stream);
 
 /* Stage entry points, one per reference wrapper (wrappers.cuh:10-99). */
 /* integrateSystem (integration.cu:122-135): x_old = x; x += (v + g dt) dt. */
@@ -454,6 +513,9 @@ uint32_t pbd_num_distance_constraints(const pbd_system *sys);
  * keeps the state every `checkpoint_every` steps in device memory for
  * pbd_backward.  Memory: 32 bytes per particle per checkpoint. */
 int pbd_rollout(pbd_system *sys, float dt, uint32_t steps, uint32_t checkpoint_every, void *stream);
+/* pbd_rollout under the contract's name (the forward pass pbd_backward
+ * differentiates). */
+int pbd_record(pbd_system *sys, float dt, uint32_t steps, uint32_t checkpoint_every, void *stream);
 /* Gradients of a loss L(x_T, v_T) of the last rollout's final state.
  * Device arrays: dL_dx, dL_dv float4[n] (w ignored; NULL = zero);
  * outputs dL_dx0, dL_dv0 float4[n] (w = 0) with respect to the rollout's

@@ -122,6 +122,31 @@ class PbdTuning(ctypes.Structure):
                 ("reserved", ctypes.c_uint32 * 4)]
 
 
+class PbdEmitter(ctypes.Structure):
+    """Mirror of ``pbd_emitter`` (include/pbd.h)."""
+
+    _fields_ = [("position", ctypes.c_float * 3), ("rate", ctypes.c_float), ("duration", ctypes.c_float),
+                ("phase", ctypes.c_int32), ("inverse_mass", ctypes.c_float), ("rest_density", ctypes.c_float),
+                ("open_gas", ctypes.c_int32), ("velocity", ctypes.c_float * 3),
+                ("velocity_jitter", ctypes.c_float * 3), ("seed", ctypes.c_uint64), ("solidify", ctypes.c_int32),
+                ("solidify_speed", ctypes.c_float), ("solidify_height", ctypes.c_float),
+                ("group_first", ctypes.c_uint32), ("group_count", ctypes.c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.inverse_mass = 1.0
+        self.rest_density = 1.0
+        self.solidify_speed = 0.06  # FluidEmitter's thresholds
+        self.solidify_height = 5.0
+        for k, v in kw.items():
+            cur = getattr(self, k)
+            if isinstance(cur, ctypes.Array):
+                for i, x in enumerate(v):
+                    cur[i] = x
+            else:
+                setattr(self, k, v)
+
+
 class PbdProfile(ctypes.Structure):
     _fields_ = [
         ("stage_ms", ctypes.c_double * 8),
@@ -178,6 +203,14 @@ _SIGNATURES = {
     "pbd_get_phases": ([_P, _PI], _I),
     "pbd_set_gas_open": ([_P, _U32, _U32, _I], _I),
     "pbd_set_rigid_sdf": ([_P, _U32, _PF], _I),
+    "pbd_add_fluid_group": ([_P, _U32, _U32, _F], _I),
+    "pbd_add_emitter": ([_P, ctypes.POINTER(PbdEmitter), _PU], _I),
+    "pbd_emit": ([_P, _F, _PU, _P], _I),
+    "pbd_add_rigid_group": ([_P, _U32, _U32, _F], _I),
+    "pbd_set_box": ([_P, _PF, _PF], _I),
+    "pbd_tick": ([_P, _F, _P], _I),
+    "pbd_batch_tick": ([_P, _F, _U32, _P], _I),
+    "pbd_record": ([_P, _F, _U32, _U32, _P], _I),
     "pbd_get_forces": ([_P, _PF], _I),
     "pbd_get_device_buffers": ([_P, ctypes.POINTER(PbdDeviceBuffers)], _I),
     "pbd_add_fluid": ([_P, _PI, _PI, _F, _F, ctypes.c_uint64], _I),
@@ -344,6 +377,27 @@ class ParticleSystem:
         b = ctypes.c_uint32()
         self._check(self.lib.pbd_add_rigid_body(self.h, first, count, stiffness, ctypes.byref(b)))
         return b.value
+
+    def add_fluid_group(self, first: int, count: int, rest_density: float):
+        """Make [first, first + count) fluid with this rest density."""
+        self._check(self.lib.pbd_add_fluid_group(self.h, int(first), int(count), float(rest_density)))
+
+    def add_emitter(self, **kw) -> int:
+        """pbd_add_emitter with the fields of PbdEmitter; returns its id."""
+        e = PbdEmitter(**kw)
+        i = ctypes.c_uint32()
+        self._check(self.lib.pbd_add_emitter(self.h, ctypes.byref(e), ctypes.byref(i)))
+        return i.value
+
+    def emit(self, dt: float, stream=None) -> int:
+        """Advance every emitter by dt; returns the particles appended."""
+        c = ctypes.c_uint32()
+        self._check(self.lib.pbd_emit(self.h, dt, ctypes.byref(c), stream))
+        return c.value
+
+    def set_box(self, box_min, box_max):
+        lo, hi = _f32(box_min).reshape(3), _f32(box_max).reshape(3)
+        self._check(self.lib.pbd_set_box(self.h, _fptr(lo), _fptr(hi)))
 
     def set_rigid_sdf(self, body: int, sdf):
         """Signed-distance data of a rigid body's particles: (count, 4)

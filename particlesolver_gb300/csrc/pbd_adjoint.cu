@@ -874,6 +874,10 @@ int pbd_rollout(pbd_system *s, float dt, uint32_t steps, uint32_t every, void *s
     return PBD_OK;
 }
 
+int pbd_record(pbd_system *s, float dt, uint32_t steps, uint32_t every, void *stream) {
+    return pbd_rollout(s, dt, steps, every, stream);
+}
+
 int pbd_backward(pbd_system *s, const float *dL_dx, const float *dL_dv, float *dL_dx0, float *dL_dv0,
                  float *dL_dstiffness, void *stream) {
     if (int rc = pbd_internal_guard(s)) return rc;

@@ -1658,6 +1658,53 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
     v[sidx[i]] = make_float4(nv.x, nv.y, nv.z, vi4.w);
 }
 
+// ----------------------------------------------------------- emitters
+
+// The solidification of FluidEmitter::tick (cpu/src/fluidemitter.cpp:14-51)
+// over the sorted slots of the last update's grid: a tagged fluid particle
+// slower than `speed` at a height <= `height` counts its timer down by 1
+// while its lambda of that update is <= 0 (the reference read lambdas[i]
+// with i its index in the fluid's particle list, not the particle's own
+// index -- here the particle's own lambda), up by dt (to 3) otherwise; at 0
+// it becomes a fixed solid at rest (Particle::imass = 0, ph = SOLID, ep = p,
+// v = f = 0).  *converted counts the conversions and list[] receives their
+// indices (the host pins them there: the GPU step moves w = 0 particles
+// like any other in its prediction, integration_kernel.cuh:159-184, and
+// holds fixed particles with point constraints, particlesystem.cpp:672-681).
+__global__ void __launch_bounds__(kBlock) k_solidify(uint32_t n, float dt, float speed, float height,
+                                                     const uint32_t *__restrict__ sidx,
+                                                     const float4 *__restrict__ sxl,
+                                                     const uint8_t *__restrict__ tag, float *__restrict__ timer,
+                                                     float4 *__restrict__ x, float4 *__restrict__ x_old,
+                                                     float4 *__restrict__ v, int *__restrict__ phase,
+                                                     float4 *__restrict__ force, uint32_t *__restrict__ converted,
+                                                     uint32_t *__restrict__ list) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t i = sidx[k];
+    if (!tag[i] || phase[i] != kFluid) return;
+    const float4 vi = v[i];
+    const float4 p = x[i];
+    if (!(len3(f3(vi)) < speed && p.y <= height)) return;
+    float t = timer[i];
+    if (sxl[k].w <= 0.f) {
+        t -= 1.f;
+        if (t <= 0.f) {
+            t = 0.f;
+            const float4 fixed = make_float4(p.x, p.y, p.z, 0.f);
+            x[i] = fixed;
+            x_old[i] = fixed;
+            v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            phase[i] = kSolid;
+            if (force) force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            list[atomicAdd(converted, 1u)] = i;
+        }
+    } else {
+        t = fminf(t + dt, 3.f);
+    }
+    timer[i] = t;
+}
+
 __global__ void __launch_bounds__(kBlock) k_finite(uint32_t n, const float4 *__restrict__ x,
                                                    const float4 *__restrict__ v,
                                                    uint32_t *__restrict__ flag) {
@@ -1893,6 +1940,15 @@ cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, fl
         PBD_TPP_DISPATCH(tpp, false, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L,
                          use_list);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solidify(uint32_t n, float dt, float speed, float height, const uint32_t *sidx, const float4 *sxl,
+                            const uint8_t *tag, float *timer, float4 *x, float4 *x_old, float4 *v, int *phase,
+                            float4 *force, uint32_t *converted, uint32_t *list, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_solidify<<<blocks_for(n), kBlock, 0, s>>>(n, dt, speed, height, sidx, sxl, tag, timer, x, x_old, v, phase,
+                                                force, converted, list);
     return cudaGetLastError();
 }
 

@@ -151,6 +151,10 @@ cudaError_t launch_velocity(const DevParams &P, uint32_t n, float dt, const floa
 // vs: scratch for the velocities in sorted order.
 cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs,
                         const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s);
+// Solidification of the fluid emitter over the sorted slots of the last grid.
+cudaError_t launch_solidify(uint32_t n, float dt, float speed, float height, const uint32_t *sidx, const float4 *sxl,
+                            const uint8_t *tag, float *timer, float4 *x, float4 *x_old, float4 *v, int *phase,
+                            float4 *force, uint32_t *converted, uint32_t *list, cudaStream_t s);
 cudaError_t launch_finite_check(uint32_t n, const float4 *x, const float4 *v, uint32_t *flag,
                                 cudaStream_t s);
 

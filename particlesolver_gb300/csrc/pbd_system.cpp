@@ -734,6 +734,10 @@ int pbd_destroy(pbd_system *s) {
     dfree(s->glam);
     dfree(s->sdf);
     dfree(s->body_of);
+    dfree(s->solid_timer);
+    dfree(s->solid_tag);
+    dfree(s->solid_count);
+    dfree(s->solid_list);
     dfree(s->flag);
     dfree(s->grid.hash);
     dfree(s->grid.slot);
@@ -1103,6 +1107,68 @@ int pbd_get_phases(pbd_system *s, int32_t *dst) {
     return PBD_OK;
 }
 
+int pbd_add_fluid_group(pbd_system *s, uint32_t first, uint32_t count, float rest_density) {
+    SYS_GUARD(s);
+    if ((uint64_t)first + count > s->n)
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "range [%u, %u) exceeds the %u particles", first, first + count, s->n);
+    if (!(rest_density > 0.f) || !std::isfinite(rest_density))
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "rest density must be finite and > 0");
+    if (count == 0) return PBD_OK;
+    CUDA_TRY(s, cudaDeviceSynchronize());
+    std::vector<int32_t> ph(count);
+    std::vector<float4> pos(count);
+    CUDA_TRY(s, cudaMemcpy(ph.data(), s->phase + first, count * 4ull, cudaMemcpyDeviceToHost));
+    CUDA_TRY(s, cudaMemcpy(pos.data(), s->x + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t k = 0; k < count; ++k) {
+        if (!(pos[k].w > 0.f)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "fluid particle %u needs inverse mass > 0", first + k);
+        for (const uint4 &r : s->body_range)
+            if (first + k >= r.x && first + k < r.x + r.y)
+                return fail(s, PBD_ERR_INVALID_ARGUMENT, "particle %u belongs to a rigid body", first + k);
+    }
+    // the phase census of every scene the range touches
+    for (uint32_t k = 0; k < count; ++k) {
+        pbd_scene &sc = s->scenes[s->batched() ? scene_of_slot(s, first + k) : 0];
+        const int p = ph[k];
+        if (p == PBD_PHASE_FLUID) continue;
+        if (p == PBD_PHASE_GAS) { --s->n_gas; --sc.n_gas; }
+        if (p >= PBD_PHASE_CLOTH) { --s->n_contact; --sc.n_contact; }
+        ++s->n_fluid;
+        ++sc.n_fluid;
+    }
+    const std::vector<int32_t> fluid(count, PBD_PHASE_FLUID);
+    const std::vector<float> ro(count, rest_density);
+    CUDA_TRY(s, cudaMemcpy(s->phase + first, fluid.data(), count * 4ull, cudaMemcpyHostToDevice));
+    CUDA_TRY(s, cudaMemcpy(s->rho0 + first, ro.data(), count * 4ull, cudaMemcpyHostToDevice));
+    if (int rc = refresh_scenes(s)) return rc;
+    if (s->n_fluid && !s->vs) CUDA_TRY(s, dalloc(&s->vs, s->cap));
+    if (s->n_fluid && !s->nbl.slot && s->list_capacity) {
+        CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
+        CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
+        s->nbl.capacity = s->list_capacity;
+        s->nbl.stride = s->cap;
+    }
+    if (int rc = alloc_skin(s)) return rc;
+    s->grid_valid = false;
+    s->list_valid = false;
+    ++s->version;
+    return PBD_OK;
+}
+
+int pbd_add_rigid_group(pbd_system *s, uint32_t first, uint32_t count, float stiffness) {
+    return pbd_add_rigid_body(s, first, count, stiffness, nullptr);
+}
+
+int pbd_set_box(pbd_system *s, const float box_min[3], const float box_max[3]) {
+    SYS_GUARD(s);
+    if (!box_min || !box_max) return fail(s, PBD_ERR_INVALID_ARGUMENT, "box_min and box_max are required");
+    pbd_params p = s->scenes.back().params;
+    for (int k = 0; k < 3; ++k) {
+        p.box_min[k] = box_min[k];
+        p.box_max[k] = box_max[k];
+    }
+    return pbd_set_scene_params(s, (uint32_t)s->scenes.size() - 1u, &p);
+}
+
 int pbd_set_gas_open(pbd_system *s, uint32_t first, uint32_t count, int open) {
     SYS_GUARD(s);
     if ((uint64_t)first + count > s->n)
@@ -1142,6 +1208,152 @@ int pbd_get_device_buffers(pbd_system *s, pbd_device_buffers *out) {
 }
 
 // --------------------------------------------------------------- stepping
+
+// splitmix64 output number k (1-based) of the stream started at seed, as a
+// U(0, 1) double (53 bits): the generator of the scene builders.
+static double splitmix_uniform(uint64_t seed, uint64_t k) {
+    uint64_t z = seed + k * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// Recounts the phase census of every scene from the device phases (after
+// a kernel changed phases).
+static int recount_phases(pbd_system *s) {
+    std::vector<int32_t> ph(s->n);
+    if (s->n) CUDA_TRY(s, cudaMemcpy(ph.data(), s->phase, s->n * 4ull, cudaMemcpyDeviceToHost));
+    s->n_fluid = s->n_contact = s->n_gas = 0;
+    for (pbd_scene &sc : s->scenes) {
+        sc.n_fluid = sc.n_contact = sc.n_gas = 0;
+        for (uint32_t k = sc.first; k < sc.first + sc.count; ++k) {
+            sc.n_fluid += ph[k] == PBD_PHASE_FLUID;
+            sc.n_gas += ph[k] == PBD_PHASE_GAS;
+            sc.n_contact += ph[k] >= PBD_PHASE_CLOTH;
+        }
+        s->n_fluid += sc.n_fluid;
+        s->n_gas += sc.n_gas;
+        s->n_contact += sc.n_contact;
+    }
+    return refresh_scenes(s);
+}
+
+int pbd_add_emitter(pbd_system *s, const pbd_emitter *e, uint32_t *id) {
+    SYS_GUARD(s);
+    if (!e) return fail(s, PBD_ERR_INVALID_ARGUMENT, "emitter is NULL");
+    if (!(e->rate > 0.f) || !std::isfinite(e->rate)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "rate must be > 0");
+    if (e->phase != PBD_PHASE_FLUID && e->phase != PBD_PHASE_GAS)
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "an emitter emits fluid or gas");
+    if (!(e->inverse_mass > 0.f) || !(e->rest_density > 0.f))
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "inverse_mass and rest_density must be > 0");
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(e->position[k]) || !std::isfinite(e->velocity[k]) || !std::isfinite(e->velocity_jitter[k]))
+            return fail(s, PBD_ERR_INVALID_ARGUMENT, "emitter position and velocity must be finite");
+    if ((uint64_t)e->group_first + e->group_count > s->n)
+        return fail(s, PBD_ERR_INVALID_ARGUMENT, "solidification group exceeds the particle count");
+    if (e->solidify) {
+        if (!s->solid_timer) {
+            CUDA_TRY(s, dalloc(&s->solid_timer, s->cap));
+            CUDA_TRY(s, dalloc(&s->solid_tag, s->cap));
+            CUDA_TRY(s, dalloc(&s->solid_count, 1));
+            CUDA_TRY(s, dalloc(&s->solid_list, s->cap));
+            const std::vector<float> four(s->cap, 4.f);
+            CUDA_TRY(s, cudaMemcpy(s->solid_timer, four.data(), s->cap * 4ull, cudaMemcpyHostToDevice));
+            CUDA_TRY(s, cudaMemset(s->solid_tag, 0, s->cap));
+        }
+        if (e->group_count) CUDA_TRY(s, cudaMemset(s->solid_tag + e->group_first, 1, e->group_count));
+    }
+    s->emitters.push_back(pbd_system::Emitter{*e});
+    if (id) *id = (uint32_t)s->emitters.size() - 1u;
+    return PBD_OK;
+}
+
+int pbd_emit(pbd_system *s, float dt, uint32_t *emitted, void *stream) {
+    SYS_GUARD(s);
+    if (emitted) *emitted = 0;
+    if (!(dt >= 0.f) || !std::isfinite(dt)) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dt must be >= 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(s, cudaStreamSynchronize(st));
+    // solidification first (the reference's order), on the last update's
+    // grid and lambdas; only where both exist
+    bool any_solid = false;
+    float speed = 0.f, height = 0.f;
+    for (const auto &e : s->emitters)
+        if (e.spec.solidify) {
+            any_solid = true;
+            speed = e.spec.solidify_speed;
+            height = e.spec.solidify_height;
+        }
+    if (any_solid && s->grid_valid && s->n_fluid && s->n) {
+        CUDA_TRY(s, cudaMemsetAsync(s->solid_count, 0, 4, st));
+        CUDA_TRY(s, pbd::launch_solidify(s->n, dt, speed, height, s->grid.sorted_idx, s->sxl, s->solid_tag,
+                                         s->solid_timer, s->x, s->x_old, s->v, s->phase, s->force, s->solid_count,
+                                         s->solid_list, st));
+        uint32_t converted = 0;
+        CUDA_TRY(s, cudaMemcpyAsync(&converted, s->solid_count, 4, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(s, cudaStreamSynchronize(st));
+        if (converted) {
+            // pin each new solid where it stopped (in index order, so the
+            // constraint order does not depend on the kernel's atomics)
+            std::vector<uint32_t> idx(converted);
+            CUDA_TRY(s, cudaMemcpy(idx.data(), s->solid_list, converted * 4ull, cudaMemcpyDeviceToHost));
+            std::sort(idx.begin(), idx.end());
+            std::vector<float> pts(3ull * converted);
+            for (uint32_t k = 0; k < converted; ++k) {
+                float4 p;
+                CUDA_TRY(s, cudaMemcpy(&p, s->x + idx[k], sizeof(float4), cudaMemcpyDeviceToHost));
+                pts[3 * k] = p.x;
+                pts[3 * k + 1] = p.y;
+                pts[3 * k + 2] = p.z;
+            }
+            if (int rc = recount_phases(s)) return rc;
+            if (int rc = pbd_add_point_constraints(s, converted, idx.data(), pts.data())) return rc;
+            s->grid_valid = false;
+            s->list_valid = false;
+            ++s->version;
+        }
+    }
+    uint32_t total = 0;
+    for (auto &e : s->emitters) {
+        const pbd_emitter &sp = e.spec;
+        e.timer += dt;
+        e.elapsed += dt;
+        uint32_t due = 0;
+        const double period = 1.0 / sp.rate;
+        while ((sp.duration <= 0.f || e.elapsed < sp.duration) && e.timer >= period) {
+            e.timer -= period;
+            ++due;
+        }
+        due = std::min<uint32_t>(due, s->cap - s->n);
+        if (!due) continue;
+        std::vector<float4> pos(due), vel(due);
+        for (uint32_t k = 0; k < due; ++k) {
+            pos[k] = make_float4(sp.position[0], sp.position[1], sp.position[2], sp.inverse_mass);
+            float u[3];
+            for (int a = 0; a < 3; ++a) u[a] = (float)splitmix_uniform(sp.seed, ++e.draws);
+            vel[k] = make_float4(sp.velocity[0] + u[0] * sp.velocity_jitter[0],
+                                 sp.velocity[1] + u[1] * sp.velocity_jitter[1],
+                                 sp.velocity[2] + u[2] * sp.velocity_jitter[2], 0.f);
+        }
+        const std::vector<int32_t> ph(due, sp.phase);
+        const std::vector<float> ro(due, sp.rest_density);
+        uint32_t first = 0;
+        if (int rc = pbd_add_particles(s, due, &pos[0].x, &vel[0].x, ph.data(), ro.data(), &first)) return rc;
+        if (sp.phase == PBD_PHASE_GAS && sp.open_gas)
+            if (int rc = pbd_set_gas_open(s, first, due, 1)) return rc;
+        if (sp.solidify) CUDA_TRY(s, cudaMemset(s->solid_tag + first, 1, due));
+        total += due;
+    }
+    if (emitted) *emitted = total;
+    return PBD_OK;
+}
+
+int pbd_tick(pbd_system *s, float dt, void *stream) { return pbd_update(s, dt, stream); }
+
+int pbd_batch_tick(pbd_system *s, float dt, uint32_t nsteps, void *stream) {
+    return pbd_update_graph(s, dt, nsteps, stream);
+}
 
 int pbd_update(pbd_system *s, float dt, void *stream) {
     SYS_GUARD(s);

@@ -47,6 +47,17 @@ struct pbd_system {
     int *body_of = nullptr;      // [cap] body of each particle, -1 for none
     std::vector<float4> sdf_host;  // host copy of sdf for the live particles
     bool any_sdf = false;
+    // emitters: host state; solidification timer and membership per particle
+    struct Emitter {
+        pbd_emitter spec;
+        double timer = 0.0, elapsed = 0.0;
+        uint64_t draws = 0;  // splitmix64 outputs used so far
+    };
+    std::vector<Emitter> emitters;
+    float *solid_timer = nullptr;   // [cap], starts at 4 (Particle::t)
+    uint8_t *solid_tag = nullptr;   // [cap], 1 = takes part in solidification
+    uint32_t *solid_count = nullptr;
+    uint32_t *solid_list = nullptr; // [cap] particles converted by the last tick
 
     pbd::GridBuffers grid{};
     uint32_t grid_cells = 0;  // cells the grid arrays were sized for

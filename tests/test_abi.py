@@ -38,22 +38,24 @@ def test_kernels_are_sm103a_only():
     assert "sm_103a" in out.stdout
 
 
-def test_params_layout_matches_c(tmp_path):
+@pytest.mark.parametrize("mirror,ctype", [(pbd.PbdParams, "pbd_params"), (pbd.PbdEmitter, "pbd_emitter"),
+                                           (pbd.PbdTuning, "pbd_tuning")])
+def test_struct_layout_matches_c(tmp_path, mirror, ctype):
     src = tmp_path / "layout.c"
-    fields = [f for f, _ in pbd.PbdParams._fields_]
-    body = "\n".join(f'printf("%zu\\n", offsetof(pbd_params, {f}));' for f in fields)
+    fields = [f for f, _ in mirror._fields_]
+    body = "\n".join(f'printf("%zu\\n", offsetof({ctype}, {f}));' for f in fields)
     src.write_text(textwrap.dedent(f"""
         #include <stddef.h>
         #include <stdio.h>
         #include "pbd.h"
-        int main(void) {{ printf("%zu\\n", sizeof(pbd_params)); {body} return 0; }}
+        int main(void) {{ printf("%zu\\n", sizeof({ctype})); {body} return 0; }}
     """))
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", str(_build.ROOT / "include"), str(src), "-o", str(exe)], check=True)
     vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    assert vals[0] == ctypes.sizeof(pbd.PbdParams)
-    for (name, _), off in zip(pbd.PbdParams._fields_, vals[1:]):
-        assert getattr(pbd.PbdParams, name).offset == off, name
+    assert vals[0] == ctypes.sizeof(mirror)
+    for (name, _), off in zip(mirror._fields_, vals[1:]):
+        assert getattr(mirror, name).offset == off, name
 
 
 def test_default_params_are_reference_values():

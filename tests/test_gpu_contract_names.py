@@ -1,0 +1,91 @@
+"""The entry points named by the hot-path contract (pbd_tick,
+pbd_batch_tick, pbd_add_fluid_group, pbd_add_rigid_group, pbd_set_box,
+pbd_record) give exactly what the calls they stand for give."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from particlesolver_gb300 import ParticleSystem, PbdError, default_params
+from particlesolver_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def load(sc):
+    g = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, g)
+    return g
+
+
+def test_tick_is_update():
+    sc = W.dam_break(16, 12, 8)
+    a, b = load(sc), load(sc)
+    for _ in range(3):
+        a.update(sc.dt)
+        assert b.lib.pbd_tick(b.h, ctypes.c_float(sc.dt), None) == 0
+    np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_batch_tick_is_update_graph():
+    scenes = [W.pbf_block(800, seed=2), W.granular_column(300, seed=3)]
+    from test_gpu_batch import load_batch
+
+    a, _ = load_batch(scenes)
+    b, _ = load_batch(scenes)
+    a.update_graph(1.0 / 60.0, 3)
+    assert b.lib.pbd_batch_tick(b.h, ctypes.c_float(1.0 / 60.0), 3, None) == 0
+    np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_add_fluid_group_equals_fluid_particles():
+    """Particles added as solid grains, then made fluid of rest density 3,
+    step exactly as particles added as fluid of that density."""
+    sc = W.dam_break(12, 12, 8)
+    rho = np.full(sc.n, 3.0, np.float32)
+    a = ParticleSystem(default_params(**sc.params), sc.n)
+    a.add_particles(sc.pos_w, None, np.full(sc.n, W.PHASE_FLUID, np.int32), rho)
+    b = ParticleSystem(default_params(**sc.params), sc.n)
+    b.add_particles(sc.pos_w, None, np.full(sc.n, W.PHASE_SOLID, np.int32), None)
+    b.add_fluid_group(0, sc.n, 3.0)
+    np.testing.assert_array_equal(b.phases(), a.phases())
+    for _ in range(3):
+        a.update(sc.dt)
+        b.update(sc.dt)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    with pytest.raises(PbdError):
+        b.add_fluid_group(0, sc.n, -1.0)
+
+
+def test_add_rigid_group_is_add_rigid_body():
+    sc = W.rigid_boxes(count=4)
+    a = load(sc)
+    b = ParticleSystem(default_params(**sc.params), sc.n)
+    b.add_particles(sc.pos_w, sc.vel, sc.phase, sc.rest_density)
+    for first, count, st in sc.bodies:
+        assert b.lib.pbd_add_rigid_group(b.h, first, count, ctypes.c_float(st)) == 0
+    for _ in range(5):
+        a.update(sc.dt)
+        b.update(sc.dt)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_set_box_is_the_params_box():
+    sc = W.reference_granular()
+    lo, hi = [-3.0, 0.5, -3.0], [3.0, 100.0, 3.0]
+    a = ParticleSystem(default_params(**{**sc.params, "box_min": lo, "box_max": hi}), sc.n)
+    W.apply_to(sc, a)
+    b = load(sc)
+    b.set_box(lo, hi)
+    for _ in range(5):
+        a.update(sc.dt)
+        b.update(sc.dt)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_record_is_rollout():
+    sc = W.cloth_ropes_grains(cloth=8, ropes=2, rope_particles=6, grains=10)
+    a, b = load(sc), load(sc)
+    a.rollout(sc.dt, 6, 3)
+    assert b.lib.pbd_record(b.h, ctypes.c_float(sc.dt), 6, 3, None) == 0
+    np.testing.assert_array_equal(a.positions(), b.positions())
