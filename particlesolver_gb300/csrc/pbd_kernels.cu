@@ -924,6 +924,25 @@ __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uin
     }
 }
 
+// Calls f(j, src[j], ok) for the cnt listed neighbours of particle i, a
+// quad at a time: the quad's four gathers are all issued before any is
+// used, so their latencies overlap; slots past cnt read particle i's own
+// entry and come with ok = false (f must then add nothing).
+template <class T, class F>
+__device__ __forceinline__ void gather_listed(const NbList &L, uint32_t i, uint32_t cnt,
+                                              const T *__restrict__ src, F &&f) {
+    for (uint32_t q = 0; 4u * q < cnt; ++q) {
+        const uint4 e = L.slot[q * L.stride + i];
+        const uint32_t left = cnt - 4u * q;
+        const uint32_t j1 = left > 1u ? e.y : i, j2 = left > 2u ? e.z : i, j3 = left > 3u ? e.w : i;
+        const T a = src[e.x], b = src[j1], c = src[j2], d = src[j3];
+        f(e.x, a, true);
+        f(j1, b, left > 1u);
+        f(j2, c, left > 2u);
+        f(j3, d, left > 3u);
+    }
+}
+
 // Stencil ranges with the radius fixed at compile time (RAD > 0; RAD = 0
 // defers to the runtime version).  The per-axis slab gaps are computed once
 // and, per z slab, all 2 RAD + 1 row ranges are fetched before any of them
@@ -1183,9 +1202,9 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
     const float inv_rho0 = 1.f / a.rho0;
     const float spiky_r = -P.spiky * inv_rho0;
     LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-    auto add = [&](uint32_t j, const float4 &pj, float d2) {
+    auto add = [&](uint32_t j, const float4 &pj, float d2, bool ok = true) {
         const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-        acc.add(P, true, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
+        acc.add(P, ok, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
     };
     if (reuse) {
         for_each_listed(L, i, L.count[i], [&](uint32_t j) {
@@ -1232,11 +1251,20 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
                 dst[q * L.stride] = make_uint4(col[k], col[k + kListBlock], col[k + 2 * kListBlock],
                                                col[k + 3 * kListBlock]);
             }
-            for (uint32_t k = 0; k < cnt; ++k) {
-                const uint32_t j = col[k * (uint32_t)kListBlock];
-                const float4 pj = __ldg(sx + j);
-                const float d2 = dist2_exact(pi, f3(pj));
-                if (!SKIN || d2 < h2) add(j, pj, d2);
+            // four gathers in flight before their sums (entries past cnt
+            // read this particle's own slot and add nothing)
+            for (uint32_t k = 0; k < cnt; k += 4u) {
+                uint32_t jj[4];
+                float4 pp[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) jj[t] = (k + t < cnt) ? col[(k + t) * (uint32_t)kListBlock] : i;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) pp[t] = __ldg(sx + jj[t]);
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float d2 = dist2_exact(pi, f3(pp[t]));
+                    add(jj[t], pp[t], d2, k + t < cnt && (!SKIN || d2 < h2));
+                }
             }
         } else {
             if (SKIN) atomicOr(L.ovf, 1u);
@@ -1266,13 +1294,11 @@ __device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t 
     const float h2 = P.h2;
     float3 delta = make_float3(0.f, 0.f, 0.f);
     uint32_t nb = 0;
-    for_each_listed(L, i, cnt, [&](uint32_t j) {
-        const float4 pl = sxl[j];
+    gather_listed(L, i, cnt, sxl, [&](uint32_t, const float4 &pl, bool valid) {
         const float d2 = dist2_exact(pi, f3(pl));
-        if (d2 < h2) {  // all of a plain list; a skin list holds more
-            delta_add(P, delta, true, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
-            ++nb;
-        }
+        const bool ok = valid && d2 < h2;  // all of a plain list; a skin list holds more
+        delta_add(P, delta, ok, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
+        nb += ok ? 1u : 0u;
     });
     const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
     return delta / div;
@@ -1600,11 +1626,19 @@ __global__ void __launch_bounds__(kBlock) k_velocity(DevParams P0, uint32_t n, f
 
 // ------------------------------------------------------------------- XSPH
 
+// Velocities in sorted order for XSPH, w = the particle's mass as a fluid
+// neighbour (1 / w for a fluid particle with w > 0, else 0), so the XSPH
+// sum needs no phase lookup.
 __global__ void __launch_bounds__(kBlock) k_xsph_gather(uint32_t n, const uint32_t *__restrict__ sidx,
+                                                        const float4 *__restrict__ sx,
+                                                        const SortedAttr *__restrict__ sattr,
                                                         const float4 *__restrict__ v, float4 *__restrict__ vs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    vs[i] = v[sidx[i]];
+    const float4 vi = v[sidx[i]];
+    const float w = sx[i].w;
+    const float m = (sattr[i].phase == kFluid && w > 0.f) ? 1.f / w : 0.f;
+    vs[i] = make_float4(vi.x, vi.y, vi.z, m);
 }
 
 // XSPH viscosity (Macklin & Mueller 2013, eq. 17) on fluid particles, made
@@ -1637,13 +1671,27 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
     };
     const uint32_t cnt = (TPP == 1 && use_list) ? L.count[i] : 0u;
     if (TPP == 1 && use_list && list_usable(P, L, cnt)) {
-        // the last lambda pass listed every neighbour of any phase
-        for_each_listed(L, i, cnt, [&](uint32_t j) {
-            if (sattr[j].phase != kFluid) return;
-            const float4 xj4 = sx[j];
-            const float d2 = dist2_exact(xi, f3(xj4));
-            if (d2 < P.h2) add(j, xj4, d2);
-        });
+        // the last lambda pass listed every neighbour of any phase; a
+        // neighbour's fluid mass rides in vs.w (0 for the other phases)
+        for (uint32_t q = 0; 4u * q < cnt; ++q) {
+            const uint4 e = L.slot[q * L.stride + i];
+            const uint32_t left = cnt - 4u * q;
+            const uint32_t jj[4] = {e.x, left > 1u ? e.y : i, left > 2u ? e.z : i, left > 3u ? e.w : i};
+            float4 xx[4], vv[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                xx[t] = sx[jj[t]];
+                vv[t] = vs[jj[t]];
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const float d2 = dist2_exact(xi, f3(xx[t]));
+                const float hm2 = P.h2 - d2;
+                const bool ok = (uint32_t)t < left && d2 < P.h2;
+                const float wgt = ok ? P.poly6 * hm2 * hm2 * hm2 * vv[t].w : 0.f;
+                acc += (f3(vv[t]) - vi) * wgt;
+            }
+        }
     } else {
         group_walk<TPP>(
             P, G, xi, grid_pos(P, xi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
@@ -1655,7 +1703,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
     acc.z = G.sum(acc.z);
     if (G.lane != 0) return;
     const float3 nv = vi + acc * (P.xsph_c / a.rho0);
-    v[sidx[i]] = make_float4(nv.x, nv.y, nv.z, vi4.w);
+    v[sidx[i]] = make_float4(nv.x, nv.y, nv.z, 0.f);  // w as the velocity update left it
 }
 
 // ----------------------------------------------------------- emitters
@@ -1932,7 +1980,7 @@ cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, fl
                         const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
-    k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, v, vs);
+    k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, g.sorted_x, g.sorted_attr, v, vs);
     if (P.table) {
         PBD_TPP_DISPATCH(tpp, true, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L,
                          use_list);
