@@ -14,6 +14,30 @@ namespace pbd {
 namespace {
 
 constexpr int kBlock = 256;
+
+// Compile-time shapes of the neighbour passes (measured on the 1M dam
+// break; a build may override them): candidates per unrolled step of the
+// list build's walk, list quads whose gathers are in flight together in
+// the delta pass, and the minimum resident blocks of the fused solve
+// kernel with one lane per particle: its full form (PBF delta, contacts,
+// walls) and its contact-and-wall form for batches without fluid
+// (0 = no register cap).
+#ifndef PBD_WALK_UNROLL
+#define PBD_WALK_UNROLL 4
+#endif
+#ifndef PBD_DELTA_QUADS
+#define PBD_DELTA_QUADS 1
+#endif
+#ifndef PBD_SOLVE_MIN_BLOCKS
+#define PBD_SOLVE_MIN_BLOCKS 4
+#endif
+#ifndef PBD_CONTACT_MIN_BLOCKS
+#define PBD_CONTACT_MIN_BLOCKS 8
+#endif
+#ifndef PBD_BATCH_SOLVE_MIN_BLOCKS
+#define PBD_BATCH_SOLVE_MIN_BLOCKS PBD_SOLVE_MIN_BLOCKS
+#endif
+constexpr int kWalkUnroll = PBD_WALK_UNROLL;
 // Block of the shared-memory list build, and the largest list capacity it
 // assembles: (capacity + 1) x kListBlock words stay under the 48 KB of
 // dynamic shared memory a launch gets without opting in.
@@ -928,18 +952,26 @@ __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uin
 // quad at a time: the quad's four gathers are all issued before any is
 // used, so their latencies overlap; slots past cnt read particle i's own
 // entry and come with ok = false (f must then add nothing).
-template <class T, class F>
+template <int QUADS = 1, class T, class F>
 __device__ __forceinline__ void gather_listed(const NbList &L, uint32_t i, uint32_t cnt,
                                               const T *__restrict__ src, F &&f) {
-    for (uint32_t q = 0; 4u * q < cnt; ++q) {
-        const uint4 e = L.slot[q * L.stride + i];
-        const uint32_t left = cnt - 4u * q;
-        const uint32_t j1 = left > 1u ? e.y : i, j2 = left > 2u ? e.z : i, j3 = left > 3u ? e.w : i;
-        const T a = src[e.x], b = src[j1], c = src[j2], d = src[j3];
-        f(e.x, a, true);
-        f(j1, b, left > 1u);
-        f(j2, c, left > 2u);
-        f(j3, d, left > 3u);
+    for (uint32_t q = 0; 4u * q < cnt; q += QUADS) {
+        uint32_t jj[4 * QUADS];
+        T v[4 * QUADS];
+#pragma unroll
+        for (int u = 0; u < QUADS; ++u) {
+            const uint32_t qq = q + (uint32_t)u;
+            const uint4 e = (4u * qq < cnt) ? L.slot[qq * L.stride + i] : make_uint4(i, i, i, i);
+            const uint32_t first = 4u * qq;
+            jj[4 * u] = first < cnt ? e.x : i;
+            jj[4 * u + 1] = first + 1u < cnt ? e.y : i;
+            jj[4 * u + 2] = first + 2u < cnt ? e.z : i;
+            jj[4 * u + 3] = first + 3u < cnt ? e.w : i;
+        }
+#pragma unroll
+        for (int t = 0; t < 4 * QUADS; ++t) v[t] = src[jj[t]];
+#pragma unroll
+        for (int t = 0; t < 4 * QUADS; ++t) f(jj[t], v[t], 4u * q + (uint32_t)t < cnt);
     }
 }
 
@@ -1233,7 +1265,7 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
         const uint32_t wend = cap * (uint32_t)kListBlock;
         uint32_t w = 0;  // word offset of this lane's next entry
         stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
-#pragma unroll 4
+#pragma unroll kWalkUnroll
             for (uint32_t j = b; j < e; ++j) {
                 const float4 q = __ldg(sx + j);
                 const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
@@ -1294,7 +1326,7 @@ __device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t 
     const float h2 = P.h2;
     float3 delta = make_float3(0.f, 0.f, 0.f);
     uint32_t nb = 0;
-    gather_listed(L, i, cnt, sxl, [&](uint32_t, const float4 &pl, bool valid) {
+    gather_listed<PBD_DELTA_QUADS>(L, i, cnt, sxl, [&](uint32_t, const float4 &pl, bool valid) {
         const float d2 = dist2_exact(pi, f3(pl));
         const bool ok = valid && d2 < h2;  // all of a plain list; a skin list holds more
         delta_add(P, delta, ok, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
@@ -1358,9 +1390,15 @@ __device__ __forceinline__ float3 world_collide(const DevParams &P, float3 e, in
 // solveFluids and collideWorld, which touch disjoint particle sets and read
 // only the sorted start-of-iteration positions, fused into one pass with one
 // write per particle.  mask selects the stages (the stage entry points run
-// them one at a time).
-template <int TPP, bool B>
-__global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint32_t mask, uint32_t iter_left,
+// them one at a time).  NOFLUID leaves the fluid and gas branches out
+// (batches without them), which frees registers for a higher occupancy.
+constexpr int solve_min_blocks(int tpp, bool batch, bool nofluid) {
+    return tpp != 1 ? 0 : nofluid ? PBD_CONTACT_MIN_BLOCKS : batch ? PBD_BATCH_SOLVE_MIN_BLOCKS : PBD_SOLVE_MIN_BLOCKS;
+}
+
+template <int TPP, bool B, bool NOFLUID = false>
+__global__ void __launch_bounds__(kBlock, solve_min_blocks(TPP, B, NOFLUID)) k_solve(DevParams P0, uint32_t n,
+                                                                                  uint32_t mask, uint32_t iter_left,
                                                   const float4 *__restrict__ sx,
                                                   const SortedAttr *__restrict__ sattr,
                                                   const uint32_t *__restrict__ sidx,
@@ -1379,12 +1417,14 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevParams P0, uint32_t n, uint
     const float4 pi4 = sx[i];
     float3 np = f3(pi4);
     bool touched = false;
-    if ((mask & kDoFluid) && a.phase == kFluid) {
-        if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, cell_first, L);
-        else np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
+    if (!NOFLUID && (mask & kDoFluid) && a.phase == kFluid) {
+        if constexpr (!NOFLUID) {
+            if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, cell_first, L);
+            else np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
+        }
         touched = true;
-    } else if ((mask & kDoFluid) && a.phase == kGas) {
-        np = np + gas_delta<TPP>(P, G, i, np, a.rho0, sx, sattr, cell_first, gas);
+    } else if (!NOFLUID && (mask & kDoFluid) && a.phase == kGas) {
+        if constexpr (!NOFLUID) np = np + gas_delta<TPP>(P, G, i, np, a.rho0, sx, sattr, cell_first, gas);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
         np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old, rs);
@@ -1669,11 +1709,13 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
         const float wgt = P.poly6 * hm2 * hm2 * hm2 * ((xj4.w > 0.f) ? 1.f / xj4.w : 0.f);
         acc += (f3(vs[j]) - vi) * wgt;
     };
-    const uint32_t cnt = (TPP == 1 && use_list) ? L.count[i] : 0u;
-    if (TPP == 1 && use_list && list_usable(P, L, cnt)) {
+    bool listed = false;
+    if constexpr (TPP == 1) {
+        const uint32_t cnt = use_list ? L.count[i] : 0u;
+        listed = use_list && list_usable(P, L, cnt);
         // the last lambda pass listed every neighbour of any phase; a
         // neighbour's fluid mass rides in vs.w (0 for the other phases)
-        for (uint32_t q = 0; 4u * q < cnt; ++q) {
+        for (uint32_t q = 0; listed && 4u * q < cnt; ++q) {
             const uint4 e = L.slot[q * L.stride + i];
             const uint32_t left = cnt - 4u * q;
             const uint32_t jj[4] = {e.x, left > 1u ? e.y : i, left > 2u ? e.z : i, left > 3u ? e.w : i};
@@ -1692,7 +1734,8 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
                 acc += (f3(vv[t]) - vi) * wgt;
             }
         }
-    } else {
+    }
+    if (!listed) {
         group_walk<TPP>(
             P, G, xi, grid_pos(P, xi), P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
             [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2 && sattr[j].phase == kFluid; },
@@ -1928,6 +1971,17 @@ cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t
                          uint32_t tpp, cudaStream_t s, const GasBuffers &gas, const RigidSdf &sdf) {
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
+    if (tpp == 1 && !(mask & kDoFluid)) {
+        if (P.table)
+            k_solve<1, true, true><<<blocks_for(n), kBlock, 0, s>>>(P, n, mask, iter_left, g.sorted_x, g.sorted_attr,
+                                                                     g.sorted_idx, g.cell_first, sxl, x_old, x, L,
+                                                                     use_list, gas, sdf);
+        else
+            k_solve<1, false, true><<<blocks_for(n), kBlock, 0, s>>>(P, n, mask, iter_left, g.sorted_x,
+                                                                      g.sorted_attr, g.sorted_idx, g.cell_first, sxl,
+                                                                      x_old, x, L, use_list, gas, sdf);
+        return cudaGetLastError();
+    }
     if (P.table) {
         PBD_TPP_DISPATCH(tpp, true, k_solve, P, n, mask, iter_left, g.sorted_x, g.sorted_attr, g.sorted_idx,
                          g.cell_first, sxl, x_old, x, L, use_list, gas, sdf);
