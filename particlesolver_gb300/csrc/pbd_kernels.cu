@@ -34,16 +34,28 @@ constexpr int kBlock = 256;
 #ifndef PBD_CONTACT_MIN_BLOCKS
 #define PBD_CONTACT_MIN_BLOCKS 8
 #endif
+#ifndef PBD_LAMBDA_MIN_BLOCKS
+#define PBD_LAMBDA_MIN_BLOCKS 6
+#endif
 #ifndef PBD_BATCH_SOLVE_MIN_BLOCKS
 #define PBD_BATCH_SOLVE_MIN_BLOCKS PBD_SOLVE_MIN_BLOCKS
 #endif
 constexpr int kWalkUnroll = PBD_WALK_UNROLL;
-// Block of the shared-memory list build, and the largest list capacity it
-// assembles: (capacity + 1) x kListBlock words stay under the 48 KB of
-// dynamic shared memory a launch gets without opting in.
+// Block of the shared-memory list build, and the entries per particle it
+// assembles in shared memory (a particle with more rebuilds its list in
+// global memory): (columns + 1) x kListBlock words.  Fewer columns leave
+// more of the SM's combined L1/shared storage to cache the candidates the
+// walk loads, but a rebuild costs its warp a second walk: 48 columns hold
+// every list of a fluid at rest density with cells of h (at most ~48
+// neighbours); skin lists, longer by (1 + skin)^3, get up to 88.
+#ifndef PBD_SLIST_COLS
+#define PBD_SLIST_COLS 48
+#endif
 constexpr int kListBlock = 128;
-constexpr uint32_t kSharedListMax = 88;
-static_assert((kSharedListMax + 1) * kListBlock * 4 <= 48 * 1024,
+constexpr uint32_t kSharedListCols = PBD_SLIST_COLS;
+constexpr uint32_t kSharedListColsSkin = 88;
+static_assert(kSharedListCols % 4 == 0 && kSharedListCols <= kSharedListColsSkin &&
+                  (kSharedListColsSkin + 1) * kListBlock * 4 <= 48 * 1024,
               "shared-memory list build exceeds the default dynamic shared memory");
 // NbList::assemble: kListShared selects the shared-memory build (any other
 // value, the register quads); both store four entries to a uint4,
@@ -1198,13 +1210,35 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
 // memory four entries to a uint4 (the layout k_lambda_list writes) and lambda
 // is summed from the shared copy.  Same neighbour sets, visiting order and
 // results as k_lambda_list.
+// The list of a particle whose shared-memory column filled up: the same
+// walk again, each entry stored straight to its word of the global list.
+// Returns the count, or capacity + 1 when the list does not fit.
+template <int RAD>
+__device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, float3 pi, int3 g, int rad,
+                                            float reach2, bool trim, const float4 *__restrict__ sx,
+                                            const uint32_t *__restrict__ cell_first, const NbList &L) {
+    uint32_t *const words = reinterpret_cast<uint32_t *>(L.slot);
+    const uint32_t cap = L.capacity;
+    uint32_t k = 0;
+    stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
+        for (uint32_t j = b; j < e; ++j) {
+            if (dist2_exact(pi, f3(__ldg(sx + j))) < reach2 && j != i) {
+                if (k < cap) words[((size_t)(k >> 2) * L.stride + i) * 4u + (k & 3u)] = j;
+                ++k;
+            }
+        }
+        return true;
+    });
+    return k > cap ? cap + 1u : k;
+}
+
 template <int RAD, bool B, bool SKIN>
-__global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
+__global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
                                                                 const float4 *__restrict__ sx,
                                                                 const SortedAttr *__restrict__ sattr,
                                                                 const uint32_t *__restrict__ cell_first,
                                                                 float4 *__restrict__ sxl, NbList L,
-                                                                GasBuffers gas) {
+                                                                GasBuffers gas, uint32_t cols) {
     extern __shared__ uint32_t s_nb[];
     const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
     if (i >= n) return;
@@ -1262,7 +1296,7 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
             }
         }
         uint32_t *const col = s_nb + threadIdx.x;
-        const uint32_t wend = cap * (uint32_t)kListBlock;
+        const uint32_t wend = cols * (uint32_t)kListBlock;
         uint32_t w = 0;  // word offset of this lane's next entry
         stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
 #pragma unroll kWalkUnroll
@@ -1274,9 +1308,17 @@ __global__ void __launch_bounds__(kListBlock, 6) k_lambda_slist(DevParams P0, ui
             }
             return true;
         });
-        const uint32_t cnt = (w == wend) ? cap + 1u : w / (uint32_t)kListBlock;
+        const bool spilled = w == wend && cols < cap;
+        const uint32_t cnt = spilled  ? spill_list<RAD>(P, i, pi, g, rad, reach2, trim, sx, cell_first, L)
+                             : (w == wend) ? cap + 1u
+                                           : w / (uint32_t)kListBlock;
         L.count[i] = cnt;
-        if (list_usable(P, L, cnt)) {
+        if (spilled && list_usable(P, L, cnt)) {
+            gather_listed(L, i, cnt, sx, [&](uint32_t j, const float4 &pj, bool valid) {
+                const float d2 = dist2_exact(pi, f3(pj));
+                add(j, pj, d2, valid && (!SKIN || d2 < h2));
+            });
+        } else if (list_usable(P, L, cnt)) {
             uint4 *const dst = L.slot + i;
             for (uint32_t q = 0; 4u * q < cnt; ++q) {
                 const uint32_t k = 4u * q * (uint32_t)kListBlock;
@@ -1920,13 +1962,14 @@ void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, co
         // the host enables a skin only where its stencil does not alias)
         rad = P.table ? 0 : (int)std::ceil(P.h * (1.f + L.skin) / P.cell * 1.000001f);
     }
-    const bool shared = L.assemble == kListShared && L.capacity <= kSharedListMax;
+    const bool shared = L.assemble == kListShared;
     const unsigned nbs = blocks_for(n, kListBlock);
-    const size_t smem = (size_t)(L.capacity + 1u) * kListBlock * sizeof(uint32_t);
+    const uint32_t cols = std::min(L.capacity, L.sref ? kSharedListColsSkin : kSharedListCols);
+    const size_t smem = (size_t)(cols + 1u) * kListBlock * sizeof(uint32_t);
 #define PBD_LIST(R, S)                                                                                      \
     if (shared)                                                                                             \
         k_lambda_slist<R, B, S><<<nbs, kListBlock, smem, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr,   \
-                                                              g.cell_first, sxl, L, gas);                   \
+                                                              g.cell_first, sxl, L, gas, cols);             \
     else                                                                                                    \
         k_lambda_list<R, B, S><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, \
                                                      sxl, L, gas)

@@ -532,16 +532,21 @@ def test_neighbor_list_capacity_and_fallback(capacity):
     assert norm_err(g.velocities()[:, :3], o.velocities()[:, :3]) < TOL_STAGE
 
 
-@pytest.mark.parametrize("capacity,skin", [(64, 0.0), (24, 0.0), (88, 0.0), (92, 0.0), (80, 0.2)])
-def test_list_assembly_shared_equals_registers(capacity, skin):
+@pytest.mark.parametrize("capacity,skin,squeeze", [(64, 0.0, 1.0), (24, 0.0, 1.0), (48, 0.0, 1.0), (92, 0.0, 1.0),
+                                                   (92, 0.0, 0.8), (44, 0.0, 0.8), (80, 0.2, 1.0), (128, 0.5, 1.0)])
+def test_list_assembly_shared_equals_registers(capacity, skin, squeeze):
     """The lambda pass assembles a particle's neighbour list in shared
     memory (list_assembly 0) or in registers (1): the same neighbours in
     the same order with the same arithmetic, so updates agree bit for bit,
-    also when particles overflow the list (24), at the largest shared
-    capacity (88), above it (92: both use registers) and with a skin
-    list."""
+    also when particles overflow the list (24), when the shared columns
+    (48 entries) are the whole list (48), and when particles with more
+    neighbours than the columns hold rebuild their lists in global memory:
+    a fluid squeezed to 0.8 of its lattice spacing (~70 neighbours; with a
+    list of 92, and of 44 where they overflow) and a skin list of 1.5 h
+    (~110 entries against 88 skin columns)."""
     mode = 0
     sc = W.dam_break(24, 20, 12)
+    sc.pos_w[:, :3] *= squeeze
     sc.params["grid_size"] = [64, 16, 16]
     a = ParticleSystem(default_params(**sc.params), sc.n)
     b = ParticleSystem(default_params(**sc.params), sc.n)
