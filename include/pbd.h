@@ -413,7 +413,7 @@ typedef struct pbd_tuning {
     uint32_t neighbor_list_capacity; /* with threads_per_particle == 1: fluid
                                       neighbours recorded per particle and
                                       iteration (multiple of 4, 0 = no list,
-                                      default 64); particles with more fall
+                                      default 128); particles with more fall
                                       back to the stencil walk              */
     float neighbor_skin;           /* with a list: its radius is (1 + skin) h
                                       and it is reused by the later
@@ -429,9 +429,10 @@ typedef struct pbd_tuning {
     uint32_t list_assembly;        /* with a list: where the lambda pass
                                       collects a particle's neighbours before
                                       storing them: 0 = shared memory, one
-                                      column per thread (default; capacities
-                                      up to 88, larger ones use registers),
-                                      1 = registers                         */
+                                      column of 48 entries per thread (88
+                                      with a skin; a longer list continues
+                                      in global memory; default), 1 =
+                                      registers                             */
     uint32_t reserved[4];          /* zero                                  */
 } pbd_tuning;
 

@@ -1210,17 +1210,31 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
 // memory four entries to a uint4 (the layout k_lambda_list writes) and lambda
 // is summed from the shared copy.  Same neighbour sets, visiting order and
 // results as k_lambda_list.
-// The list of a particle whose shared-memory column filled up: the same
-// walk again, each entry stored straight to its word of the global list.
+// The list of a particle whose shared-memory column filled up: the column's
+// entries go out as quads, then the walk resumes after the column's last
+// entry (in range `rfull` of the walk, the range in which the column
+// filled) and stores the rest straight to their words of the global list.
 // Returns the count, or capacity + 1 when the list does not fit.
 template <int RAD>
 __device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, float3 pi, int3 g, int rad,
-                                            float reach2, bool trim, const float4 *__restrict__ sx,
-                                            const uint32_t *__restrict__ cell_first, const NbList &L) {
+                                               float reach2, bool trim, const float4 *__restrict__ sx,
+                                               const uint32_t *__restrict__ cell_first, const NbList &L,
+                                               const uint32_t *col, uint32_t cols, uint32_t rfull) {
+    uint4 *const dst = L.slot + i;
+    for (uint32_t q = 0; 4u * q < cols; ++q) {
+        const uint32_t k = 4u * q * (uint32_t)kListBlock;
+        dst[q * L.stride] = make_uint4(col[k], col[k + kListBlock], col[k + 2 * kListBlock], col[k + 3 * kListBlock]);
+    }
+    const uint32_t jlast = col[(cols - 1u) * (uint32_t)kListBlock];
     uint32_t *const words = reinterpret_cast<uint32_t *>(L.slot);
     const uint32_t cap = L.capacity;
-    uint32_t k = 0;
+    uint32_t k = cols, r = 0;
     stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
+        if (r < rfull) {
+            ++r;
+            return true;
+        }
+        if (r++ == rfull) b = jlast + 1u;
         for (uint32_t j = b; j < e; ++j) {
             if (dist2_exact(pi, f3(__ldg(sx + j))) < reach2 && j != i) {
                 if (k < cap) words[((size_t)(k >> 2) * L.stride + i) * 4u + (k & 3u)] = j;
@@ -1297,7 +1311,8 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
         }
         uint32_t *const col = s_nb + threadIdx.x;
         const uint32_t wend = cols * (uint32_t)kListBlock;
-        uint32_t w = 0;  // word offset of this lane's next entry
+        uint32_t w = 0;      // word offset of this lane's next entry
+        uint32_t rfull = 0;  // ranges walked before the one that filled the column
         stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
 #pragma unroll kWalkUnroll
             for (uint32_t j = b; j < e; ++j) {
@@ -1306,10 +1321,12 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
                 if (ok) col[w] = j;
                 w = ok ? min(w + (uint32_t)kListBlock, wend) : w;
             }
+            rfull += w < wend ? 1u : 0u;
             return true;
         });
         const bool spilled = w == wend && cols < cap;
-        const uint32_t cnt = spilled  ? spill_list<RAD>(P, i, pi, g, rad, reach2, trim, sx, cell_first, L)
+        const uint32_t cnt = spilled ? spill_list<RAD>(P, i, pi, g, rad, reach2, trim, sx, cell_first, L, col, cols,
+                                                       rfull)
                              : (w == wend) ? cap + 1u
                                            : w / (uint32_t)kListBlock;
         L.count[i] = cnt;

@@ -1483,7 +1483,7 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     // with the list volume), and the lane groups
     pbd_tuning base{};
     pbd_get_tuning(s, &base);
-    const uint32_t cap0 = base.neighbor_list_capacity ? base.neighbor_list_capacity : 64u;
+    const uint32_t cap0 = base.neighbor_list_capacity ? base.neighbor_list_capacity : 128u;
     std::vector<pbd_tuning> cands;
     auto cand = [&](uint32_t tpp, float skin) {
         pbd_tuning t{};

@@ -82,7 +82,7 @@ struct pbd_system {
 
     uint32_t tpp = 1;     // lanes per particle in the neighbour passes
     pbd::NbList nbl{};    // per-iteration fluid neighbour lists
-    uint32_t list_capacity = 64;
+    uint32_t list_capacity = 128;
     float skin = 0.f;               // skin-list radius (1 + skin) h; 0 = off
     float4 *sref = nullptr;         // [cap] sorted positions at the list build
     uint32_t *skin_words = nullptr; // [pbd::kSkinWords] device decision words
