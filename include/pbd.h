@@ -187,6 +187,16 @@ uint32_t pbd_num_scenes(const pbd_system *sys);
 /* first / count / params may be NULL. */
 int pbd_get_scene(const pbd_system *sys, uint32_t scene, uint32_t *first, uint32_t *count, pbd_params *params);
 int pbd_set_scene_params(pbd_system *sys, uint32_t scene, const pbd_params *params);
+/* A batch in one call: n_scenes scenes, scene k with params[k] and the next
+ * counts[k] particles of pos_w (4 floats each), vel (4 floats each, or
+ * NULL), phase (or NULL: fluid) and rest_density (or NULL: 1.0), in scene
+ * order -- pbd_create, then pbd_begin_scene and pbd_add_particles per
+ * scene.  max_particles: capacity (0 = the sum of counts).  Constraints and
+ * bodies are added afterwards by particle index (pbd_get_scene gives each
+ * scene's first index).  On failure *out is NULL. */
+int pbd_batch_create(uint32_t n_scenes, const pbd_params *params, const uint32_t *counts, const float *pos_w,
+                     const float *vel, const int32_t *phase, const float *rest_density, uint32_t max_particles,
+                     pbd_system **out);
 
 /* --------------------------------------------------------- scene content */
 

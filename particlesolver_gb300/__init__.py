@@ -185,6 +185,7 @@ _SIGNATURES = {
     "pbd_set_params": ([_P, ctypes.POINTER(PbdParams)], _I),
     "pbd_get_params": ([_P, ctypes.POINTER(PbdParams)], _I),
     "pbd_begin_scene": ([_P, ctypes.POINTER(PbdParams), _PU], _I),
+    "pbd_batch_create": ([_U32, ctypes.POINTER(PbdParams), _PU, _PF, _PF, _PI, _PF, _U32, ctypes.POINTER(_P)], _I),
     "pbd_num_scenes": ([_P], _U32),
     "pbd_get_scene": ([_P, _U32, _PU, _PU, ctypes.POINTER(PbdParams)], _I),
     "pbd_set_scene_params": ([_P, _U32, ctypes.POINTER(PbdParams)], _I),
@@ -316,6 +317,31 @@ class ParticleSystem:
                            grid_size=grid_size, box_min=[float(v) for v in min_bounds],
                            box_max=[float(v) for v in max_bounds], iterations=iterations)
         return cls(p, max_particles)
+
+    @classmethod
+    def batch(cls, params, counts, pos_w, vel=None, phase=None, rest_density=None,
+              max_particles: int = 0) -> "ParticleSystem":
+        """pbd_batch_create: scene k takes params[k] and the next counts[k]
+        particles of the arrays (pos_w (N, 4); vel (N, 4), phase (N,) and
+        rest_density (N,) optional)."""
+        self = cls.__new__(cls)
+        self.lib = load_library()
+        S = len(params)
+        self.params = params[0] if S else None
+        par = (PbdParams * max(S, 1))(*params)
+        cnt = np.ascontiguousarray(counts, dtype=np.uint32)
+        pos = np.ascontiguousarray(pos_w, dtype=np.float32).reshape(-1, 4)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 4)
+        ph = None if phase is None else np.ascontiguousarray(phase, dtype=np.int32)
+        ro = None if rest_density is None else np.ascontiguousarray(rest_density, dtype=np.float32)
+        h = ctypes.c_void_p()
+        rc = self.lib.pbd_batch_create(S, par, cnt.ctypes.data_as(_PU), _fptr(pos), _fptr(v),
+                                       None if ph is None else ph.ctypes.data_as(_PI), _fptr(ro),
+                                       int(max_particles), ctypes.byref(h))
+        if rc:
+            raise PbdError(rc, self.lib.pbd_last_error(None).decode())
+        self.h = h
+        return self
 
     # -- lifetime -------------------------------------------------------
     def close(self):

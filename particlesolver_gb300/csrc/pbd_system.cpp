@@ -806,6 +806,42 @@ int pbd_begin_scene(pbd_system *s, const pbd_params *params, uint32_t *scene_ind
 
 uint32_t pbd_num_scenes(const pbd_system *s) { return s ? (uint32_t)s->scenes.size() : 0u; }
 
+int pbd_batch_create(uint32_t n_scenes, const pbd_params *params, const uint32_t *counts, const float *pos_w,
+                     const float *vel, const int32_t *phase, const float *rest_density, uint32_t max_particles,
+                     pbd_system **out) {
+    if (!out) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (n_scenes == 0 || n_scenes > PBD_MAX_SCENES || !params || !counts)
+        return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "n_scenes must be in [1, %u] with params and counts",
+                    (unsigned)PBD_MAX_SCENES);
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < n_scenes; ++k) total += counts[k];
+    if (total && !pos_w) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "pos_w is NULL");
+    if (total > 0xffffffffull || (max_particles && max_particles < total))
+        return fail(nullptr, PBD_ERR_CAPACITY, "the scenes hold %llu particles, capacity %u",
+                    (unsigned long long)total, max_particles);
+    pbd_system *s = nullptr;
+    if (int rc = pbd_create(&params[0], max_particles ? max_particles : (uint32_t)total, &s)) return rc;
+    uint64_t off = 0;
+    std::vector<int32_t> fluid;
+    for (uint32_t k = 0; k < n_scenes; ++k) {
+        int rc = k ? pbd_begin_scene(s, &params[k], nullptr) : PBD_OK;
+        if (!phase && fluid.size() < counts[k]) fluid.assign(counts[k], PBD_PHASE_FLUID);
+        if (!rc && counts[k])
+            rc = pbd_add_particles(s, counts[k], pos_w + 4 * off, vel ? vel + 4 * off : nullptr,
+                                   phase ? phase + off : fluid.data(), rest_density ? rest_density + off : nullptr,
+                                   nullptr);
+        if (rc) {
+            pbd_internal_set_thread_error(s->err);
+            pbd_destroy(s);
+            return rc;
+        }
+        off += counts[k];
+    }
+    *out = s;
+    return PBD_OK;
+}
+
 int pbd_get_scene(const pbd_system *s, uint32_t scene, uint32_t *first, uint32_t *count, pbd_params *params) {
     if (!s) return fail(nullptr, PBD_ERR_INVALID_ARGUMENT, "system handle is NULL");
     if (scene >= s->scenes.size()) return PBD_ERR_INVALID_ARGUMENT;

@@ -1,6 +1,6 @@
 """The entry points named by the hot-path contract (pbd_tick,
-pbd_batch_tick, pbd_add_fluid_group, pbd_add_rigid_group, pbd_set_box,
-pbd_record) give exactly what the calls they stand for give."""
+pbd_batch_create, pbd_batch_tick, pbd_add_fluid_group, pbd_add_rigid_group,
+pbd_set_box, pbd_record) give exactly what the calls they stand for give."""
 import ctypes
 
 import numpy as np
@@ -36,6 +36,42 @@ def test_batch_tick_is_update_graph():
     a.update_graph(1.0 / 60.0, 3)
     assert b.lib.pbd_batch_tick(b.h, ctypes.c_float(1.0 / 60.0), 3, None) == 0
     np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_batch_create_is_begin_scene_and_add():
+    """One pbd_batch_create call equals pbd_create + pbd_begin_scene +
+    pbd_add_particles per scene: same scenes, same slots, same steps."""
+    scenes = [W.pbf_block(800, seed=2), W.granular_column(300, seed=3), W.pbf_block(500, seed=4, iterations=3)]
+    from test_gpu_batch import load_batch
+
+    a, firsts = load_batch(scenes)
+    pos = np.concatenate([sc.pos_w for sc in scenes])
+    vel = np.concatenate([sc.vel if sc.vel is not None else np.zeros((sc.n, 4), np.float32) for sc in scenes])
+    phase = np.concatenate([sc.phase for sc in scenes])
+    rho = np.concatenate([sc.rest_density if sc.rest_density is not None else np.ones(sc.n, np.float32)
+                          for sc in scenes])
+    b = ParticleSystem.batch([default_params(**sc.params) for sc in scenes], [sc.n for sc in scenes], pos, vel,
+                             phase, rho)
+    assert b.num_scenes == len(scenes)
+    for k in range(len(scenes)):
+        assert b.scene(k)[:2] == a.scene(k)[:2] == (firsts[k], scenes[k].n)
+    a.update_graph(1.0 / 60.0, 4)
+    b.update_graph(1.0 / 60.0, 4)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+
+
+def test_batch_create_rejects_bad_input():
+    sc = W.pbf_block(100, seed=1)
+    p = default_params(**sc.params)
+    with pytest.raises(PbdError):
+        ParticleSystem.batch([p], [sc.n], sc.pos_w, max_particles=sc.n - 1)
+    with pytest.raises(PbdError):
+        ParticleSystem.batch([], [], sc.pos_w)
+    bad = default_params(**sc.params)
+    bad.kernel_radius = -1.0
+    with pytest.raises(PbdError):
+        ParticleSystem.batch([p, bad], [50, 50], sc.pos_w)
 
 
 def test_add_fluid_group_equals_fluid_particles():
