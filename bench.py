@@ -482,6 +482,7 @@ def run_ours(args, world, rank, local_rank):
         sysm.autotune(sc.dt, 2, sh)
     tpp = sysm.threads_per_particle
     tuning = sysm.tuning()
+    held = sysm.get_params()  # cell size and grid after the autotuner
     sysm.update_graph(sc.dt, 1, sh)
     torch.cuda.synchronize()
     # the end-to-end run below restarts from this state, so that both
@@ -599,7 +600,8 @@ def run_ours(args, world, rank, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, splitmix64)",
         "config": {"workload": f"pbf_dam_break_{n}", "particles": n, "lattice": [args.nx, args.ny, args.nz],
                    "h": 0.1, "iterations": 4, "grid_rebuild": "every iteration", "xsph_c": 0.01,
-                   "cell_size": sc.params["cell_size"], "grid": sc.params["grid_size"],
+                   "cell_size": round(float(held.cell_size), 6), "grid": list(held.grid_size),
+                   "cell_source": "autotuned" if not args.tpp else "given",
                    "threads_per_particle": tpp, "tpp_source": "fixed" if args.tpp else "autotuned",
                    "neighbor_skin": float(tuning.neighbor_skin),
                    "neighbor_list_capacity": int(tuning.neighbor_list_capacity),

@@ -451,10 +451,14 @@ int pbd_get_tuning(const pbd_system *sys, pbd_tuning *out);
 /* Iterations of the last step that reused a skin list (0 without one).
  * Synchronous. */
 int pbd_list_reuses(pbd_system *sys, uint32_t *count);
-/* Times `steps` updates of the current scene for every threads_per_particle
- * choice, starting each trial from a device snapshot of the state, then
- * restores the state and keeps the fastest choice (written to *chosen if
- * not NULL).  Synchronous. */
+/* Times `steps` updates for each candidate schedule, starting each trial
+ * from a device snapshot of the state, then restores the state and keeps
+ * the fastest (written to *chosen if not NULL).  Candidates: one lane per
+ * particle with lists rebuilt every iteration or kept with a skin of 0.1,
+ * 0.2 or 0.3 h, the register list build, 2-32 lanes per particle and, in a
+ * system with fluid or gas and no contacts, cells of half the size (every
+ * scene's cell_size halved and grid_size doubled; kept only if 3 % faster,
+ * and then visible in pbd_get_params / pbd_get_scene).  Synchronous. */
 int pbd_autotune(pbd_system *sys, float dt, uint32_t steps, void *stream, pbd_tuning *chosen);
 
 /* --------------------------------------------------------------- timing */

@@ -439,6 +439,13 @@ class ParticleSystem:
         self._check(self.lib.pbd_set_params(self.h, ctypes.byref(params)))
         self.params = params
 
+    def get_params(self) -> PbdParams:
+        """Scene 0's parameters as the system holds them (the autotuner may
+        have changed cell_size and grid_size)."""
+        p = PbdParams()
+        self._check(self.lib.pbd_get_params(self.h, ctypes.byref(p)))
+        return p
+
     # -- scenes ---------------------------------------------------------
     def begin_scene(self, params: PbdParams) -> int:
         """Open the next independent scene; later add_* calls fill it."""

@@ -1516,18 +1516,23 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     };
     // candidates: one lane per particle with neighbour lists rebuilt every
     // iteration or kept with a skin of 0.1, 0.2, 0.3 h (list capacity grown
-    // with the list volume), and the lane groups
+    // with the list volume), the register list build, the lane groups and,
+    // in a system without contacts, cells of half the size (the contact
+    // walk's one-cell reach needs the cell of at least the contact
+    // distance)
     pbd_tuning base{};
     pbd_get_tuning(s, &base);
     const uint32_t cap0 = base.neighbor_list_capacity ? base.neighbor_list_capacity : 128u;
     std::vector<pbd_tuning> cands;
-    auto cand = [&](uint32_t tpp, float skin) {
+    std::vector<uint32_t> divs;  // cell divisor of each candidate
+    auto cand = [&](uint32_t tpp, float skin, uint32_t div = 1u) {
         pbd_tuning t{};
         t.threads_per_particle = tpp;
         t.neighbor_skin = skin;
         const double grow = std::pow(1.0 + (double)skin, 3.0);
         t.neighbor_list_capacity = std::min<uint32_t>(1024u, 4u * (uint32_t)std::ceil(cap0 * grow / 4.0));
         cands.push_back(t);
+        divs.push_back(div);
     };
     cand(1, 0.f);
     if (s->n_fluid && base.neighbor_list_capacity)
@@ -1538,17 +1543,47 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     if (s->n_fluid && s->dev.iterations > 1 && base.neighbor_list_capacity)
         for (float f : {0.1f, 0.2f, 0.3f}) cand(1, f);
     for (uint32_t k : {2u, 4u, 8u, 16u, 32u}) cand(k, 0.f);
+    // the scenes' grids as given, and whether halving every cell stays
+    // within 2^27 cells
+    std::vector<pbd_params> given;
+    for (const pbd_scene &sc : s->scenes) given.push_back(sc.params);
+    uint64_t half_cells = 0;
+    for (const pbd_params &p : given)
+        half_cells += (uint64_t)p.grid_size[0] * (p.grid_size[0] > 1u ? 2u : 1u) * p.grid_size[1] *
+                      (p.grid_size[1] > 1u ? 2u : 1u) * p.grid_size[2] * (p.grid_size[2] > 1u ? 2u : 1u);
+    if (s->any_pbf() && !s->n_contact && half_cells <= (1ull << 27)) cand(1, 0.f, 2u);
+    uint32_t cur_div = 1u;
+    // sets every scene's cells to the given size / div; on a refusal (a
+    // parameter limit) puts the given grids back and returns the error
+    auto set_div = [&](uint32_t div) -> int {
+        if (div == cur_div) return PBD_OK;
+        for (uint32_t k = 0; k < (uint32_t)given.size(); ++k) {
+            pbd_params p = given[k];
+            p.cell_size = given[k].cell_size / (float)div;
+            for (int a = 0; a < 3; ++a)
+                if (p.grid_size[a] > 1u) p.grid_size[a] *= div;
+            if (int rc = pbd_set_scene_params(s, k, &p)) {
+                for (uint32_t j = 0; j < k; ++j) pbd_set_scene_params(s, j, &given[j]);
+                cur_div = 1u;
+                return rc;
+            }
+        }
+        cur_div = div;
+        return PBD_OK;
+    };
     cudaEvent_t a = nullptr, b = nullptr;
     int rc = PBD_OK;
     const bool saved_prof = s->profiling;
     s->profiling = false;
     pbd_tuning best = base;
+    uint32_t best_div = 1u;
     float best_ms = 0.f;
     bool have = false;
     if (copy(true) != cudaSuccess || cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
         rc = fail(s, PBD_ERR_CUDA, "autotune: setup failed");
     }
     for (size_t k = 0; rc == PBD_OK && k < cands.size(); ++k) {
+        if (set_div(divs[k]) != PBD_OK) continue;  // a grid the parameters do not allow
         if ((rc = pbd_set_tuning(s, &cands[k])) != PBD_OK) break;
         if (copy(false) != cudaSuccess || (rc = enqueue_update(s, dt, st)) != PBD_OK) break;  // untimed warm-up
         if (copy(false) != cudaSuccess) break;
@@ -1560,9 +1595,12 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
             if (!rc) rc = fail(s, PBD_ERR_CUDA, "autotune: timing failed");
             break;
         }
-        if (!have || ms < best_ms) {
+        // a change of grid has to win by 3 % (it changes the user's grid)
+        const float bar = divs[k] != 1u ? 0.97f : 1.f;
+        if (!have || ms < best_ms * bar) {
             best_ms = ms;
             best = cands[k];
+            best_div = divs[k];
             have = true;
         }
     }
@@ -1572,8 +1610,9 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     if (b) cudaEventDestroy(b);
     release();
     s->profiling = saved_prof;
+    const int rc3 = set_div(rc ? 1u : best_div);
     const int rc2 = pbd_set_tuning(s, rc ? &base : &best);
-    if (!rc) rc = rc2;
+    if (!rc) rc = rc3 ? rc3 : rc2;
     s->grid_valid = false;
     ++s->version;
     if (chosen) pbd_get_tuning(s, chosen);

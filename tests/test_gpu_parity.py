@@ -508,6 +508,28 @@ def test_autotune_restores_state():
     np.testing.assert_array_equal(a.velocities(), b.velocities())
 
 
+def test_autotune_cell_size():
+    """A fluid system may come out of the autotuner with cells of half the
+    size (grid doubled per axis); its step still matches the oracle on the
+    given grid (neighbour sets do not depend on the cell).  A system with
+    contacts keeps its cells."""
+    sc = W.dam_break(16, 16, 8)
+    g, o = make_pair(sc)
+    g.autotune(sc.dt, 2)
+    p = g.get_params()
+    assert p.cell_size in (np.float32(sc.params["cell_size"]), np.float32(sc.params["cell_size"] / 2))
+    div = round(sc.params["cell_size"] / p.cell_size)
+    assert list(p.grid_size) == [v * div for v in sc.params["grid_size"]]
+    g.update(sc.dt)
+    o.update(sc.dt)
+    assert_projection(g.positions(), o.positions(), sc.pos_w, TOL_STAGE)
+    gc = W.granular_column(200, seed=3)
+    c = ParticleSystem(default_params(**gc.params), gc.n)
+    W.apply_to(gc, c)
+    c.autotune(gc.dt, 2)
+    assert c.get_params().cell_size == np.float32(gc.params["cell_size"])
+
+
 @pytest.mark.parametrize("capacity", [0, 4, 16, 64])
 def test_neighbor_list_capacity_and_fallback(capacity):
     """Small list capacities force the exact stencil-walk fallback for some
