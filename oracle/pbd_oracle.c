@@ -118,7 +118,10 @@ static inline int floor_to_int(float v) {
 static inline void grid_cell(const orc_system *s, const float *p, int g[3]) {
     g[0] = floor_to_int((p[0] - s->p.world_origin[0]) / s->p.cell_size);
     g[1] = floor_to_int((p[1] - s->p.world_origin[1]) / s->p.cell_size);
-    g[2] = floor_to_int((p[2] - s->p.world_origin[2]) / s->p.cell_size);
+    /* 2-D mode (the TWOD build, integration_kernel.cuh:111-129, pins every
+     * particle to twod_z): all particles share twod_z's layer */
+    const float z = (s->p.flags & PBD_FLAG_TWOD) ? s->p.twod_z : p[2];
+    g[2] = floor_to_int((z - s->p.world_origin[2]) / s->p.cell_size);
 }
 
 static inline uint32_t grid_hash(const orc_system *s, const int g[3]) {
@@ -135,7 +138,9 @@ typedef int (*visit_fn)(void *ctx, uint32_t j);
 
 static void for_each_candidate(const orc_system *s, const int g[3], int rad, visit_fn f, void *ctx) {
     const uint32_t gx = s->p.grid_size[0], gy = s->p.grid_size[1], gz = s->p.grid_size[2];
-    for (int dz = -rad; dz <= rad; ++dz)
+    /* in 2-D mode the particles' layer is the only one holding particles */
+    const int zr = (s->p.flags & PBD_FLAG_TWOD) ? 0 : rad;
+    for (int dz = -zr; dz <= zr; ++dz)
         for (int dy = -rad; dy <= rad; ++dy)
             for (int dx = -rad; dx <= rad; ++dx) {
                 uint32_t x = (uint32_t)(g[0] + dx) & (gx - 1u);

@@ -65,6 +65,8 @@ struct DevParams {
     bool trim_fluid, trim_contact;
     uint32_t max_nb;
     float twod_z;
+    int twod_cz;         // z cell of twod_z: in 2-D mode every particle's
+                         // grid z (the particles sit in one layer)
     uint32_t flags;
     float solid_w;       // density weight of neighbours of phase >= CLOTH
     float rands[6];      // wall jitter uniforms
@@ -114,8 +116,13 @@ __device__ __forceinline__ int3 grid_pos(const DevParams &P, float3 p) {
     int3 g;
     g.x = __float2int_rd(__fdiv_rn(__fsub_rn(p.x, P.origin.x), P.cell));
     g.y = __float2int_rd(__fdiv_rn(__fsub_rn(p.y, P.origin.y), P.cell));
-    g.z = __float2int_rd(__fdiv_rn(__fsub_rn(p.z, P.origin.z), P.cell));
+    g.z = (P.flags & kFlagTwoD) ? P.twod_cz : __float2int_rd(__fdiv_rn(__fsub_rn(p.z, P.origin.z), P.cell));
     return g;
+}
+
+// The z offsets a stencil covers: in 2-D mode only the particles' own layer.
+__device__ __forceinline__ int stencil_zrad(const DevParams &P, int rad) {
+    return (P.flags & kFlagTwoD) ? 0 : rad;
 }
 
 // calcGridHash (integration_kernel.cuh:197-203): wrap each coordinate into
@@ -138,7 +145,8 @@ __device__ __forceinline__ uint32_t grid_hash(const DevParams &P, int3 g) {
 template <class F>
 __device__ __forceinline__ void for_each_candidate(const DevParams &P, int3 g, int rad,
                                                    const uint32_t *__restrict__ cell_first, F &&f) {
-    for (int dz = -rad; dz <= rad; ++dz) {
+    const int zr = stencil_zrad(P, rad);
+    for (int dz = -zr; dz <= zr; ++dz) {
         const uint32_t z = (uint32_t)(g.z + dz) & (P.gz - 1u);
         for (int dy = -rad; dy <= rad; ++dy) {
             const uint32_t y = (uint32_t)(g.y + dy) & (P.gy - 1u);

@@ -406,9 +406,10 @@ __device__ __forceinline__ void stencil_ranges(const DevParams &P, float3 q, int
                                                bool trim, const uint32_t *__restrict__ cell_first, F &&f) {
     const float lim = reach2 * 1.0001f + 1e-30f;
     const float inv_cell = 1.f / P.cell;
-    for (int dz = -rad; dz <= rad; ++dz) {
+    const int zr = stencil_zrad(P, rad);
+    for (int dz = -zr; dz <= zr; ++dz) {
         float gz2 = 0.f;
-        if (trim) {
+        if (trim && zr == rad) {  // (in 2-D the layer is every particle's, whatever its z)
             const float t = slab_gap(q.z, P.origin.z, P.cell, g.z + dz);
             gz2 = t * t;
             if (gz2 > lim) continue;
@@ -1012,9 +1013,10 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
         const float t = trim ? slab_gap(q.y, P.origin.y, P.cell, g.y + k - RAD) : 0.f;
         gy2[k] = t * t;
     }
+    const bool flat = (P.flags & kFlagTwoD) != 0u;  // 2-D: the particles' own z layer only
 #pragma unroll 1
-    for (int kz = 0; kz < W; ++kz) {
-        const float tz = trim ? slab_gap(q.z, P.origin.z, P.cell, g.z + kz - RAD) : 0.f;
+    for (int kz = flat ? RAD : 0; kz < (flat ? RAD + 1 : W); ++kz) {
+        const float tz = trim && !flat ? slab_gap(q.z, P.origin.z, P.cell, g.z + kz - RAD) : 0.f;
         const float gz2 = tz * tz;
         if (gz2 > lim) continue;
         const uint32_t zrow = ((uint32_t)(g.z + kz - RAD) & (P.gz - 1u)) * P.gy;

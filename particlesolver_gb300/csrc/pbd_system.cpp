@@ -105,11 +105,21 @@ pbd::DevParams make_dev(const pbd_params &p, const float rands[6]) {
     d.collide_dist = p.particle_radius * pbd::kCollideScale;
     d.collide2 = d.collide_dist * d.collide_dist;
     d.fluid_rad = (int)std::ceil(p.kernel_radius / p.cell_size);
-    const uint32_t gmin = std::min(d.gx, std::min(d.gy, d.gz));
+    // stencils do not alias when every walked axis has room for them (in
+    // 2-D the z layer is one, whatever gz)
+    const bool twod = (p.flags & PBD_FLAG_TWOD) != 0u;
+    const uint32_t gmin = twod ? std::min(d.gx, d.gy) : std::min(d.gx, std::min(d.gy, d.gz));
     d.trim_fluid = (uint32_t)(2 * d.fluid_rad + 1) <= gmin;
     d.trim_contact = 3u <= gmin;
     d.max_nb = p.max_neighbors;
     d.twod_z = p.twod_z;
+    {
+        // the device's grid_pos expression on the host: IEEE subtract and
+        // divide in FP32, then floor
+        volatile float t = (p.twod_z - p.world_origin[2]);
+        volatile float u = t / p.cell_size;
+        d.twod_cz = (int)std::floor((float)u);
+    }
     d.flags = p.flags;
     d.solid_w = p.solid_density_weight;
     for (int k = 0; k < 6; ++k) d.rands[k] = rands[k];

@@ -487,8 +487,9 @@ def granular_column(count: int = 1600, width: int | None = None, radius: float =
     partial, jitter U(-0.01r, 0.01r) in x and y; centred in a box as wide as
     twice the column, friction mu_s / mu_k on contacts and walls, z pinned
     to 0 (FLAG_TWOD), 3 iterations, dt = 1/60.  Cell 2r as the reference;
-    the grid covers the box's width and the column's height and has four
-    cells in z (the stencil must not alias there)."""
+    the grid covers the box's width and the column's height and is one cell
+    deep (in 2-D the particles share one z layer and the stencils walk only
+    that layer)."""
     d = 2.0 * radius
     width = int(width or max(1, round(math.sqrt(count))))
     rows = -(-count // width)
@@ -500,7 +501,7 @@ def granular_column(count: int = 1600, width: int | None = None, radius: float =
     half = width * d
     height = rows * d
     cell = d
-    grid = [next_pow2(2 * half / cell), next_pow2(height / cell), 4]
+    grid = [next_pow2(2 * half / cell), next_pow2(height / cell), 1]
     pos_w = np.empty((count, 4), np.float32)
     pos_w[:, :3] = pos
     pos_w[:, 3] = 1.0
@@ -568,7 +569,7 @@ def smoke_box(spacing: float = 0.63, half: float = 4.0, twod: bool = False, dens
     cell = h
     box_lo, box_hi = [-6.0, -4.0 - (2.0 if solid_floor else 0.0), -6.0], [6.0, 200.0, 6.0]
     grid = [next_pow2((box_hi[0] - box_lo[0]) / cell), next_pow2((box_hi[1] - box_lo[1]) / cell),
-            4 if twod else next_pow2((box_hi[2] - box_lo[2]) / cell)]
+            1 if twod else next_pow2((box_hi[2] - box_lo[2]) / cell)]
     origin = [box_lo[0], box_lo[1], -2.0 * cell if twod else box_lo[2]]
     params = dict(particle_radius=0.25, kernel_radius=h, cell_size=cell, grid_size=grid, world_origin=origin,
                   gravity=[0.0, -9.8, 0.0], box_min=[box_lo[0], box_lo[1], -1.0 if twod else box_lo[2]],
