@@ -755,6 +755,7 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
                 const float d2 = dist2_exact(pi, f3(pl));
                 const bool ok = d2 < P.h2 && j != i;
                 nb += ok ? 1u : 0u;
+                if (nb > P.max_nb) return false;  // over the cap: the capped walk below decides
                 delta_add(P, delta, ok, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
             }
             return true;
@@ -1231,6 +1232,7 @@ __device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, f
     uint32_t *const words = reinterpret_cast<uint32_t *>(L.slot);
     const uint32_t cap = L.capacity;
     uint32_t k = cols, r = 0;
+    bool over = false;
     stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
         if (r < rfull) {
             ++r;
@@ -1239,13 +1241,17 @@ __device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, f
         if (r++ == rfull) b = jlast + 1u;
         for (uint32_t j = b; j < e; ++j) {
             if (dist2_exact(pi, f3(__ldg(sx + j))) < reach2 && j != i) {
-                if (k < cap) words[((size_t)(k >> 2) * L.stride + i) * 4u + (k & 3u)] = j;
+                if (k == cap) {  // over capacity: the rest of the walk does not matter
+                    over = true;
+                    return false;
+                }
+                words[((size_t)(k >> 2) * L.stride + i) * 4u + (k & 3u)] = j;
                 ++k;
             }
         }
         return true;
     });
-    return k > cap ? cap + 1u : k;
+    return over ? cap + 1u : k;
 }
 
 template <int RAD, bool B, bool SKIN>

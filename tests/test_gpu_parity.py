@@ -584,6 +584,29 @@ def test_list_assembly_shared_equals_registers(capacity, skin, squeeze):
     np.testing.assert_array_equal(a.velocities(), b.velocities())
 
 
+def test_list_build_with_a_coincident_pile():
+    """600 particles stacked on one point (as a clamped corner collects
+    them in a long run): every one has more neighbours than the list holds
+    and than the 500-neighbour cap, so the list builds stop walking early
+    and the exact walk takes the first 500.  Both builds agree bit for bit
+    and the state stays finite."""
+    sc = W.dam_break(24, 20, 12)
+    sc.params["grid_size"] = [64, 16, 16]
+    sc.pos_w[:600, :3] = sc.pos_w[700, :3]
+    a = ParticleSystem(default_params(**sc.params), sc.n)
+    b = ParticleSystem(default_params(**sc.params), sc.n)
+    W.apply_to(sc, a)
+    W.apply_to(sc, b)
+    a.set_tuning(threads_per_particle=1, list_assembly=0)
+    b.set_tuning(threads_per_particle=1, list_assembly=1)
+    for _ in range(3):
+        a.update(sc.dt)
+        b.update(sc.dt)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+    a.check_finite()
+
+
 # ------------------------------------------------------------ skin lists
 
 def test_skin_list_forced_rebuild_is_bitwise_the_plain_schedule():
