@@ -127,6 +127,11 @@ class ParticleSystem {
     int3 getMinBounds() const { return minB_; }
     int3 getMaxBounds() const { return maxB_; }
     // Device float4 positions (the reference's VBO contents).
+    // The reference's render buffer content (xyz, w = 1) into dst, float4
+    // per particle, device memory, on the stream.
+    void copyVbo(float4 *dst, cudaStream_t stream = nullptr) {
+        check(pbd_get_vbo(sys_, 0, pbd_num_particles(sys_), (float *)dst, 1, stream));
+    }
     float4 *devicePositions() {
         pbd_device_buffers b;
         check(pbd_get_device_buffers(sys_, &b));

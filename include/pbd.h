@@ -250,6 +250,13 @@ int pbd_get_positions(pbd_system *sys, uint32_t first, uint32_t count, float *ds
 int pbd_get_velocities(pbd_system *sys, uint32_t first, uint32_t count, float *dst,
                        int dst_on_device, void *stream);
 int pbd_get_phases(pbd_system *sys, int32_t *dst);
+/* The reference's render buffer content (its position VBO, float4 per
+ * particle: xyz, w = 1; integration_kernel.cuh:461, particlesystem.cpp:
+ * 95-96,160) for particles [first, first+count): count float4 to dst, a
+ * device pointer (on the stream) or host memory (synchronous).  Positions
+ * keep the inverse mass in w; this is the layout a renderer or trajectory
+ * tool written for the reference reads. */
+int pbd_get_vbo(pbd_system *sys, uint32_t first, uint32_t count, float *dst, int dst_on_device, void *stream);
 /* Marks the gas particles of [first, first+count) as an open gas (open != 0)
  * or a closed one: createGas(..., open) of the CPU reference
  * (simulation.cpp:408-429, gasconstraint.cpp:80).  Non-gas particles in the

@@ -185,6 +185,7 @@ _SIGNATURES = {
     "pbd_set_params": ([_P, ctypes.POINTER(PbdParams)], _I),
     "pbd_get_params": ([_P, ctypes.POINTER(PbdParams)], _I),
     "pbd_begin_scene": ([_P, ctypes.POINTER(PbdParams), _PU], _I),
+    "pbd_get_vbo": ([_P, _U32, _U32, _P, _I, _P], _I),
     "pbd_batch_create": ([_U32, ctypes.POINTER(PbdParams), _PU, _PF, _PF, _PI, _PF, _U32, ctypes.POINTER(_P)], _I),
     "pbd_num_scenes": ([_P], _U32),
     "pbd_get_scene": ([_P, _U32, _PU, _PU, ctypes.POINTER(PbdParams)], _I),
@@ -555,6 +556,18 @@ class ParticleSystem:
     def set_velocities(self, vel, first=0):
         a = _f32(vel, 4).reshape(-1, 4)
         self._check(self.lib.pbd_set_velocities(self.h, first, a.shape[0], a.ctypes.data, 0, None))
+
+    def vbo(self, first: int = 0, count: int | None = None, device_ptr: int | None = None, stream=None):
+        """The reference's render buffer content (xyz, w = 1) of particles
+        [first, first + count): into device memory at device_ptr (on the
+        stream), or returned as an (count, 4) array."""
+        count = self.num_particles - first if count is None else int(count)
+        if device_ptr is not None:
+            self._check(self.lib.pbd_get_vbo(self.h, first, count, device_ptr, 1, stream))
+            return None
+        out = np.empty((count, 4), np.float32)
+        self._check(self.lib.pbd_get_vbo(self.h, first, count, out.ctypes.data, 0, stream))
+        return out
 
     def phases(self) -> np.ndarray:
         out = np.empty(self.num_particles, np.int32)

@@ -1863,6 +1863,15 @@ __global__ void __launch_bounds__(kBlock) k_solidify(uint32_t n, float dt, float
     timer[i] = t;
 }
 
+// The reference's collide wrote each particle as (position, 1) into its
+// render buffer (integration_kernel.cuh:461).
+__global__ void __launch_bounds__(kBlock) k_vbo(uint32_t n, const float4 *__restrict__ x, float4 *__restrict__ dst) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 p = x[k];
+    dst[k] = make_float4(p.x, p.y, p.z, 1.f);
+}
+
 __global__ void __launch_bounds__(kBlock) k_finite(uint32_t n, const float4 *__restrict__ x,
                                                    const float4 *__restrict__ v,
                                                    uint32_t *__restrict__ flag) {
@@ -2119,6 +2128,12 @@ cudaError_t launch_solidify(uint32_t n, float dt, float speed, float height, con
     if (n == 0) return cudaSuccess;
     k_solidify<<<blocks_for(n), kBlock, 0, s>>>(n, dt, speed, height, sidx, sxl, tag, timer, x, x_old, v, phase,
                                                 force, converted, list);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vbo(uint32_t n, const float4 *x, float4 *dst, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_vbo<<<blocks_for(n), kBlock, 0, s>>>(n, x, dst);
     return cudaGetLastError();
 }
 

@@ -157,5 +157,7 @@ cudaError_t launch_solidify(uint32_t n, float dt, float speed, float height, con
                             float4 *force, uint32_t *converted, uint32_t *list, cudaStream_t s);
 cudaError_t launch_finite_check(uint32_t n, const float4 *x, const float4 *v, uint32_t *flag,
                                 cudaStream_t s);
+// dst[k] = (x[k].xyz, 1): the reference's render buffer layout.
+cudaError_t launch_vbo(uint32_t n, const float4 *x, float4 *dst, cudaStream_t s);
 
 }  // namespace pbd

@@ -1145,6 +1145,22 @@ int pbd_get_velocities(pbd_system *s, uint32_t first, uint32_t count, float *dst
     return copy_state(s, s ? s->v : nullptr, first, count, dst, on_dev, st, false);
 }
 
+int pbd_get_vbo(pbd_system *s, uint32_t first, uint32_t count, float *dst, int on_dev, void *stream) {
+    SYS_GUARD(s);
+    if ((uint64_t)first + count > s->n) return fail(s, PBD_ERR_INVALID_ARGUMENT, "range exceeds particle count %u", s->n);
+    if (count == 0) return PBD_OK;
+    if (!dst) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dst is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (on_dev) {
+        CUDA_TRY(s, pbd::launch_vbo(count, s->x + first, (float4 *)dst, st));
+        return PBD_OK;
+    }
+    CUDA_TRY(s, cudaMemcpyAsync(dst, s->x + first, (size_t)count * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(s, cudaStreamSynchronize(st));
+    for (uint32_t k = 0; k < count; ++k) dst[4 * (size_t)k + 3] = 1.f;
+    return PBD_OK;
+}
+
 int pbd_get_phases(pbd_system *s, int32_t *dst) {
     SYS_GUARD(s);
     if (!dst) return fail(s, PBD_ERR_INVALID_ARGUMENT, "dst is NULL");

@@ -1,7 +1,8 @@
 // A host program written against the reference's ParticleSystem interface
 // (gpu/src/particlesystem.h), built with include/particle_system.hpp and
 // libpbd_gb300.so: the reference's constructor, scene builders, runtime
-// insertion and update loop, then a check of the result.
+// insertion and update loop, then a check of the result and of the render
+// buffer copy.
 #include <cmath>
 #include <cstdio>
 
@@ -23,6 +24,15 @@ int main() {
     int bad = 0;
     for (const float4 &q : p)
         if (!std::isfinite(q.x) || !std::isfinite(q.y) || !std::isfinite(q.z) || q.y < -1e-3f || q.y > 200.f) ++bad;
+    // the render buffer a renderer written for the reference reads
+    float4 *vbo = nullptr;
+    cudaMalloc((void **)&vbo, p.size() * sizeof(float4));
+    ps.copyVbo(vbo);
+    std::vector<float4> r(p.size());
+    cudaMemcpy(r.data(), vbo, r.size() * sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaFree(vbo);
+    for (size_t k = 0; k < p.size(); ++k)
+        if (r[k].x != p[k].x || r[k].y != p[k].y || r[k].z != p[k].z || r[k].w != 1.f) ++bad;
     bool threw = false;
     try {
         ps.makeDistanceConstraint(make_uint2(0, 1000000), 1.f);  // no such particle

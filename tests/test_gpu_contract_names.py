@@ -125,3 +125,26 @@ def test_record_is_rollout():
     a.rollout(sc.dt, 6, 3)
     assert b.lib.pbd_record(b.h, ctypes.c_float(sc.dt), 6, 3, None) == 0
     np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_vbo_is_the_reference_render_layout():
+    """pbd_get_vbo gives the reference's render buffer: each particle's
+    position with w = 1 (integration_kernel.cuh:461), to host memory or to
+    a device buffer, for any subrange."""
+    import torch
+
+    sc = W.dam_break(16, 12, 8)
+    g = load(sc)
+    for _ in range(2):
+        g.update(sc.dt)
+    x = g.positions()
+    v = g.vbo()
+    np.testing.assert_array_equal(v[:, :3], x[:, :3])
+    assert np.all(v[:, 3] == 1.0)
+    np.testing.assert_array_equal(g.vbo(5, 10), v[5:15])
+    t = torch.zeros((sc.n, 4), dtype=torch.float32, device="cuda")
+    g.vbo(device_ptr=t.data_ptr())
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(t.cpu().numpy(), v)
+    with pytest.raises(PbdError):
+        g.vbo(sc.n - 2, 5)
