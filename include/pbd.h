@@ -462,10 +462,13 @@ int pbd_list_reuses(pbd_system *sys, uint32_t *count);
  * from a device snapshot of the state, then restores the state and keeps
  * the fastest (written to *chosen if not NULL).  Candidates: one lane per
  * particle with lists rebuilt every iteration or kept with a skin of 0.1,
- * 0.2 or 0.3 h, the register list build, 2-32 lanes per particle and, in a
- * system with fluid or gas and no contacts, cells of half the size (every
- * scene's cell_size halved and grid_size doubled; kept only if 3 % faster,
- * and then visible in pbd_get_params / pbd_get_scene).  Synchronous. */
+ * 0.2 or 0.3 h, the register list build, 2-32 lanes per particle, in a
+ * system with fluid or gas and no contacts cells of half the size (every
+ * scene's cell_size halved and grid_size doubled), and in a system with
+ * more than twice as many cells as particles the same cells on half the
+ * grid per axis (positions wrap onto it as on any grid).  A changed grid is
+ * kept only if 3 % faster, and is then visible in pbd_get_params /
+ * pbd_get_scene.  Synchronous. */
 int pbd_autotune(pbd_system *sys, float dt, uint32_t steps, void *stream, pbd_tuning *chosen);
 
 /* --------------------------------------------------------------- timing */

@@ -1550,7 +1550,7 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     pbd_get_tuning(s, &base);
     const uint32_t cap0 = base.neighbor_list_capacity ? base.neighbor_list_capacity : 128u;
     std::vector<pbd_tuning> cands;
-    std::vector<uint32_t> divs;  // cell divisor of each candidate
+    std::vector<uint32_t> divs;  // cell divisor of each candidate (0: the given cells on a halved grid)
     auto cand = [&](uint32_t tpp, float skin, uint32_t div = 1u) {
         pbd_tuning t{};
         t.threads_per_particle = tpp;
@@ -1578,6 +1578,20 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
         half_cells += (uint64_t)p.grid_size[0] * (p.grid_size[0] > 1u ? 2u : 1u) * p.grid_size[1] *
                       (p.grid_size[1] > 1u ? 2u : 1u) * p.grid_size[2] * (p.grid_size[2] > 1u ? 2u : 1u);
     if (s->any_pbf() && !s->n_contact && half_cells <= (1ull << 27)) cand(1, 0.f, 2u);
+    // a grid with many more cells than particles: the same cells on half
+    // the grid per axis (the wrap puts more far-away particles in a
+    // stencil, which the distance test rejects) where every axis keeps room
+    // for its stencil
+    uint64_t given_cells = 0;
+    bool can_halve = true;
+    for (const pbd_params &p : given) {
+        given_cells += (uint64_t)p.grid_size[0] * p.grid_size[1] * p.grid_size[2];
+        const uint32_t rad = (uint32_t)std::ceil(std::max(p.kernel_radius, 2.f * p.particle_radius) / p.cell_size);
+        const bool twod = (p.flags & PBD_FLAG_TWOD) != 0u;
+        for (int a = 0; a < 3; ++a)
+            if (p.grid_size[a] > 1u && !(twod && a == 2) && p.grid_size[a] / 2u < 2u * rad + 2u) can_halve = false;
+    }
+    if (can_halve && given_cells > 2ull * n) cand(1, 0.f, 0u);
     uint32_t cur_div = 1u;
     // sets every scene's cells to the given size / div; on a refusal (a
     // parameter limit) puts the given grids back and returns the error
@@ -1585,9 +1599,15 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
         if (div == cur_div) return PBD_OK;
         for (uint32_t k = 0; k < (uint32_t)given.size(); ++k) {
             pbd_params p = given[k];
-            p.cell_size = given[k].cell_size / (float)div;
-            for (int a = 0; a < 3; ++a)
-                if (p.grid_size[a] > 1u) p.grid_size[a] *= div;
+            if (div == 0u) {  // the given cells, half the grid per axis
+                const bool twod = (p.flags & PBD_FLAG_TWOD) != 0u;
+                for (int a = 0; a < 3; ++a)
+                    if (p.grid_size[a] > 1u && !(twod && a == 2)) p.grid_size[a] /= 2u;
+            } else {
+                p.cell_size = given[k].cell_size / (float)div;
+                for (int a = 0; a < 3; ++a)
+                    if (p.grid_size[a] > 1u) p.grid_size[a] *= div;
+            }
             if (int rc = pbd_set_scene_params(s, k, &p)) {
                 for (uint32_t j = 0; j < k; ++j) pbd_set_scene_params(s, j, &given[j]);
                 cur_div = 1u;

@@ -510,16 +510,17 @@ def test_autotune_restores_state():
 
 def test_autotune_cell_size():
     """A fluid system may come out of the autotuner with cells of half the
-    size (grid doubled per axis); its step still matches the oracle on the
-    given grid (neighbour sets do not depend on the cell).  A system with
-    contacts keeps its cells."""
+    size (grid doubled per axis) or with its cells on half the grid; its
+    step still matches the oracle on the given grid (neighbour sets do not
+    depend on the grid).  A system with contacts keeps its cell size."""
     sc = W.dam_break(16, 16, 8)
     g, o = make_pair(sc)
     g.autotune(sc.dt, 2)
     p = g.get_params()
+    given = sc.params["grid_size"]
     assert p.cell_size in (np.float32(sc.params["cell_size"]), np.float32(sc.params["cell_size"] / 2))
     div = round(sc.params["cell_size"] / p.cell_size)
-    assert list(p.grid_size) == [v * div for v in sc.params["grid_size"]]
+    assert list(p.grid_size) in ([v * div for v in given], [v // 2 for v in given])
     g.update(sc.dt)
     o.update(sc.dt)
     assert_projection(g.positions(), o.positions(), sc.pos_w, TOL_STAGE)
@@ -528,6 +529,25 @@ def test_autotune_cell_size():
     W.apply_to(gc, c)
     c.autotune(gc.dt, 2)
     assert c.get_params().cell_size == np.float32(gc.params["cell_size"])
+
+
+def test_halved_grid_matches_the_oracle():
+    """The same cells on half the grid per axis (what the autotuner may
+    pick for a sparse scene): particles wrap onto it, the walks reject the
+    far ones, and a step of a mixed rope/cloth/grain scene and of a dam
+    break still matches the oracle on the given grid."""
+    dam = W.dam_break(16, 16, 8)
+    dam.params["grid_size"] = [64, 16, 16]
+    for sc in (dam, W.rope_and_cloth()):
+        g, o = make_pair(sc)
+        p = default_params(**sc.params)
+        for a in range(3):
+            p.grid_size[a] = max(1, sc.params["grid_size"][a] // 2)
+        g.set_params(p)
+        before = g.positions()
+        g.update(sc.dt)
+        o.update(sc.dt)
+        assert_projection(g.positions(), o.positions(), before, TOL_STAGE)
 
 
 @pytest.mark.parametrize("capacity", [0, 4, 16, 64])
