@@ -81,6 +81,30 @@ def test_create_without_gpu_fails_cleanly():
     assert b"CUDA" in lib.pbd_last_error(None) or b"device" in lib.pbd_last_error(None)
 
 
+def test_batch_create_checks_its_arguments_first():
+    """pbd_batch_create rejects a bad batch before it touches a device:
+    no scenes, a capacity below the particles, a missing pos_w or out."""
+    lib = pbd.load_library()
+    h = ctypes.c_void_p(123)
+    par = (pbd.PbdParams * 2)(pbd.default_params(), pbd.default_params())
+    counts = (ctypes.c_uint32 * 2)(10, 20)
+    pos = (ctypes.c_float * 120)()
+    pf = ctypes.cast(pos, ctypes.POINTER(ctypes.c_float))
+    assert lib.pbd_batch_create(0, par, counts, pf, None, None, None, 0, ctypes.byref(h)) == 1
+    assert not h.value
+    assert lib.pbd_batch_create(2, par, counts, pf, None, None, None, 29, ctypes.byref(h)) == 2  # PBD_ERR_CAPACITY
+    assert lib.pbd_batch_create(2, par, counts, None, None, None, None, 0, ctypes.byref(h)) == 1
+    assert lib.pbd_batch_create(2, par, counts, pf, None, None, None, 0, None) == 1
+    assert b"capacity" in lib.pbd_last_error(None) or b"NULL" in lib.pbd_last_error(None)
+
+
+def test_calls_on_a_null_system_fail_cleanly():
+    lib = pbd.load_library()
+    buf = (ctypes.c_float * 8)()
+    assert lib.pbd_get_vbo(None, 0, 1, ctypes.cast(buf, ctypes.c_void_p), 0, None) == 1
+    assert lib.pbd_get_positions(None, 0, 1, ctypes.cast(buf, ctypes.POINTER(ctypes.c_float)), 0, None) == 1
+
+
 def test_cpp_drop_in_header_compiles(tmp_path):
     """include/particle_system.hpp (the reference-shaped C++ class) compiles
     against the C ABI."""

@@ -86,3 +86,28 @@ def test_sdf_rigid_contact_matches_reference_golden():
     d_ref = data["reference"] - data["estimate"]
     assert np.max(np.abs(d_ref)) > 1e-3
     assert norm_err(pos - data["estimate"], d_ref) < 1e-6
+
+
+def test_oracle_2d_grid_depth_does_not_matter():
+    """In 2-D mode every particle sits in twod_z's layer and the stencils
+    walk only that layer, so a granular column steps identically on a grid
+    one cell deep and on one four cells deep (where a three-layer stencil
+    would have found the same neighbours in empty layers)."""
+    import numpy as np
+
+    from oracle import Oracle
+    from particlesolver_gb300 import default_params
+    from particlesolver_gb300 import workloads as W
+
+    sc = W.granular_column(300, seed=7)
+    out = []
+    for depth in (1, 4):
+        params = dict(sc.params)
+        params["grid_size"] = [sc.params["grid_size"][0], sc.params["grid_size"][1], depth]
+        o = Oracle(default_params(**params), sc.n, threads=1)
+        W.apply_to(sc, o)
+        for _ in range(5):
+            o.update(sc.dt)
+        out.append(o.positions())
+        assert np.all(o.positions()[:, 2] == 0.0)
+    np.testing.assert_array_equal(out[0], out[1])
