@@ -512,6 +512,27 @@ def run_ours(args, world, rank, local_rank):
     total_s = max_over_ranks(total_s, world, dev)
     value = job_throughput(args.steps, world, total_s)
 
+    # ---- density invariant after the timed steps: rho / rho0 - 1 over a
+    # seeded sample of particles (rho = poly6 sum within h, FP64 on the host)
+    density = None
+    try:
+        from scipy.spatial import cKDTree
+
+        xs = sysm.positions()[:, :3].astype(np.float64)
+        sample = np.random.default_rng(7).choice(n, min(n, 20000), replace=False)
+        h = sc.params["kernel_radius"]
+        c6 = 315.0 / (64.0 * np.pi * h ** 9)
+        nbrs = cKDTree(xs).query_ball_point(xs[sample], r=h)
+        rho = np.array([np.sum(c6 * np.clip(h * h - np.sum((xs[q] - xs[i]) ** 2, 1), 0.0, None) ** 3)
+                        for i, q in zip(sample, nbrs)])
+        err = rho / np.asarray(sc.rest_density, np.float64)[sample] - 1.0
+        density = {"mean_compression_pct": round(100.0 * float(np.mean(np.clip(err, 0.0, None))), 3),
+                   "mean_signed_pct": round(100.0 * float(np.mean(err)), 3),
+                   "max_pct": round(100.0 * float(np.max(err)), 2),
+                   "after_steps": warm + 1 + args.steps, "sample": int(len(sample))}
+    except ImportError:
+        pass
+
     # ---- per-stage device times (eager, events between stage groups)
     sysm.set_profiling(True)
     sysm.reset_profile()
@@ -623,6 +644,7 @@ def run_ours(args, world, rank, local_rank):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
+        "density_error": density,
         "batched": batched,
         "adjoint": adjoint,
         "other_configs": others,

@@ -217,3 +217,18 @@ def load_sdf_pin(system, case, fp32_inputs: bool = False):
     system.build_grid()
     system.collide()
     return np.asarray(system.positions(), np.float64)[:, :2]
+
+
+def density_error(pos, rho0, h: float, sample=None, mass: float = 1.0):
+    """Per-particle density error rho / rho0 - 1 (rho = sum of poly6 over
+    the particles within h, the particle itself included, unit mass) for
+    the particles `sample` (all if None), FP64 on the host."""
+    from scipy.spatial import cKDTree
+
+    x = np.asarray(pos, np.float64)[:, :3]
+    idx = np.arange(len(x)) if sample is None else np.asarray(sample)
+    c6 = 315.0 / (64.0 * np.pi * h ** 9)
+    nb = cKDTree(x).query_ball_point(x[idx], r=h)
+    rho = np.array([mass * np.sum(c6 * np.clip(h * h - np.sum((x[p] - x[i]) ** 2, 1), 0.0, None) ** 3)
+                    for i, p in zip(idx, nb)])
+    return rho / np.asarray(rho0, np.float64)[idx] - 1.0
