@@ -240,7 +240,10 @@ int pbd_set_rigid_sdf(pbd_system *sys, uint32_t body, const float *sdf);
  * iteration (integration.cu:326); here an explicit input, default zeros. */
 int pbd_set_wall_jitter(pbd_system *sys, const float rands[6]);
 /* Overwrite state of particles [first, first+count) (replaces setArray,
- * particlesystem.cpp:701-713).  src_on_device != 0: src is a device pointer. */
+ * particlesystem.cpp:701-713).  src_on_device != 0: src is a device pointer
+ * and the copy is asynchronous on the stream; otherwise src is host memory
+ * and the call returns after the copy (the buffer may be reused at once).
+ * The getters likewise: a host dst holds the data when they return. */
 int pbd_set_positions(pbd_system *sys, uint32_t first, uint32_t count, const float *src,
                       int src_on_device, void *stream);
 int pbd_set_velocities(pbd_system *sys, uint32_t first, uint32_t count, const float *src,
