@@ -1735,14 +1735,28 @@ __global__ void __launch_bounds__(kBlock) k_velocity(DevParams P0, uint32_t n, f
 
 // Velocities in sorted order for XSPH, w = the particle's mass as a fluid
 // neighbour (1 / w for a fluid particle with w > 0, else 0), so the XSPH
-// sum needs no phase lookup.
-__global__ void __launch_bounds__(kBlock) k_xsph_gather(uint32_t n, const uint32_t *__restrict__ sidx,
+// sum needs no phase lookup.  VEL: the velocity update (k_velocity's
+// expression) is done here, for every particle, and written to v as well.
+template <bool B, bool VEL>
+__global__ void __launch_bounds__(kBlock) k_xsph_gather(DevParams P0, uint32_t n, float dt,
+                                                        const uint32_t *__restrict__ sidx,
                                                         const float4 *__restrict__ sx,
                                                         const SortedAttr *__restrict__ sattr,
-                                                        const float4 *__restrict__ v, float4 *__restrict__ vs) {
+                                                        const float4 *__restrict__ x,
+                                                        const float4 *__restrict__ x_old, float4 *__restrict__ v,
+                                                        float4 *__restrict__ vs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 vi = v[sidx[i]];
+    const uint32_t o = sidx[i];
+    float4 vi;
+    if constexpr (VEL) {
+        const float4 p = x[o], q = x_old[o];
+        const float nd = -fminf(dt, scene_params<B>(P0, o).max_dt);
+        vi = make_float4((q.x - p.x) / nd, (q.y - p.y) / nd, (q.z - p.z) / nd, 0.f);
+        v[o] = vi;
+    } else {
+        vi = v[o];
+    }
     const float w = sx[i].w;
     const float m = (sattr[i].phase == kFluid && w > 0.f) ? 1.f / w : 0.f;
     vs[i] = make_float4(vi.x, vi.y, vi.z, m);
@@ -2108,10 +2122,20 @@ cudaError_t launch_velocity(const DevParams &P, uint32_t n, float dt, const floa
 }
 
 cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs,
-                        const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s) {
+                        const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s, float dt, const float4 *x,
+                        const float4 *x_old) {
     if (n == 0) return cudaSuccess;
     use_list = use_list && L.slot != nullptr;
-    k_xsph_gather<<<blocks_for(n), kBlock, 0, s>>>(n, g.sorted_idx, g.sorted_x, g.sorted_attr, v, vs);
+    const unsigned nb = blocks_for(n);
+    if (x && P.table)
+        k_xsph_gather<true, true><<<nb, kBlock, 0, s>>>(P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x, x_old,
+                                                         v, vs);
+    else if (x)
+        k_xsph_gather<false, true><<<nb, kBlock, 0, s>>>(P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x, x_old,
+                                                          v, vs);
+    else
+        k_xsph_gather<false, false><<<nb, kBlock, 0, s>>>(P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x,
+                                                           x_old, v, vs);
     if (P.table) {
         PBD_TPP_DISPATCH(tpp, true, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L,
                          use_list);

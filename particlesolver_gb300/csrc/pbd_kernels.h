@@ -148,9 +148,13 @@ cudaError_t launch_shapes(const DevParams &P, uint32_t iter_left, const BodyBuff
 // dt is clamped to each scene's max_dt on the device (predict and velocity).
 cudaError_t launch_velocity(const DevParams &P, uint32_t n, float dt, const float4 *x, const float4 *x_old,
                             float4 *v, cudaStream_t s);
-// vs: scratch for the velocities in sorted order.
+// vs: scratch for the velocities in sorted order.  With x (and x_old, dt)
+// the velocity update is fused in: the gather computes each particle's
+// velocity as launch_velocity does and writes it to v as well, so that
+// launch_velocity is not needed first.
 cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, float4 *v, float4 *vs,
-                        const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s);
+                        const NbList &L, bool use_list, uint32_t tpp, cudaStream_t s, float dt = 0.f,
+                        const float4 *x = nullptr, const float4 *x_old = nullptr);
 // Solidification of the fluid emitter over the sorted slots of the last grid.
 cudaError_t launch_solidify(uint32_t n, float dt, float speed, float height, const uint32_t *sidx, const float4 *sxl,
                             const uint8_t *tag, float *timer, float4 *x, float4 *x_old, float4 *v, int *phase,

@@ -579,13 +579,15 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
         }
     }
     if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec + (size_t)(1 + 3 * iters) * n, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
-    {
+    if (any_xsph(s)) {
+        // the velocity update is fused into the XSPH gather (its time shows
+        // under the XSPH stage)
+        Stage t(s, st, PBD_STAGE_XSPH, 2);
+        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, L, s->list_valid, s->tpp, st, dt, s->x,
+                                     s->x_old));
+    } else {
         Stage t(s, st, PBD_STAGE_VELOCITY, 1);
         CUDA_TRY(s, pbd::launch_velocity(P, n, dt, s->x, s->x_old, s->v, st));
-    }
-    if (any_xsph(s)) {
-        Stage t(s, st, PBD_STAGE_XSPH, 2);
-        CUDA_TRY(s, pbd::launch_xsph(P, n, s->grid, s->v, s->vs, L, s->list_valid, s->tpp, st));
     }
     ++s->steps;
     return PBD_OK;
