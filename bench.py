@@ -39,6 +39,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "1M-particle PBF steps/s: plain vs batched/adjoint, same GPU, <=1e-5 proj err"
 UNIT = "steps/s"
 
+LIST_ASSEMBLY = {0: "shared memory", 1: "registers"}
+
 # Algorithmic bytes (compulsory FP32 traffic, each array touched once per pass)
 B_LAMBDA = 20      # read x* 16 + write lambda 4, per particle
 B_DELTA = 36       # read x* 16 + read lambda_i 4 + write x 16, per particle
@@ -76,6 +78,24 @@ def read_peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def fp32_peak_gflops(stream) -> float | None:
+    """FP32 FMA throughput of this GPU (GFLOP/s) from the benchmark's probe
+    library (bench_fp32_peak.cu, built beside the product library)."""
+    import ctypes
+
+    from particlesolver_gb300 import _build
+
+    try:
+        lib = ctypes.CDLL(str(_build.build_probe()))
+    except Exception:
+        return None
+    g = ctypes.c_double()
+    fn = lib.fp32_peak_gflops
+    fn.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    return g.value if fn(ctypes.byref(g), stream) == 0 else None
 
 
 def read_traffic():
@@ -157,22 +177,57 @@ def cpu_baseline_sample(scene, threads: int):
     return time.perf_counter() - t0
 
 
+def workload_config(args, sc) -> dict:
+    """The workload keys both arms report (identical by construction)."""
+    return {"workload": f"pbf_dam_break_{sc.n}", "particles": sc.n, "lattice": [args.nx, args.ny, args.nz],
+            "h": sc.params["kernel_radius"], "iterations": sc.params["iterations"],
+            "grid_rebuild": "every iteration", "xsph_c": sc.params["xsph_c"], "dt": sc.dt,
+            "l2": "GPU arm: flushed before each timed step (256 MiB write); host arm: n/a"}
+
+
+def density_invariant(pos, sc, after_steps: int, sample_size: int = 20000):
+    """rho / rho0 - 1 over a seeded sample of particles (rho = poly6 sum
+    within h, the particle itself included, FP64 on the host): mean
+    compression (mean of the positive part), mean signed error, largest."""
+    import numpy as np
+
+    try:
+        from scipy.spatial import cKDTree
+    except ImportError:
+        return None
+    xs = np.asarray(pos, np.float64)[:, :3]
+    n = len(xs)
+    sample = np.random.default_rng(7).choice(n, min(n, sample_size), replace=False)
+    h = sc.params["kernel_radius"]
+    c6 = 315.0 / (64.0 * np.pi * h ** 9)
+    nbrs = cKDTree(xs).query_ball_point(xs[sample], r=h)
+    rho = np.array([np.sum(c6 * np.clip(h * h - np.sum((xs[q] - xs[i]) ** 2, 1), 0.0, None) ** 3)
+                    for i, q in zip(sample, nbrs)])
+    err = rho / np.asarray(sc.rest_density, np.float64)[sample] - 1.0
+    return {"mean_compression_pct": round(100.0 * float(np.mean(np.clip(err, 0.0, None))), 3),
+            "mean_signed_pct": round(100.0 * float(np.mean(err)), 3),
+            "max_pct": round(100.0 * float(np.max(err)), 2),
+            "after_steps": after_steps, "sample": int(len(sample))}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
     from particlesolver_gb300 import workloads as W
 
-    sc = W.dam_break(args.nx, args.ny, args.nz)
+    sc = W.dam_break(args.nx, args.ny, args.nz, cell_div=args.cell_div)
     threads = os.cpu_count() or 1
     from oracle import Oracle
-    from particlesolver_gb300 import PbdParams
+    from particlesolver_gb300 import host_params
 
-    p = PbdParams().update(**{**_param_defaults(), **sc.params})
-    o = Oracle(p, sc.n, threads=threads)
+    # the same parameters as the GPU arm's default_params(**sc.params),
+    # without loading the CUDA library
+    o = Oracle(host_params(**sc.params), sc.n, threads=threads)
     W.apply_to(sc, o)
     budget = args.ref_budget_s
     t_start = time.perf_counter()
-    for _ in range(min(args.warmup, 1)):
+    warm = max(3, args.warmup)
+    for _ in range(warm):
         o.update(sc.dt)
     times = []
     for _ in range(args.steps):
@@ -183,11 +238,10 @@ def run_reference(args, world, rank):
             break
     v = len(times) / sum(times)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": len(times), "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sum(times) / len(times),
+            "steps": len(times), "warmup": warm, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded dam break)",
-            "config": {"workload": f"pbf_dam_break_{sc.n}", "particles": sc.n, "iterations": 4,
-                       "lattice": [args.nx, args.ny, args.nz], "h": 0.1, "dt": sc.dt},
+            "data": "synthetic (seeded dam break, splitmix64)",
+            "config": workload_config(args, sc),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{len(times)} full oracle updates of the {sc.n}-particle dam break "
                                        f"(the reference GPU path does not build on CUDA 13; its CPU path is "
@@ -440,14 +494,6 @@ def run_adjoint(args, dev, stream):
                         f"zero velocities by Adam"}
 
 
-def _param_defaults():
-    return dict(particle_radius=0.25, kernel_radius=2.0, cell_size=0.5, grid_size=[64, 64, 64],
-                world_origin=[0, 0, 0], gravity=[0, -9.8, 0], box_min=[-50, 0, -50], box_max=[50, 200, 50],
-                iterations=5, max_dt=0.05, relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0,
-                contact_static_friction=0.005, contact_kinetic_friction=0.0002, wall_static_friction=0.005,
-                wall_kinetic_friction=0.0002, max_neighbors=500, twod_z=0.0, flags=0)
-
-
 def run_ours(args, world, rank, local_rank):
     import numpy as np
     import torch
@@ -514,24 +560,7 @@ def run_ours(args, world, rank, local_rank):
 
     # ---- density invariant after the timed steps: rho / rho0 - 1 over a
     # seeded sample of particles (rho = poly6 sum within h, FP64 on the host)
-    density = None
-    try:
-        from scipy.spatial import cKDTree
-
-        xs = sysm.positions()[:, :3].astype(np.float64)
-        sample = np.random.default_rng(7).choice(n, min(n, 20000), replace=False)
-        h = sc.params["kernel_radius"]
-        c6 = 315.0 / (64.0 * np.pi * h ** 9)
-        nbrs = cKDTree(xs).query_ball_point(xs[sample], r=h)
-        rho = np.array([np.sum(c6 * np.clip(h * h - np.sum((xs[q] - xs[i]) ** 2, 1), 0.0, None) ** 3)
-                        for i, q in zip(sample, nbrs)])
-        err = rho / np.asarray(sc.rest_density, np.float64)[sample] - 1.0
-        density = {"mean_compression_pct": round(100.0 * float(np.mean(np.clip(err, 0.0, None))), 3),
-                   "mean_signed_pct": round(100.0 * float(np.mean(err)), 3),
-                   "max_pct": round(100.0 * float(np.max(err)), 2),
-                   "after_steps": warm + 1 + args.steps, "sample": int(len(sample))}
-    except ImportError:
-        pass
+    density = density_invariant(sysm.positions(), sc, warm + 1 + args.steps)
 
     # ---- per-stage device times (eager, events between stage groups)
     sysm.set_profiling(True)
@@ -567,6 +596,33 @@ def run_ours(args, world, rank, local_rank):
     e2e_value = job_throughput(e2e_steps, world, e2e_s)
     sysm.check_finite(sh)
     reuses = sysm.list_reuses()
+
+    # ---- a later window of the same flow: from the timed region's start
+    # state, advance args.later_advance steps untimed, then time
+    # args.later_steps steps as above (the column compresses and neighbour
+    # lists lengthen as the flow develops, so steps get costlier)
+    later = None
+    if args.later_steps:
+        sysm.load_state(state0)
+        for _ in range(args.later_advance):
+            sysm.update_graph(sc.dt, 1, sh)
+        lev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.later_steps)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for a, b in lev:
+                flush.zero_()
+                a.record(stream)
+                sysm.update_graph(sc.dt, 1, sh)
+                b.record(stream)
+        torch.cuda.synchronize()
+        later_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in lev) / 1e3, world, dev)
+        sysm.check_finite(sh)
+        first = warm + 1 + args.later_advance
+        later = {"value": job_throughput(args.later_steps, world, later_s), "unit": UNIT,
+                 "ms_per_step": 1e3 * later_s / args.later_steps, "first_step": first + 1,
+                 "steps": args.later_steps, "untimed_advance": args.later_advance,
+                 "density_error": density_invariant(sysm.positions(), sc, first + args.later_steps)}
     batched = None
     if args.batch_scenes:
         sysm.close()
@@ -593,19 +649,19 @@ def run_ours(args, world, rank, local_rank):
         traffic = traffic_tab["per_launch_bytes"][dom]
     step_bytes = (B_STEP_FIXED + 4 * B_ITER) * n
     ms_per_step = 1e3 * total_s / args.steps
-    # FP32 beside HBM: the dominant kernel's FP32 flops (instruction mix
-    # measured by ncu, profiles/) over its launch time, against the FP32
-    # FMA throughput measured here
-    from particlesolver_gb300 import measure_fp32_peak
-
+    # FP32 beside HBM: the dominant kernel's FP32 flops per particle (an
+    # ncu instruction mix carried over from an earlier capture, not
+    # measured in this run) over its launch time here, against the FP32 FMA
+    # throughput measured here by the benchmark's own probe
     fp32 = None
     flops_pp = (traffic_tab or {}).get("fp32_flops_per_particle", {}).get(dom)
     if flops_pp:
-        peak32 = measure_fp32_peak(sh)
+        peak32 = fp32_peak_gflops(sh)
         ach32 = flops_pp * n / (dom_ms * 1e-3) / 1e9
         fp32 = {"kernel": dom, "flops_per_particle": flops_pp, "achieved_gflops": ach32,
-                "peak_gflops": peak32, "frac": ach32 / peak32, "peak_source": "measured (pbd_measure_fp32_peak)",
-                "flops_source": "ncu instruction mix (profiles/dam_break_131k_fp32_mix.md)"}
+                "peak_gflops": peak32, "frac": ach32 / peak32 if peak32 else None,
+                "peak_source": "measured in this run (FP32 FMA probe, bench_fp32_peak.cu)",
+                "flops_source": "carried over: " + traffic_tab.get("fp32_source_short", "ncu instruction mix")}
 
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
@@ -619,32 +675,37 @@ def run_ours(args, world, rank, local_rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, splitmix64)",
-        "config": {"workload": f"pbf_dam_break_{n}", "particles": n, "lattice": [args.nx, args.ny, args.nz],
-                   "h": 0.1, "iterations": 4, "grid_rebuild": "every iteration", "xsph_c": 0.01,
-                   "cell_size": round(float(held.cell_size), 6), "grid": list(held.grid_size),
+        "config": workload_config(args, sc),
+        "tuning": {"cell_size": round(float(held.cell_size), 6), "grid": list(held.grid_size),
                    "cell_source": "autotuned" if not args.tpp else "given",
                    "threads_per_particle": tpp, "tpp_source": "fixed" if args.tpp else "autotuned",
                    "neighbor_skin": float(tuning.neighbor_skin),
                    "neighbor_list_capacity": int(tuning.neighbor_list_capacity),
-                   "list_assembly": "shared memory" if int(tuning.list_assembly) == 0 else "registers",
-                   "list_reuses_last_step": reuses,
-                   "dt": sc.dt, "l2": "flushed before each timed step (256 MiB write)",
-                   "timing": "per-step CUDA events on the launching stream, CUDA graph replay",
+                   "list_assembly": LIST_ASSEMBLY.get(int(tuning.list_assembly), str(int(tuning.list_assembly))),
+                   "list_reuses_last_step": reuses},
+        "timing": {"how": "per-step CUDA events on the launching stream, CUDA graph replay",
                    "particle_iterations_per_s": value * n * 4,
                    "step_bytes_algorithmic": step_bytes,
                    "step_achieved_gbs": step_bytes / (ms_per_step * 1e-3) / 1e9,
                    "wall_s_timed_region": wall},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "traffic_source": ("carried over, not measured in this run: " +
+                                        (traffic_tab or {}).get("traffic_source_short", "ncu capture"))
+                     if traffic is not None else None,
                      "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "fp32": fp32,
-        "stage_ms_per_step": {k: v / prof_steps for k, v in prof["stage_ms"].items()},
+        # (stages that launched nothing are left out: with XSPH on, the
+        # velocity update runs inside the XSPH stage)
+        "stage_ms_per_step": {k: v / prof_steps for k, v in prof["stage_ms"].items()
+                              if prof["stage_launches"][k]},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 16 * n, "d2h_bytes_per_step": 2 * 16 * n,
                 "steps": e2e_steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
         "density_error": density,
+        "later_window": later,
         "batched": batched,
         "adjoint": adjoint,
         "other_configs": others,
@@ -665,6 +726,8 @@ def main():
     ap.add_argument("--tpp", type=int, default=0, help="lanes per particle (0 = autotune)")
     ap.add_argument("--cell-div", type=int, default=1, help="grid cell size = h / cell_div")
     ap.add_argument("--ref-budget-s", type=float, default=120.0)
+    ap.add_argument("--later-advance", type=int, default=50, help="untimed steps before the later window")
+    ap.add_argument("--later-steps", type=int, default=20, help="timed steps of the later window (0 = skip)")
     ap.add_argument("--batch-scenes", type=int, default=512, help="batched-scenes measurement (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--batch-single-steps", type=int, default=3)

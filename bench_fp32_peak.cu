@@ -1,9 +1,9 @@
-// FP32 FMA throughput of the device this library runs on: the denominator
-// of the step's FP32 fraction (its kernels are instruction-bound, not
-// bandwidth-bound, so the HBM fraction alone does not place them).
+// Benchmark-side probe (not part of libpbd_gb300): FP32 FMA throughput of
+// the current device, the denominator of the FP32 fraction bench.py reports
+// beside the HBM one (the neighbour passes are instruction-bound, so the
+// HBM fraction alone does not place them).  Built into its own library,
+// libpbd_fp32_probe.so, which only bench.py loads.
 #include <cuda_runtime.h>
-
-#include "pbd_system.h"
 
 namespace {
 
@@ -29,11 +29,11 @@ __global__ void __launch_bounds__(kThreads) k_fma_peak(float *out, int iters, fl
 
 }  // namespace
 
-extern "C" int pbd_measure_fp32_peak(double *gflops, void *stream) {
-    if (!gflops) {
-        pbd_internal_set_thread_error("pbd_measure_fp32_peak: gflops is NULL");
-        return PBD_ERR_INVALID_ARGUMENT;
-    }
+// GFLOP/s of a kernel of independent fused multiply-adds on every SM
+// (best of three timed launches after a warm-up).  Returns 0 on success,
+// else the CUDA error code.  Synchronous.
+extern "C" int fp32_peak_gflops(double *gflops, void *stream) {
+    if (!gflops) return (int)cudaErrorInvalidValue;
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0, sms = 0;
     float *out = nullptr;
@@ -58,11 +58,9 @@ extern "C" int pbd_measure_fp32_peak(double *gflops, void *stream) {
     if (a) cudaEventDestroy(a);
     if (b) cudaEventDestroy(b);
     if (out) cudaFree(out);
-    if (e != cudaSuccess || best <= 0.f) {
-        pbd_internal_set_thread_error(std::string("pbd_measure_fp32_peak: ") + cudaGetErrorString(e));
-        return PBD_ERR_CUDA;
-    }
+    if (e != cudaSuccess) return (int)e;
+    if (best <= 0.f) return (int)cudaErrorUnknown;
     const double flops = 2.0 * kChains * (double)iters * blocks * kThreads;
     *gflops = flops / (best * 1e-3) / 1e9;
-    return PBD_OK;
+    return 0;
 }

@@ -408,10 +408,12 @@ uint32_t pbd_num_cells(const pbd_system *sys);
  * library (~7 MiB per device, held until the process exits), so n is at
  * most PBD_NOALLOC_MAX_PARTICLES and the grid at most
  * PBD_NOALLOC_MAX_CELLS cells; larger requests return
- * PBD_ERR_INVALID_ARGUMENT.  The first call on a device looks up that
- * array's device address, so make it before any stream capture.  Every
- * call shares the array: calls that overlap on the GPU race.  Errors are
- * reported through pbd_last_error(NULL). */
+ * PBD_ERR_INVALID_ARGUMENT.  Each call outside stream capture looks up
+ * that array's device address afresh (so a cudaDeviceReset in between is
+ * harmless); a call on a capturing stream reuses the address of the last
+ * call outside capture, so make the first call on a device before any
+ * capture.  Every call shares the array: calls that overlap on the GPU
+ * race.  Errors are reported through pbd_last_error(NULL). */
 #define PBD_NOALLOC_MAX_PARTICLES (1u << 18)
 #define PBD_NOALLOC_MAX_CELLS (1u << 20)
 int pbd_build_grid_noalloc(const pbd_params *params, const float *positions, uint32_t n,
@@ -476,12 +478,6 @@ int pbd_autotune(pbd_system *sys, float dt, uint32_t steps, void *stream, pbd_tu
 
 /* --------------------------------------------------------------- timing */
 
-/* Measured FP32 FMA throughput of the current device in GFLOP/s (a
- * kernel of independent fused multiply-adds on every SM, best of three
- * timed launches): the denominator of an instruction-bound kernel's FP32
- * fraction.  Synchronous; errors via pbd_last_error(NULL). */
-int pbd_measure_fp32_peak(double *gflops, void *stream);
-
 /* Kernel groups of one step, for the per-stage device timing (no
  * counterpart in the reference, whose only readout was an FPS counter,
  * cpu/src/view.cpp:66,189). */
@@ -492,8 +488,9 @@ enum {
     PBD_STAGE_SOLVE = 3,    /* contacts + PBF delta + walls (one kernel)    */
     PBD_STAGE_DISTANCE = 4, /* distance constraints and pins                */
     PBD_STAGE_SHAPES = 5,   /* shape matching                               */
-    PBD_STAGE_VELOCITY = 6, /* velocity update                              */
-    PBD_STAGE_XSPH = 7,     /* XSPH viscosity                               */
+    PBD_STAGE_VELOCITY = 6, /* velocity update (systems without XSPH)       */
+    PBD_STAGE_XSPH = 7,     /* XSPH viscosity; when XSPH runs it also does
+                               the velocity update, and VELOCITY stays 0  */
     PBD_STAGE_COUNT = 8
 };
 

@@ -19,7 +19,10 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("PBD_REFERENCE_DIR", "/root/reference"))
+# The reference tree: PBD_REFERENCE_DIR, else a checkout named "reference"
+# beside this repository.  Where neither exists (e.g. on a machine that only
+# runs the CUDA path) the reference builds are skipped.
+REFERENCE = Path(os.environ.get("PBD_REFERENCE_DIR") or (ROOT.parent / "reference"))
 ORACLE_LIB = BUILD / "libpbd_oracle.so"
 ORACLE_DUAL_LIB = BUILD / "libpbd_oracle_dual.so"
 

@@ -248,7 +248,6 @@ _SIGNATURES = {
     "pbd_set_distance_stiffness": ([_P, _U32, _P, _I, _P], _I),
     "pbd_rollout": ([_P, _F, _U32, _U32, _P], _I),
     "pbd_list_reuses": ([_P, _PU], _I),
-    "pbd_measure_fp32_peak": ([ctypes.POINTER(ctypes.c_double), _P], _I),
     "pbd_num_distance_constraints": ([_P], _U32),
     "pbd_backward": ([_P, _P, _P, _P, _P, _P, _P], _I),
     "pbd_load_state": ([_P, _P, ctypes.c_uint64], _I),
@@ -285,6 +284,24 @@ def default_params(**kw) -> PbdParams:
     p = PbdParams()
     load_library().pbd_default_params(ctypes.byref(p))
     return p.update(**kw)
+
+
+# pbd_default_params' values (the reference's compile-time constants and
+# scene defaults, integration_kernel.cuh:20-42, particleapp.cpp:23-38), for
+# host-only users that do not load the CUDA library (a CPU checker, the
+# benchmark's reference arm); a CPU test keeps the two equal.
+PARAM_DEFAULTS = dict(
+    particle_radius=0.25, kernel_radius=2.0, cell_size=0.5, grid_size=[64, 64, 64], world_origin=[0.0, 0.0, 0.0],
+    gravity=[0.0, -9.8, 0.0], box_min=[-50.0, 0.0, -50.0], box_max=[50.0, 200.0, 50.0], iterations=5, max_dt=0.05,
+    relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2, xsph_c=0.0, contact_static_friction=0.005,
+    contact_kinetic_friction=0.0002, wall_static_friction=0.005, wall_kinetic_friction=0.0002, max_neighbors=500,
+    twod_z=0.0, flags=0, solid_density_weight=1.0, gas_gravity_scale=-0.2, gas_scorr_k=0.2, gas_scorr_dq=0.25,
+    gas_solid_density_weight=0.5, gas_drag=50.0)
+
+
+def host_params(**kw) -> PbdParams:
+    """default_params(**kw) without loading the CUDA library."""
+    return PbdParams().update(**{**PARAM_DEFAULTS, **kw})
 
 
 def _fptr(a: np.ndarray | None):
@@ -693,13 +710,3 @@ class ParticleSystem:
     def load_state(self, blob: bytes):
         buf = ctypes.create_string_buffer(blob, len(blob))
         self._check(self.lib.pbd_load_state(self.h, ctypes.cast(buf, ctypes.c_void_p), len(blob)))
-
-
-def measure_fp32_peak(stream=None) -> float:
-    """Measured FP32 FMA throughput of the current device, GFLOP/s."""
-    lib = load_library()
-    g = ctypes.c_double()
-    rc = lib.pbd_measure_fp32_peak(ctypes.byref(g), stream)
-    if rc:
-        raise PbdError(rc, lib.pbd_last_error(None).decode())
-    return g.value

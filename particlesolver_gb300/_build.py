@@ -18,7 +18,11 @@ CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_DIR = PKG_DIR / "_lib"
 LIB_NAME = "libpbd_gb300.so"
-SOURCES = ["pbd_kernels.cu", "pbd_system.cpp", "pbd_scenes.cpp", "pbd_noalloc.cu", "pbd_adjoint.cu", "pbd_peak.cu"]
+SOURCES = ["pbd_kernels.cu", "pbd_system.cpp", "pbd_scenes.cpp", "pbd_noalloc.cu", "pbd_adjoint.cu"]
+# The benchmark's FP32 probe (bench_fp32_peak.cu beside bench.py) is its own
+# library: nothing of the product links it.
+PROBE_SRC = ROOT / "bench_fp32_peak.cu"
+PROBE_NAME = "libpbd_fp32_probe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -78,6 +82,22 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, target)
+    return target
+
+
+def build_probe(force: bool = False) -> Path:
+    """Compile the benchmark's FP32 throughput probe into its own library."""
+    target = LIB_DIR / PROBE_NAME
+    if not force and target.exists() and target.stat().st_mtime >= PROBE_SRC.stat().st_mtime:
+        return target
+    LIB_DIR.mkdir(exist_ok=True)
+    tmp = target.with_suffix(".so.tmp")
+    cmd = [nvcc_path(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(PROBE_SRC), "-o", str(tmp),
+           "-lcudart"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {PROBE_SRC.name}:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, target)
     return target
 

@@ -39,14 +39,19 @@ constexpr size_t kScratchWords = kOffPartials + kPartials;
 // ~7 MiB per device, for the life of the process.
 static __device__ __align__(256) uint32_t g_grid_scratch[kScratchWords];
 
-// Device address of g_grid_scratch per device, resolved on the first call
-// made with that device current.  The host symbol itself is only a stand-in
-// and must never reach a kernel.
+// Device address of g_grid_scratch per device.  The host symbol itself is
+// only a stand-in and must never reach a kernel.  The address is looked up
+// (cudaGetSymbolAddress, with that device current) on every call made
+// outside stream capture, so a context torn down and recreated in between
+// (cudaDeviceReset reloads the module at a new address) never leaves a
+// stale pointer behind; a call on a capturing stream uses the address of
+// the last call outside capture, so the first call on a device must come
+// before any capture.
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 uint32_t *g_scratch_ptr[kMaxDevices] = {};
 
-int scratch_for_current_device(uint32_t **out, std::string &why) {
+int scratch_for_current_device(cudaStream_t stream, uint32_t **out, std::string &why) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -57,8 +62,14 @@ int scratch_for_current_device(uint32_t **out, std::string &why) {
         why = "device index out of range for the no-allocation scratch table";
         return PBD_ERR_CUDA;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess) {
+        why = std::string("cudaStreamIsCapturing failed: ") + cudaGetErrorString(e);
+        return PBD_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_grid_scratch);
         if (e != cudaSuccess || !p) {
@@ -66,6 +77,9 @@ int scratch_for_current_device(uint32_t **out, std::string &why) {
             return PBD_ERR_CUDA;
         }
         g_scratch_ptr[dev] = static_cast<uint32_t *>(p);
+    } else if (!g_scratch_ptr[dev]) {
+        why = "pbd_build_grid_noalloc: the first call on a device must come before any stream capture";
+        return PBD_ERR_INVALID_ARGUMENT;
     }
     *out = g_scratch_ptr[dev];
     return PBD_OK;
@@ -101,7 +115,8 @@ extern "C" int pbd_build_grid_noalloc(const pbd_params *params, const float *pos
     if (pbd::scan_partial_count(P.num_cells + 1u) > kPartials)
         return fail(PBD_ERR_INVALID_ARGUMENT, "pbd_build_grid_noalloc: scan scratch too small for the grid");
     uint32_t *scratch = nullptr;
-    if (int rc = scratch_for_current_device(&scratch, why)) return fail(rc, why);
+    if (int rc = scratch_for_current_device(static_cast<cudaStream_t>(stream), &scratch, why))
+        return fail(rc, why);
     const cudaError_t e = pbd::launch_sort_into_cells(
         P, n, reinterpret_cast<const float4 *>(positions), scratch + kOffHash, scratch + kOffSlot,
         scratch + kOffCells, scratch + kOffPartials, scratch + kOffTmp, sorted_index, cell_start, cell_end,

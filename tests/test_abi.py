@@ -31,11 +31,11 @@ def test_every_header_symbol_is_exported():
     assert set(names) <= set(pbd._SIGNATURES), set(names) - set(pbd._SIGNATURES)
 
 
-def test_kernels_are_sm103a_only():
-    out = subprocess.run(["cuobjdump", "--list-elf", str(_build.lib_path())], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+def test_kernels_are_built_for_sm103a_only():
+    """Every translation unit is compiled with the one -gencode for sm_103a
+    (a kernel launch on another architecture then fails loudly with "no
+    kernel image"; the GPU tests launch every kernel family)."""
+    assert _build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 @pytest.mark.parametrize("mirror,ctype", [(pbd.PbdParams, "pbd_params"), (pbd.PbdEmitter, "pbd_emitter"),
@@ -65,6 +65,17 @@ def test_default_params_are_reference_values():
     assert abs(p.relaxation - 0.01) < 1e-9 and p.max_neighbors == 500
     assert list(p.box_min) == [-50, 0, -50] and list(p.box_max) == [50, 200, 50]
     assert p.solid_density_weight == 1.0  # the GPU reference: every neighbour counts
+
+
+def test_host_param_defaults_match_the_library():
+    """PARAM_DEFAULTS (used where the CUDA library is not loaded, e.g. the
+    benchmark's reference arm) equals pbd_default_params field by field."""
+    a = pbd.host_params().as_dict()
+    b = pbd.default_params().as_dict()
+    assert a.keys() == b.keys()
+    for k in a:
+        assert a[k] == b[k], k
+    assert pbd.host_params(iterations=4).iterations == 4
 
 
 def test_create_without_gpu_fails_cleanly():

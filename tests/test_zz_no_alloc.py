@@ -54,16 +54,31 @@ def test_noalloc_grid_matches_allocating_path_twice():
 
 
 def test_noalloc_grid_rejects_sizes_beyond_its_limits():
+    """Requests beyond the fixed scratch are refused with an error code.
+    The buffers handed in are real device buffers large enough for what the
+    request claims, so that the call could not fault even if the limit
+    checks ran after a launch."""
+    torch = pytest.importorskip("torch")
     lib = pbd.load_library()
     params = pbd.default_params()
-    # too many particles: rejected before any device access
-    rc = lib.pbd_build_grid_noalloc(ctypes.byref(params), ctypes.c_void_p(16), (1 << 18) + 1, ctypes.c_void_p(16),
-                                    ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    n_big = (1 << 18) + 1
+    pos = torch.zeros((n_big, 4), dtype=torch.float32, device="cuda")
+    idx = torch.zeros(n_big, dtype=torch.int32, device="cuda")
+    cells = params.grid_size[0] * params.grid_size[1] * params.grid_size[2]
+    cs = torch.zeros(cells, dtype=torch.int32, device="cuda")
+    ce = torch.zeros(cells, dtype=torch.int32, device="cuda")
+    # too many particles
+    rc = lib.pbd_build_grid_noalloc(ctypes.byref(params), pos.data_ptr(), n_big, idx.data_ptr(), cs.data_ptr(),
+                                    ce.data_ptr(), None)
+    torch.cuda.synchronize()
     assert rc == PBD_ERR_INVALID_ARGUMENT
     assert b"exceed the limit" in lib.pbd_last_error(None)
     # too many grid cells
     big = pbd.default_params(grid_size=[2048, 1024, 1])
-    rc = lib.pbd_build_grid_noalloc(ctypes.byref(big), ctypes.c_void_p(16), 10, ctypes.c_void_p(16),
-                                    ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    cs2 = torch.zeros(2048 * 1024, dtype=torch.int32, device="cuda")
+    ce2 = torch.zeros(2048 * 1024, dtype=torch.int32, device="cuda")
+    rc = lib.pbd_build_grid_noalloc(ctypes.byref(big), pos.data_ptr(), 10, idx.data_ptr(), cs2.data_ptr(),
+                                    ce2.data_ptr(), None)
+    torch.cuda.synchronize()
     assert rc == PBD_ERR_INVALID_ARGUMENT
     assert b"grid cells exceed" in lib.pbd_last_error(None)
