@@ -76,7 +76,19 @@ typedef enum pbd_status {
  * flag the balance of the two terms depends on the scene's length unit
  * (the reference tuned its literal constants for h = 2,
  * integration_kernel.cuh:25-35,592,634). */
-#define PBD_FLAGS_ALL 0x1fu
+#define PBD_FLAG_SKIP_FIXED_NEIGHBORS (1u << 5)
+/* A fluid particle's neighbours leave out fixed particles (w = 0): no
+ * density, gradient or correction term and not counted (cpu
+ * totalfluidconstraint.cpp:59); the GPU reference counted them. */
+#define PBD_FLAG_DELTA_OVER_COUNT (1u << 6)
+/* PBF position delta divided by rho0 (n + 1), n the neighbours besides the
+ * particle itself -- the CPU reference's delta / p0 / (|neighbours incl.
+ * self| + counts) (totalfluidconstraint.cpp:108,114; the counts of other
+ * constraints are zero for fluid here) -- instead of (rho0 + n).  Not with
+ * PBD_FLAG_DELTA_OVER_RHO0.  With PBD_FLAG_DENSITY_NEIGHBOR_MASS,
+ * PBD_FLAG_SKIP_FIXED_NEIGHBORS and solid_density_weight = 0 (S_SOLID) the
+ * fluid passes are TotalFluidConstraint::project's. */
+#define PBD_FLAGS_ALL 0x7fu
 
 /* Simulation parameters (replaces SimParams, kernel.cuh:9-22, plus the
  * compile-time constants of integration_kernel.cuh:20-42 and

@@ -34,6 +34,8 @@
 #include "simulation.h"
 #include "gasconstraint.h"
 #include "rigidcontactconstraint.h"
+#include "totalfluidconstraint.h"
+#include "fluidemitter.h"
 #undef private
 
 #include <cstdint>
@@ -180,6 +182,98 @@ void refcpu_rigid_contacts(int n, const double *p, const double *ep, const doubl
         delete ps.at(i);
     }
     for (int b = 0; b < nbodies; ++b) delete bodies.at(b);
+}
+
+// The reference's fluid projection, TotalFluidConstraint::project
+// (totalfluidconstraint.cpp:41-116), on n 2-D particles: those with
+// fluid[i] != 0 form one fluid of rest density `density`, the others are
+// SOLID; imass: n inverse masses (0 = fixed); counts: the other constraints'
+// count per particle (NULL = zero).  Positions are the estimates and
+// project() runs `iterations` times.  Out: the estimates (2n doubles) and
+// the last call's lambda of each fluid particle (n doubles, 0 for the
+// others).  Used to pin the oracle's CPU-formula flags.
+void refcpu_fluid_project(int n, const double *xy, const double *imass, const int *fluid, const int *counts_in,
+                          double density, int iterations, double *xy_out, double *lambda_out) {
+    QList<Particle *> ps;
+    QList<int> members;
+    for (int i = 0; i < n; ++i) {
+        Particle *p = new Particle(glm::dvec2(xy[2 * i], xy[2 * i + 1]), 1.0, fluid[i] ? FLUID : SOLID);
+        p->imass = imass[i];
+        p->ep = p->p;
+        ps.append(p);
+        if (fluid[i]) members.append(i);
+    }
+    {
+        TotalFluidConstraint c(density, &members);
+        std::vector<int> counts(n, 0);
+        if (counts_in)
+            for (int i = 0; i < n; ++i) counts[i] = counts_in[i];
+        for (int it = 0; it < iterations; ++it) c.project(&ps, counts.data());
+        for (int i = 0; i < n; ++i) lambda_out[i] = fluid[i] ? c.lambdas[i] : 0.0;
+    }
+    for (int i = 0; i < n; ++i) {
+        xy_out[2 * i] = ps.at(i)->ep.x;
+        xy_out[2 * i + 1] = ps.at(i)->ep.y;
+        delete ps.at(i);
+    }
+}
+
+// One FluidEmitter::tick (fluidemitter.cpp:13-77) on n 2-D particles, the
+// first `members` of them FLUID members of the emitter's fluid in order
+// (so that the reference's lambdas[i], read with i the member's position in
+// the fluid, is the particle's own lambda), the rest SOLID.  In: positions
+// p and velocities v (2n doubles), inverse masses, timers t, the members'
+// lambdas, the emitter's position, rate and its two clocks (timer,
+// totalTimer), the tick length and the seed of rand() (the emitter's
+// frand() jitter).  Out: the particles' velocities, inverse masses, timers
+// and phases (1 = FLUID, 0 = SOLID) after the tick, the clocks, and the
+// emitted particles' positions and velocities (up to max_new; returns how
+// many were emitted).
+int refcpu_fluid_emitter_tick(int n, int members, const double *p, const double *v, const double *imass,
+                              const double *t, const double *lambdas, double ex, double ey, double rate,
+                              double *clocks, double secs, unsigned seed, double *v_out, double *imass_out,
+                              double *t_out, int *phase_out, int max_new, double *new_p, double *new_v) {
+    QList<Particle *> ps;
+    QList<int> fluid;
+    for (int i = 0; i < n; ++i) {
+        Particle *q = new Particle(glm::dvec2(p[2 * i], p[2 * i + 1]), 1.0, i < members ? FLUID : SOLID);
+        q->imass = imass[i];
+        q->ep = q->p;
+        q->v = glm::dvec2(v[2 * i], v[2 * i + 1]);
+        q->t = t[i];
+        ps.append(q);
+        if (i < members) fluid.append(i);
+    }
+    int emitted = 0;
+    {
+        TotalFluidConstraint fs(1.0, &fluid);
+        for (int i = 0; i < members; ++i) fs.lambdas[i] = lambdas[i];
+        FluidEmitter e(glm::dvec2(ex, ey), rate, &fs);
+        e.timer = clocks[0];
+        e.totalTimer = clocks[1];
+        srand(seed);
+        e.tick(&ps, secs);
+        clocks[0] = e.timer;
+        clocks[1] = e.totalTimer;
+        emitted = ps.size() - n;
+    }
+    for (int i = 0; i < ps.size(); ++i) {
+        const Particle *q = ps.at(i);
+        if (i < n) {
+            v_out[2 * i] = q->v.x;
+            v_out[2 * i + 1] = q->v.y;
+            imass_out[i] = q->imass;
+            t_out[i] = q->t;
+            phase_out[i] = q->ph == FLUID ? 1 : 0;
+        } else if (i - n < max_new) {
+            new_p[2 * (i - n)] = q->p.x;
+            new_p[2 * (i - n) + 1] = q->p.y;
+            new_v[2 * (i - n)] = q->v.x;
+            new_v[2 * (i - n) + 1] = q->v.y;
+        }
+        delete q;
+    }
+    return emitted;
 }
 
 }  // extern "C"

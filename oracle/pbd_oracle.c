@@ -396,6 +396,9 @@ typedef struct {
 static int fluid_visit(void *vctx, uint32_t j) {
     nb_ctx *c = (nb_ctx *)vctx;
     if (j == c->i) return 0;
+    /* PBD_FLAG_SKIP_FIXED_NEIGHBORS: fixed particles are no neighbours
+     * (totalfluidconstraint.cpp:59) */
+    if ((c->s->p.flags & PBD_FLAG_SKIP_FIXED_NEIGHBORS) && c->s->sx32[4 * j + 3] == 0.f) return 0;
     float d2 = dist2f(c->pi32, c->s->sx32 + 4 * j);
     if (d2 < c->s->h2f) {
         if (c->nb >= c->s->p.max_neighbors) return 1;
@@ -555,7 +558,12 @@ static void fluid_delta(const orc_system *s, uint32_t i, uint32_t *list, real ou
         real coef = s->lambda[i] + s->lambda[j] + corr;
         for (int d = 0; d < 3; ++d) delta[d] += coef * sg[d];
     }
-    double div = (s->p.flags & PBD_FLAG_DELTA_OVER_RHO0) ? s->srho0[i] : s->srho0[i] + (double)nb;
+    /* rho0 + n (integration_kernel.cuh:640), rho0, or rho0 (n + 1): the
+     * CPU reference's delta / p0 / (neighbours incl. self + counts, the
+     * counts zero for fluid; totalfluidconstraint.cpp:108,114) */
+    double div = (s->p.flags & PBD_FLAG_DELTA_OVER_COUNT) ? s->srho0[i] * (double)(nb + 1)
+                 : (s->p.flags & PBD_FLAG_DELTA_OVER_RHO0) ? s->srho0[i]
+                                                            : s->srho0[i] + (double)nb;
     for (int d = 0; d < 3; ++d) out[d] = delta[d] / div;
 }
 

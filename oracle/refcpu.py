@@ -43,6 +43,10 @@ def load():
         lib.refcpu_gas_project.argtypes = [I, PD, PD, PD, ctypes.POINTER(ctypes.c_int), D, I, I, PD, PD]
         PI = ctypes.POINTER(ctypes.c_int)
         lib.refcpu_rigid_contacts.argtypes = [I, PD, PD, PD, PI, PD, I, PD, I, PI, D, D, PD]
+        lib.refcpu_fluid_project.argtypes = [I, PD, PD, PI, PI, D, I, PD, PD]
+        lib.refcpu_fluid_emitter_tick.argtypes = [I, I, PD, PD, PD, PD, PD, D, D, D, PD, D, ctypes.c_uint, PD, PD,
+                                                  PD, PI, I, PD, PD]
+        lib.refcpu_fluid_emitter_tick.restype = I
         _lib = lib
     return _lib
 
@@ -126,3 +130,55 @@ def rigid_contacts(p, ep, imass, body, sdf, angles, pairs, s_friction: float, k_
                               angles.ctypes.data_as(pd), pairs.shape[0], pairs.ctypes.data_as(pi),
                               float(s_friction), float(k_friction), out.ctypes.data_as(pd))
     return out
+
+
+def fluid_project(xy, imass, fluid, density: float, iterations: int, counts=None):
+    """The reference's TotalFluidConstraint::project run `iterations` times
+    on 2-D particles (fluid[i] != 0: member of one fluid of rest density
+    `density`, else SOLID; imass 0 = fixed; counts: other constraints per
+    particle, default zero).  Returns the estimates (n, 2) and the last
+    call's lambdas (n,)."""
+    lib = load()
+    xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+    n = xy.shape[0]
+    imass = np.ascontiguousarray(imass, np.float64).reshape(n)
+    fluid = np.ascontiguousarray(fluid, np.int32).reshape(n)
+    cnt = None if counts is None else np.ascontiguousarray(counts, np.int32).reshape(n)
+    out_x = np.empty((n, 2))
+    out_l = np.empty(n)
+    pd = ctypes.POINTER(ctypes.c_double)
+    pi = ctypes.POINTER(ctypes.c_int)
+    lib.refcpu_fluid_project(n, xy.ctypes.data_as(pd), imass.ctypes.data_as(pd), fluid.ctypes.data_as(pi),
+                             None if cnt is None else cnt.ctypes.data_as(pi), float(density), int(iterations),
+                             out_x.ctypes.data_as(pd), out_l.ctypes.data_as(pd))
+    return out_x, out_l
+
+
+def fluid_emitter_tick(p, v, imass, t, lambdas, members: int, position, rate: float, clocks, secs: float,
+                       seed: int = 1, max_new: int = 1024):
+    """One FluidEmitter::tick of the reference on 2-D particles (the first
+    `members` are the emitter fluid's members, in order, with the given
+    lambdas).  Returns a dict: v, imass, t, fluid (after the tick), clocks
+    (timer, totalTimer) and the emitted particles' p and v."""
+    lib = load()
+    p = np.ascontiguousarray(p, np.float64).reshape(-1, 2)
+    n = p.shape[0]
+    v = np.ascontiguousarray(v, np.float64).reshape(n, 2)
+    imass = np.ascontiguousarray(imass, np.float64).reshape(n)
+    t = np.ascontiguousarray(t, np.float64).reshape(n)
+    lam = np.ascontiguousarray(lambdas, np.float64).reshape(-1)
+    clk = np.ascontiguousarray(clocks, np.float64).reshape(2).copy()
+    v_out, im_out, t_out = np.empty((n, 2)), np.empty(n), np.empty(n)
+    ph_out = np.empty(n, np.int32)
+    new_p, new_v = np.empty((max_new, 2)), np.empty((max_new, 2))
+    pd = ctypes.POINTER(ctypes.c_double)
+    pi = ctypes.POINTER(ctypes.c_int)
+    k = lib.refcpu_fluid_emitter_tick(n, int(members), p.ctypes.data_as(pd), v.ctypes.data_as(pd),
+                                      imass.ctypes.data_as(pd), t.ctypes.data_as(pd), lam.ctypes.data_as(pd),
+                                      float(position[0]), float(position[1]), float(rate), clk.ctypes.data_as(pd),
+                                      float(secs), int(seed), v_out.ctypes.data_as(pd), im_out.ctypes.data_as(pd),
+                                      t_out.ctypes.data_as(pd), ph_out.ctypes.data_as(pi), int(max_new),
+                                      new_p.ctypes.data_as(pd), new_v.ctypes.data_as(pd))
+    k = min(k, max_new)
+    return {"v": v_out, "imass": im_out, "t": t_out, "fluid": ph_out == 1, "clocks": clk,
+            "new_p": new_p[:k], "new_v": new_v[:k]}

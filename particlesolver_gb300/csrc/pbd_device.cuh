@@ -20,6 +20,8 @@ enum : uint32_t {
     kFlagDeltaOverRho0 = 1u << 2,
     kFlagDistanceMassWeighted = 1u << 3,
     kFlagKernelUnits = 1u << 4,
+    kFlagSkipFixedNeighbors = 1u << 5,
+    kFlagDeltaOverCount = 1u << 6,
     // Set by the host, never by the caller: the system holds gas particles,
     // so the prediction applies the per-particle force and the gas gravity
     // and keeps the step's velocity v' for the gas terms.
@@ -197,6 +199,29 @@ __device__ __forceinline__ float density_weight(const DevParams &P, AttrPtr satt
     float w = 1.f;
     if (P.solid_w != 1.f && sattr[j].phase >= kCloth) w = P.solid_w;
     return w;
+}
+#endif
+
+#if defined(__CUDACC__)
+// Whether particle j (sorted position and inverse mass q_j) can be a fluid
+// particle's neighbour: always, unless PBD_FLAG_SKIP_FIXED_NEIGHBORS leaves
+// fixed particles (w = 0) out (cpu totalfluidconstraint.cpp:59).
+__device__ __forceinline__ bool fluid_nb_ok(const DevParams &P, float wj) {
+    return !(P.flags & kFlagSkipFixedNeighbors) || wj != 0.f;
+}
+// The same for a neighbour known by its sorted slot (the inverse mass is
+// loaded only when the flag is set).
+__device__ __forceinline__ bool fluid_nb_ok_at(const DevParams &P, const float4 *__restrict__ sx, uint32_t j) {
+    return !(P.flags & kFlagSkipFixedNeighbors) || __ldg(&sx[j].w) != 0.f;
+}
+// Divisor of a fluid particle's PBF correction: rho0 + n (the GPU
+// reference, integration_kernel.cuh:640), rho0 (PBD_FLAG_DELTA_OVER_RHO0)
+// or rho0 (n + 1), the CPU reference's (neighbours + self) rest densities
+// (PBD_FLAG_DELTA_OVER_COUNT, totalfluidconstraint.cpp:108,114; its other
+// constraints' counts are zero here: fluid takes no part in contacts).
+__device__ __forceinline__ float fluid_delta_div(const DevParams &P, float rho0, uint32_t nb) {
+    if (P.flags & kFlagDeltaOverCount) return rho0 * (float)(nb + 1u);
+    return (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
 }
 #endif
 

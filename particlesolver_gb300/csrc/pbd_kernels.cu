@@ -611,7 +611,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
             for (uint32_t j = b; j < e; ++j) {
                 const float4 pj = sx[j];
                 const float d2 = dist2_exact(pi, f3(pj));
-                const bool ok = d2 < P.h2 && j != i;
+                const bool ok = d2 < P.h2 && j != i && fluid_nb_ok(P, pj.w);
                 nb += ok ? 1u : 0u;
                 const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
                 acc.add(P, ok, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
     if (capped) {
         group_walk<TPP>(
             P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+            [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok(P, pj.w); },
             [&](uint32_t j, const float4 &pj, float d2) {
                 const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
                 acc.add(P, true, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
@@ -741,6 +741,7 @@ __device__ float3 gas_delta(const DevParams &P, const Group<TPP> &G, uint32_t i,
 template <int TPP>
 __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TPP> &G, uint32_t i, float3 pi,
                                               float rho0, const float4 *__restrict__ sxl,
+                                              const float4 *__restrict__ sx,
                                               const uint32_t *__restrict__ cell_first) {
     const float lam_i = sxl[i].w;
     const float poly6_ref = P.poly6 * P.scorr_inv_ref;
@@ -753,7 +754,7 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
             for (uint32_t j = b; j < e; ++j) {
                 const float4 pl = sxl[j];
                 const float d2 = dist2_exact(pi, f3(pl));
-                const bool ok = d2 < P.h2 && j != i;
+                const bool ok = d2 < P.h2 && j != i && fluid_nb_ok_at(P, sx, j);
                 nb += ok ? 1u : 0u;
                 if (nb > P.max_nb) return false;  // over the cap: the capped walk below decides
                 delta_add(P, delta, ok, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
@@ -768,7 +769,8 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
     if (capped) {
         nb = group_walk<TPP>(
             P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sxl, cell_first, P.max_nb,
-            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+            // (sxl carries lambda in w: the inverse mass comes from sx)
+            [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok_at(P, sx, j); },
             [&](uint32_t, const float4 &pl, float d2) {
                 delta_add(P, delta, true, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
             });
@@ -776,8 +778,7 @@ __device__ __forceinline__ float3 fluid_delta(const DevParams &P, const Group<TP
         delta.y = G.sum(delta.y);
         delta.z = G.sum(delta.z);
     }
-    const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
-    return delta / div;
+    return delta / fluid_delta_div(P, rho0, nb);
 }
 
 // v rotated by the unit quaternion q (xyzw).
@@ -1135,7 +1136,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
     LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
     auto add = [&](uint32_t j, const float4 &pj, float d2) {
         const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-        acc.add(P, true, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
+        acc.add(P, fluid_nb_ok(P, pj.w), d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
     };
     if (reuse) {
         for_each_listed(L, i, L.count[i], [&](uint32_t j) {
@@ -1193,7 +1194,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
             const Group<1> G;
             group_walk<1>(
                 P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-                [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
+                [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok(P, pj.w); },
                 [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2); });
         }
     }
@@ -1217,18 +1218,19 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
 // entries go out as quads, then the walk resumes after the column's last
 // entry (in range `rfull` of the walk, the range in which the column
 // filled) and stores the rest straight to their words of the global list.
-// Returns the count, or capacity + 1 when the list does not fit.
-template <int RAD>
+// Returns the count, or capacity + 1 when the list does not fit.  CS: the
+// column's stride in words (entry k of the column at col[k * CS]).
+template <int RAD, int CS>
 __device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, float3 pi, int3 g, int rad,
                                                float reach2, bool trim, const float4 *__restrict__ sx,
                                                const uint32_t *__restrict__ cell_first, const NbList &L,
                                                const uint32_t *col, uint32_t cols, uint32_t rfull) {
     uint4 *const dst = L.slot + i;
     for (uint32_t q = 0; 4u * q < cols; ++q) {
-        const uint32_t k = 4u * q * (uint32_t)kListBlock;
-        dst[q * L.stride] = make_uint4(col[k], col[k + kListBlock], col[k + 2 * kListBlock], col[k + 3 * kListBlock]);
+        const uint32_t k = 4u * q * (uint32_t)CS;
+        dst[q * L.stride] = make_uint4(col[k], col[k + CS], col[k + 2 * CS], col[k + 3 * CS]);
     }
-    const uint32_t jlast = col[(cols - 1u) * (uint32_t)kListBlock];
+    const uint32_t jlast = col[(cols - 1u) * (uint32_t)CS];
     uint32_t *const words = reinterpret_cast<uint32_t *>(L.slot);
     const uint32_t cap = L.capacity;
     uint32_t k = cols, r = 0;
@@ -1252,6 +1254,102 @@ __device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, f
         return true;
     });
     return over ? cap + 1u : k;
+}
+
+// Particle i's list, held in its shared-memory column (entries 0 ..
+// min(cnt, cols) - 1 at col[k * CS]; with cnt > cols the rest already sits
+// in the global list): stores it to the global list four entries to a uint4
+// and sums lambda's terms over it with add(j, q_j, d2, ok).  A list that is
+// not usable (over capacity or the neighbour cap) takes the exact capped
+// walk instead.  SKIN: listed particles farther than h add nothing.
+template <int CS, bool SKIN, class Add>
+__device__ __forceinline__ void lambda_from_column(const DevParams &P, const NbList &L, uint32_t i, float3 pi,
+                                                   int3 g, const float4 *__restrict__ sx,
+                                                   const uint32_t *__restrict__ cell_first, const uint32_t *col,
+                                                   uint32_t cols, uint32_t cnt, Add &&add) {
+    const float h2 = P.h2;
+    if (cnt > cols && list_usable(P, L, cnt)) {
+        gather_listed(L, i, cnt, sx, [&](uint32_t j, const float4 &pj, bool valid) {
+            const float d2 = dist2_exact(pi, f3(pj));
+            add(j, pj, d2, valid && (!SKIN || d2 < h2));
+        });
+    } else if (list_usable(P, L, cnt)) {
+        uint4 *const dst = L.slot + i;
+        for (uint32_t q = 0; 4u * q < cnt; ++q) {
+            const uint32_t k = 4u * q * (uint32_t)CS;
+            dst[q * L.stride] = make_uint4(col[k], col[k + CS], col[k + 2 * CS], col[k + 3 * CS]);
+        }
+        // four gathers in flight before their sums (entries past cnt read
+        // this particle's own slot and add nothing)
+        for (uint32_t k = 0; k < cnt; k += 4u) {
+            uint32_t jj[4];
+            float4 pp[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) jj[t] = (k + t < cnt) ? col[(k + t) * (uint32_t)CS] : i;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) pp[t] = __ldg(sx + jj[t]);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const float d2 = dist2_exact(pi, f3(pp[t]));
+                add(jj[t], pp[t], d2, k + t < cnt && (!SKIN || d2 < h2));
+            }
+        }
+    } else {
+        if (SKIN) atomicOr(L.ovf, 1u);
+        const Group<1> G;
+        group_walk<1>(
+            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+            [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok(P, pj.w); },
+            [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2, true); });
+    }
+}
+
+// The list build of one fluid particle by its own stencil walk, the list
+// collected in its shared-memory column (stride CS words, cols entries;
+// a longer list continues in global memory, spill_list), then lambda's sums
+// over it (lambda_from_column).  Sets L.count[i].
+template <int RAD, int CS, bool SKIN, class Add>
+__device__ __forceinline__ void lambda_walk_particle(const DevParams &P, const NbList &L, uint32_t i, float3 pi,
+                                                     const float4 *__restrict__ sx,
+                                                     const uint32_t *__restrict__ cell_first, uint32_t *col,
+                                                     uint32_t cols, Add &&add) {
+    const int3 g = grid_pos(P, pi);
+    const uint32_t cap = L.capacity;
+    int rad = P.fluid_rad;
+    float reach2 = P.h2;
+    bool trim = P.trim_fluid;
+    if (SKIN) {
+        const int r = list_rad(P, L.skin);
+        if ((uint32_t)(2 * r + 1) <= min(P.gx, min(P.gy, P.gz))) {
+            const float lr = P.h * (1.f + L.skin);
+            rad = r;
+            reach2 = lr * lr;
+            trim = true;
+        } else {
+            atomicOr(L.ovf, 1u);
+        }
+    }
+    const uint32_t wend = cols * (uint32_t)CS;
+    uint32_t w = 0;      // word offset of this lane's next entry
+    uint32_t rfull = 0;  // ranges walked before the one that filled the column
+    stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
+#pragma unroll kWalkUnroll
+        for (uint32_t j = b; j < e; ++j) {
+            const float4 q = __ldg(sx + j);
+            const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
+            if (ok) col[w] = j;
+            w = ok ? min(w + (uint32_t)CS, wend) : w;
+        }
+        rfull += w < wend ? 1u : 0u;
+        return true;
+    });
+    const bool spilled = w == wend && cols < cap;
+    const uint32_t cnt = spilled ? spill_list<RAD, CS>(P, i, pi, g, rad, reach2, trim, sx, cell_first, L, col, cols,
+                                                       rfull)
+                         : (w == wend) ? cap + 1u
+                                       : w / (uint32_t)CS;
+    L.count[i] = cnt;
+    lambda_from_column<CS, SKIN>(P, L, i, pi, g, sx, cell_first, col, cols, cnt, add);
 }
 
 template <int RAD, bool B, bool SKIN>
@@ -1292,7 +1390,7 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
     LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
     auto add = [&](uint32_t j, const float4 &pj, float d2, bool ok = true) {
         const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-        acc.add(P, ok, d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
+        acc.add(P, ok && fluid_nb_ok(P, pj.w), d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
     };
     if (reuse) {
         for_each_listed(L, i, L.count[i], [&](uint32_t j) {
@@ -1301,78 +1399,7 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
             if (d2 < h2) add(j, pj, d2);
         });
     } else {
-        const int3 g = grid_pos(P, pi);
-        const uint32_t cap = L.capacity;
-        int rad = P.fluid_rad;
-        float reach2 = h2;
-        bool trim = P.trim_fluid;
-        if (SKIN) {
-            const int r = list_rad(P, L.skin);
-            if ((uint32_t)(2 * r + 1) <= min(P.gx, min(P.gy, P.gz))) {
-                const float lr = P.h * (1.f + L.skin);
-                rad = r;
-                reach2 = lr * lr;
-                trim = true;
-            } else {
-                atomicOr(L.ovf, 1u);
-            }
-        }
-        uint32_t *const col = s_nb + threadIdx.x;
-        const uint32_t wend = cols * (uint32_t)kListBlock;
-        uint32_t w = 0;      // word offset of this lane's next entry
-        uint32_t rfull = 0;  // ranges walked before the one that filled the column
-        stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
-#pragma unroll kWalkUnroll
-            for (uint32_t j = b; j < e; ++j) {
-                const float4 q = __ldg(sx + j);
-                const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
-                if (ok) col[w] = j;
-                w = ok ? min(w + (uint32_t)kListBlock, wend) : w;
-            }
-            rfull += w < wend ? 1u : 0u;
-            return true;
-        });
-        const bool spilled = w == wend && cols < cap;
-        const uint32_t cnt = spilled ? spill_list<RAD>(P, i, pi, g, rad, reach2, trim, sx, cell_first, L, col, cols,
-                                                       rfull)
-                             : (w == wend) ? cap + 1u
-                                           : w / (uint32_t)kListBlock;
-        L.count[i] = cnt;
-        if (spilled && list_usable(P, L, cnt)) {
-            gather_listed(L, i, cnt, sx, [&](uint32_t j, const float4 &pj, bool valid) {
-                const float d2 = dist2_exact(pi, f3(pj));
-                add(j, pj, d2, valid && (!SKIN || d2 < h2));
-            });
-        } else if (list_usable(P, L, cnt)) {
-            uint4 *const dst = L.slot + i;
-            for (uint32_t q = 0; 4u * q < cnt; ++q) {
-                const uint32_t k = 4u * q * (uint32_t)kListBlock;
-                dst[q * L.stride] = make_uint4(col[k], col[k + kListBlock], col[k + 2 * kListBlock],
-                                               col[k + 3 * kListBlock]);
-            }
-            // four gathers in flight before their sums (entries past cnt
-            // read this particle's own slot and add nothing)
-            for (uint32_t k = 0; k < cnt; k += 4u) {
-                uint32_t jj[4];
-                float4 pp[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) jj[t] = (k + t < cnt) ? col[(k + t) * (uint32_t)kListBlock] : i;
-#pragma unroll
-                for (int t = 0; t < 4; ++t) pp[t] = __ldg(sx + jj[t]);
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const float d2 = dist2_exact(pi, f3(pp[t]));
-                    add(jj[t], pp[t], d2, k + t < cnt && (!SKIN || d2 < h2));
-                }
-            }
-        } else {
-            if (SKIN) atomicOr(L.ovf, 1u);
-            const Group<1> G;
-            group_walk<1>(
-                P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-                [&](uint32_t j, const float4 &, float d2) { return j != i && d2 < P.h2; },
-                [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2); });
-        }
+        lambda_walk_particle<RAD, kListBlock, SKIN>(P, L, i, pi, sx, cell_first, s_nb + threadIdx.x, cols, add);
     }
     const float ro = acc.ro + P.poly6_self * inv_w;
     const float denom = acc.denom + dot3(acc.grad, acc.grad);
@@ -1381,26 +1408,27 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
 
 // solveFluidsD (integration_kernel.cuh:596-642) over the lambda pass's list.
 __device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t i, float3 pi, float rho0,
-                                                   const float4 *__restrict__ sxl,
+                                                   const float4 *__restrict__ sxl, const float4 *__restrict__ sx,
                                                    const uint32_t *__restrict__ cell_first, const NbList &L) {
     const uint32_t cnt = L.count[i];
     if (!list_usable(P, L, cnt)) {
         const Group<1> G;
-        return fluid_delta<1>(P, G, i, pi, rho0, sxl, cell_first);
+        return fluid_delta<1>(P, G, i, pi, rho0, sxl, sx, cell_first);
     }
     const float lam_i = sxl[i].w;
     const float poly6_ref = P.poly6 * P.scorr_inv_ref;
     const float h2 = P.h2;
     float3 delta = make_float3(0.f, 0.f, 0.f);
     uint32_t nb = 0;
-    gather_listed<PBD_DELTA_QUADS>(L, i, cnt, sxl, [&](uint32_t, const float4 &pl, bool valid) {
+    gather_listed<PBD_DELTA_QUADS>(L, i, cnt, sxl, [&](uint32_t j, const float4 &pl, bool valid) {
         const float d2 = dist2_exact(pi, f3(pl));
-        const bool ok = valid && d2 < h2;  // all of a plain list; a skin list holds more
+        // all of a plain list; a skin list holds more (and a list holds
+        // fixed particles, which PBD_FLAG_SKIP_FIXED_NEIGHBORS leaves out)
+        const bool ok = valid && d2 < h2 && fluid_nb_ok_at(P, sx, j);
         delta_add(P, delta, ok, d2, pi - f3(pl), lam_i + pl.w, poly6_ref);
         nb += ok ? 1u : 0u;
     });
-    const float div = (P.flags & kFlagDeltaOverRho0) ? rho0 : rho0 + (float)nb;
-    return delta / div;
+    return delta / fluid_delta_div(P, rho0, nb);
 }
 
 // collide_world_functor (integration_kernel.cuh:57-157): clamp into the box
@@ -1486,8 +1514,8 @@ __global__ void __launch_bounds__(kBlock, solve_min_blocks(TPP, B, NOFLUID)) k_s
     bool touched = false;
     if (!NOFLUID && (mask & kDoFluid) && a.phase == kFluid) {
         if constexpr (!NOFLUID) {
-            if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, cell_first, L);
-            else np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, cell_first);
+            if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, sx, cell_first, L);
+            else np = np + fluid_delta<TPP>(P, G, i, np, a.rho0, sxl, sx, cell_first);
         }
         touched = true;
     } else if (!NOFLUID && (mask & kDoFluid) && a.phase == kGas) {

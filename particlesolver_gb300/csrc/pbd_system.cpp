@@ -49,6 +49,10 @@ int validate_params(const pbd_params *p, std::string &why) {
     if (p->max_neighbors == 0) { why = "max_neighbors must be > 0"; return PBD_ERR_INVALID_ARGUMENT; }
     if (!(p->scorr_dq >= 0.f && p->scorr_dq < 1.f)) { why = "scorr_dq must be in [0, 1)"; return PBD_ERR_INVALID_ARGUMENT; }
     if (p->flags & ~PBD_FLAGS_ALL) { why = "unknown bits in flags"; return PBD_ERR_INVALID_ARGUMENT; }
+    if ((p->flags & PBD_FLAG_DELTA_OVER_RHO0) && (p->flags & PBD_FLAG_DELTA_OVER_COUNT)) {
+        why = "PBD_FLAG_DELTA_OVER_RHO0 and PBD_FLAG_DELTA_OVER_COUNT exclude each other";
+        return PBD_ERR_INVALID_ARGUMENT;
+    }
     if (!(p->solid_density_weight >= 0.f) || !std::isfinite(p->solid_density_weight)) {
         why = "solid_density_weight must be finite and >= 0";
         return PBD_ERR_INVALID_ARGUMENT;

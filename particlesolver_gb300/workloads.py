@@ -14,7 +14,10 @@ import numpy as np
 
 PHASE_FLUID, PHASE_GAS, PHASE_CLOTH, PHASE_SOLID, PHASE_RIGID = 0, 1, 2, 3, 4
 FLAG_TWOD = 1
+FLAG_DENSITY_NEIGHBOR_MASS = 1 << 1
 FLAG_KERNEL_UNITS = 1 << 4
+FLAG_SKIP_FIXED_NEIGHBORS = 1 << 5
+FLAG_DELTA_OVER_COUNT = 1 << 6
 
 
 def splitmix64(seed: int, count: int) -> np.ndarray:
@@ -579,6 +582,57 @@ def smoke_box(spacing: float = 0.63, half: float = 4.0, twod: bool = False, dens
     return Scene("smoke_box", params, pos_w, phase, rest_density=rho0,
                  open_gas=[(0, n)] if open_gas else [], dt=1.0 / 60.0,
                  info=dict(gas=n, solids=int(pos_w.shape[0] - n), seed=seed, open=open_gas))
+
+
+def cpu_fluid_box(spacing: float = 0.7, seed: int = 890, density: float = 1.75, solid_floor: bool = True,
+                  iterations: int = 3) -> Scene:
+    """The CPU reference's 2-D fluid scene (initFluid, cpu/src/simulation.cpp:
+    894-913): fluid particles of unit mass on a lattice of spacing 0.7 over
+    [-4, 4) x [-4, 2), jitter 0.2 U(-0.5, 0.5) per axis (the reference's .2
+    (frand() - .5), seeded), rest density 1.75 (its second fluid's), h = 2,
+    cell h.  With solid_floor, a fixed solid plate (w = 0) of the same
+    spacing below the fluid and a layer of movable solid grains on it, so
+    fluid particles have solid neighbours and fixed ones.  The flags select
+    the CPU reference's fluid formulas (TotalFluidConstraint::project,
+    totalfluidconstraint.cpp:41-116): neighbour masses in the density,
+    fixed particles left out, the correction over rho0 (n + 1); and
+    solid_density_weight 0 (S_SOLID, totalfluidconstraint.h:30).  2-D
+    mode, no neighbour cap in effect (the reference has none)."""
+    xs = np.arange(-4.0, 4.0 - 1e-9, spacing)
+    ys = np.arange(-4.0, 2.0 - 1e-9, spacing)
+    gx, gy = np.meshgrid(xs, ys, indexing="ij")
+    n = gx.size
+    pos = np.zeros((n, 3))
+    pos[:, 0] = gx.ravel()
+    pos[:, 1] = gy.ravel()
+    pos[:, :2] += 0.2 * uniform(seed, (n, 2), -0.5, 0.5)
+    pos_w = np.empty((n, 4), np.float32)
+    pos_w[:, :3] = pos
+    pos_w[:, 3] = 1.0
+    phase = np.full(n, PHASE_FLUID, np.int32)
+    rho0 = np.full(n, density, np.float32)
+    if solid_floor:
+        m = xs.size
+        extra = []
+        for y, w in ((-4.0 - 1.4, 0.0), (-4.0 - spacing, 1.0)):  # fixed plate, then grains
+            q = np.zeros((m, 4), np.float32)
+            q[:, 0] = xs
+            q[:, 1] = y
+            q[:, 3] = w
+            extra.append(q)
+        pos_w = np.concatenate([pos_w] + extra)
+        phase = np.concatenate([phase, np.full(2 * m, PHASE_SOLID, np.int32)])
+        rho0 = np.concatenate([rho0, np.ones(2 * m, np.float32)])
+    h = 2.0
+    box_lo, box_hi = [-8.0, -8.0, -1.0], [8.0, 40.0, 1.0]
+    grid = [next_pow2((box_hi[0] - box_lo[0]) / h), next_pow2((box_hi[1] - box_lo[1]) / h), 1]
+    params = dict(particle_radius=0.25, kernel_radius=h, cell_size=h, grid_size=grid,
+                  world_origin=[box_lo[0], box_lo[1], -2.0 * h], gravity=[0.0, -9.8, 0.0], box_min=box_lo,
+                  box_max=box_hi, iterations=iterations, relaxation=0.01, scorr_k=0.1, scorr_n=4.0, scorr_dq=0.2,
+                  xsph_c=0.0, max_dt=1.0 / 60.0, max_neighbors=100000, twod_z=0.0, solid_density_weight=0.0,
+                  flags=FLAG_TWOD | FLAG_DENSITY_NEIGHBOR_MASS | FLAG_SKIP_FIXED_NEIGHBORS | FLAG_DELTA_OVER_COUNT)
+    return Scene("cpu_fluid_box", params, pos_w, phase, rest_density=rho0, dt=1.0 / 60.0,
+                 info=dict(fluid=n, solids=int(pos_w.shape[0] - n), seed=seed))
 
 
 def batched_scenes(count: int = 512, seed: int = 512, lo: int = 1024, hi: int = 65536) -> list:

@@ -14,6 +14,12 @@ neighbours and the outputs of the reference's GasConstraint::project
 estimates and each particle's force.  sdf_contacts.npz holds 2-D body
 pairs touching at one corner each and the reference's
 RigidContactConstraint::project (rigidcontactconstraint.cpp:30-96) result.
+fluid_project.npz holds a 2-D fluid box over a fixed plate and movable
+grains and the reference's TotalFluidConstraint::project
+(totalfluidconstraint.cpp:41-116) estimates and lambdas after 1 and 3
+calls.  fluid_emitter.npz holds FluidEmitter::tick (fluidemitter.cpp:13-77)
+emission counts over 40 ticks and one solidification tick of a seeded
+state.
 """
 from __future__ import annotations
 
@@ -131,13 +137,57 @@ def sdf_fixture() -> dict:
     return dict(case, reference=out)
 
 
+def fluid_fixture() -> dict:
+    """A 2-D fluid box over a fixed plate and movable grains
+    (workloads.cpu_fluid_box) and the reference's
+    TotalFluidConstraint::project estimates and lambdas after 1 and 3
+    calls."""
+    from oracle import refcpu
+
+    sc = W.cpu_fluid_box(seed=890)
+    fluid = (sc.phase == W.PHASE_FLUID).astype(np.int32)
+    xy = sc.pos_w[:, :2].astype(np.float64)
+    out = dict(pos_w=sc.pos_w, phase=sc.phase, rest_density=sc.rest_density)
+    for k in (1, 3):
+        ex, lam = refcpu.fluid_project(xy, sc.pos_w[:, 3].astype(np.float64), fluid, 1.75, k)
+        out[f"k{k}_pos"] = ex
+        out[f"k{k}_lambda"] = lam
+    return out
+
+
+def emitter_fixture() -> dict:
+    """FluidEmitter::tick of the reference: the emission counts of 40 ticks
+    (rate 33/s, dt 1/60) and the solidification of a seeded state of 400
+    fluid members and 20 solids (velocities, timers, phases, inverse masses
+    after the tick)."""
+    from oracle import refcpu
+
+    dt, rate = 1.0 / 60.0, 33.0
+    clocks = np.zeros(2)
+    counts = []
+    for k in range(40):
+        o = refcpu.fluid_emitter_tick(np.zeros((1, 2)), np.zeros((1, 2)), np.ones(1), np.full(1, 4.0), np.zeros(0),
+                                      0, (0.5, 2.0), rate, clocks, dt, seed=k + 1)
+        clocks = o["clocks"]
+        counts.append(len(o["new_p"]))
+    m, n = 400, 420
+    p = np.stack([W.uniform(11, (n,), -5.0, 5.0), W.uniform(21, (n,), 3.0, 7.0)], 1)
+    v = W.uniform(31, (n, 2), -0.06, 0.06)
+    lam = W.uniform(41, (m,), -1.0, 1.0)
+    t = W.uniform(51, (n,), 0.5, 4.0)
+    o = refcpu.fluid_emitter_tick(p, v, np.ones(n), t, lam, m, (0.0, 100.0), 1.0, np.zeros(2), dt)
+    return dict(dt=dt, rate=rate, counts=np.array(counts), members=m, p=p, v=v, lam=lam, t=t, t_out=o["t"],
+                v_out=o["v"], imass_out=o["imass"], fluid_out=o["fluid"])
+
+
 def main():
     if not refgpu.available():
         raise SystemExit("reference sources not found")
     from oracle import refcpu
 
     if refcpu.available():
-        for name, fix in (("gas_project", gas_fixture), ("sdf_contacts", sdf_fixture)):
+        for name, fix in (("gas_project", gas_fixture), ("sdf_contacts", sdf_fixture),
+                          ("fluid_project", fluid_fixture), ("fluid_emitter", emitter_fixture)):
             path = HERE / f"{name}.npz"
             np.savez_compressed(path, **fix())
             print(path, path.stat().st_size, "bytes")

@@ -152,6 +152,17 @@ def oracle_gas_projection(pos_w, phase, rest_density, vel, params: dict, open_: 
     return o.positions()[:, :2], o.forces()[:, :2]
 
 
+def fluid_projection(system, calls: int):
+    """The fluid passes of a loaded system (oracle or CUDA) run `calls`
+    times (grid build + lambda / delta, no prediction and no walls): the
+    counterpart of one TotalFluidConstraint::project per call.  Returns the
+    positions (n, 2) and the last call's lambdas."""
+    for _ in range(calls):
+        system.build_grid()
+        system.solve_fluids()
+    return np.asarray(system.positions(), np.float64)[:, :2], np.asarray(system.lambdas(), np.float64)
+
+
 def assert_gas_projection(pos, force, ref_pos, ref_force, start, gas, tol):
     """Gas displacements and forces within tol of the reference, relative to
     the largest of each; particles that are not gas stay where they were."""
@@ -232,3 +243,38 @@ def density_error(pos, rho0, h: float, sample=None, mass: float = 1.0):
     rho = np.array([mass * np.sum(c6 * np.clip(h * h - np.sum((x[p] - x[i]) ** 2, 1), 0.0, None) ** 3)
                     for i, p in zip(idx, nb)])
     return rho / np.asarray(rho0, np.float64)[idx] - 1.0
+
+
+def emitter_counts(rate: float, duration: float, dt: float, ticks: int) -> list:
+    """Particles FluidEmitter::tick emits per tick (fluidemitter.cpp:69-76):
+    a timer advanced by dt releases one particle per 1 / rate while the
+    emitter's total time is below `duration` (the reference's 5 s; 0 = no
+    limit here)."""
+    timer = elapsed = 0.0
+    out = []
+    for _ in range(ticks):
+        timer += dt
+        elapsed += dt
+        k = 0
+        while (duration <= 0 or elapsed < duration) and timer >= 1.0 / rate:
+            timer -= 1.0 / rate
+            k += 1
+        out.append(k)
+    return out
+
+
+def solidify_rule(y, speed_of, lam, timer, fluid, dt: float, speed: float = 0.06, height: float = 5.0):
+    """FluidEmitter::tick's solidification (fluidemitter.cpp:14-51) for one
+    tick: a fluid particle slower than `speed` at a height <= `height`
+    counts its timer down by 1 while its lambda <= 0, else up by dt (to 3);
+    at <= 0 (then set to 0) it turns solid.  Returns the new timers and the
+    converted particles."""
+    t = np.array(timer, np.float64, copy=True)
+    act = np.asarray(fluid, bool) & (np.asarray(speed_of) < speed) & (np.asarray(y) <= height)
+    down = act & (np.asarray(lam) <= 0)
+    up = act & (np.asarray(lam) > 0)
+    t[down] -= 1.0
+    t[up] = np.minimum(t[up] + dt, 3.0)
+    turn = down & (t <= 0)
+    t[turn] = 0.0
+    return t, turn

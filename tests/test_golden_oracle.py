@@ -111,3 +111,47 @@ def test_oracle_2d_grid_depth_does_not_matter():
         out.append(o.positions())
         assert np.all(o.positions()[:, 2] == 0.0)
     np.testing.assert_array_equal(out[0], out[1])
+
+
+def test_cpu_fluid_formulas_match_reference_golden():
+    """The oracle's CPU fluid formulas (neighbour masses, fixed neighbours
+    left out, correction over rho0 (n + 1), S_SOLID 0) against the
+    reference's own TotalFluidConstraint::project
+    (totalfluidconstraint.cpp:41-116) on a 2-D fluid box over a fixed plate
+    and movable grains: displacements and lambdas after 1 and 3 calls, to
+    1e-7 (FP64 on both sides)."""
+    from helpers import fluid_projection, norm_err
+
+    data = np.load(GOLDEN / "fluid_project.npz")
+    sc = W.cpu_fluid_box(seed=890)
+    np.testing.assert_array_equal(sc.pos_w, data["pos_w"])
+    fluid = sc.phase == W.PHASE_FLUID
+    start = sc.pos_w[:, :2].astype(np.float64)
+    for k in (1, 3):
+        o = Oracle(params_nolib(sc.params), sc.n)
+        W.apply_to(sc, o)
+        pos, lam = fluid_projection(o, k)
+        ref = data[f"k{k}_pos"]
+        assert np.max(np.abs(ref[fluid] - start[fluid])) > 0.05
+        assert norm_err(pos[fluid] - start[fluid], ref[fluid] - start[fluid]) < 1e-7
+        assert norm_err(lam[fluid], data[f"k{k}_lambda"][fluid]) < 1e-7
+
+
+def test_emitter_rules_match_reference_golden():
+    """The emitter rules the CUDA path is tested against (emission per tick,
+    solidification) against the reference's own FluidEmitter::tick
+    (fluidemitter.cpp:13-77): emission counts of 40 ticks and one
+    solidification tick of 400 fluid members, exactly."""
+    from helpers import emitter_counts, solidify_rule
+
+    d = np.load(GOLDEN / "fluid_emitter.npz")
+    assert list(d["counts"]) == emitter_counts(float(d["rate"]), 5.0, float(d["dt"]), len(d["counts"]))
+    m = int(d["members"])
+    n = len(d["t"])
+    fluid = np.arange(n) < m
+    lam = np.concatenate([d["lam"], np.zeros(n - m)])
+    t, turn = solidify_rule(d["p"][:, 1], np.linalg.norm(d["v"], axis=1), lam, d["t"], fluid, float(d["dt"]))
+    assert turn.any()
+    np.testing.assert_array_equal(d["fluid_out"], fluid & ~turn)
+    np.testing.assert_allclose(d["t_out"][fluid], t[fluid], rtol=0, atol=1e-12)
+    assert np.all(d["imass_out"][turn] == 0.0) and np.all(d["v_out"][turn] == 0.0)

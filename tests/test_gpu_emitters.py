@@ -1,30 +1,20 @@
 """Emitters (pbd_add_emitter / pbd_emit): the CPU reference's FluidEmitter
-and OpenSmokeEmitter on the CUDA system.  Emission is checked against a
-restatement of the emitter's timer and its seeded velocity jitter; the
-solidification against its rule applied, tick by tick, to the lambdas,
-velocities and positions the CUDA system had before the tick."""
+and OpenSmokeEmitter on the CUDA system.  Emission is checked against the
+emitter's timer and its seeded velocity jitter; the solidification against
+its rule applied, tick by tick, to the lambdas, velocities and positions the
+CUDA system had before the tick.  Both rules (tests/helpers.py:
+emitter_counts, solidify_rule) are pinned to the reference's own
+FluidEmitter::tick (tests/test_oracle_vs_reference.py,
+tests/test_golden_oracle.py)."""
 import numpy as np
 import pytest
 
+from helpers import emitter_counts as expected_counts
+from helpers import solidify_rule
 from particlesolver_gb300 import ParticleSystem, PbdError, default_params
 from particlesolver_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
-
-
-def expected_counts(rate, duration, dt, ticks):
-    """FluidEmitter::tick's timer (fluidemitter.cpp:69-76) per tick."""
-    timer = elapsed = 0.0
-    out = []
-    for _ in range(ticks):
-        timer += dt
-        elapsed += dt
-        k = 0
-        while (duration <= 0 or elapsed < duration) and timer >= 1.0 / rate:
-            timer -= 1.0 / rate
-            k += 1
-        out.append(k)
-    return out
 
 
 def block_system(capacity=4096):
@@ -94,13 +84,8 @@ def test_solidification_follows_the_fluid_emitter_rule():
     for _ in range(12):
         g.update(dt)
         lam, v, x, ph = g.lambdas(), g.velocities(), g.positions(), g.phases()
-        act = (ph == W.PHASE_FLUID) & (np.linalg.norm(v[:, :3], axis=1) < speed) & (x[:, 1] <= height)
-        down = act & (lam <= 0)
-        up = act & (lam > 0)
-        timer[down] -= 1.0
-        timer[up] = np.minimum(timer[up] + np.float32(dt), 3.0)
-        turn = down & (timer <= 0)
-        timer[turn] = 0.0
+        timer, turn = solidify_rule(x[:, 1], np.linalg.norm(v[:, :3], axis=1), lam, timer, ph == W.PHASE_FLUID,
+                                    float(np.float32(dt)), speed, height)
         assert g.emit(dt) == 0
         ph2, x2 = g.phases(), g.positions()
         want = np.where(turn, W.PHASE_SOLID, ph)

@@ -582,10 +582,10 @@ def test_list_assembly_shared_equals_registers(capacity, skin, squeeze):
     the same order with the same arithmetic, so updates agree bit for bit,
     also when particles overflow the list (24), when the shared columns
     (48 entries) are the whole list (48), and when particles with more
-    neighbours than the columns hold rebuild their lists in global memory:
-    a fluid squeezed to 0.8 of its lattice spacing (~70 neighbours; with a
-    list of 92, and of 44 where they overflow) and a skin list of 1.5 h
-    (~110 entries against 88 skin columns)."""
+    neighbours than the columns hold continue their lists in global
+    memory: a fluid squeezed to 0.8 of its lattice spacing (~70
+    neighbours; with a list of 92, and of 44 where they overflow) and a
+    skin list of 1.5 h (~110 entries against 88 skin columns)."""
     mode = 0
     sc = W.dam_break(24, 20, 12)
     sc.pos_w[:, :3] *= squeeze

@@ -200,3 +200,90 @@ def test_sdf_rigid_contact_matches_reference_cpu(seed):
     o = Oracle(params_nolib(SDF_PIN_PARAMS), len(case["start"]))
     pos = load_sdf_pin(o, case)
     assert norm_err(pos - case["estimate"], ref - case["estimate"]) < 1e-6
+
+
+@pytest.mark.parametrize("seed", [891, 892])
+def test_cpu_fluid_projection_matches_reference_cpu(seed):
+    """The oracle's CPU fluid formulas (PBD_FLAG_DENSITY_NEIGHBOR_MASS,
+    PBD_FLAG_SKIP_FIXED_NEIGHBORS, PBD_FLAG_DELTA_OVER_COUNT,
+    solid_density_weight 0) against the reference's own
+    TotalFluidConstraint::project (totalfluidconstraint.cpp:41-116) compiled
+    from the reference tree, on seeded 2-D fluid boxes over a fixed plate and
+    movable grains, after 1 and 3 calls: displacements and lambdas to 1e-7.
+    Without either neighbour / divisor flag the two differ by far more."""
+    from helpers import fluid_projection
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    sc = W.cpu_fluid_box(seed=seed)
+    fluid = sc.phase == W.PHASE_FLUID
+    start = sc.pos_w[:, :2].astype(np.float64)
+    imass = sc.pos_w[:, 3].astype(np.float64)
+    for calls in (1, 3):
+        ref_pos, ref_lam = refcpu.fluid_project(start, imass, fluid.astype(np.int32), 1.75, calls)
+        o = Oracle(params_nolib(sc.params), sc.n)
+        W.apply_to(sc, o)
+        pos, lam = fluid_projection(o, calls)
+        assert norm_err(pos[fluid] - start[fluid], ref_pos[fluid] - start[fluid]) < 1e-7
+        assert norm_err(lam[fluid], ref_lam[fluid]) < 1e-7
+        assert np.max(np.abs(pos[~fluid] - start[~fluid])) == 0.0
+    ref_pos, _ = refcpu.fluid_project(start, imass, fluid.astype(np.int32), 1.75, 1)
+    from particlesolver_gb300 import workloads as WW
+    for drop in (WW.FLAG_SKIP_FIXED_NEIGHBORS, WW.FLAG_DELTA_OVER_COUNT):
+        params = dict(sc.params, flags=sc.params["flags"] & ~drop)
+        o = Oracle(params_nolib(params), sc.n)
+        W.apply_to(sc, o)
+        pos, _ = fluid_projection(o, 1)
+        assert norm_err(pos[fluid] - start[fluid], ref_pos[fluid] - start[fluid]) > 1e-3
+
+
+def test_fluid_emitter_matches_reference_cpu():
+    """The emitter rules the CUDA path is tested against (tests/helpers.py:
+    emitter_counts, solidify_rule) against the reference's own
+    FluidEmitter::tick (fluidemitter.cpp:13-77): 40 ticks of emission
+    (counts per tick, the 5 s limit, velocities (U(0, 1), 1) at the emitter),
+    and the solidification of seeded states -- speeds around the threshold,
+    heights around 5, lambdas of both signs, timers 0.5-4 -- exactly."""
+    from helpers import emitter_counts, solidify_rule
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    dt, rate = 1.0 / 60.0, 33.0
+    # emission: a lone static solid particle, clocks carried from tick to tick
+    clocks = np.zeros(2)
+    got = []
+    for k in range(40):
+        out = refcpu.fluid_emitter_tick(np.zeros((1, 2)), np.zeros((1, 2)), np.ones(1), np.full(1, 4.0),
+                                        np.zeros(0), 0, (0.5, 2.0), rate, clocks, dt, seed=k + 1)
+        clocks = out["clocks"]
+        got.append(len(out["new_p"]))
+        if len(out["new_p"]):
+            np.testing.assert_array_equal(out["new_p"], np.tile([0.5, 2.0], (len(out["new_p"]), 1)))
+            assert np.all(out["new_v"][:, 1] == 1.0)
+            assert np.all((out["new_v"][:, 0] >= 0.0) & (out["new_v"][:, 0] <= 1.0))
+    assert got == emitter_counts(rate, 5.0, dt, 40) and sum(got) > 0
+    # past the 5 s limit nothing more comes out
+    out = refcpu.fluid_emitter_tick(np.zeros((1, 2)), np.zeros((1, 2)), np.ones(1), np.full(1, 4.0), np.zeros(0),
+                                    0, (0.5, 2.0), rate, np.array([0.5, 5.0]), dt)
+    assert len(out["new_p"]) == 0
+    # solidification: members first (so the reference's lambdas[list index]
+    # is each particle's own), then a few solids
+    for seed in range(4):
+        m, ns = 400, 20
+        n = m + ns
+        p = np.stack([W.uniform(10 + seed, (n,), -5.0, 5.0), W.uniform(20 + seed, (n,), 3.0, 7.0)], 1)
+        v = W.uniform(30 + seed, (n, 2), -0.06, 0.06)
+        lam = W.uniform(40 + seed, (m,), -1.0, 1.0)
+        t = W.uniform(50 + seed, (n,), 0.5, 4.0)
+        out = refcpu.fluid_emitter_tick(p, v, np.ones(n), t, lam, m, (0.0, 100.0), 1.0, np.zeros(2), dt)
+        lam_all = np.concatenate([lam, np.zeros(ns)])
+        fluid = np.arange(n) < m
+        t_want, turn = solidify_rule(p[:, 1], np.linalg.norm(v, axis=1), lam_all, t, fluid, dt)
+        assert turn.any() and (~turn & fluid).any()
+        np.testing.assert_array_equal(out["fluid"], fluid & ~turn)
+        np.testing.assert_allclose(out["t"][fluid], t_want[fluid], rtol=0, atol=1e-12)
+        assert np.all(out["imass"][turn] == 0.0) and np.all(out["imass"][~turn] == 1.0)
+        assert np.all(out["v"][turn] == 0.0)
+        np.testing.assert_array_equal(out["v"][~turn], v[~turn])
