@@ -401,9 +401,11 @@ def run_other_configs(args, stream, flush):
                       f"4x4x4 shape-matched bodies; {mixed.info['constraints']} distance constraints, 4 iterations, "
                       f"dt 1/60")
     out["mixed_scene"] = r
-    col = W.granular_column()
+    # the CPU sand-pile path: the CPU reference's contact and wall
+    # projectors (PBD_FLAG_CPU_CONTACTS)
+    col = W.granular_column(cpu_contacts=True)
     r = time_scene(col, stream, flush, args.other_steps)
-    from oracle import Oracle
+    from oracle import Oracle, refcpu
     from particlesolver_gb300 import default_params
 
     o = Oracle(default_params(**col.params), col.n, threads=1)
@@ -415,8 +417,22 @@ def run_other_configs(args, stream, flush):
         k += 1
     cpu = k / (time.perf_counter() - t0)
     r.update(workload="2-D granular column: 40x40 lattice spacing 2r, jitter U(+-0.01r), mu_s 0.5, mu_k 0.3, "
-                      "3 iterations, dt 1/60",
+                      "3 iterations, dt 1/60, the CPU reference's contact and wall projectors",
              cpu_oracle_1_thread={"value": cpu, "unit": "steps/s", "steps": k, "kind": "port"})
+    # the reference's own 2-D CPU solver, where its sources were built on
+    # this machine (oracle/_ref); single-threaded as written
+    if refcpu.available():
+        ref = refcpu.RefCPU(col.pos_w[:, :2], mass=1.0, s_friction=0.5, k_friction=0.3)
+        t0 = time.perf_counter()
+        k = 0
+        while k < 600 and time.perf_counter() - t0 < 10.0:
+            ref.tick(col.dt)
+            k += 1
+        r["cpu_reference_1_thread"] = {"value": k / (time.perf_counter() - t0), "unit": "steps/s", "steps": k,
+                                       "kind": "reference"}
+    else:
+        r["cpu_reference_1_thread"] = {"unavailable": "the reference's CPU sources are not on this machine "
+                                                      "(oracle/_ref not built)"}
     out["granular_2d"] = r
     return out
 

@@ -88,7 +88,18 @@ typedef enum pbd_status {
  * PBD_FLAG_DELTA_OVER_RHO0.  With PBD_FLAG_DENSITY_NEIGHBOR_MASS,
  * PBD_FLAG_SKIP_FIXED_NEIGHBORS and solid_density_weight = 0 (S_SOLID) the
  * fluid passes are TotalFluidConstraint::project's. */
-#define PBD_FLAGS_ALL 0x7fu
+#define PBD_FLAG_CPU_CONTACTS (1u << 7)
+/* Contacts and walls by the CPU reference's projectors instead of collideD
+ * and collide_world_functor: pairs closer than a diameter - 1e-4 (never two
+ * fixed particles); two solid-like particles by RigidContactConstraint's
+ * plain branch (rigidcontactconstraint.cpp:35-95: the overlap and friction
+ * against the start of the step shared by the height-scaled inverse masses
+ * w e^y), a solid-like particle touching fluid by ContactConstraint
+ * (contactconstraint.cpp:13-42, no friction); each wall passed by
+ * BoundaryConstraint (boundaryconstraint.cpp:14-93, x then y then z,
+ * friction sqrt(mu) r over (x - x_old) / count); every correction averaged
+ * over the particle's contacts and walls (the reference's counts). */
+#define PBD_FLAGS_ALL 0xffu
 
 /* Simulation parameters (replaces SimParams, kernel.cuh:9-22, plus the
  * compile-time constants of integration_kernel.cuh:20-42 and

@@ -36,6 +36,8 @@
 #include "rigidcontactconstraint.h"
 #include "totalfluidconstraint.h"
 #include "fluidemitter.h"
+#include "contactconstraint.h"
+#include "boundaryconstraint.h"
 #undef private
 
 #include <cstdint>
@@ -274,6 +276,57 @@ int refcpu_fluid_emitter_tick(int n, int members, const double *p, const double 
         delete q;
     }
     return emitted;
+}
+
+// The reference's contact projectors on n 2-D particles (solid[i] != 0:
+// SOLID, else FLUID): p the start-of-step positions, ep the estimates;
+// masses height-scaled (Particle::scaleMass); the listed pairs (i1 < i2)
+// become RigidContactConstraint (both SOLID, no signed-distance data) or
+// ContactConstraint (simulation.cpp:186-193), the listed walls
+// BoundaryConstraint (idx, isX, lower; the box's value), each particle's
+// count its number of listed constraints; all projected once in order
+// (pairs, then walls).  Out: the estimates.
+void refcpu_contacts(int n, const double *p, const double *ep, const double *imass, const int *solid, int npairs,
+                     const int *pairs, int nwalls, const int *walls, double xmin, double xmax, double ymin,
+                     double ymax, double s_friction, double k_friction, double *ep_out) {
+    QList<Particle *> ps;
+    for (int i = 0; i < n; ++i) {
+        Particle *q = new Particle(glm::dvec2(p[2 * i], p[2 * i + 1]), 1.0, solid[i] ? SOLID : FLUID);
+        q->imass = imass[i];
+        q->ep = glm::dvec2(ep[2 * i], ep[2 * i + 1]);
+        q->sFriction = s_friction;
+        q->kFriction = k_friction;
+        q->scaleMass();
+        ps.append(q);
+    }
+    QList<Body *> bodies;
+    std::vector<int> counts(n, 0);
+    for (int k = 0; k < npairs; ++k) {
+        ++counts[pairs[2 * k]];
+        ++counts[pairs[2 * k + 1]];
+    }
+    for (int k = 0; k < nwalls; ++k) ++counts[walls[3 * k]];
+    for (int k = 0; k < npairs; ++k) {
+        const int a = pairs[2 * k], b = pairs[2 * k + 1];
+        if (solid[a] && solid[b]) {
+            RigidContactConstraint c(a, b, &bodies, false);
+            c.project(&ps, counts.data());
+        } else {
+            ContactConstraint c(a, b, false);
+            c.project(&ps, counts.data());
+        }
+    }
+    for (int k = 0; k < nwalls; ++k) {
+        const int idx = walls[3 * k], is_x = walls[3 * k + 1], lower = walls[3 * k + 2];
+        const double value = is_x ? (lower ? xmin : xmax) : (lower ? ymin : ymax);
+        BoundaryConstraint c(idx, value, is_x != 0, lower != 0, false);
+        c.project(&ps, counts.data());
+    }
+    for (int i = 0; i < n; ++i) {
+        ep_out[2 * i] = ps.at(i)->ep.x;
+        ep_out[2 * i + 1] = ps.at(i)->ep.y;
+        delete ps.at(i);
+    }
 }
 
 }  // extern "C"

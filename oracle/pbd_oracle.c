@@ -45,6 +45,7 @@ struct orc_system {
     uint32_t cap, n, cells;
     int fluid_rad;
     float h2f, collide2f, collidef;
+    float cpu_c2f; /* (diameter - EPSILON)^2 in FP32: the CPU contact test */
     double poly6, spiky, poly6_self, scorr_inv_ref, scorr_k, relax, ws, wk;
     double rands[6];
     /* particle state, original order */
@@ -169,6 +170,10 @@ orc_system *orc_create(const pbd_params *params, uint32_t cap) {
     s->h2f = hf * hf;
     s->collidef = params->particle_radius * 2.001f;
     s->collide2f = s->collidef * s->collidef;
+    {
+        const float c = 2.0f * params->particle_radius - 0.0001f;
+        s->cpu_c2f = c * c;
+    }
     s->fluid_rad = (int)ceilf(hf / params->cell_size);
     const double h = hf;
     s->poly6 = 315.0 / (64.0 * PI * pow(h, 9.0));
@@ -626,7 +631,10 @@ static int contact_visit(void *vctx, uint32_t j) {
     if (j == c->i) return 0;
     int phj = c->s->sphase[j];
     if (c->ph > PBD_PHASE_SOLID && c->ph == phj) return 0;
-    if (dist2f(c->s->sx32 + 4 * c->i, c->s->sx32 + 4 * j) < c->s->collide2f) {
+    const int cpu = (c->s->p.flags & PBD_FLAG_CPU_CONTACTS) != 0;
+    /* PBD_FLAG_CPU_CONTACTS: never two fixed particles (simulation.cpp:174) */
+    if (cpu && c->s->sx32[4 * c->i + 3] == 0.f && c->s->sx32[4 * j + 3] == 0.f) return 0;
+    if (dist2f(c->s->sx32 + 4 * c->i, c->s->sx32 + 4 * j) < (cpu ? c->s->cpu_c2f : c->s->collide2f)) {
         if (c->nb >= c->s->p.max_neighbors) return 1;
         c->list[c->nb++] = j;
     }
@@ -642,6 +650,41 @@ static void quat_rotate(const real q[4], const double v[3], real out[3]) {
     out[0] = v[0] + q[3] * t[0] + (q[1] * t[2] - q[2] * t[1]);
     out[1] = v[1] + q[3] * t[1] + (q[2] * t[0] - q[0] * t[2]);
     out[2] = v[2] + q[3] * t[2] + (q[0] * t[1] - q[1] * t[0]);
+}
+
+/* The correction and friction of RigidContactConstraint::project
+ * (rigidcontactconstraint.cpp:58-95) for the ordered pair (1, 2) with depth
+ * d along n, as seen by particle 1 (first) or 2: d n shared by the
+ * height-scaled inverse masses tmass = w e^y (Particle::scaleMass, at the
+ * start-of-step heights) and averaged over cnt (this particle's count, for
+ * both ends); then the tangential relative displacement since the step's
+ * start removed if below mu_s d (static), else cut by min(mu_k d / |dpt|,
+ * 1).  Adds to out. */
+static void rigid_contact_apply(const orc_system *s, int first, const real *x1, const real *x2, const real *p1,
+                                const real *p2, real d, const real n[3], double cnt, real out[3]) {
+    const double w1 = R_VAL(x1[3]), w2 = R_VAL(x2[3]);
+    real t1 = w1 * exp(p1[1]), t2 = w2 * exp(p2[1]);
+    real tsum = t1 + t2;
+    if (!(R_VAL(tsum) > 0.0)) return;
+    real a1 = t1 / tsum, a2 = t2 / tsum, dp1[3], dp2[3];
+    for (int k = 0; k < 3; ++k) {
+        dp1[k] = -a1 * d * n[k] / cnt;
+        dp2[k] = a2 * d * n[k] / cnt;
+        out[k] += first ? dp1[k] : dp2[k];
+    }
+    real nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    real nf[3] = {n[0] / nl, n[1] / nl, n[2] / nl}, dpf[3], dpt[3];
+    for (int k = 0; k < 3; ++k) dpf[k] = (x1[k] + dp1[k] - p1[k]) - (x2[k] + dp2[k] - p2[k]);
+    real dn = dpf[0] * nf[0] + dpf[1] * nf[1] + dpf[2] * nf[2];
+    for (int k = 0; k < 3; ++k) dpt[k] = dpf[k] - dn * nf[k];
+    real ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
+    if (ldpt < CPU_EPS) return;
+    real f = 1.0;
+    if (!(ldpt < (double)s->p.contact_static_friction * d)) {
+        f = (double)s->p.contact_kinetic_friction * d / ldpt;
+        if (f > 1.0) f = 1.0;
+    }
+    for (int k = 0; k < 3; ++k) out[k] += (first ? -a1 : a2) * dpt[k] * f;
 }
 
 /* RigidContactConstraint::project (rigidcontactconstraint.cpp:30-96) for a
@@ -683,44 +726,70 @@ static void sdf_contact(const orc_system *s, uint32_t self, uint32_t other, cons
         real dp = x12[0] * n[0] + x12[1] * n[1] + x12[2] * n[2];
         for (int k = 0; k < 3; ++k) n[k] = dp < 0.0 ? x12[k] - 2.0 * dp * n[k] : x12[k];
     }
-    const double w1 = R_VAL(x1[3]), w2 = R_VAL(x2[3]);
-    real t1 = w1 * exp(p1[1]), t2 = w2 * exp(p2[1]);
-    real tsum = t1 + t2;
+    rigid_contact_apply(s, first, x1, x2, p1, p2, d, n, cnt, out);
+}
+
+/* PBD_FLAG_CPU_CONTACTS, two solid-like particles without signed-distance
+ * data: RigidContactConstraint::project's plain branch
+ * (rigidcontactconstraint.cpp:35-41): d = diameter - |x2 - x1|, n = (x2 -
+ * x1) / |x2 - x1| for the pair ordered by original index; correction and
+ * friction as rigid_contact_apply.  Adds to out. */
+static void cpu_pair_contact(const orc_system *s, uint32_t self, uint32_t other, const real *xs, const real *xo,
+                             const real *ps, const real *po, double cnt, real out[3]) {
+    const int first = self < other;
+    const real *x1 = first ? xs : xo, *x2 = first ? xo : xs;
+    real x12[3] = {x2[0] - x1[0], x2[1] - x1[1], x2[2] - x1[2]};
+    real len = sqrt(x12[0] * x12[0] + x12[1] * x12[1] + x12[2] * x12[2]);
+    real d = 2.0 * (double)s->p.particle_radius - len;
+    if (d < CPU_EPS) return;
+    real n[3] = {x12[0] / len, x12[1] / len, x12[2] / len};
+    rigid_contact_apply(s, first, x1, x2, first ? ps : po, first ? po : ps, d, n, cnt, out);
+}
+
+/* PBD_FLAG_CPU_CONTACTS, a solid-like particle touching a fluid or gas one:
+ * ContactConstraint::project (contactconstraint.cpp:13-42) for this end:
+ * the overlap shared by the height-scaled inverse masses, averaged over the
+ * count, no friction (the fluid end is not moved: fluid takes no part in
+ * the contact pass).  Adds to out. */
+static void cpu_fluid_contact(const orc_system *s, const real *xs, const real *xo, const real *ps, const real *po,
+                              double cnt, real out[3]) {
+    real diff[3] = {xs[0] - xo[0], xs[1] - xo[1], xs[2] - xo[2]};
+    real dist = sqrt(diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]);
+    real mag = dist - 2.0 * (double)s->p.particle_radius;
+    if (R_VAL(mag) > 0.0 || R_VAL(dist) == 0.0) return;
+    real ts = xs[3] * exp(ps[1]), to = xo[3] * exp(po[1]);
+    real tsum = ts + to;
     if (!(R_VAL(tsum) > 0.0)) return;
-    real a1 = t1 / tsum, a2 = t2 / tsum, dp1[3], dp2[3];
-    for (int k = 0; k < 3; ++k) {
-        dp1[k] = -a1 * d * n[k] / cnt;
-        dp2[k] = a2 * d * n[k] / cnt;
-        out[k] += first ? dp1[k] : dp2[k];
-    }
-    real nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    real nf[3] = {n[0] / nl, n[1] / nl, n[2] / nl}, dpf[3], dpt[3];
-    for (int k = 0; k < 3; ++k) dpf[k] = (x1[k] + dp1[k] - p1[k]) - (x2[k] + dp2[k] - p2[k]);
-    real dn = dpf[0] * nf[0] + dpf[1] * nf[1] + dpf[2] * nf[2];
-    for (int k = 0; k < 3; ++k) dpt[k] = dpf[k] - dn * nf[k];
-    real ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
-    if (ldpt < CPU_EPS) return;
-    real f = 1.0;
-    if (!(ldpt < (double)s->p.contact_static_friction * d)) {
-        f = (double)s->p.contact_kinetic_friction * d / ldpt;
-        if (f > 1.0) f = 1.0;
-    }
-    for (int k = 0; k < 3; ++k) out[k] += (first ? -a1 : a2) * dpt[k] * f;
+    for (int k = 0; k < 3; ++k) out[k] += -(ts / tsum) * mag * diff[k] / (dist * cnt);
+}
+
+/* Walls a particle touches (the CPU reference's boundary detection,
+ * simulation.cpp:202-224: per axis the lower wall, else the upper). */
+static int cpu_wall_count(const orc_system *s, const real *e) {
+    const double r = s->p.particle_radius;
+    int k = 0;
+    k += (e[0] < s->p.box_min[0] + r || e[0] > s->p.box_max[0] - r);
+    k += (e[1] < s->p.box_min[1] + r || e[1] > s->p.box_max[1] - r);
+    if (!(s->p.flags & PBD_FLAG_TWOD)) k += (e[2] < s->p.box_min[2] + r || e[2] > s->p.box_max[2] - r);
+    return k;
 }
 
 /* collideD + collideCell (integration_kernel.cuh:303-462).  Pairs with zero
  * total inverse mass or zero separation are skipped (NaN in the reference). */
-static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real out[3]) {
+static double contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real out[3]) {
     ct_ctx c = {s, i, 0, s->sphase[i], list};
     int g[3];
     grid_cell(s, s->sx32 + 4 * i, g);
     for_each_candidate(s, g, 1, contact_visit, &c);
     s->nb_contact[s->sorted_idx[i]] = c.nb;
     out[0] = out[1] = out[2] = 0;
-    if (!c.nb) return;
+    const int cpu = (s->p.flags & PBD_FLAG_CPU_CONTACTS) != 0;
     const real *pi = s->sx + 4 * i;
+    /* the CPU reference averages over every constraint of the group:
+     * contacts and walls (updateCounts) */
+    const double fnb = (double)c.nb + (cpu ? (double)cpu_wall_count(s, pi) : 0.0);
+    if (!c.nb) return fnb;
     const real w = pi[3], sw = scaled_w(w, pi[1]);
-    const double fnb = (double)c.nb;
     const real *prev = s->x_old + 4 * s->sorted_idx[i];
     const int ph = s->sphase[i];
     const double cdist = (double)s->collidef;
@@ -733,6 +802,12 @@ static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real 
         if (sdf_i && phj >= PBD_PHASE_SOLID && s->sdf[4 * s->sorted_idx[j] + 3] >= 0.0) {
             const uint32_t oj = s->sorted_idx[j];
             sdf_contact(s, oi, oj, pi, pj, prev, s->x_old + 4 * oj, fnb, out);
+            continue;
+        }
+        if (cpu) {
+            const uint32_t oj = s->sorted_idx[j];
+            if (phj >= PBD_PHASE_CLOTH) cpu_pair_contact(s, oi, oj, pi, pj, prev, s->x_old + 4 * oj, fnb, out);
+            else cpu_fluid_contact(s, pi, pj, prev, s->x_old + 4 * oj, fnb, out);
             continue;
         }
         real diff[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
@@ -768,10 +843,61 @@ static void contact_delta(const orc_system *s, uint32_t i, uint32_t *list, real 
             for (int d = 0; d < 3; ++d) out[d] -= dpt[d] * f;
         }
     }
+    return fnb;
 }
 
-/* collide_world_functor (integration_kernel.cuh:57-157). */
-static void world_collide(const orc_system *s, real e[3], int phase, const real *xold) {
+/* PBD_FLAG_CPU_CONTACTS: BoundaryConstraint::project (boundaryconstraint.cpp:
+ * 14-93) for each wall passed, x then y (then z): back to the wall + r (the
+ * reference's fluid jitter left out), then the tangential part of (e -
+ * p_old) / count removed if below sqrt(mu_s) r, else cut by min(sqrt(mu_k)
+ * r / |dpt|, 1). */
+static void cpu_boundaries(const orc_system *s, real e[3], const real *xold, double count) {
+    const double r = s->p.particle_radius;
+    const int twod = (s->p.flags & PBD_FLAG_TWOD) != 0;
+    const int axes = twod ? 2 : 3;
+    for (int a = 0; a < axes; ++a) {
+        const double lo = s->p.box_min[a], hi = s->p.box_max[a];
+        double sgn;
+        if (e[a] < lo + r) {
+            e[a] = lo + r;
+            sgn = 1.0;
+        } else if (e[a] > hi - r) {
+            e[a] = hi - r;
+            sgn = -1.0;
+        } else {
+            continue;
+        }
+        real pold[3] = {xold[0], xold[1], twod ? (real)s->p.twod_z : xold[2]};
+        real dp[3], nrm[3] = {0, 0, 0};
+        nrm[a] = sgn;
+        for (int k = 0; k < 3; ++k) dp[k] = (e[k] - pold[k]) / count;
+        real dn = dp[a] * sgn;
+        real dpt[3] = {dp[0] - dn * nrm[0], dp[1] - dn * nrm[1], dp[2] - dn * nrm[2]};
+        real ldpt = sqrt(dpt[0] * dpt[0] + dpt[1] * dpt[1] + dpt[2] * dpt[2]);
+        if (ldpt < CPU_EPS) continue;
+        if (ldpt < s->ws * r) {
+            for (int k = 0; k < 3; ++k) e[k] -= dpt[k];
+        } else {
+            real f = fmin(s->wk * r / ldpt, 1.0);
+            for (int k = 0; k < 3; ++k) e[k] -= dpt[k] * f;
+        }
+    }
+    if (twod) e[2] = s->p.twod_z;
+}
+
+/* collide_world_functor (integration_kernel.cuh:57-157); with
+ * PBD_FLAG_CPU_CONTACTS the CPU reference's boundaries, averaged over
+ * `count` (contacts and walls of a contact particle; 0 = walls only). */
+static void world_collide(const orc_system *s, real e[3], int phase, const real *xold, double count) {
+    if (s->p.flags & PBD_FLAG_CPU_CONTACTS) {
+        if (count < 1.0) count = (double)cpu_wall_count(s, e);
+        if (count < 1.0) {
+            if (s->p.flags & PBD_FLAG_TWOD) e[2] = s->p.twod_z;
+            return;
+        }
+        cpu_boundaries(s, e, xold, count);
+        return;
+    }
     const double r = s->p.particle_radius, d = r;
     const double *bmin = NULL;
     double lo[3] = {s->p.box_min[0], s->p.box_min[1], s->p.box_min[2]};
@@ -826,6 +952,7 @@ static void solve_pass(orc_system *s, int mask) {
             int ph = s->sphase[i];
             real np[3] = {s->sx[4 * i], s->sx[4 * i + 1], s->sx[4 * i + 2]}, dd[3];
             int t = 0;
+            double count = 0.0;
             if ((mask & DO_FLUID) && ph == PBD_PHASE_FLUID) {
                 fluid_delta(s, i, list, dd);
                 for (int d = 0; d < 3; ++d) np[d] += dd[d];
@@ -835,14 +962,14 @@ static void solve_pass(orc_system *s, int mask) {
                 for (int d = 0; d < 3; ++d) np[d] += dd[d];
                 t = 1;
             } else if ((mask & DO_CONTACT) && ph >= PBD_PHASE_CLOTH) {
-                contact_delta(s, i, list, dd);
+                count = contact_delta(s, i, list, dd);
                 for (int d = 0; d < 3; ++d) np[d] += dd[d];
                 t = 1;
             }
             if (mask & DO_WORLD) {
                 if (!t)
                     for (int d = 0; d < 3; ++d) np[d] = s->x[4 * o + d];
-                world_collide(s, np, ph, s->x_old + 4 * o);
+                world_collide(s, np, ph, s->x_old + 4 * o, count);
                 t = 1;
             }
             if (t) {

@@ -47,6 +47,7 @@ def load():
         lib.refcpu_fluid_emitter_tick.argtypes = [I, I, PD, PD, PD, PD, PD, D, D, D, PD, D, ctypes.c_uint, PD, PD,
                                                   PD, PI, I, PD, PD]
         lib.refcpu_fluid_emitter_tick.restype = I
+        lib.refcpu_contacts.argtypes = [I, PD, PD, PD, PI, I, PI, I, PI, D, D, D, D, D, D, PD]
         _lib = lib
     return _lib
 
@@ -182,3 +183,27 @@ def fluid_emitter_tick(p, v, imass, t, lambdas, members: int, position, rate: fl
     k = min(k, max_new)
     return {"v": v_out, "imass": im_out, "t": t_out, "fluid": ph_out == 1, "clocks": clk,
             "new_p": new_p[:k], "new_v": new_v[:k]}
+
+
+def contacts(p, ep, imass, solid, pairs, walls, box, s_friction: float, k_friction: float):
+    """The reference's contact projectors once each, in order: the listed
+    pairs (i1 < i2; RigidContactConstraint between two SOLID particles,
+    else ContactConstraint), then the listed walls (idx, is_x, lower) as
+    BoundaryConstraint of the box (xmin, xmax, ymin, ymax); start positions
+    p and estimates ep (n, 2).  Returns the estimates."""
+    lib = load()
+    p = np.ascontiguousarray(p, np.float64).reshape(-1, 2)
+    n = p.shape[0]
+    ep = np.ascontiguousarray(ep, np.float64).reshape(n, 2)
+    imass = np.ascontiguousarray(imass, np.float64).reshape(n)
+    solid = np.ascontiguousarray(solid, np.int32).reshape(n)
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    walls = np.ascontiguousarray(walls, np.int32).reshape(-1, 3)
+    out = np.empty((n, 2))
+    pd = ctypes.POINTER(ctypes.c_double)
+    pi = ctypes.POINTER(ctypes.c_int)
+    lib.refcpu_contacts(n, p.ctypes.data_as(pd), ep.ctypes.data_as(pd), imass.ctypes.data_as(pd),
+                        solid.ctypes.data_as(pi), pairs.shape[0], pairs.ctypes.data_as(pi), walls.shape[0],
+                        walls.ctypes.data_as(pi), float(box[0]), float(box[1]), float(box[2]), float(box[3]),
+                        float(s_friction), float(k_friction), out.ctypes.data_as(pd))
+    return out

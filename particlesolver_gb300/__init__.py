@@ -22,7 +22,7 @@ __all__ = [
     "PbdParams", "PbdError", "ParticleSystem", "load_library", "default_params", "header_functions",
     "PHASE_FLUID", "PHASE_GAS", "PHASE_CLOTH", "PHASE_SOLID", "PHASE_RIGID",
     "FLAG_TWOD", "FLAG_DENSITY_NEIGHBOR_MASS", "FLAG_DELTA_OVER_RHO0", "FLAG_DISTANCE_MASS_WEIGHTED",
-    "FLAG_KERNEL_UNITS", "FLAG_SKIP_FIXED_NEIGHBORS", "FLAG_DELTA_OVER_COUNT", "PARAM_DEFAULTS", "host_params",
+    "FLAG_KERNEL_UNITS", "FLAG_SKIP_FIXED_NEIGHBORS", "FLAG_DELTA_OVER_COUNT", "FLAG_CPU_CONTACTS", "PARAM_DEFAULTS", "host_params",
 ]
 
 PHASE_FLUID, PHASE_GAS, PHASE_CLOTH, PHASE_SOLID, PHASE_RIGID = 0, 1, 2, 3, 4
@@ -33,6 +33,7 @@ FLAG_DISTANCE_MASS_WEIGHTED = 1 << 3
 FLAG_KERNEL_UNITS = 1 << 4
 FLAG_SKIP_FIXED_NEIGHBORS = 1 << 5
 FLAG_DELTA_OVER_COUNT = 1 << 6
+FLAG_CPU_CONTACTS = 1 << 7
 
 HEADER = _build.ROOT / "include" / "pbd.h"
 

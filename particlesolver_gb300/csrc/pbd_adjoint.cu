@@ -758,17 +758,19 @@ cudaError_t grow(T **p, size_t &have, size_t want) {
 }
 
 // The adjoint covers every stage of the step except the gas phase, the
-// signed-distance rigid contact and the CPU reference's PBF rules.
+// signed-distance rigid contact and the CPU reference's PBF and contact
+// rules.
 int differentiable(pbd_system *s) {
     if (s->n_gas)
         return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED, "the adjoint does not cover the gas phase (the system holds gas particles)");
     if (s->any_sdf)
         return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED, "the adjoint does not cover the signed-distance rigid contact (a body has sdf data)");
     for (const pbd_scene &sc : s->scenes)
-        if (sc.params.flags & (PBD_FLAG_SKIP_FIXED_NEIGHBORS | PBD_FLAG_DELTA_OVER_COUNT))
+        if (sc.params.flags & (PBD_FLAG_SKIP_FIXED_NEIGHBORS | PBD_FLAG_DELTA_OVER_COUNT | PBD_FLAG_CPU_CONTACTS))
             return pbd_internal_fail(s, PBD_ERR_UNSUPPORTED,
                                      "the adjoint does not cover the CPU reference's PBF neighbour and divisor rules "
-                                     "(PBD_FLAG_SKIP_FIXED_NEIGHBORS, PBD_FLAG_DELTA_OVER_COUNT)");
+                                     "or its contact projectors (PBD_FLAG_SKIP_FIXED_NEIGHBORS, "
+                                     "PBD_FLAG_DELTA_OVER_COUNT, PBD_FLAG_CPU_CONTACTS)");
     return PBD_OK;
 }
 

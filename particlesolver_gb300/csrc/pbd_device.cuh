@@ -22,6 +22,7 @@ enum : uint32_t {
     kFlagKernelUnits = 1u << 4,
     kFlagSkipFixedNeighbors = 1u << 5,
     kFlagDeltaOverCount = 1u << 6,
+    kFlagCpuContacts = 1u << 7,
     // Set by the host, never by the caller: the system holds gas particles,
     // so the prediction applies the per-particle force and the gas gravity
     // and keeps the step's velocity v' for the gas terms.

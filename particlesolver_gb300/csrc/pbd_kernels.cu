@@ -808,6 +808,86 @@ constexpr float kEpsCpu = 0.0001f;
 // contact friction does.  Friction: the tangential relative displacement
 // since the step's start, removed if below sqrt(mu_s mu_s) d (static), else
 // cut by min(sqrt(mu_k mu_k) d / |dpt|, 1).
+// The correction and friction of RigidContactConstraint::project
+// (rigidcontactconstraint.cpp:58-95) for the ordered pair (1, 2) with depth
+// d along n, as seen by particle 1 (first) or 2: d n shared by the
+// height-scaled inverse masses tmass = w e^y (Particle::scaleMass,
+// particle.h:67-73, at the start-of-step heights p.y; formed as the
+// overflow-free shares tmass_k / (tmass_1 + tmass_2)) and averaged over
+// the contact count cnt (this particle's, for both ends: the Jacobi form
+// of the reference's sequential projection, exact when each particle has
+// one constraint); then the tangential relative displacement since the
+// step's start removed if below sqrt(mu_s mu_s) d (static), else cut by
+// min(sqrt(mu_k mu_k) d / |dpt|, 1).  cs, ck: the contact friction
+// coefficients.  One compiled copy (not inlined), so that the batched and
+// the single-scene solve kernels round its arithmetic alike.
+__device__ __noinline__ float3 rigid_contact_apply(float cs, float ck, bool first, float3 x1, float3 x2, float3 p1,
+                                                   float3 p2, float w1, float w2, float d, float3 n, float cnt) {
+    const float m = fmaxf(p1.y, p2.y);
+    const float t1 = w1 * expf(p1.y - m), t2 = w2 * expf(p2.y - m);
+    const float tsum = t1 + t2;
+    if (!(tsum > 0.f)) return make_float3(0.f, 0.f, 0.f);
+    const float a1 = t1 / tsum, a2 = t2 / tsum;
+    const float3 dp1 = n * (-a1 * d / cnt), dp2 = n * (a2 * d / cnt);
+    float3 out = first ? dp1 : dp2;
+    const float3 nf = n * rsqrtf(dot3(n, n));
+    // (x1 + dp1 - p1) - (x2 + dp2 - p2), grouped so that the large
+    // coordinates cancel before the small corrections are added
+    const float3 dpf = ((x1 - p1) - (x2 - p2)) + (dp1 - dp2);
+    const float3 dpt = dpf - nf * dot3(dpf, nf);
+    const float ldpt = len3(dpt);
+    if (ldpt < kEpsCpu) return out;
+    const float3 slip = (ldpt < cs * d) ? dpt : dpt * fminf(ck * d / ldpt, 1.f);
+    out += first ? slip * -a1 : slip * a2;
+    return out;
+}
+
+// PBD_FLAG_CPU_CONTACTS, a pair of solid-like particles without
+// signed-distance data: RigidContactConstraint::project's plain branch
+// (rigidcontactconstraint.cpp:35-41): d = diameter - |x2 - x1| (nothing
+// below EPSILON), n = (x2 - x1) / |x2 - x1|, with the pair ordered by
+// original index; correction and friction as rigid_contact_apply.
+__device__ __forceinline__ float3 cpu_pair_contact(const DevParams &P, uint32_t self, uint32_t other, float3 xs,
+                                                   float3 xo, float3 ps, float3 po, float ws, float wo, float cnt) {
+    const bool first = self < other;
+    const float3 x1 = first ? xs : xo, x2 = first ? xo : xs;
+    const float3 x12 = x2 - x1;
+    const float len = len3(x12);
+    const float d = 2.f * P.r - len;
+    if (d < kEpsCpu) return make_float3(0.f, 0.f, 0.f);
+    return rigid_contact_apply(P.cs, P.ck, first, x1, x2, first ? ps : po, first ? po : ps, first ? ws : wo,
+                               first ? wo : ws, d, x12 / len, cnt);
+}
+
+// PBD_FLAG_CPU_CONTACTS, a solid-like particle touching a fluid or gas one:
+// ContactConstraint::project (contactconstraint.cpp:13-42) for this
+// particle's end: the overlap diameter - |x_s - x_o| shared by the
+// height-scaled inverse masses, averaged over the count, no friction (the
+// fluid end is not moved here: fluid takes no part in the contact pass, as
+// on the reference GPU).
+__device__ __forceinline__ float3 cpu_fluid_contact(const DevParams &P, float3 xs, float3 xo, float3 ps, float3 po,
+                                                    float ws, float wo, float cnt) {
+    const float3 diff = xs - xo;
+    const float dist = len3(diff);
+    const float mag = dist - 2.f * P.r;
+    if (mag > 0.f || dist == 0.f) return make_float3(0.f, 0.f, 0.f);
+    const float m = fmaxf(ps.y, po.y);
+    const float ts = ws * expf(ps.y - m), to = wo * expf(po.y - m);
+    const float tsum = ts + to;
+    if (!(tsum > 0.f)) return make_float3(0.f, 0.f, 0.f);
+    return diff * (-(ts / tsum) * mag / (dist * cnt));
+}
+
+// Walls a particle touches at e (the CPU reference's boundary detection,
+// simulation.cpp:202-224: per axis the lower wall, else the upper one).
+__device__ __forceinline__ uint32_t cpu_wall_count(const DevParams &P, float3 e) {
+    uint32_t k = 0;
+    k += (e.x < P.bmin.x + P.r || e.x > P.bmax.x - P.r) ? 1u : 0u;
+    k += (e.y < P.bmin.y + P.r || e.y > P.bmax.y - P.r) ? 1u : 0u;
+    if (!(P.flags & kFlagTwoD)) k += (e.z < P.bmin.z + P.r || e.z > P.bmax.z - P.r) ? 1u : 0u;
+    return k;
+}
+
 __device__ __forceinline__ float3 sdf_contact(const DevParams &P, uint32_t self, uint32_t other, float3 xs,
                                               float3 xo, float3 ps, float3 po, float ws, float wo, float ds,
                                               float dso, float3 ns, float3 no, float cnt) {
@@ -835,23 +915,7 @@ __device__ __forceinline__ float3 sdf_contact(const DevParams &P, uint32_t self,
         const float dp = dot3(x12, n);
         n = dp < 0.f ? x12 - n * (2.f * dp) : x12;
     }
-    const float m = fmaxf(p1.y, p2.y);
-    const float t1 = w1 * expf(p1.y - m), t2 = w2 * expf(p2.y - m);
-    const float tsum = t1 + t2;
-    if (!(tsum > 0.f)) return make_float3(0.f, 0.f, 0.f);
-    const float a1 = t1 / tsum, a2 = t2 / tsum;
-    const float3 dp1 = n * (-a1 * d / cnt), dp2 = n * (a2 * d / cnt);
-    float3 out = first ? dp1 : dp2;
-    const float3 nf = n * rsqrtf(dot3(n, n));
-    // (x1 + dp1 - p1) - (x2 + dp2 - p2), grouped so that the large
-    // coordinates cancel before the small corrections are added
-    const float3 dpf = ((x1 - p1) - (x2 - p2)) + (dp1 - dp2);
-    const float3 dpt = dpf - nf * dot3(dpf, nf);
-    const float ldpt = len3(dpt);
-    if (ldpt < kEpsCpu) return out;
-    const float3 slip = (ldpt < P.cs * d) ? dpt : dpt * fminf(P.ck * d / ldpt, 1.f);
-    out += first ? slip * -a1 : slip * a2;
-    return out;
+    return rigid_contact_apply(P.cs, P.ck, first, x1, x2, p1, p2, w1, w2, d, n, cnt);
 }
 
 // collideD + collideCell (integration_kernel.cuh:303-462): contacts of a
@@ -874,21 +938,31 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
                                                 const SortedAttr *__restrict__ sattr,
                                                 const uint32_t *__restrict__ sidx,
                                                 const uint32_t *__restrict__ cell_first,
-                                                const float4 *__restrict__ x_old, const RigidSdf &rs) {
+                                                const float4 *__restrict__ x_old, const RigidSdf &rs,
+                                                float &count_out) {
     const float3 pi = f3(pi4);
     const int3 g = grid_pos(P, pi);
-    auto test = [&](uint32_t j, const float4 &, float d2) {
-        if (j == i || !(d2 < P.collide2)) return false;
+    const bool cpu = (P.flags & kFlagCpuContacts) != 0u;
+    // the CPU reference's contact test: closer than a diameter - EPSILON,
+    // and never between two fixed particles (simulation.cpp:171-184)
+    const float cpu_c = 2.f * P.r - kEpsCpu;
+    const float reach2 = cpu ? cpu_c * cpu_c : P.collide2;
+    auto test = [&](uint32_t j, const float4 &qj, float d2) {
+        if (j == i || !(d2 < reach2)) return false;
+        if (cpu && pi4.w == 0.f && qj.w == 0.f) return false;
         const int phj = sattr[j].phase;
         return !(ph > kSolid && ph == phj);
     };
-    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, P.max_nb,
+    const uint32_t nb = group_walk<TPP>(P, G, pi, g, 1, reach2, P.trim_contact, sx, cell_first, P.max_nb,
                                         test, [](uint32_t, const float4 &, float) {});
+    // the CPU reference averages over every constraint of the group:
+    // contacts and walls (updateCounts)
+    const float fnb = (float)nb + (cpu ? (float)cpu_wall_count(P, pi) : 0.f);
+    count_out = fnb;
     float3 delta = make_float3(0.f, 0.f, 0.f);
     if (nb == 0) return delta;
     const float w = pi4.w;
     const float3 prev = f3(x_old[orig]);
-    const float fnb = (float)nb;
     // this particle's signed-distance data, its normal in the world frame
     float4 si = make_float4(0.f, 0.f, 0.f, -1.f);
     float3 ni = make_float3(0.f, 0.f, 0.f);
@@ -896,7 +970,7 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
         si = rs.sdf[orig];
         if (si.w >= 0.f) ni = quat_rotate(rs.quat[rs.body[orig]], f3(si));
     }
-    group_walk<TPP>(P, G, pi, g, 1, P.collide2, P.trim_contact, sx, cell_first, nb, test,
+    group_walk<TPP>(P, G, pi, g, 1, reach2, P.trim_contact, sx, cell_first, nb, test,
                     [&](uint32_t j, const float4 &pj4, float) {
         const int phj = sattr[j].phase;
         if (si.w >= 0.f && phj >= kSolid) {
@@ -907,6 +981,12 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
                                      quat_rotate(rs.quat[rs.body[oj]], f3(sj)), fnb);
                 return;
             }
+        }
+        if (cpu) {
+            const uint32_t oj = sidx[j];
+            if (phj >= kCloth) delta += cpu_pair_contact(P, orig, oj, pi, f3(pj4), prev, f3(x_old[oj]), w, pj4.w, fnb);
+            else delta += cpu_fluid_contact(P, pi, f3(pj4), prev, f3(x_old[oj]), w, pj4.w, fnb);
+            return;
         }
         const float3 pj = f3(pj4);
         const float3 diff = pi - pj;
@@ -1434,8 +1514,53 @@ __device__ __forceinline__ float3 fluid_delta_list(const DevParams &P, uint32_t 
 // collide_world_functor (integration_kernel.cuh:57-157): clamp into the box
 // shrunk by r with the jitter uniforms, then boundary friction against the
 // start-of-step position for phases >= CLOTH.
+// PBD_FLAG_CPU_CONTACTS: BoundaryConstraint::project (cpu/src/constraint/
+// boundaryconstraint.cpp:14-93) for each wall the particle passed, x then y
+// (then z), in turn: back to the wall + r (the reference's extra jitter of
+// fluid and gas, frand() * .003, left out), then the tangential part of
+// (e - p_old) / count removed if below sqrt(mu_s) r, else cut by
+// min(sqrt(mu_k) r / |dpt|, 1).  count: the particle's contacts and walls.
+__device__ __forceinline__ float3 cpu_boundaries(const DevParams &P, float3 e, float3 pold, float count) {
+    const float r = P.r;
+    const int axes = (P.flags & kFlagTwoD) ? 2 : 3;
+    if (P.flags & kFlagTwoD) pold.z = P.twod_z;
+    for (int a = 0; a < axes; ++a) {
+        const float lo = a == 0 ? P.bmin.x : a == 1 ? P.bmin.y : P.bmin.z;
+        const float hi = a == 0 ? P.bmax.x : a == 1 ? P.bmax.y : P.bmax.z;
+        float v = a == 0 ? e.x : a == 1 ? e.y : e.z;
+        float sgn;
+        if (v < lo + r) {
+            v = lo + r;
+            sgn = 1.f;
+        } else if (v > hi - r) {
+            v = hi - r;
+            sgn = -1.f;
+        } else {
+            continue;
+        }
+        if (a == 0) e.x = v;
+        else if (a == 1) e.y = v;
+        else e.z = v;
+        const float3 nrm = make_float3(a == 0 ? sgn : 0.f, a == 1 ? sgn : 0.f, a == 2 ? sgn : 0.f);
+        const float3 dp = (e - pold) / count;
+        const float3 dpt = dp - nrm * dot3(dp, nrm);
+        const float ldpt = len3(dpt);
+        if (ldpt < kEpsCpu) continue;
+        if (ldpt < P.ws * r) e -= dpt;
+        else e -= dpt * fminf(P.wk * r / ldpt, 1.f);
+    }
+    if (P.flags & kFlagTwoD) e.z = P.twod_z;
+    return e;
+}
+
 __device__ __forceinline__ float3 world_collide(const DevParams &P, float3 e, int phase,
-                                                const float4 *__restrict__ x_old, uint32_t orig) {
+                                                const float4 *__restrict__ x_old, uint32_t orig,
+                                                float count = 0.f) {
+    if (P.flags & kFlagCpuContacts) {
+        if (count < 1.f) count = (float)cpu_wall_count(P, e);
+        if (count < 1.f) return (P.flags & kFlagTwoD) ? make_float3(e.x, e.y, P.twod_z) : e;
+        return cpu_boundaries(P, e, f3(x_old[orig]), count);
+    }
     const float d = P.r;
     float eps = (phase < kSolid) ? d * 0.01f : d * 0.f;
     float3 nrm = make_float3(0.f, 0.f, 0.f);
@@ -1512,6 +1637,7 @@ __global__ void __launch_bounds__(kBlock, solve_min_blocks(TPP, B, NOFLUID)) k_s
     const float4 pi4 = sx[i];
     float3 np = f3(pi4);
     bool touched = false;
+    float count = 0.f;  // contacts (and, with PBD_FLAG_CPU_CONTACTS, walls) of a contact particle
     if (!NOFLUID && (mask & kDoFluid) && a.phase == kFluid) {
         if constexpr (!NOFLUID) {
             if (TPP == 1 && use_list) np = np + fluid_delta_list(P, i, np, a.rho0, sxl, sx, cell_first, L);
@@ -1522,13 +1648,13 @@ __global__ void __launch_bounds__(kBlock, solve_min_blocks(TPP, B, NOFLUID)) k_s
         if constexpr (!NOFLUID) np = np + gas_delta<TPP>(P, G, i, np, a.rho0, sx, sattr, cell_first, gas);
         touched = true;
     } else if ((mask & kDoContact) && a.phase >= kCloth) {
-        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old, rs);
+        np = np + contact_delta<TPP>(P, G, i, pi4, a.phase, orig, sx, sattr, sidx, cell_first, x_old, rs, count);
         touched = true;
     }
     if (G.lane != 0) return;
     if (mask & kDoWorld) {
         if (!touched) np = f3(x[orig]);
-        np = world_collide(P, np, a.phase, x_old, orig);
+        np = world_collide(P, np, a.phase, x_old, orig, count);
         touched = true;
     }
     if (touched) x[orig] = make_float4(np.x, np.y, np.z, pi4.w);

@@ -18,6 +18,7 @@ FLAG_DENSITY_NEIGHBOR_MASS = 1 << 1
 FLAG_KERNEL_UNITS = 1 << 4
 FLAG_SKIP_FIXED_NEIGHBORS = 1 << 5
 FLAG_DELTA_OVER_COUNT = 1 << 6
+FLAG_CPU_CONTACTS = 1 << 7
 
 
 def splitmix64(seed: int, count: int) -> np.ndarray:
@@ -483,7 +484,8 @@ def pbf_block(count: int, h: float = 0.1, seed: int = 2024, iterations: int = 4,
 
 
 def granular_column(count: int = 1600, width: int | None = None, radius: float = 0.25, seed: int = 1600,
-                    iterations: int = 3, static_friction: float = 0.5, kinetic_friction: float = 0.3) -> Scene:
+                    iterations: int = 3, static_friction: float = 0.5, kinetic_friction: float = 0.3,
+                    cpu_contacts: bool = False) -> Scene:
     """2-D granular column collapse: `count` solid particles (unit inverse
     mass) on a lattice of spacing 2r, `width` columns (default round(sqrt
     (count)), 40 for 1,600), rows from y = r up, the top row possibly
@@ -492,7 +494,9 @@ def granular_column(count: int = 1600, width: int | None = None, radius: float =
     to 0 (FLAG_TWOD), 3 iterations, dt = 1/60.  Cell 2r as the reference;
     the grid covers the box's width and the column's height and is one cell
     deep (in 2-D the particles share one z layer and the stencils walk only
-    that layer)."""
+    that layer).  cpu_contacts: the CPU reference's contact and boundary
+    projectors (PBD_FLAG_CPU_CONTACTS) and its open-topped box (walls at
+    x = +-half and y = 0; the top at 1e6), as its sand pile runs them."""
     d = 2.0 * radius
     width = int(width or max(1, round(math.sqrt(count))))
     rows = -(-count // width)
@@ -515,8 +519,11 @@ def granular_column(count: int = 1600, width: int | None = None, radius: float =
                   max_neighbors=500, contact_static_friction=static_friction,
                   contact_kinetic_friction=kinetic_friction, wall_static_friction=static_friction,
                   wall_kinetic_friction=kinetic_friction, twod_z=0.0, flags=FLAG_TWOD)
+    if cpu_contacts:
+        params["flags"] = FLAG_TWOD | FLAG_CPU_CONTACTS
+        params["box_max"] = [half, 1e6, 1.0]
     return Scene("granular_column", params, pos_w, np.full(count, PHASE_SOLID, np.int32), dt=1.0 / 60.0,
-                 info=dict(width=width, rows=rows, seed=seed))
+                 info=dict(width=width, rows=rows, seed=seed, cpu_contacts=cpu_contacts))
 
 
 def smoke_box(spacing: float = 0.63, half: float = 4.0, twod: bool = False, density: float | None = None,
@@ -633,6 +640,58 @@ def cpu_fluid_box(spacing: float = 0.7, seed: int = 890, density: float = 1.75, 
                   flags=FLAG_TWOD | FLAG_DENSITY_NEIGHBOR_MASS | FLAG_SKIP_FIXED_NEIGHBORS | FLAG_DELTA_OVER_COUNT)
     return Scene("cpu_fluid_box", params, pos_w, phase, rest_density=rho0, dt=1.0 / 60.0,
                  info=dict(fluid=n, solids=int(pos_w.shape[0] - n), seed=seed))
+
+
+CPU_CONTACT_BOX = (-20.0, 400.0, 0.0, 50.0)  # xmin, xmax, ymin, ymax of the contact pinning case
+
+
+def cpu_contact_case(pairs: int = 24, fluid_pairs: int = 12, walls: int = 16, radius: float = 0.25,
+                     seed: int = 31) -> dict:
+    """2-D pinning case of the CPU reference's contact projectors, each
+    particle in exactly one constraint (so the reference's sequential
+    projection and a Jacobi pass coincide): `pairs` pairs of solid grains
+    touching at a centre distance U(1.5 r, 1.95 r) in a seeded direction,
+    `fluid_pairs` grains each touching one fluid particle the same way, and
+    `walls` grains each past one wall of the box CPU_CONTACT_BOX by U(0.1 r,
+    0.8 r) (lower and upper x, lower and upper y in turn; at most 17 so
+    that no grain is past two walls).  Objects stand 10 apart along x at
+    heights 3 + U(0, 4) (the masses are height-scaled); estimates = start +
+    U(-0.08 r, 0.08 r); inverse masses U(0.5, 2).  Returns the start and
+    estimate positions (n, 2), inverse masses, solid flags, the touching
+    pairs (i1 < i2) and the walls (idx, is_x, lower)."""
+    xmin, xmax, ymin, ymax = CPU_CONTACT_BOX
+    start, solid, plist, wlist = [], [], [], []
+    u = uniform(seed, (pairs + fluid_pairs, 4), 0.0, 1.0)
+    for k in range(pairs + fluid_pairs):
+        base = np.array([10.0 * k, 3.0 + 4.0 * u[k, 0]])
+        ang = 2.0 * np.pi * u[k, 1]
+        gap = (1.5 + 0.45 * u[k, 2]) * radius
+        i = len(start)
+        start += [base, base + gap * np.array([np.cos(ang), np.sin(ang)])]
+        solid += [1, 1 if k < pairs else 0]
+        plist.append((i, i + 1))
+    wu = uniform(seed + 1, (walls, 2), 0.0, 1.0)
+    for k in range(walls):
+        side = k % 4
+        depth = (0.1 + 0.7 * wu[k, 0]) * radius
+        along = 10.0 + 4.0 * (k // 4) + wu[k, 1]  # walls' grains 3 or more apart
+        if side == 0:
+            q, is_x, lower = (xmin + radius - depth, along), 1, 1
+        elif side == 1:
+            q, is_x, lower = (xmax - radius + depth, along), 1, 0
+        elif side == 2:
+            q, is_x, lower = (40.0 + 20.0 * k, ymin + radius - depth), 0, 1
+        else:
+            q, is_x, lower = (40.0 + 20.0 * k, ymax - radius + depth), 0, 0
+        wlist.append((len(start), is_x, lower))
+        start.append(np.array(q))
+        solid.append(1)
+    start = np.asarray(start)
+    n = start.shape[0]
+    est = start + uniform(seed + 2, (n, 2), -0.08 * radius, 0.08 * radius)
+    return dict(start=start, estimate=est, imass=uniform(seed + 3, (n,), 0.5, 2.0),
+                solid=np.asarray(solid, np.int32), pairs=np.asarray(plist, np.int32),
+                walls=np.asarray(wlist, np.int32))
 
 
 def batched_scenes(count: int = 512, seed: int = 512, lo: int = 1024, hi: int = 65536) -> list:

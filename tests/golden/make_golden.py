@@ -19,7 +19,10 @@ grains and the reference's TotalFluidConstraint::project
 (totalfluidconstraint.cpp:41-116) estimates and lambdas after 1 and 3
 calls.  fluid_emitter.npz holds FluidEmitter::tick (fluidemitter.cpp:13-77)
 emission counts over 40 ticks and one solidification tick of a seeded
-state.
+state.  cpu_contacts.npz holds 2-D grains each in one contact or wall
+constraint and the reference's RigidContactConstraint / ContactConstraint /
+BoundaryConstraint results; granular_pile.npz the reference Simulation's
+granular column after 600 steps.
 """
 from __future__ import annotations
 
@@ -180,6 +183,35 @@ def emitter_fixture() -> dict:
                 v_out=o["v"], imass_out=o["imass"], fluid_out=o["fluid"])
 
 
+def contact_fixture() -> dict:
+    """The CPU-contact pinning case (workloads.cpu_contact_case, seed 31,
+    inputs rounded to FP32) and the reference's RigidContactConstraint /
+    ContactConstraint / BoundaryConstraint estimates, with mu 0.4 / 0.3 and
+    0.01 / 0.005."""
+    from oracle import refcpu
+
+    case = W.cpu_contact_case(seed=31)
+    # inputs rounded to FP32 first, so that the CUDA path sees them exactly
+    for key in ("start", "estimate", "imass"):
+        case[key] = case[key].astype(np.float32).astype(np.float64)
+    out = dict(case)
+    for tag, fr in (("f1", (0.4, 0.3)), ("f2", (0.01, 0.005))):
+        out[f"reference_{tag}"] = refcpu.contacts(case["start"], case["estimate"], case["imass"], case["solid"],
+                                                  case["pairs"], case["walls"], W.CPU_CONTACT_BOX, *fr)
+    return out
+
+
+def pile_fixture() -> dict:
+    """The 2-D granular column (1,600 grains) after 600 steps of the
+    reference's own Simulation: positions."""
+    from oracle import refcpu
+
+    sc = W.granular_column(cpu_contacts=True)
+    r = refcpu.RefCPU(sc.pos_w[:, :2], mass=1.0, s_friction=0.5, k_friction=0.3)
+    r.tick(sc.dt, 600)
+    return dict(start=sc.pos_w[:, :2], steps=600, positions=r.state()[0])
+
+
 def main():
     if not refgpu.available():
         raise SystemExit("reference sources not found")
@@ -187,7 +219,8 @@ def main():
 
     if refcpu.available():
         for name, fix in (("gas_project", gas_fixture), ("sdf_contacts", sdf_fixture),
-                          ("fluid_project", fluid_fixture), ("fluid_emitter", emitter_fixture)):
+                          ("fluid_project", fluid_fixture), ("fluid_emitter", emitter_fixture),
+                          ("cpu_contacts", contact_fixture), ("granular_pile", pile_fixture)):
             path = HERE / f"{name}.npz"
             np.savez_compressed(path, **fix())
             print(path, path.stat().st_size, "bytes")

@@ -278,3 +278,54 @@ def solidify_rule(y, speed_of, lam, timer, fluid, dt: float, speed: float = 0.06
     turn = down & (t <= 0)
     t[turn] = 0.0
     return t, turn
+
+
+def cpu_contact_params(static_friction: float = 0.4, kinetic_friction: float = 0.3) -> dict:
+    """Parameters of the CPU-contact pinning case (workloads.cpu_contact_case):
+    2-D, PBD_FLAG_CPU_CONTACTS, its box, no gravity, r = 0.25."""
+    from particlesolver_gb300 import workloads as W
+
+    xmin, xmax, ymin, ymax = W.CPU_CONTACT_BOX
+    return dict(particle_radius=0.25, kernel_radius=1.0, cell_size=0.5, grid_size=[1024, 128, 1],
+                world_origin=[xmin, ymin, -1.0], gravity=[0.0, 0.0, 0.0], box_min=[xmin, ymin, -1.0],
+                box_max=[xmax, ymax, 1.0], iterations=1, max_dt=1.0, contact_static_friction=static_friction,
+                contact_kinetic_friction=kinetic_friction, wall_static_friction=static_friction,
+                wall_kinetic_friction=kinetic_friction, twod_z=0.0, max_neighbors=500,
+                flags=W.FLAG_TWOD | W.FLAG_CPU_CONTACTS)
+
+
+def load_cpu_contact_pin(system, case, fp32_inputs: bool = False):
+    """One contact and wall pass of the CPU-contact pinning case on `system`
+    (the CUDA system or the oracle): the start positions become x_old by a
+    prediction at rest, then the estimates are set and the grid, the
+    contact pass and the wall pass run.  fp32_inputs rounds the inputs to
+    FP32 first.  Returns the positions (n, 2)."""
+    from particlesolver_gb300 import workloads as W
+
+    n = len(case["start"])
+    rnd = (lambda a: a.astype(np.float32).astype(np.float64)) if fp32_inputs else (lambda a: a)  # noqa: E731
+    st = np.zeros((n, 4))
+    st[:, :2] = case["start"]
+    st[:, 3] = case["imass"]
+    st = rnd(st)
+    phase = np.where(case["solid"] != 0, W.PHASE_SOLID, W.PHASE_FLUID).astype(np.int32)
+    system.add_particles(st, None, phase, None)
+    system.set_velocities(np.zeros((n, 4)))
+    system.integrate(1.0 / 60.0)
+    est = st.copy()
+    est[:, :2] = case["estimate"]
+    est = rnd(est)
+    system.set_positions(est)
+    system.build_grid()
+    system.collide()
+    system.collide_world()
+    return np.asarray(system.positions(), np.float64)[:, :2]
+
+
+def pile_invariants(xy) -> dict:
+    """Invariants of a 2-D granular pile, whose particle trajectories are
+    chaotic: mean height, horizontal spread (standard deviation of x),
+    runout (largest |x|) and the 99th percentile of the height."""
+    xy = np.asarray(xy, np.float64)
+    return {"mean_height": float(xy[:, 1].mean()), "spread": float(xy[:, 0].std()),
+            "runout": float(np.abs(xy[:, 0]).max()), "top": float(np.percentile(xy[:, 1], 99))}

@@ -155,3 +155,20 @@ def test_emitter_rules_match_reference_golden():
     np.testing.assert_array_equal(d["fluid_out"], fluid & ~turn)
     np.testing.assert_allclose(d["t_out"][fluid], t[fluid], rtol=0, atol=1e-12)
     assert np.all(d["imass_out"][turn] == 0.0) and np.all(d["v_out"][turn] == 0.0)
+
+
+@pytest.mark.parametrize("tag,friction", [("f1", (0.4, 0.3)), ("f2", (0.01, 0.005))])
+def test_cpu_contacts_match_reference_golden(tag, friction):
+    """The oracle's CPU contact projectors against the reference's own
+    RigidContactConstraint (plain branch), ContactConstraint and
+    BoundaryConstraint (tests/golden/cpu_contacts.npz): grains in one
+    constraint each, static and kinetic friction, to 1e-7."""
+    from helpers import cpu_contact_params, load_cpu_contact_pin, norm_err
+
+    d = dict(np.load(GOLDEN / "cpu_contacts.npz"))
+    o = Oracle(params_nolib(cpu_contact_params(*friction)), len(d["start"]))
+    pos = load_cpu_contact_pin(o, d)
+    grain = d["solid"] != 0
+    d_ref = d[f"reference_{tag}"] - d["estimate"]
+    assert np.max(np.abs(d_ref[grain])) > 0.05
+    assert norm_err(pos[grain] - d["estimate"][grain], d_ref[grain]) < 1e-7

@@ -287,3 +287,55 @@ def test_fluid_emitter_matches_reference_cpu():
         assert np.all(out["imass"][turn] == 0.0) and np.all(out["imass"][~turn] == 1.0)
         assert np.all(out["v"][turn] == 0.0)
         np.testing.assert_array_equal(out["v"][~turn], v[~turn])
+
+
+@pytest.mark.parametrize("seed,friction", [(31, (0.4, 0.3)), (34, (0.4, 0.3)), (35, (0.01, 0.005))])
+def test_cpu_contacts_match_reference_cpu(seed, friction):
+    """The oracle's CPU contact projectors (PBD_FLAG_CPU_CONTACTS) against
+    the reference's own RigidContactConstraint (plain branch),
+    ContactConstraint and BoundaryConstraint compiled from the reference
+    tree, on seeded 2-D grains each in exactly one constraint (touching
+    grain pairs, grains touching fluid, grains past a wall), with static and
+    kinetic friction: the grains' corrections to 1e-7 (FP64 both sides; the
+    fluid ends, which the contact pass leaves to the fluid solve, stay)."""
+    from helpers import cpu_contact_params, load_cpu_contact_pin
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    case = W.cpu_contact_case(seed=seed)
+    ref = refcpu.contacts(case["start"], case["estimate"], case["imass"], case["solid"], case["pairs"],
+                          case["walls"], W.CPU_CONTACT_BOX, *friction)
+    o = Oracle(params_nolib(cpu_contact_params(*friction)), len(case["start"]))
+    pos = load_cpu_contact_pin(o, case)
+    grain = case["solid"] != 0
+    d_ref = ref - case["estimate"]
+    assert np.max(np.abs(d_ref[grain])) > 0.05
+    assert norm_err(pos[grain] - case["estimate"][grain], d_ref[grain]) < 1e-7
+    assert np.max(np.abs(pos[~grain] - case["estimate"][~grain])) == 0.0
+
+
+def test_cpu_contact_column_settles_like_the_reference():
+    """The 2-D granular column (1,600 grains, mu_s 0.5, mu_k 0.3, 600 steps of
+    1/60 s) with the CPU contact projectors in the oracle's Jacobi pass,
+    against the reference's own Simulation (sequential projection, cpu/src/
+    simulation.cpp:115-369): the settled pile's mean height, spread and
+    99th-percentile height within 10 %, runout within 2 %.  (The default
+    contact model, the GPU reference's, leaves the column standing: mean
+    height 9.0 against 5.1.)"""
+    from helpers import pile_invariants
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    sc = W.granular_column(cpu_contacts=True)
+    r = refcpu.RefCPU(sc.pos_w[:, :2], mass=1.0, s_friction=0.5, k_friction=0.3)
+    r.tick(sc.dt, 600)
+    ref = pile_invariants(r.state()[0])
+    o = Oracle(params_nolib(sc.params), sc.n)
+    W.apply_to(sc, o)
+    for _ in range(600):
+        o.update(sc.dt)
+    got = pile_invariants(o.positions()[:, :2])
+    for key, tol in (("mean_height", 0.1), ("spread", 0.1), ("top", 0.1), ("runout", 0.02)):
+        assert abs(got[key] - ref[key]) <= tol * ref[key], (key, got, ref)
