@@ -489,25 +489,55 @@ def run_adjoint(args, dev, stream):
         bwd.append(1e3 * (t2 - t1))
     fwd_ms, bwd_ms = statistics.median(fwd), statistics.median(bwd)
     grains = torch.tensor(np.concatenate([sc.phase == 3 for sc in scenes]), device=dev)
+
+    def errors(st, vv):
+        return (float((st - s_hidden).abs().mean()), float((vv - v_hidden)[grains, :3].norm(dim=1).mean()))
+
+    def loss_at(st, vv, steps, tgt):
+        with torch.no_grad():
+            xT, _ = rollout(sysm, st, x0, vv, dt, steps, every)
+            return float(((xT[:, :3] - tgt[:, :3]) ** 2).sum(1).mean())
+
+    # the hidden run's positions after a short horizon, for the curriculum
+    T1 = min(30, T)
+    with torch.no_grad():
+        target1, _ = rollout(sysm, s_hidden, x0, v_hidden, dt, T1, every)
+    # identifiability: how much the final positions change with stiffness
+    # alone and with velocities alone (the other set at its hidden value)
+    sens = {}
+    for steps, tgt in ((T1, target1), (T, target)):
+        sens[f"steps_{steps}"] = {"loss_stiffness_wrong": loss_at(s0, v_hidden, steps, tgt),
+                                  "loss_velocities_wrong": loss_at(s_hidden, v_init, steps, tgt),
+                                  "loss_both_wrong": loss_at(s0, v_init, steps, tgt)}
     t0 = time.perf_counter()
-    st_fit, v_fit, losses = fit(sysm, x0, target, s0, v_init, dt, T, every, args.adjoint_iters)
+    # recovery by a horizon curriculum: both parameter sets fitted to the
+    # hidden run's positions after T1 steps, then after T
+    st1, v1, losses1 = fit(sysm, x0, target1, s0, v_init, dt, T1, every, 2 * args.adjoint_iters, 0.02, 0.05)
+    st2, v2, losses2 = fit(sysm, x0, target, st1, v1, dt, T, every, args.adjoint_iters, 0.01, 0.005)
     torch.cuda.synchronize()
     fit_s = time.perf_counter() - t0
-    s_err0 = float((s0 - s_hidden).abs().mean())
-    s_err1 = float((st_fit - s_hidden).abs().mean())
-    v_err0 = float((v_init - v_hidden)[grains, :3].norm(dim=1).mean())
-    v_err1 = float((v_fit - v_hidden)[grains, :3].norm(dim=1).mean())
+    # stiffness alone, from the hidden velocities, on the final positions
+    st3, _, losses3 = fit(sysm, x0, target, s0, v_hidden, dt, T, every, args.adjoint_iters, 0.02, 0.0)
+    e0, e1, e2, e3 = errors(s0, v_init), errors(st1, v1), errors(st2, v2), errors(st3, v_hidden)
     return {"scenes": len(scenes), "particles": n, "constraints": m, "steps": T, "checkpoint_every": every,
             "dt": dt, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
             "timing": "wall clock between device synchronisations, median of 3 after 2 warm-up passes",
             "backward_over_forward": bwd_ms / fwd_ms, "particle_steps_per_s_fwd_bwd": n * T / ((fwd_ms + bwd_ms) * 1e-3),
-            "fit_iterations": len(losses), "fit_s": fit_s, "loss_first": losses[0] if losses else None,
-            "loss_last": losses[-1] if losses else None, "loss_min": min(losses) if losses else None,
-            "stiffness_mae_start": s_err0, "stiffness_mae_end": s_err1,
-            "grain_velocity_err_start": v_err0, "grain_velocity_err_end": v_err1,
+            "start": {"stiffness_mae": e0[0], "grain_velocity_err": e0[1], "loss": sens[f"steps_{T}"]["loss_both_wrong"]},
+            "curriculum": [
+                {"steps": T1, "iterations": len(losses1), "loss_first": losses1[0], "loss_last": losses1[-1],
+                 "stiffness_mae": e1[0], "grain_velocity_err": e1[1], f"loss_at_{T}": loss_at(st1, v1, T, target)},
+                {"steps": T, "iterations": len(losses2), "loss_first": losses2[0], "loss_last": losses2[-1],
+                 "stiffness_mae": e2[0], "grain_velocity_err": e2[1]}],
+            "fit_s": fit_s,
+            "stiffness_only_from_hidden_velocities": {"steps": T, "iterations": len(losses3),
+                                                      "loss_first": losses3[0], "loss_last": losses3[-1],
+                                                      "stiffness_mae_start": e0[0], "stiffness_mae_end": e3[0]},
+            "sensitivity": sens,
             "workload": f"{len(scenes)} scenes of a 64x64 cloth (stretch, pinned edges) + 8 ropes x 32 + 200 "
                         f"grains, hidden stiffness U(0.2, 1) and grain velocities; fit from stiffness 0.6 and "
-                        f"zero velocities by Adam"}
+                        f"zero velocities by Adam through the adjoint, on the hidden run's positions after "
+                        f"{T1} steps, then after {T}"}
 
 
 def run_ours(args, world, rank, local_rank):
@@ -596,18 +626,17 @@ def run_ours(args, world, rank, local_rank):
     pos_h = torch.empty((n, 4), dtype=torch.float32).pin_memory()
     vel_h = torch.empty((n, 4), dtype=torch.float32).pin_memory()
     lib = sysm.lib
-    sysm._check(lib.pbd_get_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
-    sysm._check(lib.pbd_get_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
+    sysm._check(lib.pbd_get_positions_velocities(sysm.h, 0, n, pos_h.data_ptr(), vel_h.data_ptr(), 0, sh))
     e2e_steps = max(3, args.steps)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sysm._check(lib.pbd_set_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
-        sysm._check(lib.pbd_set_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
+        # the state goes up and comes back every step, positions and
+        # velocities copied concurrently (pbd_set/get_positions_velocities)
+        sysm._check(lib.pbd_set_positions_velocities(sysm.h, 0, n, pos_h.data_ptr(), vel_h.data_ptr(), 0, sh))
         sysm.update_graph(sc.dt, 1, sh)
-        sysm._check(lib.pbd_get_positions(sysm.h, 0, n, pos_h.data_ptr(), 0, sh))
-        sysm._check(lib.pbd_get_velocities(sysm.h, 0, n, vel_h.data_ptr(), 0, sh))
+        sysm._check(lib.pbd_get_positions_velocities(sysm.h, 0, n, pos_h.data_ptr(), vel_h.data_ptr(), 0, sh))
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
     e2e_value = job_throughput(e2e_steps, world, e2e_s)
     sysm.check_finite(sh)

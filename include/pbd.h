@@ -275,6 +275,17 @@ int pbd_get_positions(pbd_system *sys, uint32_t first, uint32_t count, float *ds
                       int dst_on_device, void *stream);
 int pbd_get_velocities(pbd_system *sys, uint32_t first, uint32_t count, float *dst,
                        int dst_on_device, void *stream);
+/* Positions and velocities of [first, first+count) in one call (no
+ * counterpart in the reference, whose state stayed in its GL buffer): the
+ * two copies run concurrently, on the stream and on a side stream of the
+ * system ordered after it, so a host that keeps the state in its own memory
+ * pays for the slower copy rather than the sum.  Same rules as the single
+ * calls: synchronous for host memory, asynchronous on the stream for device
+ * pointers; either pointer may be NULL. */
+int pbd_set_positions_velocities(pbd_system *sys, uint32_t first, uint32_t count, const float *x,
+                                 const float *v, int on_device, void *stream);
+int pbd_get_positions_velocities(pbd_system *sys, uint32_t first, uint32_t count, float *x, float *v,
+                                 int on_device, void *stream);
 int pbd_get_phases(pbd_system *sys, int32_t *dst);
 /* The reference's render buffer content (its position VBO, float4 per
  * particle: xyz, w = 1; integration_kernel.cuh:461, particlesystem.cpp:
@@ -458,7 +469,7 @@ typedef struct pbd_tuning {
     uint32_t neighbor_list_capacity; /* with threads_per_particle == 1: fluid
                                       neighbours recorded per particle and
                                       iteration (multiple of 4, 0 = no list,
-                                      default 128); particles with more fall
+                                      default 256); particles with more fall
                                       back to the stencil walk              */
     float neighbor_skin;           /* with a list: its radius is (1 + skin) h
                                       and it is reused by the later

@@ -252,6 +252,8 @@ _SIGNATURES = {
     "pbd_rollout": ([_P, _F, _U32, _U32, _P], _I),
     "pbd_list_reuses": ([_P, _PU], _I),
     "pbd_num_distance_constraints": ([_P], _U32),
+    "pbd_set_positions_velocities": ([_P, _U32, _U32, _P, _P, _I, _P], _I),
+    "pbd_get_positions_velocities": ([_P, _U32, _U32, _P, _P, _I, _P], _I),
     "pbd_backward": ([_P, _P, _P, _P, _P, _P, _P], _I),
     "pbd_load_state": ([_P, _P, ctypes.c_uint64], _I),
 }

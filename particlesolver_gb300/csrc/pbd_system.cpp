@@ -730,6 +730,9 @@ int pbd_destroy(pbd_system *s) {
     cudaSetDevice(s->device);
     drop_graph(s);
     if (s->graph_stream) cudaStreamDestroy(s->graph_stream);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->copy_fork) cudaEventDestroy(s->copy_fork);
+    if (s->copy_join) cudaEventDestroy(s->copy_join);
     for (auto &t : s->pending) {
         cudaEventDestroy(t.start);
         cudaEventDestroy(t.stop);
@@ -1149,6 +1152,50 @@ int pbd_get_positions(pbd_system *s, uint32_t first, uint32_t count, float *dst,
 }
 int pbd_get_velocities(pbd_system *s, uint32_t first, uint32_t count, float *dst, int on_dev, void *st) {
     return copy_state(s, s ? s->v : nullptr, first, count, dst, on_dev, st, false);
+}
+
+// Positions and velocities copied concurrently: x on the caller's stream,
+// v on the system's side stream, forked from and joined back into the
+// caller's stream with events (so the pair is ordered like one operation
+// on that stream); for host memory the call returns after both.
+static int copy_pair(pbd_system *s, uint32_t first, uint32_t count, float *x, float *v, int on_device,
+                     void *stream, bool to_sys) {
+    SYS_GUARD(s);
+    if ((uint64_t)first + count > s->n) return fail(s, PBD_ERR_INVALID_ARGUMENT, "range exceeds particle count %u", s->n);
+    if (count == 0 || (!x && !v)) return PBD_OK;
+    if (!x || !v) {  // one of the two: the plain copy
+        return copy_state(s, x ? s->x : s->v, first, count, x ? x : v, on_device, stream, to_sys);
+    }
+    if (!s->copy_stream) CUDA_TRY(s, cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+    if (!s->copy_fork) CUDA_TRY(s, cudaEventCreateWithFlags(&s->copy_fork, cudaEventDisableTiming));
+    if (!s->copy_join) CUDA_TRY(s, cudaEventCreateWithFlags(&s->copy_join, cudaEventDisableTiming));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t bytes = (size_t)count * sizeof(float4);
+    const cudaMemcpyKind kind =
+        on_device ? cudaMemcpyDeviceToDevice : (to_sys ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+    CUDA_TRY(s, cudaEventRecord(s->copy_fork, st));
+    CUDA_TRY(s, cudaStreamWaitEvent(s->copy_stream, s->copy_fork, 0));
+    if (to_sys) {
+        CUDA_TRY(s, cudaMemcpyAsync(s->x + first, x, bytes, kind, st));
+        CUDA_TRY(s, cudaMemcpyAsync(s->v + first, v, bytes, kind, s->copy_stream));
+    } else {
+        CUDA_TRY(s, cudaMemcpyAsync(x, s->x + first, bytes, kind, st));
+        CUDA_TRY(s, cudaMemcpyAsync(v, s->v + first, bytes, kind, s->copy_stream));
+    }
+    CUDA_TRY(s, cudaEventRecord(s->copy_join, s->copy_stream));
+    CUDA_TRY(s, cudaStreamWaitEvent(st, s->copy_join, 0));
+    if (!on_device) CUDA_TRY(s, cudaStreamSynchronize(st));
+    if (to_sys) s->grid_valid = false;
+    return PBD_OK;
+}
+
+int pbd_set_positions_velocities(pbd_system *s, uint32_t first, uint32_t count, const float *x, const float *v,
+                                 int on_device, void *stream) {
+    return copy_pair(s, first, count, const_cast<float *>(x), const_cast<float *>(v), on_device, stream, true);
+}
+int pbd_get_positions_velocities(pbd_system *s, uint32_t first, uint32_t count, float *x, float *v, int on_device,
+                                 void *stream) {
+    return copy_pair(s, first, count, x, v, on_device, stream, false);
 }
 
 int pbd_get_vbo(pbd_system *s, uint32_t first, uint32_t count, float *dst, int on_dev, void *stream) {

@@ -82,7 +82,7 @@ struct pbd_system {
 
     uint32_t tpp = 1;     // lanes per particle in the neighbour passes
     pbd::NbList nbl{};    // per-iteration fluid neighbour lists
-    uint32_t list_capacity = 128;
+    uint32_t list_capacity = 256;
     float skin = 0.f;               // skin-list radius (1 + skin) h; 0 = off
     float4 *sref = nullptr;         // [cap] sorted positions at the list build
     uint32_t *skin_words = nullptr; // [pbd::kSkinWords] device decision words
@@ -108,6 +108,10 @@ struct pbd_system {
     // captured step graph
     cudaGraphExec_t graph_exec = nullptr;
     cudaStream_t graph_stream = nullptr;
+    // side stream and fork / join events of the paired state copies
+    // (pbd_set/get_positions_velocities), created on first use
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_fork = nullptr, copy_join = nullptr;
     float graph_dt = 0.f;
     uint64_t graph_version = 0;
     uint64_t version = 1;  // bumped whenever a captured graph would go stale

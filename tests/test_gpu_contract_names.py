@@ -148,3 +148,38 @@ def test_vbo_is_the_reference_render_layout():
     np.testing.assert_array_equal(t.cpu().numpy(), v)
     with pytest.raises(PbdError):
         g.vbo(sc.n - 2, 5)
+
+
+def test_paired_state_copies_equal_the_single_ones():
+    """pbd_set/get_positions_velocities (the two copies run concurrently)
+    move exactly what pbd_set/get_positions and _velocities move, from host
+    and from device memory, and a step after either gives the same state."""
+    torch = pytest.importorskip("torch")
+    sc = W.dam_break(16, 12, 8)
+    a, b = load(sc), load(sc)
+    a.update(sc.dt)
+    b.update(sc.dt)
+    n = sc.n
+    rng = np.random.default_rng(3)
+    x = (a.positions() + rng.uniform(-1e-3, 1e-3, (n, 4)).astype(np.float32) * [1, 1, 1, 0]).astype(np.float32)
+    v = rng.uniform(-1, 1, (n, 4)).astype(np.float32)
+    a.set_positions(x)
+    a.set_velocities(v)
+    assert b.lib.pbd_set_positions_velocities(b.h, 0, n, x.ctypes.data, v.ctypes.data, 0, None) == 0
+    xo, vo = np.empty_like(x), np.empty_like(v)
+    assert b.lib.pbd_get_positions_velocities(b.h, 0, n, xo.ctypes.data, vo.ctypes.data, 0, None) == 0
+    np.testing.assert_array_equal(xo, a.positions())
+    np.testing.assert_array_equal(vo, a.velocities())
+    # device pointers, a sub-range and one of the two alone
+    xd = torch.tensor(x[5:40], device="cuda")
+    vd = torch.tensor(v[5:40] * 2, device="cuda")
+    assert b.lib.pbd_set_positions_velocities(b.h, 5, 35, xd.data_ptr(), vd.data_ptr(), 1, None) == 0
+    a.set_velocities(v[5:40] * 2, first=5)
+    assert b.lib.pbd_set_positions_velocities(b.h, 0, n, None, None, 0, None) == 0
+    a.update(sc.dt)
+    assert b.lib.pbd_update(b.h, ctypes.c_float(sc.dt), None) == 0
+    xs = torch.empty((n, 4), device="cuda")
+    assert b.lib.pbd_get_positions_velocities(b.h, 0, n, xs.data_ptr(), None, 1, None) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(xs.cpu().numpy(), a.positions())
+    assert b.lib.pbd_get_positions_velocities(b.h, 0, n + 1, xo.ctypes.data, vo.ctypes.data, 0, None) != 0
