@@ -38,6 +38,7 @@
 #include "fluidemitter.h"
 #include "contactconstraint.h"
 #include "boundaryconstraint.h"
+#include "opensmokeemitter.h"  // last: it defines the macros H, H2, H6, H9
 #undef private
 
 #include <cstdint>
@@ -327,6 +328,43 @@ void refcpu_contacts(int n, const double *p, const double *ep, const double *ima
         ep_out[2 * i + 1] = ps.at(i)->ep.y;
         delete ps.at(i);
     }
+}
+
+// The reference's own OpenSmokeEmitter::tick (opensmokeemitter.cpp:17-43)
+// with its gas constraint, `ticks` ticks of `secs` after an estimates list
+// of n particles: per tick the number of particles it appends to the
+// estimates (counts), and for each appended particle its position, inverse
+// mass, phase (1 = GAS) and whether the gas constraint took its index
+// (new_* hold the first max_new).  Returns the total appended.
+int refcpu_smoke_emitter_tick(int n, double ex, double ey, double rate, double secs, int ticks, int *counts,
+                              int max_new, double *new_p, double *new_imass, int *new_gas, int *new_member) {
+    QList<Particle *> ps;
+    for (int i = 0; i < n; ++i) ps.append(new Particle(glm::dvec2(0.0, 0.0), 1.0, SOLID));
+    QList<int> members;
+    int total = 0;
+    {
+        GasConstraint gs(1.0, &members, true);
+        OpenSmokeEmitter e(glm::dvec2(ex, ey), rate, &gs);
+        for (int k = 0; k < ticks; ++k) {
+            const int before = ps.size();
+            e.tick(&ps, secs);
+            counts[k] = ps.size() - before;
+        }
+        total = ps.size() - n;
+        for (int i = n; i < ps.size(); ++i) {
+            const Particle *q = ps.at(i);
+            const int m = i - n;
+            if (m >= max_new) break;
+            new_p[2 * m] = q->p.x;
+            new_p[2 * m + 1] = q->p.y;
+            new_imass[m] = q->imass;
+            new_gas[m] = q->ph == GAS ? 1 : 0;
+            new_member[m] = gs.ps.contains(i) ? 1 : 0;
+        }
+        for (Particle *q : *e.getParticles()) delete q;  // the drawing-only tracers
+    }
+    for (Particle *q : ps) delete q;
+    return total;
 }
 
 }  // extern "C"

@@ -48,6 +48,8 @@ def load():
                                                   PD, PI, I, PD, PD]
         lib.refcpu_fluid_emitter_tick.restype = I
         lib.refcpu_contacts.argtypes = [I, PD, PD, PD, PI, I, PI, I, PI, D, D, D, D, D, D, PD]
+        lib.refcpu_smoke_emitter_tick.argtypes = [I, D, D, D, D, I, PI, I, PD, PD, PI, PI]
+        lib.refcpu_smoke_emitter_tick.restype = I
         _lib = lib
     return _lib
 
@@ -183,6 +185,26 @@ def fluid_emitter_tick(p, v, imass, t, lambdas, members: int, position, rate: fl
     k = min(k, max_new)
     return {"v": v_out, "imass": im_out, "t": t_out, "fluid": ph_out == 1, "clocks": clk,
             "new_p": new_p[:k], "new_v": new_v[:k]}
+
+
+def smoke_emitter_ticks(n: int, position, rate: float, secs: float, ticks: int, max_new: int = 4096):
+    """`ticks` OpenSmokeEmitter::tick calls of the reference (with its gas
+    constraint) after an estimates list of n particles.  Returns a dict:
+    counts per tick, and the appended particles' p, imass, gas (phase GAS)
+    and member (index taken by the gas constraint)."""
+    lib = load()
+    counts = np.zeros(ticks, np.int32)
+    new_p, new_im = np.empty((max_new, 2)), np.empty(max_new)
+    gas, member = np.empty(max_new, np.int32), np.empty(max_new, np.int32)
+    pd = ctypes.POINTER(ctypes.c_double)
+    pi = ctypes.POINTER(ctypes.c_int)
+    k = lib.refcpu_smoke_emitter_tick(int(n), ctypes.c_double(position[0]), ctypes.c_double(position[1]),
+                                      ctypes.c_double(rate), ctypes.c_double(secs), int(ticks),
+                                      counts.ctypes.data_as(pi), int(max_new), new_p.ctypes.data_as(pd),
+                                      new_im.ctypes.data_as(pd), gas.ctypes.data_as(pi), member.ctypes.data_as(pi))
+    k = min(k, max_new)
+    return {"counts": counts, "new_p": new_p[:k], "new_imass": new_im[:k], "gas": gas[:k] == 1,
+            "member": member[:k] == 1}
 
 
 def contacts(p, ep, imass, solid, pairs, walls, box, s_friction: float, k_friction: float):

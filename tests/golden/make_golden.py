@@ -19,7 +19,8 @@ grains and the reference's TotalFluidConstraint::project
 (totalfluidconstraint.cpp:41-116) estimates and lambdas after 1 and 3
 calls.  fluid_emitter.npz holds FluidEmitter::tick (fluidemitter.cpp:13-77)
 emission counts over 40 ticks and one solidification tick of a seeded
-state.  cpu_contacts.npz holds 2-D grains each in one contact or wall
+state; smoke_emitter.npz OpenSmokeEmitter::tick (opensmokeemitter.cpp:
+17-43) emission counts over 6 s of ticks at three rates.  cpu_contacts.npz holds 2-D grains each in one contact or wall
 constraint and the reference's RigidContactConstraint / ContactConstraint /
 BoundaryConstraint results; granular_pile.npz the reference Simulation's
 granular column after 600 steps.
@@ -183,6 +184,20 @@ def emitter_fixture() -> dict:
                 v_out=o["v"], imass_out=o["imass"], fluid_out=o["fluid"])
 
 
+def smoke_fixture() -> dict:
+    """OpenSmokeEmitter::tick of the reference: emission counts over 6 s of
+    ticks at three rates and steps, and the emitted particles' inverse
+    masses."""
+    from oracle import refcpu
+
+    out = {}
+    for k, (rate, dt) in enumerate(((15.0, 1.0 / 60.0), (40.0, 1.0 / 120.0), (7.0, 0.05))):
+        o = refcpu.smoke_emitter_ticks(5, (0.5, -2.0), rate, dt, int(np.ceil(6.0 / dt)))
+        out[f"rate{k}"], out[f"dt{k}"], out[f"counts{k}"] = rate, dt, o["counts"]
+        out[f"imass{k}"], out[f"gas{k}"] = o["new_imass"], o["gas"] & o["member"]
+    return out
+
+
 def contact_fixture() -> dict:
     """The CPU-contact pinning case (workloads.cpu_contact_case, seed 31,
     inputs rounded to FP32) and the reference's RigidContactConstraint /
@@ -220,6 +235,7 @@ def main():
     if refcpu.available():
         for name, fix in (("gas_project", gas_fixture), ("sdf_contacts", sdf_fixture),
                           ("fluid_project", fluid_fixture), ("fluid_emitter", emitter_fixture),
+                          ("smoke_emitter", smoke_fixture),
                           ("cpu_contacts", contact_fixture), ("granular_pile", pile_fixture)):
             path = HERE / f"{name}.npz"
             np.savez_compressed(path, **fix())

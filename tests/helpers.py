@@ -249,7 +249,7 @@ def emitter_counts(rate: float, duration: float, dt: float, ticks: int) -> list:
     """Particles FluidEmitter::tick emits per tick (fluidemitter.cpp:69-76):
     a timer advanced by dt releases one particle per 1 / rate while the
     emitter's total time is below `duration` (the reference's 5 s; 0 = no
-    limit here)."""
+    limit, as OpenSmokeEmitter::tick, opensmokeemitter.cpp:17-28)."""
     timer = elapsed = 0.0
     out = []
     for _ in range(ticks):

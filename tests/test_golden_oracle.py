@@ -157,6 +157,20 @@ def test_emitter_rules_match_reference_golden():
     assert np.all(d["imass_out"][turn] == 0.0) and np.all(d["v_out"][turn] == 0.0)
 
 
+
+def test_smoke_emitter_rule_matches_reference_golden():
+    """The gas emitter's emission rule (emitter_counts with no time limit)
+    against the reference's own OpenSmokeEmitter::tick
+    (opensmokeemitter.cpp:17-43, tests/golden/smoke_emitter.npz): 6 s of
+    ticks at three rates, each particle a gas particle of inverse mass 1."""
+    from helpers import emitter_counts
+
+    d = np.load(GOLDEN / "smoke_emitter.npz")
+    for k in range(3):
+        counts = list(d[f"counts{k}"])
+        assert counts == emitter_counts(float(d[f"rate{k}"]), 0.0, float(d[f"dt{k}"]), len(counts))
+        assert np.all(d[f"imass{k}"] == 1.0) and np.all(d[f"gas{k}"])
+
 @pytest.mark.parametrize("tag,friction", [("f1", (0.4, 0.3)), ("f2", (0.01, 0.005))])
 def test_cpu_contacts_match_reference_golden(tag, friction):
     """The oracle's CPU contact projectors against the reference's own

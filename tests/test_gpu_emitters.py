@@ -4,8 +4,8 @@ emitter's timer and its seeded velocity jitter; the solidification against
 its rule applied, tick by tick, to the lambdas, velocities and positions the
 CUDA system had before the tick.  Both rules (tests/helpers.py:
 emitter_counts, solidify_rule) are pinned to the reference's own
-FluidEmitter::tick (tests/test_oracle_vs_reference.py,
-tests/test_golden_oracle.py)."""
+FluidEmitter::tick and OpenSmokeEmitter::tick
+(tests/test_oracle_vs_reference.py, tests/test_golden_oracle.py)."""
 import numpy as np
 import pytest
 
@@ -68,6 +68,26 @@ def test_smoke_emitter_feeds_an_open_gas():
     assert np.all(g.phases()[new] == W.PHASE_GAS)
     assert np.max(np.abs(g.forces()[new, :3])) > 0.0  # open drag / vorticity reach the emitted gas
 
+
+
+def test_gas_emitter_follows_the_smoke_emitter():
+    """A gas emitter without a time limit emits as OpenSmokeEmitter::tick
+    (opensmokeemitter.cpp:17-28; the rule pinned to it by
+    tests/test_oracle_vs_reference.py and tests/test_golden_oracle.py): 6 s
+    of ticks, past the fluid emitter's 5 s, each particle a gas particle of
+    inverse mass 1 at rest at the emitter."""
+    sc = W.smoke_box(open_gas=True, solid_floor=True)
+    g = ParticleSystem(default_params(**sc.params), sc.n + 100)
+    W.apply_to(sc, g)
+    pos, rate, dt = [0.25, -1.5, 0.0], 7.0, float(np.float32(0.05))
+    g.add_emitter(position=pos, rate=rate, duration=0.0, phase=W.PHASE_GAS, inverse_mass=1.0, rest_density=1.0,
+                  open_gas=1, seed=5)
+    ticks = int(np.ceil(6.0 / dt))
+    got = [g.emit(dt) for _ in range(ticks)]
+    assert got == expected_counts(rate, 0.0, dt, ticks) and sum(got) > rate * 5.0
+    new = slice(sc.n, sc.n + sum(got))
+    np.testing.assert_array_equal(g.positions()[new], np.tile(np.float32(pos + [1.0]), (sum(got), 1)))
+    assert np.all(g.velocities()[new, :3] == 0.0) and np.all(g.phases()[new] == W.PHASE_GAS)
 
 def test_solidification_follows_the_fluid_emitter_rule():
     """A resting fluid block whose particles all take part: every tick, the

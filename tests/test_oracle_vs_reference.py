@@ -289,6 +289,27 @@ def test_fluid_emitter_matches_reference_cpu():
         np.testing.assert_array_equal(out["v"][~turn], v[~turn])
 
 
+
+def test_smoke_emitter_matches_reference_cpu():
+    """The emission rule the CUDA path's gas emitter is tested against
+    (tests/helpers.py: emitter_counts with no time limit) against the
+    reference's own OpenSmokeEmitter::tick (opensmokeemitter.cpp:17-43): 6 s
+    of ticks (past the fluid emitter's 5 s, which this emitter does not have),
+    each emitted particle a gas particle of inverse mass 1 at the emitter,
+    taken by the gas constraint."""
+    from helpers import emitter_counts
+    from oracle import refcpu
+
+    if not refcpu.available():
+        pytest.skip("reference CPU solver not built")
+    for rate, dt in ((15.0, 1.0 / 60.0), (40.0, 1.0 / 120.0), (7.0, 0.05)):
+        ticks = int(np.ceil(6.0 / dt))
+        out = refcpu.smoke_emitter_ticks(5, (0.5, -2.0), rate, dt, ticks)
+        assert list(out["counts"]) == emitter_counts(rate, 0.0, dt, ticks)
+        assert sum(out["counts"]) > rate * 5.0
+        np.testing.assert_array_equal(out["new_p"], np.tile([0.5, -2.0], (len(out["new_p"]), 1)))
+        assert np.all(out["new_imass"] == 1.0) and out["gas"].all() and out["member"].all()
+
 @pytest.mark.parametrize("seed,friction", [(31, (0.4, 0.3)), (34, (0.4, 0.3)), (35, (0.01, 0.005))])
 def test_cpu_contacts_match_reference_cpu(seed, friction):
     """The oracle's CPU contact projectors (PBD_FLAG_CPU_CONTACTS) against
