@@ -41,25 +41,22 @@ constexpr int kBlock = 256;
 #define PBD_BATCH_SOLVE_MIN_BLOCKS PBD_SOLVE_MIN_BLOCKS
 #endif
 constexpr int kWalkUnroll = PBD_WALK_UNROLL;
-// Block of the shared-memory list build, and the entries per particle it
-// assembles in shared memory (a particle with more rebuilds its list in
-// global memory): (columns + 1) x kListBlock words.  Fewer columns leave
-// more of the SM's combined L1/shared storage to cache the candidates the
-// walk loads, but a rebuild costs its warp a second walk: 48 columns hold
-// every list of a fluid at rest density with cells of h (at most ~48
-// neighbours); skin lists, longer by (1 + skin)^3, get up to 88.
+// Block of the shared-memory list build, and the row chunks per particle
+// it keeps in shared memory (further chunks go straight to the global
+// list): columns x kListBlock uint2.  A particle at rest density with cells
+// of h has about nine rows with neighbours, one chunk each; skin lists,
+// whose rows are longer, get more.  Fewer columns leave more of the SM's
+// combined L1/shared storage to cache the candidates the walk loads.
 #ifndef PBD_SLIST_COLS
-#define PBD_SLIST_COLS 48
+#define PBD_SLIST_COLS 12
 #endif
 constexpr int kListBlock = 128;
 constexpr uint32_t kSharedListCols = PBD_SLIST_COLS;
-constexpr uint32_t kSharedListColsSkin = 88;
-static_assert(kSharedListCols % 4 == 0 && kSharedListCols <= kSharedListColsSkin &&
-                  (kSharedListColsSkin + 1) * kListBlock * 4 <= 48 * 1024,
+constexpr uint32_t kSharedListColsSkin = 20;
+static_assert(kSharedListCols <= kSharedListColsSkin && kSharedListColsSkin * kListBlock * 8 <= 48 * 1024,
               "shared-memory list build exceeds the default dynamic shared memory");
 // NbList::assemble: kListShared selects the shared-memory build (any other
-// value, the register quads); both store four entries to a uint4,
-// [capacity / 4][stride].
+// value: chunks stored straight to the global list).
 constexpr uint32_t kListShared = 0u;
 
 inline unsigned blocks_for(uint32_t n, int per_block = kBlock) {
@@ -1023,16 +1020,56 @@ __device__ __forceinline__ float3 contact_delta(const DevParams &P, const Group<
 // neighbour's sorted index in visiting order (four to a uint4, slot-major
 // so that reading slot q of 32 consecutive particles is one coalesced
 // 512-byte load); the per-neighbour arithmetic of lambda, delta and XSPH
-// then runs over the list.  Particles with more neighbours than the list
-// holds (or than the reference's cap) use the exact stencil walk instead.
+// then runs over the list.  The walk itself records row chunks (NbList):
+// per run of up to 32 consecutive candidates of a stencil row, its first
+// sorted slot and a bit per candidate that is a neighbour (|r| below the
+// list radius, any phase, self excluded); lambda's sums step through the
+// chunks and store the indices as they go.  Particles whose list does not
+// fit (or with more neighbours than the reference's cap) use the exact
+// stencil walk instead.
 
-__device__ __forceinline__ bool list_usable(const DevParams &P, const NbList &L, uint32_t cnt) {
-    return cnt <= L.capacity && cnt <= P.max_nb;
+// The lambda pass's count word: neighbours in the low 16 bits, chunks in
+// the high 16 (kListNone: no usable list).
+constexpr uint32_t kListNone = 0xffff0000u;
+__device__ __forceinline__ uint32_t list_nnb(uint32_t c) { return c & 0xffffu; }
+__device__ __forceinline__ uint32_t list_nch(uint32_t c) { return c >> 16; }
+
+__device__ __forceinline__ bool list_usable(const DevParams &P, const NbList &L, uint32_t c) {
+    return list_nch(c) <= L.chunks && list_nnb(c) <= L.capacity && list_nnb(c) <= P.max_nb;
 }
 
-// Calls f(j) for the cnt listed neighbours of particle i.
+// Steps through a chunk list: next() returns the next neighbour's sorted
+// slot, or `self` past the end.  load(q) returns chunk q.  The chunk after
+// the current one is loaded when the current one is taken up, so its load
+// overlaps the current chunk's neighbours instead of waiting at the chunk
+// boundary.
+struct ChunkCursor {
+    uint32_t b = 0u, m = 0u, q = 0u;
+    uint2 nxt = make_uint2(0u, 0u);
+    template <class Load>
+    __device__ __forceinline__ void start(uint32_t nch, Load &&load) {
+        if (nch > 0u) nxt = load(0u);
+        q = 1u;
+    }
+    template <class Load>
+    __device__ __forceinline__ uint32_t next(uint32_t nch, uint32_t self, Load &&load) {
+        if (m == 0u && q <= nch) {
+            b = nxt.x;
+            m = nxt.y;
+            if (q < nch) nxt = load(q);
+            ++q;
+        }
+        if (m == 0u) return self;
+        const uint32_t k = (uint32_t)__ffs(m) - 1u;
+        m &= m - 1u;
+        return b + k;
+    }
+};
+
+// Calls f(j) for the listed neighbours of particle i (count word c).
 template <class F>
-__device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uint32_t cnt, F &&f) {
+__device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uint32_t c, F &&f) {
+    const uint32_t cnt = min(list_nnb(c), L.capacity);
     for (uint32_t q = 0; 4u * q < cnt; ++q) {
         const uint4 e = L.slot[q * L.stride + i];
         const uint32_t left = cnt - 4u * q;
@@ -1043,13 +1080,15 @@ __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uin
     }
 }
 
-// Calls f(j, src[j], ok) for the cnt listed neighbours of particle i, a
-// quad at a time: the quad's four gathers are all issued before any is
-// used, so their latencies overlap; slots past cnt read particle i's own
-// entry and come with ok = false (f must then add nothing).
+// Calls f(j, src[j], ok) for the listed neighbours of particle i (count
+// word c), a quad at a time: the quad's four gathers are all issued before
+// any is used, so their latencies overlap; slots past the end read
+// particle i's own entry and come with ok = false (f must then add
+// nothing).
 template <int QUADS = 1, class T, class F>
-__device__ __forceinline__ void gather_listed(const NbList &L, uint32_t i, uint32_t cnt,
+__device__ __forceinline__ void gather_listed(const NbList &L, uint32_t i, uint32_t c,
                                               const T *__restrict__ src, F &&f) {
+    const uint32_t cnt = min(list_nnb(c), L.capacity);
     for (uint32_t q = 0; 4u * q < cnt; q += QUADS) {
         uint32_t jj[4 * QUADS];
         T v[4 * QUADS];
@@ -1068,6 +1107,26 @@ __device__ __forceinline__ void gather_listed(const NbList &L, uint32_t i, uint3
 #pragma unroll
         for (int t = 0; t < 4 * QUADS; ++t) f(jj[t], v[t], 4u * q + (uint32_t)t < cnt);
     }
+}
+
+// The chunks of candidates [b, e) of one stencil row for particle i at pi
+// (list radius^2 reach2), in order: emit(chunk) for each chunk holding a
+// neighbour.  Returns false when emit does (the list is full).
+template <class Emit>
+__device__ __forceinline__ bool row_chunks(uint32_t i, float3 pi, float reach2, uint32_t b, uint32_t e,
+                                           const float4 *__restrict__ sx, Emit &&emit) {
+    for (uint32_t c = b; c < e; c += 32u) {
+        const uint32_t len = min(32u, e - c);
+        uint32_t m = 0u;
+#pragma unroll kWalkUnroll
+        for (uint32_t k = 0; k < len; ++k) {
+            const float4 q = __ldg(sx + c + k);
+            m |= (dist2_exact(pi, f3(q)) < reach2 ? 1u : 0u) << k;
+        }
+        if (i - c < len) m &= ~(1u << (i - c));  // not itself
+        if (m && !emit(make_uint2(c, m))) return false;
+    }
+    return true;
 }
 
 // Stencil ranges with the radius fixed at compile time (RAD > 0; RAD = 0
@@ -1171,230 +1230,20 @@ __device__ __forceinline__ int list_rad(const DevParams &P, float skin) {
     return (int)ceilf(P.h * (1.f + skin) / P.cell * 1.000001f);
 }
 
-// findLambdasD (integration_kernel.cuh:481-593) with the list build: the
-// walk records the neighbours (|r| below the list radius, any phase,
-// visiting order) and lambda is summed over the listed particles closer
-// than h.  The candidate loop is branch-free: the neighbour test drives
-// predicated register inserts and a predicated 16-byte store per four
-// neighbours.  SKIN: the list has a skin (radius (1 + skin) h, build
-// positions kept in L.sref), and when it is reused (*L.reuse) there is no
-// walk: the old list is filtered at the refreshed positions.  Output as
-// k_lambda.
-template <int RAD, bool B, bool SKIN>
-__global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_t n, uint32_t iter_left,
-                                                        const float4 *__restrict__ sx,
-                                                        const SortedAttr *__restrict__ sattr,
-                                                        const uint32_t *__restrict__ cell_first,
-                                                        float4 *__restrict__ sxl, NbList L, GasBuffers gas) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const DevParams P = scene_params<B>(P0, i);
-    const bool reuse = SKIN && L.reuse && *L.reuse;
-    // A scene sitting out this iteration needs nothing -- except when a skin
-    // list is built: every scene's list must exist for the later
-    // iterations that reuse it.
-    if (!scene_active<B>(P, iter_left) && (reuse || !SKIN)) return;
-    const SortedAttr a = sattr[i];
-    const float4 pi4 = sx[i];
-    const float3 pi = f3(pi4);
-    if (SKIN && !reuse) L.sref[i] = pi4;
-    if (a.phase == kGas) {  // no list: the gas passes walk the grid (skin lists are off with gas)
-        L.count[i] = 0u;
-        gas_lambda<1>(P, Group<1>(), i, pi4, a.rho0, sx, sattr, cell_first, gas, sxl);
-        return;
-    }
-    if (a.phase != kFluid) {
-        sxl[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
-        if (!reuse) L.count[i] = 0u;
-        return;
-    }
-    const float h2 = P.h2;
-    const bool nb_mass = (P.flags & kFlagDensityNeighborMass) != 0u;
-    const float inv_w = 1.f / pi4.w;
-    const float inv_rho0 = 1.f / a.rho0;
-    const float spiky_r = -P.spiky * inv_rho0;
-    LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-    auto add = [&](uint32_t j, const float4 &pj, float d2) {
-        const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
-        acc.add(P, fluid_nb_ok(P, pj.w), d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
-    };
-    if (reuse) {
-        for_each_listed(L, i, L.count[i], [&](uint32_t j) {
-            const float4 pj = __ldg(sx + j);
-            const float d2 = dist2_exact(pi, f3(pj));
-            if (d2 < h2) add(j, pj, d2);
-        });
-    } else {
-        const int3 g = grid_pos(P, pi);
-        uint32_t cnt = 0;
-        uint4 pend = make_uint4(0u, 0u, 0u, 0u);
-        uint4 *const row_base = L.slot + i;
-        const uint32_t cap = L.capacity;
-        int rad = P.fluid_rad;
-        float reach2 = h2;
-        bool trim = P.trim_fluid;
-        if (SKIN) {
-            const int r = list_rad(P, L.skin);
-            if ((uint32_t)(2 * r + 1) <= min(P.gx, min(P.gy, P.gz))) {
-                const float lr = P.h * (1.f + L.skin);
-                rad = r;
-                reach2 = lr * lr;
-                trim = true;
-            } else {
-                // the skin's stencil would alias on this grid (cells seen
-                // twice): a plain list, and no reuse this step
-                atomicOr(L.ovf, 1u);
-            }
-        }
-        stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
-#pragma unroll 2
-            for (uint32_t j = b; j < e; ++j) {
-                const float4 q = __ldg(sx + j);
-                const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
-                const uint32_t s4 = cnt & 3u;
-                pend.x = (ok && s4 == 0u) ? j : pend.x;
-                pend.y = (ok && s4 == 1u) ? j : pend.y;
-                pend.z = (ok && s4 == 2u) ? j : pend.z;
-                pend.w = (ok && s4 == 3u) ? j : pend.w;
-                if (ok && s4 == 3u && cnt < cap) row_base[(cnt >> 2) * L.stride] = pend;
-                cnt += ok ? 1u : 0u;
-            }
-            return true;
-        });
-        if (cnt < cap && (cnt & 3u)) row_base[(cnt >> 2) * L.stride] = pend;
-        L.count[i] = cnt;
-        if (list_usable(P, L, cnt)) {
-            for_each_listed(L, i, cnt, [&](uint32_t j) {
-                const float4 pj = __ldg(sx + j);
-                const float d2 = dist2_exact(pi, f3(pj));
-                if (!SKIN || d2 < h2) add(j, pj, d2);
-            });
-        } else {
-            if (SKIN) atomicOr(L.ovf, 1u);  // this list cannot be reused
-            const Group<1> G;
-            group_walk<1>(
-                P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-                [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok(P, pj.w); },
-                [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2); });
-        }
-    }
-    const float ro = acc.ro + P.poly6_self * inv_w;
-    const float denom = acc.denom + dot3(acc.grad, acc.grad);
-    sxl[i] = make_float4(pi.x, pi.y, pi.z, -(ro * inv_rho0 - 1.f) / (denom + P.relax));
-}
-
-// k_lambda_list with the list assembled in shared memory.  Each lane owns
-// one column of a [capacity + 1][kListBlock] word array (the word index is
-// row * kListBlock + lane, so every store of a warp lands in its own bank
-// whatever the lanes' counts), and the candidate loop costs one predicated
-// 4-byte store and a clamped column-offset bump per candidate instead of
-// k_lambda_list's register quad and 16-byte store.  Row `capacity` absorbs
-// stores past capacity; a particle that reaches it counts as over capacity
-// and takes the exact stencil walk.  The finished list goes to global
-// memory four entries to a uint4 (the layout k_lambda_list writes) and lambda
-// is summed from the shared copy.  Same neighbour sets, visiting order and
-// results as k_lambda_list.
-// The list of a particle whose shared-memory column filled up: the column's
-// entries go out as quads, then the walk resumes after the column's last
-// entry (in range `rfull` of the walk, the range in which the column
-// filled) and stores the rest straight to their words of the global list.
-// Returns the count, or capacity + 1 when the list does not fit.  CS: the
-// column's stride in words (entry k of the column at col[k * CS]).
-template <int RAD, int CS>
-__device__ __forceinline__ uint32_t spill_list(const DevParams &P, uint32_t i, float3 pi, int3 g, int rad,
-                                               float reach2, bool trim, const float4 *__restrict__ sx,
-                                               const uint32_t *__restrict__ cell_first, const NbList &L,
-                                               const uint32_t *col, uint32_t cols, uint32_t rfull) {
-    uint4 *const dst = L.slot + i;
-    for (uint32_t q = 0; 4u * q < cols; ++q) {
-        const uint32_t k = 4u * q * (uint32_t)CS;
-        dst[q * L.stride] = make_uint4(col[k], col[k + CS], col[k + 2 * CS], col[k + 3 * CS]);
-    }
-    const uint32_t jlast = col[(cols - 1u) * (uint32_t)CS];
-    uint32_t *const words = reinterpret_cast<uint32_t *>(L.slot);
-    const uint32_t cap = L.capacity;
-    uint32_t k = cols, r = 0;
-    bool over = false;
-    stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
-        if (r < rfull) {
-            ++r;
-            return true;
-        }
-        if (r++ == rfull) b = jlast + 1u;
-        for (uint32_t j = b; j < e; ++j) {
-            if (dist2_exact(pi, f3(__ldg(sx + j))) < reach2 && j != i) {
-                if (k == cap) {  // over capacity: the rest of the walk does not matter
-                    over = true;
-                    return false;
-                }
-                words[((size_t)(k >> 2) * L.stride + i) * 4u + (k & 3u)] = j;
-                ++k;
-            }
-        }
-        return true;
-    });
-    return over ? cap + 1u : k;
-}
-
-// Particle i's list, held in its shared-memory column (entries 0 ..
-// min(cnt, cols) - 1 at col[k * CS]; with cnt > cols the rest already sits
-// in the global list): stores it to the global list four entries to a uint4
-// and sums lambda's terms over it with add(j, q_j, d2, ok).  A list that is
-// not usable (over capacity or the neighbour cap) takes the exact capped
-// walk instead.  SKIN: listed particles farther than h add nothing.
-template <int CS, bool SKIN, class Add>
-__device__ __forceinline__ void lambda_from_column(const DevParams &P, const NbList &L, uint32_t i, float3 pi,
-                                                   int3 g, const float4 *__restrict__ sx,
-                                                   const uint32_t *__restrict__ cell_first, const uint32_t *col,
-                                                   uint32_t cols, uint32_t cnt, Add &&add) {
-    const float h2 = P.h2;
-    if (cnt > cols && list_usable(P, L, cnt)) {
-        gather_listed(L, i, cnt, sx, [&](uint32_t j, const float4 &pj, bool valid) {
-            const float d2 = dist2_exact(pi, f3(pj));
-            add(j, pj, d2, valid && (!SKIN || d2 < h2));
-        });
-    } else if (list_usable(P, L, cnt)) {
-        uint4 *const dst = L.slot + i;
-        for (uint32_t q = 0; 4u * q < cnt; ++q) {
-            const uint32_t k = 4u * q * (uint32_t)CS;
-            dst[q * L.stride] = make_uint4(col[k], col[k + CS], col[k + 2 * CS], col[k + 3 * CS]);
-        }
-        // four gathers in flight before their sums (entries past cnt read
-        // this particle's own slot and add nothing)
-        for (uint32_t k = 0; k < cnt; k += 4u) {
-            uint32_t jj[4];
-            float4 pp[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) jj[t] = (k + t < cnt) ? col[(k + t) * (uint32_t)CS] : i;
-#pragma unroll
-            for (int t = 0; t < 4; ++t) pp[t] = __ldg(sx + jj[t]);
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const float d2 = dist2_exact(pi, f3(pp[t]));
-                add(jj[t], pp[t], d2, k + t < cnt && (!SKIN || d2 < h2));
-            }
-        }
-    } else {
-        if (SKIN) atomicOr(L.ovf, 1u);
-        const Group<1> G;
-        group_walk<1>(
-            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
-            [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok(P, pj.w); },
-            [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2, true); });
-    }
-}
-
-// The list build of one fluid particle by its own stencil walk, the list
-// collected in its shared-memory column (stride CS words, cols entries;
-// a longer list continues in global memory, spill_list), then lambda's sums
-// over it (lambda_from_column).  Sets L.count[i].
+// The list build of one fluid particle by its own stencil walk, then
+// lambda's sums over the list (add(j, q_j, d2, ok)), which also store its
+// indices to the index list.  The walk's first `cols` chunks stay in the
+// lane's shared-memory column (chunk q at col[q * CS]); later ones go to
+// the global chunk buffer.  A list that does not fit, or passes the
+// neighbour cap, takes the exact capped walk instead.  SKIN: the list radius is
+// (1 + skin) h, and listed particles farther than h add nothing.  Sets
+// L.count[i].
 template <int RAD, int CS, bool SKIN, class Add>
 __device__ __forceinline__ void lambda_walk_particle(const DevParams &P, const NbList &L, uint32_t i, float3 pi,
                                                      const float4 *__restrict__ sx,
-                                                     const uint32_t *__restrict__ cell_first, uint32_t *col,
+                                                     const uint32_t *__restrict__ cell_first, uint2 *col,
                                                      uint32_t cols, Add &&add) {
     const int3 g = grid_pos(P, pi);
-    const uint32_t cap = L.capacity;
     int rad = P.fluid_rad;
     float reach2 = P.h2;
     bool trim = P.trim_fluid;
@@ -1406,41 +1255,75 @@ __device__ __forceinline__ void lambda_walk_particle(const DevParams &P, const N
             reach2 = lr * lr;
             trim = true;
         } else {
+            // the skin's stencil would alias on this grid (cells seen
+            // twice): a plain list, and no reuse this step
             atomicOr(L.ovf, 1u);
         }
     }
-    const uint32_t wend = cols * (uint32_t)CS;
-    uint32_t w = 0;      // word offset of this lane's next entry
-    uint32_t rfull = 0;  // ranges walked before the one that filled the column
+    const uint32_t cap = L.chunks;
+    uint32_t nch = 0, nnb = 0;
+    bool full = false;
     stencil_ranges_fixed<RAD>(P, pi, g, rad, reach2, trim, cell_first, [&](uint32_t b, uint32_t e) {
-#pragma unroll kWalkUnroll
-        for (uint32_t j = b; j < e; ++j) {
-            const float4 q = __ldg(sx + j);
-            const bool ok = dist2_exact(pi, f3(q)) < reach2 && j != i;
-            if (ok) col[w] = j;
-            w = ok ? min(w + (uint32_t)CS, wend) : w;
-        }
-        rfull += w < wend ? 1u : 0u;
-        return true;
+        return row_chunks(i, pi, reach2, b, e, sx, [&](uint2 ch) {
+            if (nch == cap) {  // does not fit: the rest of the walk does not matter
+                full = true;
+                return false;
+            }
+            if (nch < cols) col[nch * (uint32_t)CS] = ch;
+            else L.chunk[(size_t)nch * L.stride + i] = ch;
+            ++nch;
+            nnb += (uint32_t)__popc(ch.y);
+            return true;
+        });
     });
-    const bool spilled = w == wend && cols < cap;
-    const uint32_t cnt = spilled ? spill_list<RAD, CS>(P, i, pi, g, rad, reach2, trim, sx, cell_first, L, col, cols,
-                                                       rfull)
-                         : (w == wend) ? cap + 1u
-                                       : w / (uint32_t)CS;
-    L.count[i] = cnt;
-    lambda_from_column<CS, SKIN>(P, L, i, pi, g, sx, cell_first, col, cols, cnt, add);
+    const uint32_t c = full ? kListNone : (nch << 16) | nnb;
+    L.count[i] = c;
+    if (list_usable(P, L, c)) {
+        // four gathers in flight before their sums (slots past the end
+        // read this particle's own position and add nothing); each four
+        // neighbours go to the index list as one uint4
+        const float h2 = P.h2;
+        ChunkCursor cur;
+        auto load = [&](uint32_t q) { return q < cols ? col[q * (uint32_t)CS] : L.chunk[(size_t)q * L.stride + i]; };
+        cur.start(nch, load);
+        for (uint32_t k = 0; k < nnb; k += 4u) {
+            uint32_t jj[4];
+            float4 pp[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) jj[t] = cur.next(nch, i, load);
+            L.slot[(k >> 2) * L.stride + i] = make_uint4(jj[0], jj[1], jj[2], jj[3]);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) pp[t] = __ldg(sx + jj[t]);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const float d2 = dist2_exact(pi, f3(pp[t]));
+                add(jj[t], pp[t], d2, k + (uint32_t)t < nnb && (!SKIN || d2 < h2));
+            }
+        }
+    } else {
+        if (SKIN) atomicOr(L.ovf, 1u);  // this list cannot be reused
+        const Group<1> G;
+        group_walk<1>(
+            P, G, pi, g, P.fluid_rad, P.h2, P.trim_fluid, sx, cell_first, P.max_nb,
+            [&](uint32_t j, const float4 &pj, float d2) { return j != i && d2 < P.h2 && fluid_nb_ok(P, pj.w); },
+            [&](uint32_t j, const float4 &pj, float d2) { add(j, pj, d2, true); });
+    }
 }
 
-template <int RAD, bool B, bool SKIN>
-__global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
-                                                                const float4 *__restrict__ sx,
-                                                                const SortedAttr *__restrict__ sattr,
-                                                                const uint32_t *__restrict__ cell_first,
-                                                                float4 *__restrict__ sxl, NbList L,
-                                                                GasBuffers gas, uint32_t cols) {
-    extern __shared__ uint32_t s_nb[];
-    const uint32_t i = blockIdx.x * kListBlock + threadIdx.x;
+// findLambdasD (integration_kernel.cuh:481-593) with the list build, one
+// lane per particle (lambda_walk_particle; the first `cols` chunks of each
+// list in shared memory, col = s_col + lane with stride CS = the block
+// size, or none with cols = 0).  SKIN: the list has a skin (build
+// positions kept in L.sref), and when it is reused (*L.reuse) there is no
+// walk: the old list is filtered at the refreshed positions.  Output as
+// k_lambda.
+template <int RAD, bool B, bool SKIN, int CS>
+__device__ __forceinline__ void lambda_list_body(const DevParams &P0, uint32_t i, uint32_t n, uint32_t iter_left,
+                                                 const float4 *__restrict__ sx,
+                                                 const SortedAttr *__restrict__ sattr,
+                                                 const uint32_t *__restrict__ cell_first,
+                                                 float4 *__restrict__ sxl, const NbList &L,
+                                                 const GasBuffers &gas, uint2 *col, uint32_t cols) {
     if (i >= n) return;
     const DevParams P = scene_params<B>(P0, i);
     const bool reuse = SKIN && L.reuse && *L.reuse;
@@ -1468,7 +1351,7 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
     const float inv_rho0 = 1.f / a.rho0;
     const float spiky_r = -P.spiky * inv_rho0;
     LambdaAcc acc{0.f, 0.f, make_float3(0.f, 0.f, 0.f)};
-    auto add = [&](uint32_t j, const float4 &pj, float d2, bool ok = true) {
+    auto add = [&](uint32_t j, const float4 &pj, float d2, bool ok) {
         const float mf = nb_mass ? ((pj.w > 0.f) ? 1.f / pj.w : 0.f) : inv_w;
         acc.add(P, ok && fluid_nb_ok(P, pj.w), d2, pi - f3(pj), mf, spiky_r, density_weight(P, sattr, j));
     };
@@ -1476,14 +1359,40 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
         for_each_listed(L, i, L.count[i], [&](uint32_t j) {
             const float4 pj = __ldg(sx + j);
             const float d2 = dist2_exact(pi, f3(pj));
-            if (d2 < h2) add(j, pj, d2);
+            if (d2 < h2) add(j, pj, d2, true);
         });
     } else {
-        lambda_walk_particle<RAD, kListBlock, SKIN>(P, L, i, pi, sx, cell_first, s_nb + threadIdx.x, cols, add);
+        lambda_walk_particle<RAD, CS, SKIN>(P, L, i, pi, sx, cell_first, col, cols, add);
     }
     const float ro = acc.ro + P.poly6_self * inv_w;
     const float denom = acc.denom + dot3(acc.grad, acc.grad);
     sxl[i] = make_float4(pi.x, pi.y, pi.z, -(ro * inv_rho0 - 1.f) / (denom + P.relax));
+}
+
+// The list build with every chunk stored straight to the global list.
+template <int RAD, bool B, bool SKIN>
+__global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                        const float4 *__restrict__ sx,
+                                                        const SortedAttr *__restrict__ sattr,
+                                                        const uint32_t *__restrict__ cell_first,
+                                                        float4 *__restrict__ sxl, NbList L, GasBuffers gas) {
+    lambda_list_body<RAD, B, SKIN, 1>(P0, blockIdx.x * blockDim.x + threadIdx.x, n, iter_left, sx, sattr,
+                                      cell_first, sxl, L, gas, nullptr, 0u);
+}
+
+// The list build with each lane's first `cols` chunks in its column of a
+// [cols][kListBlock] uint2 array in shared memory (a warp's chunk stores
+// are 32 consecutive uint2, free of bank conflicts).
+template <int RAD, bool B, bool SKIN>
+__global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
+                                                                const float4 *__restrict__ sx,
+                                                                const SortedAttr *__restrict__ sattr,
+                                                                const uint32_t *__restrict__ cell_first,
+                                                                float4 *__restrict__ sxl, NbList L,
+                                                                GasBuffers gas, uint32_t cols) {
+    extern __shared__ uint2 s_col[];
+    lambda_list_body<RAD, B, SKIN, kListBlock>(P0, blockIdx.x * kListBlock + threadIdx.x, n, iter_left, sx, sattr,
+                                               cell_first, sxl, L, gas, s_col + threadIdx.x, cols);
 }
 
 // solveFluidsD (integration_kernel.cuh:596-642) over the lambda pass's list.
@@ -1946,11 +1855,12 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
     };
     bool listed = false;
     if constexpr (TPP == 1) {
-        const uint32_t cnt = use_list ? L.count[i] : 0u;
-        listed = use_list && list_usable(P, L, cnt);
+        const uint32_t c = use_list ? L.count[i] : 0u;
+        listed = use_list && list_usable(P, L, c);
+        const uint32_t cnt = listed ? list_nnb(c) : 0u;
         // the last lambda pass listed every neighbour of any phase; a
         // neighbour's fluid mass rides in vs.w (0 for the other phases)
-        for (uint32_t q = 0; listed && 4u * q < cnt; ++q) {
+        for (uint32_t q = 0; 4u * q < cnt; ++q) {
             const uint4 e = L.slot[q * L.stride + i];
             const uint32_t left = cnt - 4u * q;
             const uint32_t jj[4] = {e.x, left > 1u ? e.y : i, left > 2u ? e.z : i, left > 3u ? e.w : i};
@@ -2166,8 +2076,8 @@ void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, co
     }
     const bool shared = L.assemble == kListShared;
     const unsigned nbs = blocks_for(n, kListBlock);
-    const uint32_t cols = std::min(L.capacity, L.sref ? kSharedListColsSkin : kSharedListCols);
-    const size_t smem = (size_t)(cols + 1u) * kListBlock * sizeof(uint32_t);
+    const uint32_t cols = std::min(L.chunks, L.sref ? kSharedListColsSkin : kSharedListCols);
+    const size_t smem = (size_t)cols * kListBlock * sizeof(uint2);
 #define PBD_LIST(R, S)                                                                                      \
     if (shared)                                                                                             \
         k_lambda_slist<R, B, S><<<nbs, kListBlock, smem, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr,   \

@@ -22,13 +22,19 @@ struct GridBuffers {
     SortedAttr *sorted_attr;  // [cap] phase and rest density, sorted
 };
 
-// Per-iteration fluid neighbour lists (sorted indices in the reference's
-// visiting order, four per uint4, slot-major).
+// Per-iteration fluid neighbour lists: sorted indices in the reference's
+// visiting order, four per uint4, slot-major.  The lambda pass's walk first
+// records them as row chunks: chunk (b, m) stands for the sorted slots
+// b .. b + 31 of one stencil row, bit k of m set when slot b + k is a
+// neighbour; the chunks a particle's walk does not keep in shared memory
+// go to `chunk`.
 struct NbList {
     uint4 *slot;        // [capacity / 4][stride]
-    uint32_t *count;    // [stride] neighbours found (may exceed capacity)
+    uint32_t *count;    // [stride] neighbours (low 16 bits), chunks (high 16 bits); 0xffff0000: no list
     uint32_t capacity;  // neighbours per particle, a multiple of 4
     uint32_t stride;    // particles per slot row
+    uint2 *chunk;       // [chunks][stride]
+    uint32_t chunks;    // chunks per particle
     // Skin lists (reused by later iterations; all null / 0 when off): the
     // list radius is (1 + skin) h; sref holds the sorted positions it was
     // built from; *reuse (set on the device each iteration) selects
@@ -38,8 +44,9 @@ struct NbList {
     float4 *sref;
     const uint32_t *reuse;
     uint32_t *ovf;
-    // Where the lambda pass assembles a list before storing it: 0 = shared
-    // memory (capacities up to 88), 1 = registers.
+    // Where the lambda pass keeps a list's first chunks while it walks:
+    // 0 = shared memory, 1 = none (every chunk stored straight to the
+    // global list).
     uint32_t assemble;
 };
 

@@ -192,9 +192,26 @@ void free_grid(pbd_system *s) {
 
 void free_list(pbd_system *s) {
     dfree(s->nbl.slot);
+    dfree(s->nbl.chunk);
     dfree(s->nbl.count);
     s->nbl.capacity = 0;
+    s->nbl.chunks = 0;
     s->list_valid = false;
+}
+
+// The neighbour lists of a system with fluid: list_capacity indices per
+// particle, and as many row chunks as a quarter of that (a chunk holds a
+// neighbour or more).
+int alloc_list(pbd_system *s) {
+    if (!s->n_fluid || s->nbl.slot || !s->list_capacity) return PBD_OK;
+    const uint32_t chunks = s->list_capacity / 4u;
+    CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
+    CUDA_TRY(s, dalloc(&s->nbl.chunk, (size_t)chunks * s->cap));
+    CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
+    s->nbl.capacity = s->list_capacity;
+    s->nbl.chunks = chunks;
+    s->nbl.stride = s->cap;
+    return PBD_OK;
 }
 
 // Buffers of the skin-list schedule, once fluid and a skin are both there.
@@ -977,12 +994,7 @@ int pbd_add_particles(pbd_system *s, uint32_t n, const float *pos_w, const float
     if ((nf && cur.n_fluid == nf) || (ng && s->n_gas == ng))
         if (int rc = refresh_scenes(s)) return rc;
     if (s->n_fluid && !s->vs) CUDA_TRY(s, dalloc(&s->vs, s->cap));
-    if (s->n_fluid && !s->nbl.slot && s->list_capacity) {
-        CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
-        CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
-        s->nbl.capacity = s->list_capacity;
-        s->nbl.stride = s->cap;
-    }
+    if (int rc = alloc_list(s)) return rc;
     if (int rc = alloc_skin(s)) return rc;
     s->grid_valid = false;
     ++s->version;
@@ -1256,12 +1268,7 @@ int pbd_add_fluid_group(pbd_system *s, uint32_t first, uint32_t count, float res
     CUDA_TRY(s, cudaMemcpy(s->rho0 + first, ro.data(), count * 4ull, cudaMemcpyHostToDevice));
     if (int rc = refresh_scenes(s)) return rc;
     if (s->n_fluid && !s->vs) CUDA_TRY(s, dalloc(&s->vs, s->cap));
-    if (s->n_fluid && !s->nbl.slot && s->list_capacity) {
-        CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(s->list_capacity / 4u) * s->cap));
-        CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
-        s->nbl.capacity = s->list_capacity;
-        s->nbl.stride = s->cap;
-    }
+    if (int rc = alloc_list(s)) return rc;
     if (int rc = alloc_skin(s)) return rc;
     s->grid_valid = false;
     s->list_valid = false;
@@ -1538,12 +1545,7 @@ int pbd_set_tuning(pbd_system *s, const pbd_tuning *t) {
     if (cap != s->list_capacity) {
         free_list(s);
         s->list_capacity = cap;
-        if (s->n_fluid && cap) {
-            CUDA_TRY(s, dalloc(&s->nbl.slot, (size_t)(cap / 4u) * s->cap));
-            CUDA_TRY(s, dalloc(&s->nbl.count, s->cap));
-            s->nbl.capacity = cap;
-            s->nbl.stride = s->cap;
-        }
+        if (int rc = alloc_list(s)) return rc;
     }
     s->list_valid = false;
     ++s->version;

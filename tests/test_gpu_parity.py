@@ -577,15 +577,17 @@ def test_neighbor_list_capacity_and_fallback(capacity):
 @pytest.mark.parametrize("capacity,skin,squeeze", [(64, 0.0, 1.0), (24, 0.0, 1.0), (48, 0.0, 1.0), (92, 0.0, 1.0),
                                                    (92, 0.0, 0.8), (44, 0.0, 0.8), (80, 0.2, 1.0), (128, 0.5, 1.0)])
 def test_list_assembly_shared_equals_registers(capacity, skin, squeeze):
-    """The lambda pass assembles a particle's neighbour list in shared
-    memory (list_assembly 0) or in registers (1): the same neighbours in
-    the same order with the same arithmetic, so updates agree bit for bit,
-    also when particles overflow the list (24), when the shared columns
-    (48 entries) are the whole list (48), and when particles with more
-    neighbours than the columns hold continue their lists in global
-    memory: a fluid squeezed to 0.8 of its lattice spacing (~70
-    neighbours; with a list of 92, and of 44 where they overflow) and a
-    skin list of 1.5 h (~110 entries against 88 skin columns)."""
+    """The lambda pass keeps the first row chunks of a particle's walk in
+    shared memory (list_assembly 0) or stores every chunk to the global
+    chunk buffer (1): the same neighbours in the same order with the same
+    arithmetic, so updates agree bit for bit, also when particles overflow
+    the list (24 entries, 6 chunks), when the chunk buffer is as large as
+    the shared columns (48 entries: 12 chunks), and when particles have
+    more chunks than the shared columns hold and continue in global memory:
+    a fluid squeezed to 0.8 of its lattice spacing (~70 neighbours, rows of
+    more than 32 candidates; with a list of 92, and of 44 where they
+    overflow) and a skin list of 1.5 h (a 25-row stencil against 20 skin
+    columns)."""
     mode = 0
     sc = W.dam_break(24, 20, 12)
     sc.pos_w[:, :3] *= squeeze
