@@ -1039,25 +1039,15 @@ __device__ __forceinline__ bool list_usable(const DevParams &P, const NbList &L,
 }
 
 // Steps through a chunk list: next() returns the next neighbour's sorted
-// slot, or `self` past the end.  load(q) returns chunk q.  The chunk after
-// the current one is loaded when the current one is taken up, so its load
-// overlaps the current chunk's neighbours instead of waiting at the chunk
-// boundary.
+// slot, or `self` past the end.  load(q) returns chunk q.
 struct ChunkCursor {
     uint32_t b = 0u, m = 0u, q = 0u;
-    uint2 nxt = make_uint2(0u, 0u);
-    template <class Load>
-    __device__ __forceinline__ void start(uint32_t nch, Load &&load) {
-        if (nch > 0u) nxt = load(0u);
-        q = 1u;
-    }
     template <class Load>
     __device__ __forceinline__ uint32_t next(uint32_t nch, uint32_t self, Load &&load) {
-        if (m == 0u && q <= nch) {
-            b = nxt.x;
-            m = nxt.y;
-            if (q < nch) nxt = load(q);
-            ++q;
+        if (m == 0u && q < nch) {
+            const uint2 c = load(q++);
+            b = c.x;
+            m = c.y;
         }
         if (m == 0u) return self;
         const uint32_t k = (uint32_t)__ffs(m) - 1u;
@@ -1117,12 +1107,16 @@ __device__ __forceinline__ bool row_chunks(uint32_t i, float3 pi, float reach2, 
                                            const float4 *__restrict__ sx, Emit &&emit) {
     for (uint32_t c = b; c < e; c += 32u) {
         const uint32_t len = min(32u, e - c);
+        // candidate k shifts in its test bit: the sign of d2 - reach2 is
+        // the test d2 < reach2 (the rounded difference keeps the sign of
+        // the exact one, and a NaN result is positive on the GPU)
         uint32_t m = 0u;
 #pragma unroll kWalkUnroll
         for (uint32_t k = 0; k < len; ++k) {
             const float4 q = __ldg(sx + c + k);
-            m |= (dist2_exact(pi, f3(q)) < reach2 ? 1u : 0u) << k;
+            m = (m << 1) | (__float_as_uint(__fsub_rn(dist2_exact(pi, f3(q)), reach2)) >> 31);
         }
+        m = __brev(m) >> (32u - len);            // candidate k at bit k
         if (i - c < len) m &= ~(1u << (i - c));  // not itself
         if (m && !emit(make_uint2(c, m))) return false;
     }
@@ -1285,7 +1279,6 @@ __device__ __forceinline__ void lambda_walk_particle(const DevParams &P, const N
         const float h2 = P.h2;
         ChunkCursor cur;
         auto load = [&](uint32_t q) { return q < cols ? col[q * (uint32_t)CS] : L.chunk[(size_t)q * L.stride + i]; };
-        cur.start(nch, load);
         for (uint32_t k = 0; k < nnb; k += 4u) {
             uint32_t jj[4];
             float4 pp[4];
