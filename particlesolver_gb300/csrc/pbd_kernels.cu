@@ -1125,9 +1125,9 @@ __device__ __forceinline__ bool row_chunks(uint32_t i, float3 pi, float reach2, 
 
 // Stencil ranges with the radius fixed at compile time (RAD > 0; RAD = 0
 // defers to the runtime version).  The per-axis slab gaps are computed once
-// and, per z slab, all 2 RAD + 1 row ranges are fetched before any of them
-// is walked, so their cell-offset loads overlap instead of each row waiting
-// for its own.  The x extent of a kept row comes from a reciprocal square
+// and, per z slab, all 2 RAD + 1 row ranges are fetched together, one slab
+// ahead of the walk, so their cell-offset loads overlap each other and the
+// walk of the slab before.  The x extent of a kept row comes from a reciprocal square
 // root (its rounding is covered by the 1e-3-cell widening).  Same visiting
 // order and the same exactness conditions as stencil_ranges; a slab with a
 // wrapping row is walked row by row, cell by cell where it wraps.
@@ -1149,19 +1149,19 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
         gy2[k] = t * t;
     }
     const bool flat = (P.flags & kFlagTwoD) != 0u;  // 2-D: the particles' own z layer only
-#pragma unroll 1
-    for (int kz = flat ? RAD : 0; kz < (flat ? RAD + 1 : W); ++kz) {
+    const int kz0 = flat ? RAD : 0, kz1 = flat ? RAD + 1 : W;
+    // The row ranges of slab kz (empty rows: b = e = 0); true when a kept
+    // row wraps in x.
+    auto fetch = [&](int kz, uint32_t (&rb)[W], uint32_t (&re)[W]) {
         const float tz = trim && !flat ? slab_gap(q.z, P.origin.z, P.cell, g.z + kz - RAD) : 0.f;
         const float gz2 = tz * tz;
-        if (gz2 > lim) continue;
         const uint32_t zrow = ((uint32_t)(g.z + kz - RAD) & (P.gz - 1u)) * P.gy;
-        uint32_t rb[W], re[W];
         bool wraps = false;
 #pragma unroll
         for (int ky = 0; ky < W; ++ky) {
             rb[ky] = re[ky] = 0u;  // empty unless kept
             const float gyz2 = gz2 + gy2[ky];
-            if (gyz2 <= lim) {
+            if (gz2 <= lim && gyz2 <= lim) {
                 int a = -RAD, b = RAD;
                 if (trim) {
                     const float r2 = lim - gyz2;
@@ -1182,6 +1182,16 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
                 }
             }
         }
+        return wraps;
+    };
+    // the next slab's cell-offset loads are issued before this slab is
+    // walked, so they arrive during the walk
+    uint32_t rb[W], re[W], nb[W], ne[W];
+    bool wraps = fetch(kz0, rb, re);
+#pragma unroll 1
+    for (int kz = kz0; kz < kz1; ++kz) {
+        bool nwraps = false;
+        if (kz + 1 < kz1) nwraps = fetch(kz + 1, nb, ne);
         if (!wraps) {
 #pragma unroll
             for (int ky = 0; ky < W; ++ky)
@@ -1189,10 +1199,13 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
         } else {
             // rare: recompute each row (no indexed arrays, which would live
             // in local memory) and walk wrapping rows cell by cell
+            const float tz = trim && !flat ? slab_gap(q.z, P.origin.z, P.cell, g.z + kz - RAD) : 0.f;
+            const float gz2 = tz * tz;
+            const uint32_t zrow = ((uint32_t)(g.z + kz - RAD) & (P.gz - 1u)) * P.gy;
 #pragma unroll 1
             for (int ky = 0; ky < W; ++ky) {
                 const float gyz2 = gz2 + (trim ? sq(slab_gap(q.y, P.origin.y, P.cell, g.y + ky - RAD)) : 0.f);
-                if (gyz2 > lim) continue;
+                if (gz2 > lim || gyz2 > lim) continue;
                 int a = -RAD, b = RAD;
                 if (trim) {
                     const float r2 = lim - gyz2;
@@ -1213,6 +1226,12 @@ __device__ __forceinline__ void stencil_ranges_fixed(const DevParams &P, float3 
                     }
                 }
             }
+        }
+        wraps = nwraps;
+#pragma unroll
+        for (int ky = 0; ky < W; ++ky) {
+            rb[ky] = nb[ky];
+            re[ky] = ne[ky];
         }
     }
 }
