@@ -29,7 +29,7 @@ constexpr int kBlock = 256;
 #define PBD_DELTA_QUADS 1
 #endif
 #ifndef PBD_SOLVE_MIN_BLOCKS
-#define PBD_SOLVE_MIN_BLOCKS 4
+#define PBD_SOLVE_MIN_BLOCKS 5
 #endif
 #ifndef PBD_CONTACT_MIN_BLOCKS
 #define PBD_CONTACT_MIN_BLOCKS 8
@@ -38,7 +38,7 @@ constexpr int kBlock = 256;
 #define PBD_LAMBDA_MIN_BLOCKS 6
 #endif
 #ifndef PBD_BATCH_SOLVE_MIN_BLOCKS
-#define PBD_BATCH_SOLVE_MIN_BLOCKS PBD_SOLVE_MIN_BLOCKS
+#define PBD_BATCH_SOLVE_MIN_BLOCKS 4
 #endif
 constexpr int kWalkUnroll = PBD_WALK_UNROLL;
 // Block of the shared-memory list build, and the row chunks per particle
@@ -1259,7 +1259,12 @@ __device__ __forceinline__ void lambda_walk_particle(const DevParams &P, const N
     const int3 g = grid_pos(P, pi);
     int rad = P.fluid_rad;
     float reach2 = P.h2;
-    bool trim = P.trim_fluid;
+    // A three-cell stencil is walked whole: the walk is bound by L1 sectors,
+    // and lanes of one cell then walk the same rows and load the same
+    // candidates together, which saves more sectors than trimming each
+    // particle's rows and cells saves candidates.  Wider stencils (cells
+    // smaller than h: about one particle per cell) are trimmed.
+    bool trim = RAD == 1 ? false : P.trim_fluid && rad > 1;
     if (SKIN) {
         const int r = list_rad(P, L.skin);
         if ((uint32_t)(2 * r + 1) <= min(P.gx, min(P.gy, P.gz))) {
