@@ -8,6 +8,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <utility>
 
 namespace pbd {
 
@@ -63,6 +64,42 @@ inline unsigned blocks_for(uint32_t n, int per_block = kBlock) {
     return (unsigned)((n + (uint32_t)per_block - 1u) / (uint32_t)per_block);
 }
 
+// Programmatic dependent launch.  The step's kernels are launched with
+// pdl_launch; pdl_launch<true> (the grid build's short kernels) lets a
+// kernel be scheduled while its predecessor in the stream is still
+// running.  Each of these kernels starts with pdl_entry(): it waits there
+// until the predecessor has completed and its writes are visible, and then
+// allows its own successor to be scheduled (once every one of its blocks
+// has got that far), so launch latencies and prologues overlap the
+// predecessors' last waves.  A kernel launched the usual way
+// (pdl_launch<false>) passes pdl_entry() at once.  Measured on the 1M dam
+// break: eager grid builds 0.249 -> 0.200 ms per step; in graph replay the
+// grid kernels gain nothing measurable, and early launch of the long
+// per-particle passes cost 1.5 %, so those are launched the usual way.
+#ifndef PBD_PDL
+#define PBD_PDL 1
+#endif
+__device__ __forceinline__ void pdl_entry() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <bool PDL = true, typename... KArgs, typename... Args>
+inline void pdl_launch(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                       Args &&...args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = PDL && PBD_PDL;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // ---------------------------------------------------------------- predict
 
 // integrate_functor + copyToXstar (integration_kernel.cuh:159-184,
@@ -86,6 +123,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(DevParams P0, uint32_t n, fl
                                                     uint32_t *__restrict__ slot,
                                                     uint32_t *__restrict__ counts,
                                                     GasBuffers gas) {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DevParams P = scene_params<B>(P0, i);
@@ -127,6 +165,7 @@ __global__ void __launch_bounds__(kBlock) k_hash_count(DevParams P0, uint32_t n,
                                                        uint32_t *__restrict__ slot,
                                                        uint32_t *__restrict__ counts,
                                                        const uint32_t *__restrict__ skip) {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (skip && *skip)) return;
     const DevParams P = scene_params<B>(P0, i);
@@ -173,6 +212,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__
                                                               uint32_t elements,
                                                               uint32_t *__restrict__ partials,
                                                               const uint32_t *__restrict__ skip) {
+    pdl_entry();
     if (skip && *skip) return;
     __shared__ uint32_t smem[32];
     const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -188,6 +228,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__
 __global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t *__restrict__ partials,
                                                                 uint32_t count,
                                                                 const uint32_t *__restrict__ skip) {
+    pdl_entry();
     if (skip && *skip) return;
     __shared__ uint32_t smem[32];
     uint32_t carry = 0;
@@ -214,6 +255,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint32_t *__restric
                                                              uint32_t elements,
                                                              const uint32_t *__restrict__ partials,
                                                              const uint32_t *__restrict__ skip) {
+    pdl_entry();
     if (skip && *skip) return;
     __shared__ uint32_t smem[32];
     const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -238,6 +280,7 @@ __global__ void __launch_bounds__(kBlock) k_bucket(uint32_t n, const uint32_t *_
                                                    const uint32_t *__restrict__ slot,
                                                    const uint32_t *__restrict__ cell_first,
                                                    uint32_t *__restrict__ tmp, const uint32_t *__restrict__ skip) {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (skip && *skip)) return;
     tmp[cell_first[hash[i]] + slot[i]] = i;
@@ -261,6 +304,7 @@ __global__ void __launch_bounds__(kBlock) k_rank_reorder(uint32_t n, const uint3
                                                          float4 *__restrict__ sorted_x,
                                                          SortedAttr *__restrict__ sorted_attr,
                                                          const uint32_t *__restrict__ skip) {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (skip && *skip)) return;
     const uint32_t h = hash[i];
@@ -314,6 +358,7 @@ __global__ void __launch_bounds__(kBlock) k_refresh_sorted(uint32_t n, const uin
 // Cell counts cleared (the memset of a grid build), unless *skip.
 __global__ void __launch_bounds__(kBlock) k_clear_counts(uint32_t elements, uint32_t *__restrict__ counts,
                                                          const uint32_t *__restrict__ skip) {
+    pdl_entry();
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= elements || *skip) return;
     counts[c] = 0u;
@@ -579,6 +624,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams P0, uint32_t n, uin
                                                    const SortedAttr *__restrict__ sattr,
                                                    const uint32_t *__restrict__ cell_first,
                                                    float4 *__restrict__ sxl, GasBuffers gas) {
+    pdl_entry();
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -1393,6 +1439,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
                                                         const SortedAttr *__restrict__ sattr,
                                                         const uint32_t *__restrict__ cell_first,
                                                         float4 *__restrict__ sxl, NbList L, GasBuffers gas) {
+    pdl_entry();
     lambda_list_body<RAD, B, SKIN, 1>(P0, blockIdx.x * blockDim.x + threadIdx.x, n, iter_left, sx, sattr,
                                       cell_first, sxl, L, gas, nullptr, 0u);
 }
@@ -1407,6 +1454,7 @@ __global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_sl
                                                                 const uint32_t *__restrict__ cell_first,
                                                                 float4 *__restrict__ sxl, NbList L,
                                                                 GasBuffers gas, uint32_t cols) {
+    pdl_entry();
     extern __shared__ uint2 s_col[];
     lambda_list_body<RAD, B, SKIN, kListBlock>(P0, blockIdx.x * kListBlock + threadIdx.x, n, iter_left, sx, sattr,
                                                cell_first, sxl, L, gas, s_col + threadIdx.x, cols);
@@ -1553,6 +1601,7 @@ __global__ void __launch_bounds__(kBlock, solve_min_blocks(TPP, B, NOFLUID)) k_s
                                                   const float4 *__restrict__ x_old,
                                                   float4 *__restrict__ x, NbList L, bool use_list,
                                                   GasBuffers gas, RigidSdf rs) {
+    pdl_entry();
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -1607,6 +1656,7 @@ __global__ void __launch_bounds__(kBlock) k_distance_gather(DevParams P0, uint32
                                                             const float *__restrict__ occ,
                                                             const float4 *__restrict__ x,
                                                             float4 *__restrict__ out) {
+    pdl_entry();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= count) return;
     const uint32_t k = particle[s];
@@ -1645,6 +1695,7 @@ __global__ void __launch_bounds__(kBlock) k_distance_apply(DevParams P0, uint32_
                                                            const float4 *__restrict__ pin,
                                                            int apply_distance, int apply_pins,
                                                            float4 *__restrict__ x) {
+    pdl_entry();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= count) return;
     const uint32_t k = particle[s];
@@ -1738,6 +1789,7 @@ __global__ void __launch_bounds__(kBlock) k_shapes(DevParams P0, uint32_t iter_l
                                                    const float4 *__restrict__ rest,
                                                    float4 *__restrict__ quat,
                                                    float4 *__restrict__ x) {
+    pdl_entry();
     const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (b >= bodies) return;
@@ -1804,6 +1856,7 @@ __global__ void __launch_bounds__(kBlock) k_velocity(DevParams P0, uint32_t n, f
                                                      const float4 *__restrict__ x,
                                                      const float4 *__restrict__ x_old,
                                                      float4 *__restrict__ v) {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = x[i], o = x_old[i];
@@ -1825,6 +1878,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph_gather(DevParams P0, uint32_t n
                                                         const float4 *__restrict__ x,
                                                         const float4 *__restrict__ x_old, float4 *__restrict__ v,
                                                         float4 *__restrict__ vs) {
+    pdl_entry();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t o = sidx[i];
@@ -1854,6 +1908,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
                                                  const uint32_t *__restrict__ cell_first,
                                                  const float4 *__restrict__ vs,
                                                  float4 *__restrict__ v, NbList L, bool use_list) {
+    pdl_entry();
     const Group<TPP> G;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     if (i >= n) return;
@@ -1990,26 +2045,26 @@ cudaError_t launch_predict(const DevParams &P, uint32_t n, float dt, float4 *x, 
                            float4 *x_old, uint32_t *hash, uint32_t *slot, uint32_t *counts,
                            cudaStream_t s, const GasBuffers &gas) {
     if (n == 0) return cudaSuccess;
-    if (P.table) k_predict<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts, gas);
-    else k_predict<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, v, x_old, hash, slot, counts, gas);
+    if (P.table) pdl_launch<false>(k_predict<true>, blocks_for(n), kBlock, 0, s, P, n, dt, x, v, x_old, hash, slot, counts, gas);
+    else pdl_launch<false>(k_predict<false>, blocks_for(n), kBlock, 0, s, P, n, dt, x, v, x_old, hash, slot, counts, gas);
     return cudaGetLastError();
 }
 
 cudaError_t launch_hash_count(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash,
                               uint32_t *slot, uint32_t *counts, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (P.table) k_hash_count<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, nullptr);
-    else k_hash_count<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, nullptr);
+    if (P.table) pdl_launch(k_hash_count<true>, blocks_for(n), kBlock, 0, s, P, n, x, hash, slot, counts, nullptr);
+    else pdl_launch(k_hash_count<false>, blocks_for(n), kBlock, 0, s, P, n, x, hash, slot, counts, nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_grid_begin(const DevParams &P, uint32_t n, const float4 *x, uint32_t *hash, uint32_t *slot,
                               uint32_t *counts, const uint32_t *skip, cudaStream_t s) {
     const uint32_t elements = P.num_cells + 1u;
-    k_clear_counts<<<blocks_for(elements), kBlock, 0, s>>>(elements, counts, skip);
+    pdl_launch(k_clear_counts, blocks_for(elements), kBlock, 0, s, elements, counts, skip);
     if (n) {
-        if (P.table) k_hash_count<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, skip);
-        else k_hash_count<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, x, hash, slot, counts, skip);
+        if (P.table) pdl_launch(k_hash_count<true>, blocks_for(n), kBlock, 0, s, P, n, x, hash, slot, counts, skip);
+        else pdl_launch(k_hash_count<false>, blocks_for(n), kBlock, 0, s, P, n, x, hash, slot, counts, skip);
     }
     return cudaGetLastError();
 }
@@ -2029,9 +2084,9 @@ cudaError_t launch_skin_check(const DevParams &P, uint32_t n, uint32_t iter, flo
 cudaError_t launch_exclusive_scan(uint32_t *data, uint32_t elements, uint32_t *partials,
                                   cudaStream_t s, const uint32_t *skip) {
     const uint32_t tiles = (uint32_t)scan_partial_count(elements);
-    k_scan_reduce<<<tiles, kScanThreads, 0, s>>>(data, elements, partials, skip);
-    k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, tiles, skip);
-    k_scan_apply<<<tiles, kScanThreads, 0, s>>>(data, elements, partials, skip);
+    pdl_launch(k_scan_reduce, tiles, kScanThreads, 0, s, data, elements, partials, skip);
+    pdl_launch(k_scan_partials, 1, kScanThreads, 0, s, partials, tiles, skip);
+    pdl_launch(k_scan_apply, tiles, kScanThreads, 0, s, data, elements, partials, skip);
     return cudaGetLastError();
 }
 
@@ -2040,8 +2095,8 @@ cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers
                                cudaStream_t s, const uint32_t *skip) {
     cudaError_t e = launch_exclusive_scan(g.cell_first, P.num_cells + 1u, g.scan_part, s, skip);
     if (e != cudaSuccess || n == 0) return e;
-    k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.slot, g.cell_first, g.tmp, skip);
-    k_rank_reorder<<<blocks_for(n), kBlock, 0, s>>>(n, g.hash, g.cell_first, g.tmp, x, phase, rho0,
+    pdl_launch(k_bucket, blocks_for(n), kBlock, 0, s, n, g.hash, g.slot, g.cell_first, g.tmp, skip);
+    pdl_launch(k_rank_reorder, blocks_for(n), kBlock, 0, s, n, g.hash, g.cell_first, g.tmp, x, phase, rho0,
                                                     g.sorted_idx, g.sorted_x, g.sorted_attr, skip);
     return cudaGetLastError();
 }
@@ -2054,7 +2109,7 @@ cudaError_t launch_sort_into_cells(const DevParams &P, uint32_t n, const float4 
     if ((e = launch_hash_count(P, n, x, hash, slot, cell_first, s)) != cudaSuccess) return e;
     if ((e = launch_exclusive_scan(cell_first, P.num_cells + 1u, partials, s)) != cudaSuccess) return e;
     if (n) {
-        k_bucket<<<blocks_for(n), kBlock, 0, s>>>(n, hash, slot, cell_first, tmp, nullptr);
+        pdl_launch(k_bucket, blocks_for(n), kBlock, 0, s, n, hash, slot, cell_first, tmp, nullptr);
         k_rank_only<<<blocks_for(n), kBlock, 0, s>>>(n, hash, cell_first, tmp, sorted_idx);
     }
     k_cell_ranges<<<blocks_for(P.num_cells), kBlock, 0, s>>>(P.num_cells, cell_first, cell_start, cell_end);
@@ -2071,12 +2126,12 @@ cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4
 // Dispatches a kernel template over the supported group sizes (B: batched).
 #define PBD_TPP_DISPATCH(tpp, B, KERNEL, ...)                                             \
     switch (tpp) {                                                                        \
-    case 1: KERNEL<1, B><<<blocks_for(n * 1u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 2: KERNEL<2, B><<<blocks_for(n * 2u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 4: KERNEL<4, B><<<blocks_for(n * 4u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 8: KERNEL<8, B><<<blocks_for(n * 8u), kBlock, 0, s>>>(__VA_ARGS__); break;      \
-    case 16: KERNEL<16, B><<<blocks_for(n * 16u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
-    default: KERNEL<32, B><<<blocks_for(n * 32u), kBlock, 0, s>>>(__VA_ARGS__); break;   \
+    case 1: pdl_launch<false>(KERNEL<1, B>, blocks_for(n * 1u), kBlock, 0, s, __VA_ARGS__); break;      \
+    case 2: pdl_launch<false>(KERNEL<2, B>, blocks_for(n * 2u), kBlock, 0, s, __VA_ARGS__); break;      \
+    case 4: pdl_launch<false>(KERNEL<4, B>, blocks_for(n * 4u), kBlock, 0, s, __VA_ARGS__); break;      \
+    case 8: pdl_launch<false>(KERNEL<8, B>, blocks_for(n * 8u), kBlock, 0, s, __VA_ARGS__); break;      \
+    case 16: pdl_launch<false>(KERNEL<16, B>, blocks_for(n * 16u), kBlock, 0, s, __VA_ARGS__); break;   \
+    default: pdl_launch<false>(KERNEL<32, B>, blocks_for(n * 32u), kBlock, 0, s, __VA_ARGS__); break;   \
     }
 
 template <bool B>
@@ -2097,10 +2152,10 @@ void lambda_list_dispatch(const DevParams &P, uint32_t n, uint32_t iter_left, co
     const size_t smem = (size_t)cols * kListBlock * sizeof(uint2);
 #define PBD_LIST(R, S)                                                                                      \
     if (shared)                                                                                             \
-        k_lambda_slist<R, B, S><<<nbs, kListBlock, smem, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr,   \
+        pdl_launch<false>(k_lambda_slist<R, B, S>, nbs, kListBlock, smem, s, P, n, iter_left, g.sorted_x, g.sorted_attr,   \
                                                               g.cell_first, sxl, L, gas, cols);             \
     else                                                                                                    \
-        k_lambda_list<R, B, S><<<nb, kBlock, 0, s>>>(P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, \
+        pdl_launch<false>(k_lambda_list<R, B, S>, nb, kBlock, 0, s, P, n, iter_left, g.sorted_x, g.sorted_attr, g.cell_first, \
                                                      sxl, L, gas)
     if (L.sref) {
         if (rad == 1) {
@@ -2145,11 +2200,11 @@ cudaError_t launch_solve(const DevParams &P, uint32_t n, uint32_t mask, uint32_t
     use_list = use_list && L.slot != nullptr;
     if (tpp == 1 && !(mask & kDoFluid)) {
         if (P.table)
-            k_solve<1, true, true><<<blocks_for(n), kBlock, 0, s>>>(P, n, mask, iter_left, g.sorted_x, g.sorted_attr,
+            pdl_launch<false>(k_solve<1, true, true>, blocks_for(n), kBlock, 0, s, P, n, mask, iter_left, g.sorted_x, g.sorted_attr,
                                                                      g.sorted_idx, g.cell_first, sxl, x_old, x, L,
                                                                      use_list, gas, sdf);
         else
-            k_solve<1, false, true><<<blocks_for(n), kBlock, 0, s>>>(P, n, mask, iter_left, g.sorted_x,
+            pdl_launch<false>(k_solve<1, false, true>, blocks_for(n), kBlock, 0, s, P, n, mask, iter_left, g.sorted_x,
                                                                       g.sorted_attr, g.sorted_idx, g.cell_first, sxl,
                                                                       x_old, x, L, use_list, gas, sdf);
         return cudaGetLastError();
@@ -2174,14 +2229,14 @@ cudaError_t launch_distance(const DevParams &P, uint32_t iter_left, const Constr
     const int ad = apply_distance ? 1 : 0, ap = apply_pins ? 1 : 0;
     if (P.table) {
         if (apply_distance)
-            k_distance_gather<true><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.row, c.other, c.rest,
+            pdl_launch<false>(k_distance_gather<true>, nb, kBlock, 0, s, P, c.count, iter_left, c.particle, c.row, c.other, c.rest,
                                                           c.stiff, c.occ, x, c.tmp);
-        k_distance_apply<true><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.tmp, c.pin, ad, ap, x);
+        pdl_launch<false>(k_distance_apply<true>, nb, kBlock, 0, s, P, c.count, iter_left, c.particle, c.tmp, c.pin, ad, ap, x);
     } else {
         if (apply_distance)
-            k_distance_gather<false><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.row, c.other, c.rest,
+            pdl_launch<false>(k_distance_gather<false>, nb, kBlock, 0, s, P, c.count, iter_left, c.particle, c.row, c.other, c.rest,
                                                            c.stiff, c.occ, x, c.tmp);
-        k_distance_apply<false><<<nb, kBlock, 0, s>>>(P, c.count, iter_left, c.particle, c.tmp, c.pin, ad, ap, x);
+        pdl_launch<false>(k_distance_apply<false>, nb, kBlock, 0, s, P, c.count, iter_left, c.particle, c.tmp, c.pin, ad, ap, x);
     }
     return cudaGetLastError();
 }
@@ -2189,16 +2244,16 @@ cudaError_t launch_distance(const DevParams &P, uint32_t iter_left, const Constr
 cudaError_t launch_shapes(const DevParams &P, uint32_t iter_left, const BodyBuffers &b, float4 *x, cudaStream_t s) {
     if (b.count == 0) return cudaSuccess;
     const unsigned nb = blocks_for(b.count * 32u);
-    if (P.table) k_shapes<true><<<nb, kBlock, 0, s>>>(P, iter_left, b.count, b.range, b.stiff, b.rest, b.quat, x);
-    else k_shapes<false><<<nb, kBlock, 0, s>>>(P, iter_left, b.count, b.range, b.stiff, b.rest, b.quat, x);
+    if (P.table) pdl_launch<false>(k_shapes<true>, nb, kBlock, 0, s, P, iter_left, b.count, b.range, b.stiff, b.rest, b.quat, x);
+    else pdl_launch<false>(k_shapes<false>, nb, kBlock, 0, s, P, iter_left, b.count, b.range, b.stiff, b.rest, b.quat, x);
     return cudaGetLastError();
 }
 
 cudaError_t launch_velocity(const DevParams &P, uint32_t n, float dt, const float4 *x, const float4 *x_old,
                             float4 *v, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    if (P.table) k_velocity<true><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, x_old, v);
-    else k_velocity<false><<<blocks_for(n), kBlock, 0, s>>>(P, n, dt, x, x_old, v);
+    if (P.table) pdl_launch<false>(k_velocity<true>, blocks_for(n), kBlock, 0, s, P, n, dt, x, x_old, v);
+    else pdl_launch<false>(k_velocity<false>, blocks_for(n), kBlock, 0, s, P, n, dt, x, x_old, v);
     return cudaGetLastError();
 }
 
@@ -2209,13 +2264,13 @@ cudaError_t launch_xsph(const DevParams &P, uint32_t n, const GridBuffers &g, fl
     use_list = use_list && L.slot != nullptr;
     const unsigned nb = blocks_for(n);
     if (x && P.table)
-        k_xsph_gather<true, true><<<nb, kBlock, 0, s>>>(P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x, x_old,
+        pdl_launch<false>(k_xsph_gather<true, true>, nb, kBlock, 0, s, P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x, x_old,
                                                          v, vs);
     else if (x)
-        k_xsph_gather<false, true><<<nb, kBlock, 0, s>>>(P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x, x_old,
+        pdl_launch<false>(k_xsph_gather<false, true>, nb, kBlock, 0, s, P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x, x_old,
                                                           v, vs);
     else
-        k_xsph_gather<false, false><<<nb, kBlock, 0, s>>>(P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x,
+        pdl_launch<false>(k_xsph_gather<false, false>, nb, kBlock, 0, s, P, n, dt, g.sorted_idx, g.sorted_x, g.sorted_attr, x,
                                                            x_old, v, vs);
     if (P.table) {
         PBD_TPP_DISPATCH(tpp, true, k_xsph, P, n, g.sorted_x, g.sorted_attr, g.sorted_idx, g.cell_first, vs, v, L,
