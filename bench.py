@@ -39,7 +39,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "1M-particle PBF steps/s: plain vs batched/adjoint, same GPU, <=1e-5 proj err"
 UNIT = "steps/s"
 
-LIST_ASSEMBLY = {0: "shared memory", 1: "registers"}
+LIST_ASSEMBLY = {0: "row chunks in shared memory", 1: "row chunks in global memory"}
 
 # Algorithmic bytes (compulsory FP32 traffic, each array touched once per pass)
 B_LAMBDA = 20      # read x* 16 + write lambda 4, per particle

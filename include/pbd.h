@@ -469,8 +469,9 @@ typedef struct pbd_tuning {
     uint32_t neighbor_list_capacity; /* with threads_per_particle == 1: fluid
                                       neighbours recorded per particle and
                                       iteration (multiple of 4, 0 = no list,
-                                      default 256); particles with more fall
-                                      back to the stencil walk              */
+                                      default 256), and a quarter as many row
+                                      chunks; particles with more fall back
+                                      to the stencil walk                   */
     float neighbor_skin;           /* with a list: its radius is (1 + skin) h
                                       and it is reused by the later
                                       iterations of a step while no particle
@@ -482,13 +483,14 @@ typedef struct pbd_tuning {
                                       the summation order differs.  0 = off
                                       (grid and list rebuilt every
                                       iteration, the reference's schedule)  */
-    uint32_t list_assembly;        /* with a list: where the lambda pass
-                                      collects a particle's neighbours before
-                                      storing them: 0 = shared memory, one
-                                      column of 48 entries per thread (88
-                                      with a skin; a longer list continues
-                                      in global memory; default), 1 =
-                                      registers                             */
+    uint32_t list_assembly;        /* with a list: where the lambda pass's
+                                      walk keeps a particle's row chunks (a
+                                      run of up to 32 candidates of one
+                                      stencil row and a bit per neighbour):
+                                      0 = the first 12 in shared memory (20
+                                      with a skin), the rest in a global
+                                      buffer (default); 1 = all in the
+                                      global buffer                         */
     uint32_t reserved[4];          /* zero                                  */
 } pbd_tuning;
 

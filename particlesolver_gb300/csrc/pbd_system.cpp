@@ -1597,7 +1597,7 @@ int pbd_autotune(pbd_system *s, float dt, uint32_t steps, void *stream, pbd_tuni
     };
     // candidates: one lane per particle with neighbour lists rebuilt every
     // iteration or kept with a skin of 0.1, 0.2, 0.3 h (list capacity grown
-    // with the list volume), the register list build, the lane groups and,
+    // with the list volume), the list build without shared memory, the lane groups and,
     // in a system without contacts, cells of half the size (the contact
     // walk's one-cell reach needs the cell of at least the contact
     // distance)
