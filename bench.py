@@ -302,6 +302,11 @@ def run_batched(args, dev, stream, flush):
     torch.cuda.synchronize()
     t_batch = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     launches = batch.profile()["kernel_launches"]
+    tun = batch.tuning()
+    tuning = {"threads_per_particle": int(tun.threads_per_particle), "neighbor_skin": round(float(tun.neighbor_skin), 4),
+              "neighbor_list_capacity": int(tun.neighbor_list_capacity),
+              "list_assembly": LIST_ASSEMBLY.get(int(tun.list_assembly), str(int(tun.list_assembly))),
+              "list_reuses_last_step": batch.list_reuses()}
     batch.check_finite(sh)
     del batch
 
@@ -339,7 +344,7 @@ def run_batched(args, dev, stream, flush):
     v_graph = S * k_single / t_graph
     return {"unit": "scenes*steps/s", "value": v_batch, "scenes": S, "particles": total,
             "pbf_blocks": kinds.count("pbf_block"), "granular_columns": kinds.count("granular_column"),
-            "steps": K, "ms_per_step": 1e3 * t_batch / K, "gpu_launches": launches,
+            "steps": K, "ms_per_step": 1e3 * t_batch / K, "gpu_launches": launches, "tuning": tuning,
             "per_scene_plain": {"value": v_eager, "steps": k_single, "ms_per_step": 1e3 * t_eager / k_single,
                                 "how": "one system per scene, pbd_update each, same stream"},
             "per_scene_graph": {"value": v_graph, "steps": k_single, "ms_per_step": 1e3 * t_graph / k_single,
