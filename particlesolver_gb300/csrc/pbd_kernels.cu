@@ -1102,12 +1102,76 @@ struct ChunkCursor {
     }
 };
 
+// A quad of the index list, read once per pass: PBD_LIST_LOAD 1 keeps it
+// out of L1 (which then holds more of the neighbours' gathered values),
+// 2 also marks it first for eviction from L2.  Measured on the 1M dam
+// break: 514.0 / 518.6 / 520.0 steps/s for 0 / 1 / 2.
+#ifndef PBD_LIST_LOAD
+#define PBD_LIST_LOAD 2
+#endif
+__device__ __forceinline__ uint4 ld_list(const uint4 *p) {
+    uint4 r;
+#if PBD_LIST_LOAD == 2
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(p), "l"(pol));
+#elif PBD_LIST_LOAD == 1
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(p));
+#else
+    r = __ldg(p);
+#endif
+    return r;
+}
+
+// A quad of the index list written by the lambda pass: PBD_LIST_STORE 1
+// marks it first for eviction from L2 (the list is larger than L2; the
+// positions the walk reads then stay longer).  Measured on the 1M dam
+// break: 520.7 -> 524.9 steps/s.
+#ifndef PBD_LIST_STORE
+#define PBD_LIST_STORE 1
+#endif
+__device__ __forceinline__ void st_list(uint4 *p, uint4 v) {
+#if PBD_LIST_STORE == 1
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile("st.global.L1::no_allocate.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;"
+                 :
+                 : "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
+                 : "memory");
+#else
+    *p = v;
+#endif
+}
+
+// A candidate's sorted position in the walk: PBD_CAND_LOAD 1 marks it last
+// for eviction from L2 (measured: 520.7 -> 513.5 steps/s, so off).
+#ifndef PBD_CAND_LOAD
+#define PBD_CAND_LOAD 0
+#endif
+__device__ __forceinline__ float4 ld_cand(const float4 *p) {
+#if PBD_CAND_LOAD == 1
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    float4 r;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+        : "l"(p), "l"(pol));
+    return r;
+#else
+    return __ldg(p);
+#endif
+}
+
 // Calls f(j) for the listed neighbours of particle i (count word c).
 template <class F>
 __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uint32_t c, F &&f) {
     const uint32_t cnt = min(list_nnb(c), L.capacity);
     for (uint32_t q = 0; 4u * q < cnt; ++q) {
-        const uint4 e = L.slot[q * L.stride + i];
+        const uint4 e = ld_list(L.slot + q * L.stride + i);
         const uint32_t left = cnt - 4u * q;
         f(e.x);
         if (left > 1u) f(e.y);
@@ -1131,7 +1195,7 @@ __device__ __forceinline__ void gather_listed(const NbList &L, uint32_t i, uint3
 #pragma unroll
         for (int u = 0; u < QUADS; ++u) {
             const uint32_t qq = q + (uint32_t)u;
-            const uint4 e = (4u * qq < cnt) ? L.slot[qq * L.stride + i] : make_uint4(i, i, i, i);
+            const uint4 e = (4u * qq < cnt) ? ld_list(L.slot + qq * L.stride + i) : make_uint4(i, i, i, i);
             const uint32_t first = 4u * qq;
             jj[4 * u] = first < cnt ? e.x : i;
             jj[4 * u + 1] = first + 1u < cnt ? e.y : i;
@@ -1159,7 +1223,7 @@ __device__ __forceinline__ bool row_chunks(uint32_t i, float3 pi, float reach2, 
         uint32_t m = 0u;
 #pragma unroll kWalkUnroll
         for (uint32_t k = 0; k < len; ++k) {
-            const float4 q = __ldg(sx + c + k);
+            const float4 q = ld_cand(sx + c + k);
             m = (m << 1) | (__float_as_uint(__fsub_rn(dist2_exact(pi, f3(q)), reach2)) >> 31);
         }
         m = __brev(m) >> (32u - len);            // candidate k at bit k
@@ -1354,7 +1418,7 @@ __device__ __forceinline__ void lambda_walk_particle(const DevParams &P, const N
             float4 pp[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) jj[t] = cur.next(nch, i, load);
-            L.slot[(k >> 2) * L.stride + i] = make_uint4(jj[0], jj[1], jj[2], jj[3]);
+            st_list(L.slot + (k >> 2) * L.stride + i, make_uint4(jj[0], jj[1], jj[2], jj[3]));
 #pragma unroll
             for (int t = 0; t < 4; ++t) pp[t] = __ldg(sx + jj[t]);
 #pragma unroll
@@ -1933,7 +1997,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph(DevParams P0, uint32_t n, const
         // the last lambda pass listed every neighbour of any phase; a
         // neighbour's fluid mass rides in vs.w (0 for the other phases)
         for (uint32_t q = 0; 4u * q < cnt; ++q) {
-            const uint4 e = L.slot[q * L.stride + i];
+            const uint4 e = ld_list(L.slot + q * L.stride + i);
             const uint32_t left = cnt - 4u * q;
             const uint32_t jj[4] = {e.x, left > 1u ? e.y : i, left > 2u ? e.z : i, left > 3u ? e.w : i};
             float4 xx[4], vv[4];
