@@ -99,6 +99,31 @@ def test_batch_one_step_equals_each_scene_alone():
         assert_same_state(vel[sl], alone.velocities(), f"scene {k} ({sc.name}) velocities")
 
 
+def test_batch_with_long_neighbour_rows():
+    """A batch with a PBF block squeezed to 0.6 of its lattice spacing (rows
+    of more than 32 candidates, more row chunks than the 12 a walk keeps in
+    shared memory), a plain block and a granular column: each scene equals
+    its solo run, and the batch's list path equals the batch's exact walk
+    (no lists) bit for bit."""
+    dense = W.pbf_block(3000, seed=21)
+    dense.pos_w[:, :3] *= 0.6
+    scenes = [dense, W.pbf_block(1500, seed=22), W.granular_column(400, seed=23)]
+    a, firsts = load_batch(scenes)
+    b, _ = load_batch(scenes)
+    b.set_tuning(threads_per_particle=1, neighbor_list_capacity=0)
+    for _ in range(2):
+        a.update(1.0 / 60.0)
+        b.update(1.0 / 60.0)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+    pos = a.positions()
+    for k, sc in enumerate(scenes):
+        alone = load_alone(sc)
+        for _ in range(2):
+            alone.update(1.0 / 60.0)
+        assert_same_state(pos[firsts[k]:firsts[k] + sc.n], alone.positions(), f"scene {k} ({sc.name}) positions")
+
+
 def test_batch_trajectories_match_oracle():
     """Several steps: every scene of the batch against the FP64 oracle run
     on that scene alone, by invariants."""
