@@ -514,6 +514,18 @@ def run_adjoint(args, dev, stream):
         sens[f"steps_{steps}"] = {"loss_stiffness_wrong": loss_at(s0, v_hidden, steps, tgt),
                                   "loss_velocities_wrong": loss_at(s_hidden, v_init, steps, tgt),
                                   "loss_both_wrong": loss_at(s0, v_init, steps, tgt)}
+    base = {"scenes": len(scenes), "particles": n, "constraints": m, "steps": T, "checkpoint_every": every,
+            "dt": dt, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "timing": "wall clock between device synchronisations, median of 3 after 2 warm-up passes",
+            "backward_over_forward": bwd_ms / fwd_ms, "particle_steps_per_s_fwd_bwd": n * T / ((fwd_ms + bwd_ms) * 1e-3),
+            "workload": f"{len(scenes)} scenes of a 64x64 cloth (stretch, pinned edges) + 8 ropes x 32 + 200 "
+                        f"grains, hidden stiffness U(0.2, 1) and grain velocities; fit from stiffness 0.6 and "
+                        f"zero velocities by Adam through the adjoint, on the hidden run's positions after "
+                        f"{T1} steps, then after {T}"}
+    e0 = errors(s0, v_init)
+    base["start"] = {"stiffness_mae": e0[0], "grain_velocity_err": e0[1], "loss": sens[f"steps_{T}"]["loss_both_wrong"]}
+    if args.adjoint_iters <= 0:  # timing only: no recovery
+        return {**base, "sensitivity": sens}
     t0 = time.perf_counter()
     # recovery by a horizon curriculum: both parameter sets fitted to the
     # hidden run's positions after T1 steps, then after T
@@ -523,12 +535,8 @@ def run_adjoint(args, dev, stream):
     fit_s = time.perf_counter() - t0
     # stiffness alone, from the hidden velocities, on the final positions
     st3, _, losses3 = fit(sysm, x0, target, s0, v_hidden, dt, T, every, args.adjoint_iters, 0.02, 0.0)
-    e0, e1, e2, e3 = errors(s0, v_init), errors(st1, v1), errors(st2, v2), errors(st3, v_hidden)
-    return {"scenes": len(scenes), "particles": n, "constraints": m, "steps": T, "checkpoint_every": every,
-            "dt": dt, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
-            "timing": "wall clock between device synchronisations, median of 3 after 2 warm-up passes",
-            "backward_over_forward": bwd_ms / fwd_ms, "particle_steps_per_s_fwd_bwd": n * T / ((fwd_ms + bwd_ms) * 1e-3),
-            "start": {"stiffness_mae": e0[0], "grain_velocity_err": e0[1], "loss": sens[f"steps_{T}"]["loss_both_wrong"]},
+    e1, e2, e3 = errors(st1, v1), errors(st2, v2), errors(st3, v_hidden)
+    return {**base,
             "curriculum": [
                 {"steps": T1, "iterations": len(losses1), "loss_first": losses1[0], "loss_last": losses1[-1],
                  "stiffness_mae": e1[0], "grain_velocity_err": e1[1], f"loss_at_{T}": loss_at(st1, v1, T, target)},
@@ -538,11 +546,7 @@ def run_adjoint(args, dev, stream):
             "stiffness_only_from_hidden_velocities": {"steps": T, "iterations": len(losses3),
                                                       "loss_first": losses3[0], "loss_last": losses3[-1],
                                                       "stiffness_mae_start": e0[0], "stiffness_mae_end": e3[0]},
-            "sensitivity": sens,
-            "workload": f"{len(scenes)} scenes of a 64x64 cloth (stretch, pinned edges) + 8 ropes x 32 + 200 "
-                        f"grains, hidden stiffness U(0.2, 1) and grain velocities; fit from stiffness 0.6 and "
-                        f"zero velocities by Adam through the adjoint, on the hidden run's positions after "
-                        f"{T1} steps, then after {T}"}
+            "sensitivity": sens}
 
 
 def run_ours(args, world, rank, local_rank):
