@@ -38,6 +38,12 @@ constexpr int kBlock = 256;
 #ifndef PBD_LAMBDA_MIN_BLOCKS
 #define PBD_LAMBDA_MIN_BLOCKS 6
 #endif
+// The batched list build reads each slot's parameter block (76 registers
+// uncapped): capped at 64 for 8 blocks per SM (512-scene batch: 49,060 ->
+// 50,017 scenes*steps/s).
+#ifndef PBD_BATCH_LAMBDA_MIN_BLOCKS
+#define PBD_BATCH_LAMBDA_MIN_BLOCKS 8
+#endif
 #ifndef PBD_BATCH_SOLVE_MIN_BLOCKS
 #define PBD_BATCH_SOLVE_MIN_BLOCKS 4
 #endif
@@ -1512,7 +1518,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_lambda_list(DevParams P0, uint32_
 // [cols][kListBlock] uint2 array in shared memory (a warp's chunk stores
 // are 32 consecutive uint2, free of bank conflicts).
 template <int RAD, bool B, bool SKIN>
-__global__ void __launch_bounds__(kListBlock, PBD_LAMBDA_MIN_BLOCKS) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
+__global__ void __launch_bounds__(kListBlock, B ? PBD_BATCH_LAMBDA_MIN_BLOCKS : PBD_LAMBDA_MIN_BLOCKS) k_lambda_slist(DevParams P0, uint32_t n, uint32_t iter_left,
                                                                 const float4 *__restrict__ sx,
                                                                 const SortedAttr *__restrict__ sattr,
                                                                 const uint32_t *__restrict__ cell_first,
