@@ -326,6 +326,64 @@ __global__ void __launch_bounds__(kBlock) k_rank_reorder(uint32_t n, const uint3
     sorted_attr[p] = a;
 }
 
+// The whole grid build of a small single-scene system in one block: the
+// steps of k_clear_counts / k_hash_count, the scan, k_bucket and
+// k_rank_reorder, separated by block barriers instead of launches, with the
+// cell counts, hashes, arrival slots and buckets in shared memory (one
+// global pass over the particles and the cell offsets).
+constexpr int kSmallGridThreads = kScanThreads;
+__global__ void __launch_bounds__(kSmallGridThreads) k_grid_small(DevParams P, uint32_t n,
+                                                                  const float4 *__restrict__ x,
+                                                                  const int *__restrict__ phase,
+                                                                  const float *__restrict__ rho0, GridBuffers g) {
+    pdl_entry();
+    extern __shared__ uint32_t s_small[];
+    __shared__ uint32_t smem[32];
+    const uint32_t cells = P.num_cells + 1u;
+    uint32_t *const cnt = s_small;  // [cells]: counts, then offsets
+    uint32_t *const hs = cnt + cells;  // [n] cell of each particle
+    uint32_t *const sl = hs + n;       // [n] arrival slot in its cell
+    uint32_t *const tmp = sl + n;      // [n] cell-bucketed indices
+    for (uint32_t c = threadIdx.x; c < cells; c += blockDim.x) cnt[c] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t h = grid_hash(P, grid_pos(P, f3(x[i])));
+        hs[i] = h;
+        g.hash[i] = h;
+        sl[i] = atomicAdd(cnt + h, 1u);
+    }
+    __syncthreads();
+    // exclusive scan, each thread over a contiguous run of cells
+    const uint32_t per = (cells + blockDim.x - 1u) / blockDim.x;
+    const uint32_t c0 = min(threadIdx.x * per, cells), c1 = min(c0 + per, cells);
+    uint32_t sum = 0;
+    for (uint32_t c = c0; c < c1; ++c) sum += cnt[c];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(sum, smem, total);
+    for (uint32_t c = c0; c < c1; ++c) {
+        const uint32_t v = cnt[c];
+        cnt[c] = run;
+        g.cell_first[c] = run;
+        run += v;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) tmp[cnt[hs[i]] + sl[i]] = i;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t h = hs[i];
+        const uint32_t b = cnt[h], e = cnt[h + 1];
+        uint32_t rank = 0;
+        for (uint32_t k = b; k < e; ++k) rank += (tmp[k] < i) ? 1u : 0u;
+        const uint32_t p = b + rank;
+        g.sorted_idx[p] = i;
+        g.sorted_x[p] = x[i];
+        SortedAttr a;
+        a.phase = phase[i];
+        a.rho0 = rho0[i];
+        g.sorted_attr[p] = a;
+    }
+}
+
 // Stable in-cell rank only (k_rank_reorder without the data gather).
 __global__ void __launch_bounds__(kBlock) k_rank_only(uint32_t n, const uint32_t *__restrict__ hash,
                                                       const uint32_t *__restrict__ cell_first,
@@ -2168,6 +2226,25 @@ cudaError_t launch_grid_finish(const DevParams &P, uint32_t n, const GridBuffers
     pdl_launch(k_bucket, blocks_for(n), kBlock, 0, s, n, g.hash, g.slot, g.cell_first, g.tmp, skip);
     pdl_launch(k_rank_reorder, blocks_for(n), kBlock, 0, s, n, g.hash, g.cell_first, g.tmp, x, phase, rho0,
                                                     g.sorted_idx, g.sorted_x, g.sorted_attr, skip);
+    return cudaGetLastError();
+}
+
+size_t small_grid_smem(uint32_t num_cells, uint32_t n) {
+    return ((size_t)num_cells + 1u + 3u * (size_t)n) * sizeof(uint32_t);
+}
+
+cudaError_t launch_grid_small(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
+                              const int *phase, const float *rho0, cudaStream_t s) {
+    const size_t smem = small_grid_smem(P.num_cells, n);
+    if (n > kSmallGridN || smem > kSmallGridSmem || P.table) return cudaErrorInvalidValue;
+    static bool attr_set = false;  // per process; the attribute holds for every later launch
+    if (!attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(k_grid_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)kSmallGridSmem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    pdl_launch(k_grid_small, 1u, (unsigned)kSmallGridThreads, smem, s, P, n, x, phase, rho0, g);
     return cudaGetLastError();
 }
 

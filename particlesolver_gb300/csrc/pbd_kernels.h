@@ -133,6 +133,16 @@ cudaError_t launch_sort_into_cells(const DevParams &P, uint32_t n, const float4 
                                    uint32_t *cell_start, uint32_t *cell_end, cudaStream_t s);
 cudaError_t launch_refresh_sorted(uint32_t n, const GridBuffers &g, const float4 *x,
                                   cudaStream_t s);
+// The whole grid build of a small single-scene system in one block of 1024
+// threads (cell counts, scan, bucket, stable rank and reorder in shared
+// memory; the same result as the multi-kernel build): n <= kSmallGridN and
+// small_grid_smem(num_cells, n) <= kSmallGridSmem.  One launch instead of
+// six and a memset per build.
+constexpr uint32_t kSmallGridN = 8192;
+constexpr size_t kSmallGridSmem = 200u * 1024u;
+size_t small_grid_smem(uint32_t num_cells, uint32_t n);
+cudaError_t launch_grid_small(const DevParams &P, uint32_t n, const GridBuffers &g, const float4 *x,
+                              const int *phase, const float *rho0, cudaStream_t s);
 // tpp: lanes sharing one particle's neighbour walk (1, 2, 4, 8, 16, 32).
 // sxl: per sorted slot (position xyz, lambda) -- written by the lambda pass,
 // read by the solve pass.

@@ -497,8 +497,22 @@ int collect_profile(pbd_system *s) {
 
 // ------------------------------------------------------------- the step
 
+// A single-scene system small enough for the one-block grid build (no
+// skin lists: their later iterations use the multi-kernel build).
+bool small_grid(const pbd_system *s) {
+    return !s->batched() && s->n > 0 && s->n <= pbd::kSmallGridN &&
+           pbd::small_grid_smem(s->dev.num_cells, s->n) <= pbd::kSmallGridSmem && s->skin <= 0.f;
+}
+
 int build_grid(pbd_system *s, cudaStream_t st, bool hashed_in_predict) {
     const pbd::DevParams &P = s->dev;
+    if (small_grid(s)) {  // the prediction did not hash: the block does it all
+        Stage t(s, st, PBD_STAGE_GRID, 1u);
+        CUDA_TRY(s, pbd::launch_grid_small(P, s->n, s->grid, s->x, s->phase, s->rho0, st));
+        s->grid_valid = true;
+        s->list_valid = false;
+        return PBD_OK;
+    }
     Stage t(s, st, PBD_STAGE_GRID, (hashed_in_predict ? 0u : 1u) + 3u + (s->n ? 2u : 0u));
     if (!hashed_in_predict) {
         CUDA_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
@@ -535,10 +549,12 @@ int enqueue_update(pbd_system *s, float dt, cudaStream_t st, float4 *rec = nullp
     if (rec) CUDA_TRY(s, cudaMemcpyAsync(rec, s->x, nbytes, cudaMemcpyDeviceToDevice, st));
     {
         // predict, with the first grid build's hash and cell counts fused in
+        // (not for the one-block grid build, which hashes itself)
         Stage t(s, st, PBD_STAGE_PREDICT, 1);
-        CUDA_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
+        const bool small = small_grid(s);
+        if (!small) CUDA_TRY(s, cudaMemsetAsync(s->grid.cell_first, 0, ((size_t)P.num_cells + 1u) * 4u, st));
         CUDA_TRY(s, pbd::launch_predict(P, n, dt, s->x, s->v, s->x_old, s->grid.hash, s->grid.slot,
-                                        s->grid.cell_first, st, s->gas_buffers()));
+                                        small ? nullptr : s->grid.cell_first, st, s->gas_buffers()));
     }
     const uint32_t mask = solve_mask(s);
     const uint32_t dist_kernels =
