@@ -1211,25 +1211,6 @@ __device__ __forceinline__ void st_list(uint4 *p, uint4 v) {
 #endif
 }
 
-// A candidate's sorted position in the walk: PBD_CAND_LOAD 1 marks it last
-// for eviction from L2 (measured: 520.7 -> 513.5 steps/s, so off).
-#ifndef PBD_CAND_LOAD
-#define PBD_CAND_LOAD 0
-#endif
-__device__ __forceinline__ float4 ld_cand(const float4 *p) {
-#if PBD_CAND_LOAD == 1
-    uint64_t pol;
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-    float4 r;
-    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
-        : "l"(p), "l"(pol));
-    return r;
-#else
-    return __ldg(p);
-#endif
-}
-
 // Calls f(j) for the listed neighbours of particle i (count word c).
 template <class F>
 __device__ __forceinline__ void for_each_listed(const NbList &L, uint32_t i, uint32_t c, F &&f) {
@@ -1287,7 +1268,7 @@ __device__ __forceinline__ bool row_chunks(uint32_t i, float3 pi, float reach2, 
         uint32_t m = 0u;
 #pragma unroll kWalkUnroll
         for (uint32_t k = 0; k < len; ++k) {
-            const float4 q = ld_cand(sx + c + k);
+            const float4 q = __ldg(sx + c + k);
             m = (m << 1) | (__float_as_uint(__fsub_rn(dist2_exact(pi, f3(q)), reach2)) >> 31);
         }
         m = __brev(m) >> (32u - len);            // candidate k at bit k
